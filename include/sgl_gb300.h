@@ -1,0 +1,137 @@
+/*
+ * sgl_gb300.h -- C ABI of the GB300 (sm_103a) engine for the hot path of the stochastic
+ * weak-lensing magnification PDF: the compensated compound-Poisson characteristic exponent
+ * ln Phi(k_kappa, k_gamma) of a binned lens population, its xi_lin (gauss) clustering term,
+ * and the Hankel/Fourier inversion to dP/dln(mu).
+ *
+ * Every entry point takes plain host pointers and sizes (no framework types), returns an
+ * sgl_status, and is synchronous with respect to the host on the context's own CUDA stream.
+ * A context is re-entrant but must not be shared by two host threads at once.
+ *
+ * Each function names the reference (sgl_analytic v0.2.0, src/sgl_analytic/) interface it
+ * replaces.  The reference-side binding (a ctypes stub) is shown in INTEGRATION.md.
+ */
+#ifndef SGL_GB300_H
+#define SGL_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SGL_ABI_VERSION 1
+
+typedef struct sgl_ctx sgl_ctx;
+
+/* Status codes.  The Python layer maps SGL_ERR_VALUE to ValueError and SGL_ERR_NONFINITE to
+ * RuntimeError, the reference's exception types for bad input (api.py:14-22,
+ * pipeline.py:144-164) and non-finite output (api.py:73-74). */
+typedef enum {
+    SGL_OK = 0,
+    SGL_ERR_VALUE = 1,        /* invalid argument (size, NaN, ordering) */
+    SGL_ERR_CUDA = 2,         /* CUDA runtime error; see sgl_last_error */
+    SGL_ERR_NONFINITE = 3,    /* a result was NaN / Inf */
+    SGL_ERR_STATE = 4,        /* call order (e.g. lnphi before set_cells) */
+    SGL_ERR_UNSUPPORTED = 5   /* configuration outside the implemented path */
+} sgl_status;
+
+/* Arithmetic of the Lambda evaluation and of the inversion. */
+typedef enum {
+    SGL_FP64 = 0,   /* FP64 throughout: parity path, max|d lnPhi| <= 1e-10 vs the reference */
+    SGL_MIXED = 1   /* float-float phase reduction + FP32 sincos/GEMMs, FP64 cross-tile sums */
+} sgl_precision;
+
+/* Options of the inversion; defaults = pipeline.run's gauss chain (pipeline.py:221-239). */
+typedef struct {
+    int precision;        /* sgl_precision for Lambda and the transforms */
+    int tail_box;         /* 1: widen the box to kappa 0.99, gamma 0.8 (sgl_full.py:33-36) */
+    double phi_tol;       /* |Phi| at the k-reach cut (pipeline default 1e-8) */
+    int n_xi_wide;        /* normalisation / moment grid points (500 for gauss) */
+    int n_k_int;          /* points per constant-mu path (2400) */
+    double xi_reach;      /* moment grid reach in sigma_xi = 2 sigma (24) */
+} sgl_invert_opts;
+
+/* Grid and moments of one inversion (the reference's meta["grid"] and meta moments,
+ * sgl_full.py:366-374). */
+typedef struct {
+    int64_t nk_k, nk_g, n_kap, n_gam;
+    double k_k_max, k_g_max, kap_min, kap_max, gam_max, xi_min, xi_max, sigma;
+    double phi_at_k_cut, phi_at_g_cut;
+    double mean, var, skew, sigmaDL, norm;
+    double ms_lambda, ms_transform, ms_path;   /* device time of the three stages */
+} sgl_invert_meta;
+
+/* Library / context ------------------------------------------------------------------- */
+int sgl_abi_version(void);
+
+/* Creates a context on CUDA device `device` (its own stream, device arena). */
+sgl_status sgl_ctx_create(int device, sgl_ctx** out);
+void sgl_ctx_destroy(sgl_ctx* ctx);
+
+/* Last error message of this context (or of the last failed sgl_ctx_create when ctx is
+ * NULL), copied into buf.  Returns the message length. */
+int sgl_last_error(const sgl_ctx* ctx, char* buf, int buflen);
+
+/* The context's CUDA stream (a cudaStream_t), so a caller can record events on it. */
+sgl_status sgl_ctx_stream(sgl_ctx* ctx, void** stream);
+
+/* Per-kernel device-time statistics.  enable = 1 records CUDA events around every launch of
+ * the engine's hot kernels (sweep, GEMMs, transforms, path integral) and accumulates, per kernel
+ * tag: launches, device milliseconds, algorithmic FLOPs and bytes.  sgl_stats_json writes them
+ * as a JSON object into buf (returns the full length); reset = 1 clears them afterwards.
+ * No counterpart in the reference (its stage timers are wall-clock, pipeline.py:170-243). */
+sgl_status sgl_ctx_profile(sgl_ctx* ctx, int enable);
+int sgl_stats_json(sgl_ctx* ctx, char* buf, int buflen, int reset);
+
+/* Population ---------------------------------------------------------------------------- */
+/* Occupied fine (kappa, gamma) cells: weight w0, weight-averaged centroid (k0, g0), fine gamma
+ * bin index ig, the fine gamma bin edges fe_g, and the weak-arm variance V.
+ * Replaces the cell compaction of Lam.__init__ (sgl_full.py:2759-2775). */
+sgl_status sgl_lam_set_cells(sgl_ctx* ctx, int64_t n_cells, const double* w0, const double* k0,
+                             const double* g0, const int32_t* ig, const double* fe_g, int n_fe_g,
+                             double V);
+
+/* xi_lin two-point groups in the reference's raw form (Cells.xi_groups, sgl_full.py:1478-1523):
+ * group g has harmonic m[g], nrow[g] rows over nidx[g] coarse cells (flat index idx into the
+ * coarse lattice, gamma-fastest) plus one residual column: rows are nrow x (nidx + 1), row-major,
+ * concatenated over groups.  ce_k / ce_g: coarse lattice edges.  prune: Lam's xi_prune (1e-7);
+ * s0 > 0 overrides the largest row norm that prune is relative to (for subsets of groups).
+ * Replaces the xi part of Lam.__init__ (sgl_full.py:2799-2861). */
+sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const int32_t* nrow,
+                          const int32_t* nidx, const int32_t* idx, const double* rows,
+                          const double* ce_k, int n_ce_k, const double* ce_g, int n_ce_g,
+                          double prune, double s0);
+
+/* Total sigma_kappa.  Replaces Lam.sigma (sgl_full.py:3437-3452) for the default chain. */
+sgl_status sgl_lam_sigma(sgl_ctx* ctx, double* sigma);
+
+/* ln Phi on the tensor grid kk x kg (row-major, nkk x nkg), real and imaginary planes.
+ * Replaces Lam.__call__ / Lam._direct_call (sgl_full.py:3088-3160): the separable Psi_1 for
+ * grids of >= 200000 points (direct sums otherwise), -1/2 k^2 V, and the gauss xi_lin term
+ * (101^2 coarse grid + not-a-knot bicubic spline above 101^2 points, exact otherwise). */
+sgl_status sgl_lnphi(sgl_ctx* ctx, const double* kk, int nkk, const double* kg, int nkg,
+                     int precision, double* out_re, double* out_im);
+
+/* The exact xi_lin (gauss) two-point term Psi_2 on the tensor grid kk x kg, without coarse-grid
+ * interpolation, real and imaginary planes (nkk x nkg, row-major).  k_gamma = {0} and
+ * k_kappa = {0} take the 1-D reach paths.  Replaces Lam._Qxi / Lam._Qxi_gauss
+ * (sgl_full.py:2863-2951).  Requires sgl_lam_set_xi with at least one group. */
+sgl_status sgl_xi_term(sgl_ctx* ctx, const double* kk, int nkk, const double* kg, int nkg, int precision,
+                       double* out_re, double* out_im);
+
+/* Fills opts with the pipeline defaults above. */
+void sgl_invert_opts_default(sgl_invert_opts* opts);
+
+/* Phi = exp(ln Phi) -> P_s(ln mu) at xi_out (n_xi points), normalised on the wide grid.
+ * Replaces sgl_full.invert (sgl_full.py:159-375) with sgl.vector_grid (sgl.py:1229-1258) and
+ * sgl.P_vector_joint (sgl.py:1127-1156): measured k-reach, width-relative grid with the tail
+ * box, Hankel + Fourier transforms, Euler-Maclaurin endpoint term, constant-mu path integral.
+ * P_out: n_xi doubles (host).  meta may be NULL. */
+sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_invert_opts* opts,
+                   double* P_out, sgl_invert_meta* meta);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SGL_GB300_H */

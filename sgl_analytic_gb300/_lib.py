@@ -1,0 +1,198 @@
+"""ctypes binding of ``libsgl_gb300.so`` (declared in ``include/sgl_gb300.h``).
+
+There is no CPU fallback: if the library is missing or no CUDA device is present, every entry
+point raises.  Status codes map to the reference's exception types: bad input -> ValueError,
+non-finite output -> RuntimeError (sgl_analytic api.py:14-22, 73-74).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().with_name("libsgl_gb300.so")
+
+SGL_OK, SGL_ERR_VALUE, SGL_ERR_CUDA, SGL_ERR_NONFINITE, SGL_ERR_STATE, SGL_ERR_UNSUPPORTED = range(6)
+SGL_FP64, SGL_MIXED = 0, 1
+PRECISIONS = {"fp64": SGL_FP64, "mixed": SGL_MIXED}
+
+# every symbol the header declares (checked by the CPU test suite)
+EXPORTS = ("sgl_abi_version", "sgl_ctx_create", "sgl_ctx_destroy", "sgl_last_error", "sgl_ctx_stream",
+           "sgl_ctx_profile", "sgl_stats_json", "sgl_lam_set_cells",
+           "sgl_lam_set_xi", "sgl_lam_sigma", "sgl_lnphi", "sgl_xi_term", "sgl_invert_opts_default", "sgl_pdf")
+
+
+class InvertOpts(C.Structure):
+    _fields_ = [("precision", C.c_int), ("tail_box", C.c_int), ("phi_tol", C.c_double),
+                ("n_xi_wide", C.c_int), ("n_k_int", C.c_int), ("xi_reach", C.c_double)]
+
+
+class InvertMeta(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("nk_k", "nk_g", "n_kap", "n_gam")] + \
+               [(n, C.c_double) for n in ("k_k_max", "k_g_max", "kap_min", "kap_max", "gam_max", "xi_min",
+                                          "xi_max", "sigma", "phi_at_k_cut", "phi_at_g_cut", "mean", "var",
+                                          "skew", "sigmaDL", "norm", "ms_lambda", "ms_transform", "ms_path")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib():
+    """Loads the engine library (once).  Raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH.name} is not built; run `python sgl_analytic_gb300/_build.py` "
+                               "(or __graft_entry__.build()) -- there is no CPU fallback")
+        L = C.CDLL(str(LIB_PATH))
+        dp = C.POINTER(C.c_double)
+        ip = C.POINTER(C.c_int32)
+        vp = C.c_void_p
+        L.sgl_abi_version.restype = C.c_int
+        L.sgl_ctx_create.argtypes = [C.c_int, C.POINTER(vp)]
+        L.sgl_ctx_destroy.argtypes = [vp]
+        L.sgl_ctx_destroy.restype = None
+        L.sgl_last_error.argtypes = [vp, C.c_char_p, C.c_int]
+        L.sgl_ctx_stream.argtypes = [vp, C.POINTER(vp)]
+        L.sgl_ctx_profile.argtypes = [vp, C.c_int]
+        L.sgl_stats_json.argtypes = [vp, C.c_char_p, C.c_int, C.c_int]
+        L.sgl_stats_json.restype = C.c_int
+        L.sgl_lam_set_cells.argtypes = [vp, C.c_int64, dp, dp, dp, ip, dp, C.c_int, C.c_double]
+        L.sgl_lam_set_xi.argtypes = [vp, C.c_int, ip, ip, ip, ip, dp, dp, C.c_int, dp, C.c_int, C.c_double,
+                                     C.c_double]
+        L.sgl_lam_sigma.argtypes = [vp, dp]
+        L.sgl_lnphi.argtypes = [vp, dp, C.c_int, dp, C.c_int, C.c_int, dp, dp]
+        L.sgl_xi_term.argtypes = [vp, dp, C.c_int, dp, C.c_int, C.c_int, dp, dp]
+        L.sgl_invert_opts_default.argtypes = [C.POINTER(InvertOpts)]
+        L.sgl_invert_opts_default.restype = None
+        L.sgl_pdf.argtypes = [vp, dp, C.c_int, C.POINTER(InvertOpts), dp, C.POINTER(InvertMeta)]
+        for name in ("sgl_ctx_create", "sgl_ctx_stream", "sgl_ctx_profile", "sgl_lam_set_cells", "sgl_lam_set_xi", "sgl_lam_sigma", "sgl_lnphi",
+                     "sgl_xi_term", "sgl_pdf"):
+            getattr(L, name).restype = C.c_int
+        if L.sgl_abi_version() != 1:
+            raise RuntimeError("libsgl_gb300.so ABI version mismatch; rebuild it")
+        _lib = L
+    return _lib
+
+
+def _ptr(a, ctype=C.c_double):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def _raise(status, msg):
+    if status == SGL_ERR_VALUE:
+        raise ValueError(msg)
+    if status == SGL_ERR_UNSUPPORTED:
+        raise NotImplementedError(msg)
+    raise RuntimeError(msg)
+
+
+class Engine:
+    """One engine context on one CUDA device (own stream and device arena)."""
+
+    def __init__(self, device=0):
+        L = lib()
+        h = C.c_void_p()
+        st = L.sgl_ctx_create(int(device), C.byref(h))
+        if st != SGL_OK:
+            buf = C.create_string_buffer(512)
+            L.sgl_last_error(None, buf, 512)
+            _raise(st, "sgl_ctx_create: " + buf.value.decode())
+        self._h = h
+        self._L = L
+        self.device = int(device)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.sgl_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st, what):
+        if st != SGL_OK:
+            buf = C.create_string_buffer(1024)
+            self._L.sgl_last_error(self._h, buf, 1024)
+            _raise(st, f"{what}: {buf.value.decode()}")
+
+    @property
+    def stream(self):
+        """The engine's cudaStream_t as an integer handle (for torch.cuda.ExternalStream)."""
+        h = C.c_void_p()
+        self._check(self._L.sgl_ctx_stream(self._h, C.byref(h)), "sgl_ctx_stream")
+        return h.value or 0
+
+    def profile(self, enable=True):
+        self._check(self._L.sgl_ctx_profile(self._h, int(bool(enable))), "sgl_ctx_profile")
+
+    def stats(self, reset=False):
+        import json
+        n = self._L.sgl_stats_json(self._h, None, 0, 0)
+        buf = C.create_string_buffer(n + 1)
+        self._L.sgl_stats_json(self._h, buf, n + 1, int(bool(reset)))
+        return json.loads(buf.value.decode())
+
+    # ---------------------------------------------------------------- population
+    def set_cells(self, w0, k0, g0, ig, fe_g, V):
+        w0, k0, g0, fe_g = (np.ascontiguousarray(a, np.float64) for a in (w0, k0, g0, fe_g))
+        ig = np.ascontiguousarray(ig, np.int32)
+        n = w0.size
+        if not (k0.size == g0.size == ig.size == n):
+            raise ValueError("cell arrays must have equal length")
+        self._check(self._L.sgl_lam_set_cells(self._h, n, _ptr(w0), _ptr(k0), _ptr(g0), _ptr(ig, C.c_int32),
+                                              _ptr(fe_g), fe_g.size, float(V)), "sgl_lam_set_cells")
+
+    def set_xi(self, m, nrow, nidx, idx, rows, ce_k, ce_g, prune=1e-7, s0=0.0):
+        m, nrow, nidx, idx = (np.ascontiguousarray(a, np.int32) for a in (m, nrow, nidx, idx))
+        rows, ce_k, ce_g = (np.ascontiguousarray(a, np.float64) for a in (rows, ce_k, ce_g))
+        if rows.size != int(np.sum(nrow.astype(np.int64) * (nidx.astype(np.int64) + 1))):
+            raise ValueError("rows size does not match nrow x (nidx + 1)")
+        if idx.size != int(np.sum(nidx.astype(np.int64))):
+            raise ValueError("idx size does not match nidx")
+        self._check(self._L.sgl_lam_set_xi(self._h, m.size, _ptr(m, C.c_int32), _ptr(nrow, C.c_int32),
+                                           _ptr(nidx, C.c_int32), _ptr(idx, C.c_int32), _ptr(rows), _ptr(ce_k),
+                                           ce_k.size, _ptr(ce_g), ce_g.size, float(prune), float(s0)),
+                    "sgl_lam_set_xi")
+
+    def sigma(self):
+        s = C.c_double()
+        self._check(self._L.sgl_lam_sigma(self._h, C.byref(s)), "sgl_lam_sigma")
+        return s.value
+
+    def lnphi(self, kk, kg, precision=SGL_FP64):
+        kk = np.ascontiguousarray(np.atleast_1d(kk), np.float64)
+        kg = np.ascontiguousarray(np.atleast_1d(kg), np.float64)
+        re = np.empty((kk.size, kg.size))
+        im = np.empty((kk.size, kg.size))
+        self._check(self._L.sgl_lnphi(self._h, _ptr(kk), kk.size, _ptr(kg), kg.size, int(precision), _ptr(re),
+                                      _ptr(im)), "sgl_lnphi")
+        return re + 1j * im
+
+    def xi_term(self, kk, kg, precision=SGL_FP64):
+        kk = np.ascontiguousarray(np.atleast_1d(kk), np.float64)
+        kg = np.ascontiguousarray(np.atleast_1d(kg), np.float64)
+        re = np.empty((kk.size, kg.size))
+        im = np.empty((kk.size, kg.size))
+        self._check(self._L.sgl_xi_term(self._h, _ptr(kk), kk.size, _ptr(kg), kg.size, int(precision), _ptr(re),
+                                        _ptr(im)), "sgl_xi_term")
+        return re + 1j * im
+
+    def pdf(self, xi_out, precision=SGL_FP64, tail_box=True, phi_tol=1e-8, n_xi_wide=500, n_k_int=2400,
+            xi_reach=24.0):
+        x = np.ascontiguousarray(xi_out, np.float64)
+        out = np.empty(x.size)
+        o = InvertOpts()
+        self._L.sgl_invert_opts_default(C.byref(o))
+        o.precision, o.tail_box, o.phi_tol = int(precision), int(bool(tail_box)), float(phi_tol)
+        o.n_xi_wide, o.n_k_int, o.xi_reach = int(n_xi_wide), int(n_k_int), float(xi_reach)
+        meta = InvertMeta()
+        self._check(self._L.sgl_pdf(self._h, _ptr(x), x.size, C.byref(o), _ptr(out), C.byref(meta)), "sgl_pdf")
+        return out, meta.as_dict()

@@ -1,0 +1,1250 @@
+// Host runtime and C ABI: context, device arena, per-population plans, and the per-PDF pipeline
+// (grid plan -> reach probes -> ln Phi -> exp -> transforms -> path integral -> moments).
+// Mirrors the control flow of the reference's Lam (sgl_full.py:2711-3452) and invert
+// (sgl_full.py:159-375) for the default gauss chain.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "kernels.cuh"
+
+using namespace sgl;
+
+namespace {
+
+// ------------------------------------------------------------------ constants (reference)
+constexpr double kSepTheta = 0.5;          // sgl_full.py:3036
+constexpr int kSepMg = 8;
+constexpr int kSepSmax = 64;
+constexpr long long kSepMinPoints = 200000;  // sgl_full.py:3038
+constexpr int kXiCoarse = 101;             // Lam(xi_coarse=101)
+// sgl.py:1176-1193 and sgl_full.py:33-60
+constexpr double kSigReach = 12.0, kPppK = 18.0, kPppG = 96.0, kBoxReach = 6.0;
+constexpr double kPtsPerSigKap = 72.0, kPtsPerSigGam = 36.0;
+constexpr double kTailKapMax = 0.99, kTailGamMax = 0.8, kTailPppG = 12.0;
+constexpr double kInvertBlockPts = 20000000.0, kOutGridMax = 3.4e7;
+
+thread_local std::string g_create_error;
+
+struct Arena {                         // grow-only named device buffers
+    std::unordered_map<std::string, std::pair<void*, size_t>> bufs;
+    void* get(const std::string& name, size_t bytes) {
+        auto it = bufs.find(name);
+        if (bytes == 0) bytes = 16;
+        if (it != bufs.end() && it->second.second >= bytes) return it->second.first;
+        if (it != bufs.end()) { cudaFree(it->second.first); bufs.erase(it); }
+        void* p = nullptr;
+        if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+        bufs[name] = {p, bytes};
+        return p;
+    }
+    void* find(const std::string& name) const {
+        auto it = bufs.find(name);
+        return it == bufs.end() ? nullptr : it->second.first;
+    }
+    void release() { for (auto& kv : bufs) cudaFree(kv.second.first); bufs.clear(); }
+};
+
+struct SepHost {
+    double key = -1.0;
+    int n_cells = 0, n_groups = 0, n_cols = 0, n_cols_sep = 0, n_direct = 0;
+    std::vector<int> chunk_begin;
+    double max_sep_node = 0.0;
+};
+
+struct XiHost {
+    bool on = false;
+    int n_groups = 0, n_kmc = 0, n_gmc = 0, total_p = 0;
+    std::vector<int> m, r, nP;
+    std::vector<long long> p_prefix_rowel;   // p_prefix (n_groups+1) then rowel_off (n_groups)
+    std::vector<double> kmc, gmc;
+    // sigma contribution: sum over m=0 rows of (rows . kc + res)^2
+    double sigma_var = 0.0;
+    int R0 = 0, Rm[3] = {0, 0, 0};
+};
+
+struct SplineHost {
+    int n = 0;
+    std::vector<double> knots, minv;
+};
+
+struct StatRow { long long launches = 0; double ms = 0, flops = 0, bytes = 0; };
+struct Pending { std::string tag; cudaEvent_t a, b; double flops, bytes; };
+
+}  // namespace
+
+struct sgl_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    Arena arena;
+    // population (host copies)
+    std::vector<double> w0, k0, g0, fe_g;
+    std::vector<int> ig;
+    double V = 0.0;
+    bool has_cells = false;
+    SepHost sep;
+    SepDevice sepd;
+    int sep_precision_ready = -1;
+    XiHost xi;
+    XiDevice xid;
+    SplineHost spline;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // per-kernel statistics (sgl_ctx_profile)
+    bool profiling = false;
+    long long launches_at_enable = 0;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<Pending> pending;
+    std::unordered_map<std::string, StatRow> stats;
+};
+
+namespace {
+
+// ------------------------------------------------------------------ error helpers
+sgl_status fail(sgl_ctx* c, sgl_status s, const std::string& msg) {
+    if (c) c->err = msg;
+    return s;
+}
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(ctx, SGL_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define CKLAUNCH()                                                                            \
+    do {                                                                                      \
+        cudaError_t e_ = cudaGetLastError();                                                  \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(ctx, SGL_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e_));   \
+    } while (0)
+
+#define CKS(expr)                                                                             \
+    do {                                                                                      \
+        sgl_status s_ = (expr);                                                               \
+        if (s_ != SGL_OK) return s_;                                                          \
+    } while (0)
+
+template <typename T>
+T* dbuf(sgl_ctx* ctx, const std::string& name, size_t count) {
+    return (T*)ctx->arena.get(name, count * sizeof(T));
+}
+
+#define DBUF(var, T, name, count)                                                             \
+    T* var = dbuf<T>(ctx, name, (size_t)(count));                                             \
+    if (!var) return fail(ctx, SGL_ERR_CUDA, std::string("device allocation failed: ") + name)
+
+template <typename T>
+sgl_status upload(sgl_ctx* ctx, T* dst, const T* src, size_t n) {
+    if (n == 0) return SGL_OK;
+    CK(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    return SGL_OK;
+}
+
+// numpy.linspace: a + i * step (separately rounded), last point = b exactly
+std::vector<double> linspace(double a, double b, long long n) {
+    std::vector<double> v((size_t)n);
+    if (n == 1) { v[0] = a; return v; }
+    const double step = (b - a) / (double)(n - 1);
+    for (long long i = 0; i < n; ++i) { volatile double t = (double)i * step; v[(size_t)i] = t + a; }
+    v[(size_t)n - 1] = b;
+    return v;
+}
+
+size_t elem_size(int precision) { return precision == SGL_FP64 ? sizeof(double) : sizeof(float); }
+
+// Scoped device timer of one tagged launch (only when profiling is on).
+struct Timed {
+    sgl_ctx* c; std::string tag; double flops, bytes; cudaEvent_t a = nullptr, b = nullptr;
+    Timed(sgl_ctx* c_, std::string t, double f, double by) : c(c_), tag(std::move(t)), flops(f), bytes(by) {
+        if (!c->profiling) return;
+        a = take(); b = take();
+        cudaEventRecord(a, c->stream);
+    }
+    cudaEvent_t take() {
+        if (c->ev_pool.empty()) { cudaEvent_t e; cudaEventCreate(&e); return e; }
+        cudaEvent_t e = c->ev_pool.back(); c->ev_pool.pop_back(); return e;
+    }
+    ~Timed() {
+        if (!c->profiling) return;
+        cudaEventRecord(b, c->stream);
+        c->pending.push_back(Pending{tag, a, b, flops, bytes});
+    }
+};
+
+void resolve_stats(sgl_ctx* c) {
+    if (c->pending.empty()) return;
+    cudaStreamSynchronize(c->stream);
+    for (auto& p : c->pending) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p.a, p.b);
+        StatRow& r = c->stats[p.tag];
+        r.launches += 1; r.ms += ms; r.flops += p.flops; r.bytes += p.bytes;
+        c->ev_pool.push_back(p.a); c->ev_pool.push_back(p.b);
+    }
+    c->pending.clear();
+}
+
+// ------------------------------------------------------------------ GEMM dispatch
+template <typename T>
+sgl_status run_gemms(sgl_ctx* ctx, std::vector<GemmDesc<T>>& d, const std::string& tag) {
+    if (d.empty()) return SGL_OK;
+    const int tiles = gemm_plan(d.data(), (int)d.size());
+    DBUF(dd, GemmDesc<T>, "gemm_desc_" + tag, d.size());
+    CKS(upload(ctx, dd, d.data(), d.size()));
+    double fl = 0.0;
+    for (auto& g : d) fl += 2.0 * g.M * (double)g.N * g.K;
+    {
+        Timed t(ctx, std::string(sizeof(T) == 8 ? "gemm_f64_" : "gemm_f32_") + tag, fl, 0.0);
+        launch_grouped_gemm<T>(dd, (int)d.size(), tiles, ctx->stream);
+    }
+    CKLAUNCH();
+    return SGL_OK;
+}
+
+template <typename T>
+GemmDesc<T> gd(int M, int N, int K, const void* A, long long ars, long long acs, const void* B, long long brs,
+               long long bcs, void* C, long long ldc, double alpha = 1.0, double beta = 0.0) {
+    GemmDesc<T> g{};
+    g.M = M; g.N = N; g.K = K;
+    g.A = (const T*)A; g.a_rs = ars; g.a_cs = acs;
+    g.B = (const T*)B; g.b_rs = brs; g.b_cs = bcs;
+    g.C = (T*)C; g.ldc = ldc;
+    g.alpha = (T)alpha; g.beta = (T)beta;
+    return g;
+}
+
+// One GEMM with split-K when it would under-fill the GPU: K slices write workspace slices,
+// then a fixed-order sum (deterministic).
+template <typename T>
+sgl_status gemm_splitk(sgl_ctx* ctx, GemmDesc<T> g, const std::string& tag) {
+    GemmDesc<T> tmp = g;
+    const int tiles = gemm_plan(&tmp, 1);
+    int split = 1;
+    if (tiles < 2 * kNumSMs) split = std::min(ceil_div(2 * kNumSMs, tiles), std::max(1, g.K / 512));
+    if (split <= 1) { std::vector<GemmDesc<T>> v{g}; return run_gemms(ctx, v, tag); }
+    const long long slice = (long long)g.M * g.N;
+    DBUF(ws, T, "splitk_ws_" + tag, slice * split);
+    std::vector<GemmDesc<T>> v;
+    const int kc = ceil_div(g.K, split);
+    for (int s = 0; s < split; ++s) {
+        const int k0 = s * kc, k1 = std::min(g.K, k0 + kc);
+        if (k1 <= k0) continue;
+        GemmDesc<T> p = g;
+        p.K = k1 - k0;
+        p.A = g.A + (long long)k0 * g.a_cs;
+        p.B = g.B + (long long)k0 * g.b_rs;
+        p.C = ws + (long long)v.size() * slice;
+        p.ldc = g.N;
+        p.beta = T(0);
+        v.push_back(p);
+    }
+    CKS(run_gemms(ctx, v, tag));
+    launch_sum_slices<T>(ws, (int)v.size(), g.M, g.N, g.C, g.ldc, g.beta, ctx->stream);
+    CKLAUNCH();
+    return SGL_OK;
+}
+
+// ------------------------------------------------------------------ separable plan
+// Restates _sep_gamma_nodes (sgl_full.py:2631-2661) for kg_max = key.
+sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
+    if (ctx->sep.key == key && ctx->sep_precision_ready >= 0) return SGL_OK;
+    const long long N = (long long)ctx->w0.size();
+    const double* fe = ctx->fe_g.data();
+    double t[kSepMg];
+    for (int a = 0; a < kSepMg; ++a) {
+        const int b = kSepMg - 1 - a;
+        t[a] = std::cos((double)(2 * b + 1) * M_PI / (double)(2 * kSepMg));
+    }
+    std::vector<long long> keyv((size_t)N);
+    std::vector<double> sl((size_t)N), sh((size_t)N);
+    std::vector<char> direct((size_t)N, 0);
+    for (long long c = 0; c < N; ++c) {
+        const int b = ctx->ig[(size_t)c];
+        const double lo = fe[b], hi = fe[b + 1], wd = hi - lo;
+        double nsd = std::ceil(key * wd / (2.0 * kSepTheta));
+        long long ns = std::max(1LL, (long long)nsd);
+        if (ns > kSepSmax) { direct[(size_t)c] = 1; keyv[(size_t)c] = -1; continue; }
+        long long j = (long long)((ctx->g0[(size_t)c] - lo) / wd * (double)ns);
+        j = std::min(j, ns - 1);
+        sl[(size_t)c] = lo + (double)j * wd / (double)ns;
+        sh[(size_t)c] = lo + (double)(j + 1) * wd / (double)ns;
+        keyv[(size_t)c] = (long long)b * (kSepSmax + 1) + j;
+    }
+    // order: sep cells by (bin, sub-bin) (stable), then direct cells in original order
+    std::vector<long long> order;
+    order.reserve((size_t)N);
+    for (long long c = 0; c < N; ++c) if (!direct[(size_t)c]) order.push_back(c);
+    std::stable_sort(order.begin(), order.end(), [&](long long a, long long b) { return keyv[(size_t)a] < keyv[(size_t)b]; });
+    const long long n_sep = (long long)order.size();
+    for (long long c = 0; c < N; ++c) if (direct[(size_t)c]) order.push_back(c);
+    const long long n_dir = N - n_sep;
+
+    std::vector<double> kap((size_t)N), w((size_t)N), wl((size_t)N * 8, 0.0), nodes;
+    std::vector<float> kh((size_t)N), kl((size_t)N), wf((size_t)N), wlf((size_t)N * 8, 0.f);
+    std::vector<int> grp((size_t)N), gcol0, gncol;
+    int ng = -1;
+    long long prev = -2;
+    double maxnode = 0.0;
+    for (long long i = 0; i < n_sep; ++i) {
+        const long long c = order[(size_t)i];
+        if (keyv[(size_t)c] != prev) {
+            ++ng; prev = keyv[(size_t)c];
+            gcol0.push_back(ng * kSepMg); gncol.push_back(kSepMg);
+            const double lo_s = sl[(size_t)c], hi_s = sh[(size_t)c];
+            for (int a = 0; a < kSepMg; ++a) {
+                const double v = 0.5 * (lo_s + hi_s) + (0.5 * (hi_s - lo_s)) * t[a];
+                nodes.push_back(v);
+                maxnode = std::max(maxnode, v);
+            }
+        }
+        grp[(size_t)i] = ng;
+        const double lo_s = sl[(size_t)c], hi_s = sh[(size_t)c];
+        const double u = ((2.0 * ctx->g0[(size_t)c] - lo_s) - hi_s) / (hi_s - lo_s);
+        for (int a = 0; a < kSepMg; ++a) {
+            double L = 1.0;
+            for (int b2 = 0; b2 < kSepMg; ++b2)
+                if (b2 != a) L = L * ((u - t[b2]) / (t[a] - t[b2]));
+            wl[(size_t)i * 8 + a] = ctx->w0[(size_t)c] * L;
+        }
+    }
+    const int n_sep_groups = ng + 1;
+    const int n_cols_sep = n_sep_groups * kSepMg;
+    for (long long i = n_sep; i < N; ++i) {
+        const long long c = order[(size_t)i];
+        ++ng;
+        gcol0.push_back(n_cols_sep + (int)(i - n_sep));
+        gncol.push_back(1);
+        grp[(size_t)i] = ng;
+        wl[(size_t)i * 8] = ctx->w0[(size_t)c];
+        nodes.push_back(ctx->g0[(size_t)c]);
+    }
+    const int n_groups = ng + 1;
+    for (long long i = 0; i < N; ++i) {
+        const long long c = order[(size_t)i];
+        kap[(size_t)i] = ctx->k0[(size_t)c];
+        w[(size_t)i] = ctx->w0[(size_t)c];
+        const ff f = ff_from_double(kap[(size_t)i]);
+        kh[(size_t)i] = f.hi; kl[(size_t)i] = f.lo;
+        wf[(size_t)i] = (float)w[(size_t)i];
+        for (int a = 0; a < 8; ++a) wlf[(size_t)i * 8 + a] = (float)wl[(size_t)i * 8 + a];
+    }
+    // chunks of whole groups: ~4 CTAs per SM over (row tiles x chunks)
+    const int row_tiles = std::max(1, ceil_div(nk, 128));
+    int nchunks = std::max(1, std::min(n_groups, ceil_div(4 * kNumSMs, row_tiles)));
+    const long long target = std::max(1LL, (N + nchunks - 1) / nchunks);
+    std::vector<int> cb{0};
+    long long acc = 0;
+    for (long long i = 0; i < N; ++i) {
+        if (i > 0 && grp[(size_t)i] != grp[(size_t)i - 1] && acc >= target) { cb.push_back((int)i); acc = 0; }
+        ++acc;
+    }
+    cb.push_back((int)N);
+
+    SepHost& S = ctx->sep;
+    S.key = key; S.n_cells = (int)N; S.n_groups = n_groups; S.n_cols_sep = n_cols_sep;
+    S.n_cols = n_cols_sep + (int)n_dir; S.n_direct = (int)n_dir; S.chunk_begin = cb; S.max_sep_node = maxnode;
+
+    DBUF(d_kap, double, "sep_kap", N);
+    DBUF(d_w, double, "sep_w", N);
+    DBUF(d_wl, double, "sep_wl", N * 8);
+    DBUF(d_kh, float, "sep_kh", N);
+    DBUF(d_kl, float, "sep_kl", N);
+    DBUF(d_wf, float, "sep_wf", N);
+    DBUF(d_wlf, float, "sep_wlf", N * 8);
+    DBUF(d_grp, int, "sep_grp", N);
+    DBUF(d_gc0, int, "sep_gcol0", n_groups);
+    DBUF(d_gnc, int, "sep_gncol", n_groups);
+    DBUF(d_cb, int, "sep_chunks", cb.size());
+    DBUF(d_nodes, double, "sep_nodes", nodes.size());
+    CKS(upload(ctx, d_kap, kap.data(), kap.size()));
+    CKS(upload(ctx, d_w, w.data(), w.size()));
+    CKS(upload(ctx, d_wl, wl.data(), wl.size()));
+    CKS(upload(ctx, d_kh, kh.data(), kh.size()));
+    CKS(upload(ctx, d_kl, kl.data(), kl.size()));
+    CKS(upload(ctx, d_wf, wf.data(), wf.size()));
+    CKS(upload(ctx, d_wlf, wlf.data(), wlf.size()));
+    CKS(upload(ctx, d_grp, grp.data(), grp.size()));
+    CKS(upload(ctx, d_gc0, gcol0.data(), gcol0.size()));
+    CKS(upload(ctx, d_gnc, gncol.data(), gncol.size()));
+    CKS(upload(ctx, d_cb, cb.data(), cb.size()));
+    CKS(upload(ctx, d_nodes, nodes.data(), nodes.size()));
+    CK(cudaStreamSynchronize(ctx->stream));   // host staging vectors go out of scope
+    SepDevice& D = ctx->sepd;
+    D.n_cells = (int)N; D.n_groups = n_groups; D.n_cols = S.n_cols; D.n_cols_sep = n_cols_sep;
+    D.nchunks = (int)cb.size() - 1;
+    D.kap = d_kap; D.w = d_w; D.wl = d_wl; D.kap_hi = d_kh; D.kap_lo = d_kl; D.w_f = d_wf; D.wl_f = d_wlf;
+    D.grp = d_grp; D.gcol0 = d_gc0; D.gncol = d_gnc; D.chunk_begin = d_cb;
+    ctx->sep_precision_ready = 1;
+    return SGL_OK;
+}
+
+// ------------------------------------------------------------------ spline (not-a-knot)
+// Cubic B-spline basis at s for knots t (ncoef coefficients): interval l and 4 values.
+void bspline_basis_host(const std::vector<double>& t, int ncoef, double s, int& l0, double N[4]) {
+    int lo = 3, hi = ncoef - 1;
+    while (lo < hi) { const int mid = (lo + hi + 1) >> 1; if (t[(size_t)mid] <= s) lo = mid; else hi = mid - 1; }
+    const int l = lo;
+    double left[4], right[4];
+    N[0] = 1.0;
+    for (int j = 1; j <= 3; ++j) {
+        left[j] = s - t[(size_t)(l + 1 - j)];
+        right[j] = t[(size_t)(l + j)] - s;
+        double saved = 0.0;
+        for (int r = 0; r < j; ++r) {
+            const double temp = N[r] / (right[r + 1] + left[j - r]);
+            N[r] = saved + right[r + 1] * temp;
+            saved = left[j - r] * temp;
+        }
+        N[j] = saved;
+    }
+    l0 = l - 3;
+}
+
+// Knots of the not-a-knot cubic interpolant on s = linspace(0, 1, n) and the inverse of its
+// collocation matrix (coefficients = Minv @ values), as make_interp_spline(s, y, k=3) builds.
+bool spline_setup(SplineHost& S, int n) {
+    if (S.n == n) return true;
+    const std::vector<double> s = linspace(0.0, 1.0, n);
+    std::vector<double> t;
+    for (int i = 0; i < 4; ++i) t.push_back(s[0]);
+    for (int i = 2; i < n - 2; ++i) t.push_back(s[(size_t)i]);
+    for (int i = 0; i < 4; ++i) t.push_back(s[(size_t)n - 1]);
+    std::vector<double> A((size_t)n * n, 0.0), I((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        int l0; double N[4];
+        bspline_basis_host(t, n, s[(size_t)i], l0, N);
+        for (int a = 0; a < 4; ++a) A[(size_t)i * n + l0 + a] = N[a];
+        I[(size_t)i * n + i] = 1.0;
+    }
+    // Gauss-Jordan with partial pivoting
+    for (int col = 0; col < n; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < n; ++r) if (std::fabs(A[(size_t)r * n + col]) > std::fabs(A[(size_t)piv * n + col])) piv = r;
+        if (A[(size_t)piv * n + col] == 0.0) return false;
+        if (piv != col)
+            for (int k = 0; k < n; ++k) { std::swap(A[(size_t)piv * n + k], A[(size_t)col * n + k]); std::swap(I[(size_t)piv * n + k], I[(size_t)col * n + k]); }
+        const double d = A[(size_t)col * n + col];
+        for (int k = 0; k < n; ++k) { A[(size_t)col * n + k] /= d; I[(size_t)col * n + k] /= d; }
+        for (int r = 0; r < n; ++r) {
+            if (r == col) continue;
+            const double f = A[(size_t)r * n + col];
+            if (f == 0.0) continue;
+            for (int k = 0; k < n; ++k) { A[(size_t)r * n + k] -= f * A[(size_t)col * n + k]; I[(size_t)r * n + k] -= f * I[(size_t)col * n + k]; }
+        }
+    }
+    S.n = n; S.knots = t; S.minv = I;
+    return true;
+}
+
+// ------------------------------------------------------------------ xi_lin term on a grid
+// Exact Psi_2 on kk x kg (device in/out, double planes).  1-D fast paths for the probes.
+sgl_status xi_eval(sgl_ctx* ctx, int precision, const double* d_kk, const double* h_kk, int nk, const double* d_kg,
+                   const double* h_kg, int nkg, double* d_re, double* d_im) {
+    XiHost& X = ctx->xi;
+    const cudaStream_t st = ctx->stream;
+    if (nkg == 1 && h_kg[0] == 0.0 && X.R0 > 0) {
+        launch_xi_line_k(ctx->xid, d_kk, nk, d_re, d_im, st); CKLAUNCH(); return SGL_OK;
+    }
+    if (nk == 1 && h_kk[0] == 0.0 && (X.Rm[0] + X.Rm[1] + X.Rm[2]) > 0) {
+        launch_xi_line_g(ctx->xid, d_kg, nkg, d_re, d_im, st); CKLAUNCH(); return SGL_OK;
+    }
+    const size_t es = elem_size(precision);
+    // offsets
+    std::vector<long long> T_off(X.n_groups), E_off(X.n_groups), G_off(X.n_groups);
+    long long tT = 0, tE = 0, tG = 0;
+    for (int g = 0; g < X.n_groups; ++g) {
+        T_off[g] = tT; E_off[g] = tE; G_off[g] = tG;
+        tT += (long long)X.nP[g] * X.r[g] * nkg;
+        tE += 2LL * nk * X.nP[g];
+        tG += 2LL * nk * X.r[g] * nkg;
+    }
+    DBUF(d_off, long long, "xi_off", 3 * X.n_groups);
+    CKS(upload(ctx, d_off, T_off.data(), X.n_groups));
+    CKS(upload(ctx, d_off + X.n_groups, E_off.data(), X.n_groups));
+    CKS(upload(ctx, d_off + 2 * X.n_groups, G_off.data(), X.n_groups));
+    void* J = ctx->arena.get("xi_J", 3ULL * X.n_gmc * nkg * es);
+    void* T = ctx->arena.get("xi_T", (size_t)tT * es);
+    void* E = ctx->arena.get("xi_E", (size_t)tE * es);
+    void* G = ctx->arena.get("xi_G", (size_t)tG * es);
+    if (!J || !T || !E || !G) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (xi)");
+    const long long* d_pp = (const long long*)ctx->arena.find("xi_pprefix");
+    launch_bessel_tables(precision, ctx->xid.gmc, X.n_gmc, d_kg, nkg, J, st); CKLAUNCH();
+    {
+        Timed t(ctx, "xi_stageA", 0.0, (double)tT * es);
+        launch_xi_stageA(precision, ctx->xid, d_pp, X.total_p, d_off, J, nkg, T, st);
+    }
+    CKLAUNCH();
+    launch_xi_E(precision, ctx->xid, d_kk, nk, d_off + X.n_groups, d_pp, X.total_p, E, st); CKLAUNCH();
+    if (precision == SGL_FP64) {
+        std::vector<GemmDesc<double>> v;
+        for (int g = 0; g < X.n_groups; ++g) {
+            const int N = X.r[g] * nkg;
+            v.push_back(gd<double>(2 * nk, N, X.nP[g], (const double*)E + E_off[g], X.nP[g], 1,
+                                   (const double*)T + T_off[g], N, 1, (double*)G + G_off[g], N));
+        }
+        CKS(run_gemms(ctx, v, "xi"));
+    } else {
+        std::vector<GemmDesc<float>> v;
+        for (int g = 0; g < X.n_groups; ++g) {
+            const int N = X.r[g] * nkg;
+            v.push_back(gd<float>(2 * nk, N, X.nP[g], (const float*)E + E_off[g], X.nP[g], 1,
+                                  (const float*)T + T_off[g], N, 1, (float*)G + G_off[g], N));
+        }
+        CKS(run_gemms(ctx, v, "xi"));
+    }
+    {
+        Timed t(ctx, "xi_square", 0.0, (double)tG * es);
+        launch_xi_square(precision, ctx->xid, d_off + 2 * X.n_groups, G, d_kk, nk, d_kg, nkg, d_re, d_im, st);
+    }
+    CKLAUNCH();
+    return SGL_OK;
+}
+
+// ------------------------------------------------------------------ Lambda on a grid
+// Separable Psi_1 GEMM stage: writes the (2nk x nkg) plane pair of TT into Gout.
+template <typename TT>
+sgl_status sep_gemms(sgl_ctx* ctx, int precision, const double* h_kg, const double* d_kg, int nk, int nkg,
+                     void* Tt, void* Gout) {
+    SepHost& S = ctx->sep;
+    const cudaStream_t st = ctx->stream;
+    const double Kg = nkg ? h_kg[nkg - 1] : 0.0;
+    const int Nch = (S.n_cols_sep > 0 && Kg > 0) ? (int)(0.65 * S.max_sep_node * Kg + 50.0) : 0;
+    const long long ld = 2LL * nk;
+    const double* d_nodes = (const double*)ctx->arena.find("sep_nodes");
+    if (S.n_cols_sep > 0) {
+        if (nkg > 1 && Nch > 0 && Nch < 0.6 * nkg && h_kg[0] >= 0.0) {
+            DBUF(d_t, double, "cheb_t", Nch);
+            launch_cheb_points(Kg, Nch, d_t, st); CKLAUNCH();
+            void* Bc = ctx->arena.get("cheb_B", (size_t)S.n_cols_sep * Nch * sizeof(TT));
+            void* L = ctx->arena.get("cheb_L", (size_t)nkg * Nch * sizeof(TT));
+            void* U = ctx->arena.get("cheb_U", (size_t)ld * Nch * sizeof(TT));
+            if (!Bc || !L || !U) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (cheb)");
+            launch_j0m1_table(precision, d_nodes, S.n_cols_sep, d_t, Nch, Bc, st); CKLAUNCH();
+            launch_cheb_matrix(precision, Kg, Nch, d_kg, nkg, L, st); CKLAUNCH();
+            CKS(gemm_splitk<TT>(ctx, gd<TT>((int)ld, Nch, S.n_cols_sep, Tt, 1, ld, Bc, Nch, 1, U, Nch), "sep1"));
+            CKS(gemm_splitk<TT>(ctx, gd<TT>((int)ld, nkg, Nch, U, Nch, 1, L, 1, Nch, Gout, nkg), "sep2"));
+        } else {
+            void* Bn = ctx->arena.get("sep_Bn", (size_t)S.n_cols_sep * nkg * sizeof(TT));
+            if (!Bn) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (Bn)");
+            launch_j0m1_table(precision, d_nodes, S.n_cols_sep, d_kg, nkg, Bn, st); CKLAUNCH();
+            CKS(gemm_splitk<TT>(ctx, gd<TT>((int)ld, nkg, S.n_cols_sep, Tt, 1, ld, Bn, nkg, 1, Gout, nkg), "sep1"));
+        }
+    } else {
+        CK(cudaMemsetAsync(Gout, 0, (size_t)ld * nkg * sizeof(TT), st));
+    }
+    if (S.n_direct > 0) {
+        void* Bd = ctx->arena.get("sep_Bd", (size_t)S.n_direct * nkg * sizeof(TT));
+        if (!Bd) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (Bd)");
+        launch_j0m1_table(precision, d_nodes + S.n_cols_sep, S.n_direct, d_kg, nkg, Bd, st); CKLAUNCH();
+        const TT* Td = (const TT*)Tt + (long long)S.n_cols_sep * ld;
+        CKS(gemm_splitk<TT>(ctx, gd<TT>((int)ld, nkg, S.n_direct, Td, 1, ld, Bd, nkg, 1, Gout, nkg, 1.0, 1.0), "sep3"));
+    }
+    return SGL_OK;
+}
+
+// ln Phi on kk x kg into device planes (Lam._direct_call, sgl_full.py:3088-3131):
+//   Psi_1: separable for >= 200000 points and nkg > 1, dense direct sums otherwise;
+//   -1/2 k^2 V;
+//   xi term: 101^2 coarse grid + not-a-knot bicubic spline when the grid has more than 101^2
+//   points (and both axes > 1 point, both maxima > 0), exact otherwise.
+// write_phi = 1 writes Phi = exp(ln Phi) in the precision's element type (inversion path).
+sgl_status lambda_eval(sgl_ctx* ctx, int precision, const double* h_kk, int nk, const double* h_kg, int nkg,
+                       int write_phi, void* out_re, void* out_im) {
+    const cudaStream_t st = ctx->stream;
+    const long long npt = (long long)nk * nkg;
+    DBUF(d_kk, double, "grid_kk", nk);
+    DBUF(d_kg, double, "grid_kg", nkg);
+    CKS(upload(ctx, d_kk, h_kk, nk));
+    CKS(upload(ctx, d_kg, h_kg, nkg));
+    const bool use_sep = npt >= kSepMinPoints && nkg > 1;
+    const int n = kXiCoarse;
+    const bool use_interp = ctx->xi.on && npt > (long long)n * n && nk > 1 && nkg > 1 && h_kk[nk - 1] > 0 &&
+                            h_kg[nkg - 1] > 0;
+    const bool exact_xi = ctx->xi.on && !use_interp;
+    if (exact_xi && write_phi) return fail(ctx, SGL_ERR_UNSUPPORTED, "exact xi term on an inversion grid");
+
+    const void* G = nullptr;
+    const double2* A1 = nullptr;
+    int fin_precision = precision;
+    if (use_sep) {
+        CKS(build_sep(ctx, h_kg[nkg - 1], nk));
+        const size_t es = elem_size(precision);
+        const long long ld = 2LL * nk;
+        void* Tt = ctx->arena.get("sep_T", (size_t)ctx->sep.n_cols * ld * es);
+        DBUF(d_Ap, double2, "sep_Apart", (long long)ctx->sepd.nchunks * nk);
+        DBUF(d_A1, double2, "sep_A1", nk);
+        void* Gout = ctx->arena.get("lam_G", (size_t)ld * nkg * es);
+        if (!Tt || !Gout) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (lambda)");
+        {
+            Timed t(ctx, precision == SGL_FP64 ? "sep_sweep_f64" : "sep_sweep_mixed", (double)nk * ctx->sep.n_cells,
+                    (double)ctx->sep.n_cols * ld * es);
+            launch_sep_sweep(precision, d_kk, nk, ctx->sepd, Tt, d_Ap, d_A1, st);
+        }
+        CKLAUNCH();
+        if (precision == SGL_FP64) CKS(sep_gemms<double>(ctx, precision, h_kg, d_kg, nk, nkg, Tt, Gout));
+        else CKS(sep_gemms<float>(ctx, precision, h_kg, d_kg, nk, nkg, Tt, Gout));
+        G = Gout; A1 = d_A1;
+    } else {
+        DBUF(d_dir, double, "lam_direct", 2 * npt);
+        DBUF(d_zero, double2, "lam_zero", nk);
+        const double* d_k0 = (const double*)ctx->arena.find("cells_k0");
+        const double* d_g0 = (const double*)ctx->arena.find("cells_g0");
+        const double* d_w0 = (const double*)ctx->arena.find("cells_w0");
+        launch_psi1_direct(d_kk, nk, d_kg, nkg, d_k0, d_g0, d_w0, (int64_t)ctx->w0.size(), d_dir, d_dir + npt, st);
+        CKLAUNCH();
+        CK(cudaMemsetAsync(d_zero, 0, (size_t)nk * sizeof(double2), st));
+        G = d_dir; A1 = d_zero; fin_precision = SGL_FP64;
+    }
+
+    const double* Cre = nullptr; const double* Cim = nullptr;
+    SplineAxis sk, sg;
+    int ncg = 0;
+    if (use_interp) {
+        if (!spline_setup(ctx->spline, n)) return fail(ctx, SGL_ERR_VALUE, "singular spline collocation");
+        const std::vector<double> s = linspace(0.0, 1.0, n);
+        std::vector<double> kkc(n), kgc(n);
+        const double kkm = h_kk[nk - 1], kgm = h_kg[nkg - 1];
+        for (int i = 0; i < n; ++i) { kkc[i] = kkm * (s[i] * s[i]); kgc[i] = kgm * (s[i] * s[i]); }
+        DBUF(d_kkc, double, "xi_kkc", n);
+        DBUF(d_kgc, double, "xi_kgc", n);
+        CKS(upload(ctx, d_kkc, kkc.data(), n));
+        CKS(upload(ctx, d_kgc, kgc.data(), n));
+        DBUF(d_Q, double, "xi_Qc", 2 * n * n);
+        CKS(xi_eval(ctx, precision, d_kkc, kkc.data(), n, d_kgc, kgc.data(), n, d_Q, d_Q + n * n));
+        // C = Minv Qc Minv^T for the real and imaginary parts (FP64)
+        DBUF(d_M, double, "spl_minv", n * n);
+        DBUF(d_knots, double, "spl_knots", n + 4);
+        CKS(upload(ctx, d_M, ctx->spline.minv.data(), (size_t)n * n));
+        CKS(upload(ctx, d_knots, ctx->spline.knots.data(), (size_t)n + 4));
+        DBUF(d_tmp, double, "spl_tmp", 2 * n * n);
+        DBUF(d_C, double, "spl_C", 2 * n * n);
+        std::vector<GemmDesc<double>> a{gd<double>(n, n, n, d_M, n, 1, d_Q, n, 1, d_tmp, n),
+                                        gd<double>(n, n, n, d_M, n, 1, d_Q + n * n, n, 1, d_tmp + n * n, n)};
+        CKS(run_gemms(ctx, a, "spl_a"));
+        std::vector<GemmDesc<double>> b{gd<double>(n, n, n, d_tmp, n, 1, d_M, 1, n, d_C, n),
+                                        gd<double>(n, n, n, d_tmp + n * n, n, 1, d_M, 1, n, d_C + n * n, n)};
+        CKS(run_gemms(ctx, b, "spl_b"));
+        DBUF(d_lk, int, "spl_lk", nk);
+        DBUF(d_bk, double, "spl_bk", 4 * nk);
+        DBUF(d_lg, int, "spl_lg", nkg);
+        DBUF(d_bg, double, "spl_bg", 4 * nkg);
+        launch_spline_basis(d_kk, nk, kkm, d_knots, n, d_lk, d_bk, st); CKLAUNCH();
+        launch_spline_basis(d_kg, nkg, kgm, d_knots, n, d_lg, d_bg, st); CKLAUNCH();
+        sk.l = d_lk; sk.b = d_bk; sg.l = d_lg; sg.b = d_bg;
+        Cre = d_C; Cim = d_C + n * n; ncg = n;
+    }
+    if (write_phi && fin_precision != precision) return fail(ctx, SGL_ERR_UNSUPPORTED, "inversion grid below 2e5 points");
+    {
+        Timed t(ctx, "finalize", 0.0, (double)npt * 2 * (elem_size(fin_precision) + (write_phi ? elem_size(precision) : 8)));
+        launch_finalize(fin_precision, write_phi, G, nk, nkg, A1, d_kk, ctx->V, Cre, Cim, ncg, sk, sg, out_re, out_im,
+                        nkg, st);
+    }
+    CKLAUNCH();
+    if (exact_xi) {
+        DBUF(d_qr, double, "xi_full", 2 * npt);
+        CKS(xi_eval(ctx, precision, d_kk, h_kk, nk, d_kg, h_kg, nkg, d_qr, d_qr + npt));
+        launch_sum_slices<double>(d_qr, 1, nk, nkg, (double*)out_re, nkg, 1.0, st); CKLAUNCH();
+        launch_sum_slices<double>(d_qr + npt, 1, nk, nkg, (double*)out_im, nkg, 1.0, st); CKLAUNCH();
+    }
+    return SGL_OK;
+}
+
+// Direct evaluation on a small grid into HOST planes (Lam._direct_call for < 200000 points).
+sgl_status lambda_direct(sgl_ctx* ctx, const double* h_kk, int nk, const double* h_kg, int nkg, double* re,
+                         double* im) {
+    const cudaStream_t st = ctx->stream;
+    const long long npt = (long long)nk * nkg;
+    DBUF(d_kk, double, "dir_kk", nk);
+    DBUF(d_kg, double, "dir_kg", nkg);
+    DBUF(d_out, double, "dir_out", 4 * npt);
+    CKS(upload(ctx, d_kk, h_kk, nk));
+    CKS(upload(ctx, d_kg, h_kg, nkg));
+    const double* d_k0 = (const double*)ctx->arena.find("cells_k0");
+    const double* d_g0 = (const double*)ctx->arena.find("cells_g0");
+    const double* d_w0 = (const double*)ctx->arena.find("cells_w0");
+    launch_psi1_direct(d_kk, nk, d_kg, nkg, d_k0, d_g0, d_w0, (int64_t)ctx->w0.size(), d_out, d_out + npt, st);
+    CKLAUNCH();
+    bool xi = false;
+    if (ctx->xi.on) {
+        CKS(xi_eval(ctx, SGL_FP64, d_kk, h_kk, nk, d_kg, h_kg, nkg, d_out + 2 * npt, d_out + 3 * npt));
+        xi = true;
+    }
+    std::vector<double> h((size_t)(4 * npt));
+    CK(cudaMemcpyAsync(h.data(), d_out, (size_t)(xi ? 4 : 2) * npt * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (long long e = 0; e < npt; ++e) {
+        const int n = (int)(e / nkg);
+        double r = h[(size_t)e] - 0.5 * (h_kk[n] * h_kk[n] * ctx->V);
+        double i = h[(size_t)(npt + e)];
+        if (xi) { r += h[(size_t)(2 * npt + e)]; i += h[(size_t)(3 * npt + e)]; }
+        re[e] = r; im[e] = i;
+    }
+    return SGL_OK;
+}
+
+double trapz(const double* y, const double* x, int n) {
+    double s = 0.0;
+    for (int i = 0; i + 1 < n; ++i) s += (x[i + 1] - x[i]) * (y[i + 1] + y[i]) / 2.0;
+    return s;
+}
+
+}  // namespace
+
+// ================================================================== C ABI
+extern "C" {
+
+int sgl_abi_version(void) { return SGL_ABI_VERSION; }
+
+sgl_status sgl_ctx_create(int device, sgl_ctx** out) {
+    if (!out) { g_create_error = "out is NULL"; return SGL_ERR_VALUE; }
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        g_create_error = std::string("no CUDA device: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "count 0");
+        return SGL_ERR_CUDA;
+    }
+    if (device < 0 || device >= n) { g_create_error = "device index out of range"; return SGL_ERR_VALUE; }
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) { g_create_error = cudaGetErrorString(e); return SGL_ERR_CUDA; }
+    sgl_ctx* ctx = new sgl_ctx();
+    ctx->device = device;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        g_create_error = "stream creation failed"; delete ctx; return SGL_ERR_CUDA;
+    }
+    for (auto& ev : ctx->ev) cudaEventCreate(&ev);
+    *out = ctx;
+    return SGL_OK;
+}
+
+void sgl_ctx_destroy(sgl_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->arena.release();
+    for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
+    resolve_stats(ctx);
+    for (auto& ev : ctx->ev_pool) cudaEventDestroy(ev);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+int sgl_last_error(const sgl_ctx* ctx, char* buf, int buflen) {
+    const std::string& m = ctx ? ctx->err : g_create_error;
+    if (buf && buflen > 0) {
+        const int n = std::min((int)m.size(), buflen - 1);
+        std::memcpy(buf, m.data(), (size_t)n);
+        buf[n] = 0;
+    }
+    return (int)m.size();
+}
+
+sgl_status sgl_ctx_stream(sgl_ctx* ctx, void** stream) {
+    if (!ctx || !stream) return SGL_ERR_VALUE;
+    *stream = (void*)ctx->stream;
+    return SGL_OK;
+}
+
+sgl_status sgl_ctx_profile(sgl_ctx* ctx, int enable) {
+    if (!ctx) return SGL_ERR_VALUE;
+    resolve_stats(ctx);
+    if (enable && !ctx->profiling) ctx->launches_at_enable = sgl::launch_counter();
+    if (!enable && ctx->profiling) ctx->stats["_launches"].launches += sgl::launch_counter() - ctx->launches_at_enable;
+    ctx->profiling = enable != 0;
+    return SGL_OK;
+}
+
+int sgl_stats_json(sgl_ctx* ctx, char* buf, int buflen, int reset) {
+    if (!ctx) return -1;
+    resolve_stats(ctx);
+    if (ctx->profiling) {
+        ctx->stats["_launches"].launches += sgl::launch_counter() - ctx->launches_at_enable;
+        ctx->launches_at_enable = sgl::launch_counter();
+    }
+    std::string js = "{";
+    bool first = true;
+    char tmp[512];
+    for (auto& kv : ctx->stats) {
+        std::snprintf(tmp, sizeof(tmp), "%s\"%s\": {\"launches\": %lld, \"ms\": %.6f, \"flops\": %.6e, \"bytes\": %.6e}",
+                      first ? "" : ", ", kv.first.c_str(), kv.second.launches, kv.second.ms, kv.second.flops,
+                      kv.second.bytes);
+        js += tmp;
+        first = false;
+    }
+    js += "}";
+    if (buf && buflen > 0) {
+        const int n = std::min((int)js.size(), buflen - 1);
+        std::memcpy(buf, js.data(), (size_t)n);
+        buf[n] = 0;
+    }
+    if (reset) ctx->stats.clear();
+    return (int)js.size();
+}
+
+sgl_status sgl_lam_set_cells(sgl_ctx* ctx, int64_t n_cells, const double* w0, const double* k0, const double* g0,
+                             const int32_t* ig, const double* fe_g, int n_fe_g, double V) {
+    if (!ctx) return SGL_ERR_VALUE;
+    if (n_cells < 0 || (n_cells > 0 && (!w0 || !k0 || !g0 || !ig)) || !fe_g || n_fe_g < 2)
+        return fail(ctx, SGL_ERR_VALUE, "invalid cell arrays");
+    if (!std::isfinite(V)) return fail(ctx, SGL_ERR_VALUE, "V must be finite");
+    for (int64_t c = 0; c < n_cells; ++c) {
+        if (!std::isfinite(w0[c]) || !std::isfinite(k0[c]) || !std::isfinite(g0[c]))
+            return fail(ctx, SGL_ERR_VALUE, "non-finite cell value");
+        if (ig[c] < 0 || ig[c] + 1 >= n_fe_g) return fail(ctx, SGL_ERR_VALUE, "gamma bin index out of range");
+    }
+    CK(cudaSetDevice(ctx->device));
+    ctx->w0.assign(w0, w0 + n_cells);
+    ctx->k0.assign(k0, k0 + n_cells);
+    ctx->g0.assign(g0, g0 + n_cells);
+    ctx->ig.assign(ig, ig + n_cells);
+    ctx->fe_g.assign(fe_g, fe_g + n_fe_g);
+    ctx->V = V;
+    DBUF(dk, double, "cells_k0", n_cells);
+    DBUF(dg, double, "cells_g0", n_cells);
+    DBUF(dw, double, "cells_w0", n_cells);
+    CKS(upload(ctx, dk, k0, (size_t)n_cells));
+    CKS(upload(ctx, dg, g0, (size_t)n_cells));
+    CKS(upload(ctx, dw, w0, (size_t)n_cells));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->sep = SepHost();
+    ctx->sep_precision_ready = -1;
+    ctx->has_cells = true;
+    return SGL_OK;
+}
+
+sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const int32_t* nrow, const int32_t* nidx,
+                          const int32_t* idx, const double* rows, const double* ce_k, int n_ce_k, const double* ce_g,
+                          int n_ce_g, double prune, double s0_override) {
+    if (!ctx) return SGL_ERR_VALUE;
+    if (n_groups < 0 || n_ce_k < 2 || n_ce_g < 2 || !ce_k || !ce_g) return fail(ctx, SGL_ERR_VALUE, "invalid xi arrays");
+    CK(cudaSetDevice(ctx->device));
+    XiHost X;
+    X.n_kmc = n_ce_k - 1; X.n_gmc = n_ce_g - 1;
+    const int ngc = X.n_gmc;
+    // centres: signed-log kappa (sgl_full.py:466-468), geometric gamma
+    for (int i = 0; i < X.n_kmc; ++i) {
+        const double a = ce_k[i], b = ce_k[i + 1];
+        X.kmc.push_back(a * b > 0 ? (b > 0 ? 1.0 : -1.0) * std::sqrt(std::fabs(a * b)) : 0.0);
+    }
+    for (int i = 0; i < X.n_gmc; ++i) X.gmc.push_back(std::sqrt(ce_g[i] * ce_g[i + 1]));
+    // prune (sgl_full.py:2823-2830): rows with norm <= prune * (largest row norm of any group)
+    std::vector<long long> idx_off(n_groups + 1, 0), row_off(n_groups + 1, 0);
+    for (int g = 0; g < n_groups; ++g) {
+        if (nrow[g] < 0 || nidx[g] < 1) return fail(ctx, SGL_ERR_VALUE, "xi group with no rows or no coarse cells");
+        idx_off[g + 1] = idx_off[g] + nidx[g];
+        row_off[g + 1] = row_off[g] + (long long)nrow[g] * (nidx[g] + 1);
+    }
+    std::vector<std::vector<double>> norms(n_groups);
+    double s0 = 0.0;
+    for (int g = 0; g < n_groups; ++g) {
+        const int w = nidx[g] + 1;
+        for (int r = 0; r < nrow[g]; ++r) {
+            double s = 0.0;
+            const double* row = rows + row_off[g] + (long long)r * w;
+            for (int e = 0; e < w; ++e) s += row[e] * row[e];
+            norms[g].push_back(std::sqrt(s));
+            s0 = std::max(s0, std::sqrt(s));
+        }
+    }
+    if (s0_override > 0) s0 = s0_override;
+    // device staging
+    std::vector<int> g_m, g_r, g_nP, idx_p, p_ptr{0}, ent_qg;
+    std::vector<long long> g_p_off, g_ent_off, g_row_off, p_prefix{0}, rowel_off;
+    std::vector<double> rows_t, res, sum_rows;
+    std::vector<double> W0, res0, sum0, U[3], resm[3], summ[3];
+    long long ent_total = 0, row_total = 0, rowel_total = 0;
+    double sigma_var = 0.0;
+    for (int g = 0; g < n_groups; ++g) {
+        const int w = nidx[g] + 1;
+        std::vector<int> keep;
+        for (int r = 0; r < nrow[g]; ++r)
+            if (!(prune > 0) || norms[g][(size_t)r] > prune * s0) keep.push_back(r);
+        if (keep.empty()) continue;
+        const int R = (int)keep.size(), mg = m[g];
+        if (mg < 0 || mg > 2) return fail(ctx, SGL_ERR_UNSUPPORTED, "xi harmonic m must be 0, 1 or 2");
+        const int32_t* id = idx + idx_off[g];
+        std::vector<int> pg(nidx[g]), qg(nidx[g]);
+        for (int e = 0; e < nidx[g]; ++e) {
+            if (id[e] < 0 || id[e] >= X.n_kmc * ngc) return fail(ctx, SGL_ERR_VALUE, "coarse index out of range");
+            pg[e] = id[e] / ngc; qg[e] = id[e] % ngc;
+        }
+        // unique p (sorted) and CSR of entries by p
+        std::vector<int> order(nidx[g]);
+        for (int e = 0; e < nidx[g]; ++e) order[e] = e;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pg[a] < pg[b]; });
+        int nP = 0;
+        for (int i = 0; i < nidx[g]; ++i) {
+            const int e = order[i];
+            if (i == 0 || pg[e] != pg[order[i - 1]]) {
+                if (i > 0) p_ptr.push_back((int)(ent_total + i));
+                idx_p.push_back(pg[e]);
+                ++nP;
+            }
+        }
+        p_ptr.push_back((int)(ent_total + nidx[g]));
+        // entries in p-order: global q index and rows (entry-major, R values each)
+        for (int i = 0; i < nidx[g]; ++i) {
+            const int e = order[i];
+            ent_qg.push_back(qg[e]);
+            for (int rr = 0; rr < R; ++rr) rows_t.push_back(rows[row_off[g] + (long long)keep[rr] * w + e]);
+        }
+        std::vector<double> resg(R), sumg(R);
+        for (int rr = 0; rr < R; ++rr) {
+            const double* row = rows + row_off[g] + (long long)keep[rr] * w;
+            double s = 0.0;
+            for (int e = 0; e < nidx[g]; ++e) s += row[e];
+            resg[rr] = row[nidx[g]];
+            sumg[rr] = s;
+            res.push_back(resg[rr]);
+            sum_rows.push_back(s);
+        }
+        // 1-D reach stacks (sgl_full.py:2846-2861) and the sigma term (sgl_full.py:3441-3447)
+        if (mg == 0) {
+            for (int rr = 0; rr < R; ++rr) {
+                std::vector<double> wrow(X.n_kmc, 0.0);
+                const double* row = rows + row_off[g] + (long long)keep[rr] * w;
+                double dot = 0.0;
+                for (int e = 0; e < nidx[g]; ++e) { wrow[pg[e]] += row[e]; dot += row[e] * X.kmc[pg[e]]; }
+                W0.insert(W0.end(), wrow.begin(), wrow.end());
+                res0.push_back(resg[rr]); sum0.push_back(sumg[rr]);
+                const double v = dot + resg[rr];
+                sigma_var += v * v;
+            }
+            X.R0 += R;
+        }
+        {
+            for (int rr = 0; rr < R; ++rr) {
+                std::vector<double> urow(X.n_gmc, 0.0);
+                const double* row = rows + row_off[g] + (long long)keep[rr] * w;
+                for (int e = 0; e < nidx[g]; ++e) urow[qg[e]] += row[e];
+                U[mg].insert(U[mg].end(), urow.begin(), urow.end());
+                resm[mg].push_back(resg[rr]); summ[mg].push_back(sumg[rr]);
+            }
+            X.Rm[mg] += R;
+        }
+        g_m.push_back(mg); g_r.push_back(R); g_nP.push_back(nP);
+        g_p_off.push_back(p_prefix.back());
+        g_ent_off.push_back(ent_total);
+        g_row_off.push_back(row_total);
+        rowel_off.push_back(rowel_total);
+        p_prefix.push_back(p_prefix.back() + nP);
+        ent_total += nidx[g];
+        row_total += R;
+        rowel_total += (long long)R * nidx[g];
+        X.m.push_back(mg); X.r.push_back(R); X.nP.push_back(nP);
+    }
+    X.n_groups = (int)g_m.size();
+    X.total_p = (int)p_prefix.back();
+    X.sigma_var = sigma_var;
+    X.on = X.n_groups > 0;
+    // upload
+    XiDevice D;
+    D.n_groups = X.n_groups; D.n_kmc = X.n_kmc; D.n_gmc = X.n_gmc;
+    DBUF(d_kmc, double, "xi_kmc", X.n_kmc);
+    DBUF(d_gmc, double, "xi_gmc", X.n_gmc);
+    CKS(upload(ctx, d_kmc, X.kmc.data(), X.kmc.size()));
+    CKS(upload(ctx, d_gmc, X.gmc.data(), X.gmc.size()));
+    D.kmc = d_kmc; D.gmc = d_gmc;
+    if (X.on) {
+        DBUF(d_gm, int, "xi_gm", X.n_groups);
+        DBUF(d_gr, int, "xi_gr", X.n_groups);
+        DBUF(d_gnP, int, "xi_gnP", X.n_groups);
+        DBUF(d_goff, long long, "xi_goff", 3 * X.n_groups);
+        DBUF(d_pp, long long, "xi_pprefix", 2 * X.n_groups + 1);
+        DBUF(d_idxp, int, "xi_idxp", idx_p.size());
+        DBUF(d_pptr, int, "xi_pptr", p_ptr.size());
+        DBUF(d_qg, int, "xi_entq", ent_qg.size());
+        DBUF(d_rows, double, "xi_rows", rows_t.size());
+        DBUF(d_res, double, "xi_res", res.size());
+        DBUF(d_sum, double, "xi_sum", sum_rows.size());
+        std::vector<long long> goff;
+        goff.insert(goff.end(), g_p_off.begin(), g_p_off.end());
+        goff.insert(goff.end(), g_ent_off.begin(), g_ent_off.end());
+        goff.insert(goff.end(), g_row_off.begin(), g_row_off.end());
+        std::vector<long long> pp = p_prefix;      // n_groups + 1
+        pp.insert(pp.end(), rowel_off.begin(), rowel_off.end());
+        CKS(upload(ctx, d_gm, g_m.data(), g_m.size()));
+        CKS(upload(ctx, d_gr, g_r.data(), g_r.size()));
+        CKS(upload(ctx, d_gnP, g_nP.data(), g_nP.size()));
+        CKS(upload(ctx, d_goff, goff.data(), goff.size()));
+        CKS(upload(ctx, d_pp, pp.data(), pp.size()));
+        CKS(upload(ctx, d_idxp, idx_p.data(), idx_p.size()));
+        CKS(upload(ctx, d_pptr, p_ptr.data(), p_ptr.size()));
+        CKS(upload(ctx, d_qg, ent_qg.data(), ent_qg.size()));
+        CKS(upload(ctx, d_rows, rows_t.data(), rows_t.size()));
+        CKS(upload(ctx, d_res, res.data(), res.size()));
+        CKS(upload(ctx, d_sum, sum_rows.data(), sum_rows.size()));
+        D.g_m = d_gm; D.g_r = d_gr; D.g_nP = d_gnP;
+        D.g_p_off = d_goff; D.g_ent_off = d_goff + X.n_groups; D.g_row_off = d_goff + 2 * X.n_groups;
+        D.idx_p = d_idxp; D.p_ptr = d_pptr; D.ent_qg = d_qg; D.rows = d_rows; D.res = d_res; D.sum_rows = d_sum;
+        D.R0 = X.R0;
+        if (X.R0 > 0) {
+            DBUF(d_W0, double, "xi_W0", W0.size());
+            DBUF(d_r0, double, "xi_res0", res0.size());
+            DBUF(d_s0, double, "xi_sum0", sum0.size());
+            CKS(upload(ctx, d_W0, W0.data(), W0.size()));
+            CKS(upload(ctx, d_r0, res0.data(), res0.size()));
+            CKS(upload(ctx, d_s0, sum0.data(), sum0.size()));
+            D.W0 = d_W0; D.res0 = d_r0; D.sum0 = d_s0;
+        }
+        for (int mm = 0; mm < 3; ++mm) {
+            D.Rm[mm] = X.Rm[mm];
+            if (X.Rm[mm] == 0) continue;
+            const std::string sfx = std::to_string(mm);
+            DBUF(d_U, double, "xi_U" + sfx, U[mm].size());
+            DBUF(d_rm, double, "xi_resm" + sfx, resm[mm].size());
+            DBUF(d_sm, double, "xi_summ" + sfx, summ[mm].size());
+            CKS(upload(ctx, d_U, U[mm].data(), U[mm].size()));
+            CKS(upload(ctx, d_rm, resm[mm].data(), resm[mm].size()));
+            CKS(upload(ctx, d_sm, summ[mm].data(), summ[mm].size()));
+            D.U[mm] = d_U; D.resm[mm] = d_rm; D.summ[mm] = d_sm;
+        }
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->xi = X;
+    ctx->xid = D;
+    return SGL_OK;
+}
+
+sgl_status sgl_lam_sigma(sgl_ctx* ctx, double* sigma) {
+    if (!ctx || !sigma) return SGL_ERR_VALUE;
+    if (!ctx->has_cells) return fail(ctx, SGL_ERR_STATE, "cells not set");
+    double v = 0.0;
+    for (size_t c = 0; c < ctx->w0.size(); ++c) v += ctx->w0[c] * ctx->k0[c] * ctx->k0[c];
+    v += ctx->V;
+    if (ctx->xi.on) v += ctx->xi.sigma_var;
+    *sigma = std::sqrt(v);
+    return SGL_OK;
+}
+
+sgl_status sgl_lnphi(sgl_ctx* ctx, const double* kk, int nkk, const double* kg, int nkg, int precision,
+                     double* out_re, double* out_im) {
+    if (!ctx) return SGL_ERR_VALUE;
+    if (!ctx->has_cells) return fail(ctx, SGL_ERR_STATE, "cells not set");
+    if (nkk < 1 || nkg < 1 || !kk || !kg || !out_re || !out_im) return fail(ctx, SGL_ERR_VALUE, "empty grid");
+    if (precision != SGL_FP64 && precision != SGL_MIXED) return fail(ctx, SGL_ERR_VALUE, "unknown precision");
+    for (int i = 0; i < nkk; ++i) if (!std::isfinite(kk[i])) return fail(ctx, SGL_ERR_VALUE, "non-finite kk");
+    for (int i = 0; i < nkg; ++i) if (!std::isfinite(kg[i]) || kg[i] < 0) return fail(ctx, SGL_ERR_VALUE, "kg must be finite, >= 0");
+    CK(cudaSetDevice(ctx->device));
+    const long long npt = (long long)nkk * nkg;
+    DBUF(d_re, double, "lnphi_re", npt);
+    DBUF(d_im, double, "lnphi_im", npt);
+    CKS(lambda_eval(ctx, precision, kk, nkk, kg, nkg, 0, d_re, d_im));
+    CK(cudaMemcpyAsync(out_re, d_re, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(out_im, d_im, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (long long e = 0; e < npt; ++e)
+        if (!std::isfinite(out_re[e]) || !std::isfinite(out_im[e])) return fail(ctx, SGL_ERR_NONFINITE, "non-finite ln Phi");
+    return SGL_OK;
+}
+
+sgl_status sgl_xi_term(sgl_ctx* ctx, const double* kk, int nkk, const double* kg, int nkg, int precision,
+                       double* out_re, double* out_im) {
+    if (!ctx) return SGL_ERR_VALUE;
+    if (!ctx->xi.on) return fail(ctx, SGL_ERR_STATE, "xi groups not set");
+    if (nkk < 1 || nkg < 1 || !kk || !kg || !out_re || !out_im) return fail(ctx, SGL_ERR_VALUE, "empty grid");
+    if (precision != SGL_FP64 && precision != SGL_MIXED) return fail(ctx, SGL_ERR_VALUE, "unknown precision");
+    for (int i = 0; i < nkk; ++i) if (!std::isfinite(kk[i])) return fail(ctx, SGL_ERR_VALUE, "non-finite kk");
+    for (int i = 0; i < nkg; ++i) if (!std::isfinite(kg[i]) || kg[i] < 0) return fail(ctx, SGL_ERR_VALUE, "kg must be finite, >= 0");
+    CK(cudaSetDevice(ctx->device));
+    const long long npt = (long long)nkk * nkg;
+    DBUF(d_kk, double, "xt_kk", nkk);
+    DBUF(d_kg, double, "xt_kg", nkg);
+    DBUF(d_o, double, "xt_out", 2 * npt);
+    CKS(upload(ctx, d_kk, kk, nkk));
+    CKS(upload(ctx, d_kg, kg, nkg));
+    CKS(xi_eval(ctx, precision, d_kk, kk, nkk, d_kg, kg, nkg, d_o, d_o + npt));
+    CK(cudaMemcpyAsync(out_re, d_o, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(out_im, d_o + npt, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SGL_OK;
+}
+
+void sgl_invert_opts_default(sgl_invert_opts* o) {
+    if (!o) return;
+    o->precision = SGL_FP64;
+    o->tail_box = 1;
+    o->phi_tol = 1e-8;
+    o->n_xi_wide = 500;
+    o->n_k_int = 2400;
+    o->xi_reach = 24.0;
+}
+
+sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_invert_opts* opts, double* P_out,
+                   sgl_invert_meta* meta) {
+    if (!ctx) return SGL_ERR_VALUE;
+    if (!ctx->has_cells) return fail(ctx, SGL_ERR_STATE, "cells not set");
+    if (n_xi < 0 || (n_xi > 0 && (!xi_out || !P_out))) return fail(ctx, SGL_ERR_VALUE, "invalid output grid");
+    sgl_invert_opts o;
+    sgl_invert_opts_default(&o);
+    if (opts) o = *opts;
+    if (o.precision != SGL_FP64 && o.precision != SGL_MIXED) return fail(ctx, SGL_ERR_VALUE, "unknown precision");
+    if (o.n_xi_wide < 2 || o.n_k_int < 2 || !(o.phi_tol > 0) || !(o.xi_reach > 0))
+        return fail(ctx, SGL_ERR_VALUE, "invalid inversion options");
+    for (int i = 0; i < n_xi; ++i) if (!std::isfinite(xi_out[i])) return fail(ctx, SGL_ERR_VALUE, "non-finite xi_out");
+    CK(cudaSetDevice(ctx->device));
+    const cudaStream_t st = ctx->stream;
+    double sigma;
+    CKS(sgl_lam_sigma(ctx, &sigma));
+    if (!(sigma > 0) || !std::isfinite(sigma)) return fail(ctx, SGL_ERR_VALUE, "sigma_kappa must be positive");
+    // ---- vector_grid (sgl.py:1229-1258)
+    const double sig_xi = 2.0 * sigma;
+    const double xi_max = o.xi_reach * sig_xi, xi_min = -kBoxReach * sig_xi;
+    double kap_max = 1.0 - std::exp(-0.5 * xi_max);
+    const double kap_min = -kBoxReach * sigma;
+    double gam_max = kBoxReach * sigma;
+    const double g0 = gam_max;
+    double k_k_max = kSigReach / sigma, k_g_max = kSigReach / sigma;
+    long long n_kap = (long long)std::ceil((kap_max - kap_min) / (sigma / kPtsPerSigKap)) + 1;
+    long long n_gam = (long long)std::ceil(gam_max / (sigma / kPtsPerSigGam)) + 1;
+    // ---- invert grid logic (sgl_full.py:191-262)
+    double kap_max_new = kap_max, gam_max_new = gam_max;
+    if (o.tail_box) { kap_max_new = std::max(kap_max, kTailKapMax); gam_max_new = std::max(g0, kTailGamMax); }
+    double dk_k = 2.0 * M_PI / (kPppK * std::max(std::fabs(kap_min), kap_max));
+    double dk_g = 2.0 * M_PI / (kPppG * gam_max);
+    if (o.tail_box && kTailPppG > 0) dk_g = std::min(dk_g, 2.0 * M_PI / (kTailPppG * gam_max_new));
+    if (kap_max_new != kap_max || gam_max_new != gam_max) {
+        kap_max = kap_max_new; gam_max = gam_max_new;
+        n_kap = (long long)std::ceil((kap_max - kap_min) / (sigma / kPtsPerSigKap)) + 1;
+        n_gam = (long long)std::ceil(gam_max / (sigma / kPtsPerSigGam)) + 1;
+    }
+    // ---- measured reach (_reach, sgl_full.py:38-47): 20 probes k0 * 1.25^j per axis
+    const int nprobe = (int)std::ceil(std::log(64.0) / std::log(1.25)) + 1;
+    double reach[2], phic[2];
+    for (int ax = 0; ax < 2; ++ax) {
+        const double k0v = ax == 0 ? k_k_max : k_g_max;
+        std::vector<double> ks(nprobe), re(nprobe), im(nprobe);
+        for (int j = 0; j < nprobe; ++j) ks[j] = k0v * std::pow(1.25, (double)j);
+        const double zero = 0.0;
+        if (ax == 0) CKS(lambda_direct(ctx, ks.data(), nprobe, &zero, 1, re.data(), im.data()));
+        else CKS(lambda_direct(ctx, &zero, 1, ks.data(), nprobe, re.data(), im.data()));
+        int pick = -1, amin = 0;
+        double best = 1e300;
+        for (int j = 0; j < nprobe; ++j) {
+            const double phi = std::fabs(std::exp(re[j]));   // |exp(L)| = exp(Re L)
+            if (phi <= o.phi_tol && pick < 0) pick = j;
+            if (phi < best) { best = phi; amin = j; }
+        }
+        const int i = pick >= 0 ? pick : amin;
+        reach[ax] = ks[i];
+        phic[ax] = std::exp(re[i]);
+    }
+    k_k_max = reach[0]; k_g_max = reach[1];
+    const long long nk_k = (long long)std::ceil(k_k_max / dk_k) + 1;
+    const long long nk_g = (long long)std::ceil(k_g_max / dk_g) + 1;
+    if ((double)n_kap * (double)n_gam > kOutGridMax)
+        return fail(ctx, SGL_ERR_UNSUPPORTED, "geometric output grid (n_kap * n_gam > OUT_GRID_MAX) not implemented");
+    if ((double)nk_k * (double)nk_g > kInvertBlockPts)
+        return fail(ctx, SGL_ERR_UNSUPPORTED, "blocked inversion (nk_k * nk_g > 2e7) not implemented");
+    if (nk_k < 2 || nk_g < 2) return fail(ctx, SGL_ERR_VALUE, "degenerate k grid");
+    const std::vector<double> kk = linspace(0.0, k_k_max, nk_k);
+    const std::vector<double> kg = linspace(0.0, k_g_max, nk_g);
+    const std::vector<double> kap = linspace(kap_min, kap_max, n_kap);
+    const std::vector<double> gam = linspace(0.0, gam_max, n_gam);
+    const int nk = (int)nk_k, nkg = (int)nk_g, nkap = (int)n_kap, ngam = (int)n_gam;
+    const int P = o.precision;
+    const size_t es = elem_size(P);
+
+    cudaEventRecord(ctx->ev[0], st);
+    // ---- Phi = exp(ln Phi) on the full grid
+    void* Phi = ctx->arena.get("phi", 2ULL * nk * nkg * es);
+    if (!Phi) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (phi)");
+    CKS(lambda_eval(ctx, P, kk.data(), nk, kg.data(), nkg, 1, Phi, (char*)Phi + (size_t)nk * nkg * es));
+    cudaEventRecord(ctx->ev[1], st);
+    // ---- transforms: F = Phi @ M (Hankel), P3ext = c CS @ [F | va | vb]
+    DBUF(d_kk, double, "inv_kk", nk);
+    DBUF(d_kg, double, "inv_kg", nkg);
+    DBUF(d_kap, double, "inv_kap", nkap);
+    DBUF(d_gam, double, "inv_gam", ngam);
+    CKS(upload(ctx, d_kk, kk.data(), nk));
+    CKS(upload(ctx, d_kg, kg.data(), nkg));
+    CKS(upload(ctx, d_kap, kap.data(), nkap));
+    CKS(upload(ctx, d_gam, gam.data(), ngam));
+    const int ldF = ngam + 2;
+    void* M = ctx->arena.get("inv_M", (size_t)nkg * ldF * es);
+    void* F = ctx->arena.get("inv_F", 2ULL * nk * ldF * es);
+    void* CS = ctx->arena.get("inv_CS", (size_t)nkap * 2 * nk * es);
+    void* P3e = ctx->arena.get("inv_P3e", (size_t)nkap * ldF * es);
+    DBUF(d_P3, double, "inv_P3", (long long)nkap * ngam);
+    if (!M || !F || !CS || !P3e) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (transforms)");
+    const double dkg = kg[1] - kg[0], dkk = kk[1] - kk[0];
+    launch_hankel_matrix(P, d_kg, nkg, dkg, d_gam, ngam, ldF, M, st); CKLAUNCH();
+    launch_kappa_matrix(P, d_kk, nk, dkk, d_kap, nkap, CS, st); CKLAUNCH();
+    const double c = 1.0 / (2.0 * M_PI * M_PI);
+    if (P == SGL_FP64) {
+        CKS(gemm_splitk<double>(ctx, gd<double>(2 * nk, ngam, nkg, Phi, nkg, 1, M, ldF, 1, F, ldF), "hankel"));
+    } else {
+        CKS(gemm_splitk<float>(ctx, gd<float>(2 * nk, ngam, nkg, Phi, nkg, 1, M, ldF, 1, F, ldF), "hankel"));
+    }
+    launch_em_columns(P, Phi, nk, nkg, dkg, F, ldF, ngam, st); CKLAUNCH();
+    if (P == SGL_FP64) {
+        CKS(gemm_splitk<double>(ctx, gd<double>(nkap, ldF, 2 * nk, CS, 2 * nk, 1, F, ldF, 1, P3e, ldF, c), "kappa"));
+    } else {
+        CKS(gemm_splitk<float>(ctx, gd<float>(nkap, ldF, 2 * nk, CS, 2 * nk, 1, F, ldF, 1, P3e, ldF, c), "kappa"));
+    }
+    launch_p3_finish(P, P3e, nkap, ngam, ldF, d_gam, d_P3, st); CKLAUNCH();
+    cudaEventRecord(ctx->ev[2], st);
+    // ---- path integral on the wide grid and the output grid in one launch
+    const int nw = o.n_xi_wide;
+    const std::vector<double> xw = linspace(xi_min, xi_max, nw);
+    std::vector<double> xall(xw);
+    xall.insert(xall.end(), xi_out, xi_out + n_xi);
+    DBUF(d_x, double, "path_x", xall.size());
+    DBUF(d_pi, double, "path_out", xall.size());
+    CKS(upload(ctx, d_x, xall.data(), xall.size()));
+    const double g_def = std::min(g0, gam_max);
+    {
+        Timed t(ctx, "path_integral", 0.0, (double)xall.size() * o.n_k_int * 2 * 4 * 8);
+        launch_path_integral(d_P3, nkap, ngam, kap.front(), kap.back(), gam.back(), d_x, (int)xall.size(), gam_max,
+                             g_def, o.n_k_int, d_pi, st);
+    }
+    CKLAUNCH();
+    cudaEventRecord(ctx->ev[3], st);
+    std::vector<double> pall(xall.size());
+    CK(cudaMemcpyAsync(pall.data(), d_pi, pall.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    // ---- normalisation and moments (sgl_full.py:362-372)
+    const double* pw = pall.data();
+    const double norm = trapz(pw, xw.data(), nw);
+    std::vector<double> ps(nw), tmp(nw);
+    for (int i = 0; i < nw; ++i) ps[i] = pw[i] / norm;
+    for (int i = 0; i < nw; ++i) tmp[i] = xw[i] * ps[i];
+    const double mean = trapz(tmp.data(), xw.data(), nw);
+    for (int i = 0; i < nw; ++i) { const double d = xw[i] - mean; tmp[i] = d * d * ps[i]; }
+    const double var = trapz(tmp.data(), xw.data(), nw);
+    for (int i = 0; i < nw; ++i) { const double d = xw[i] - mean; tmp[i] = d * d * d * ps[i]; }
+    const double skew = trapz(tmp.data(), xw.data(), nw) / std::pow(var, 1.5);
+    std::vector<double> xe(nw);
+    for (int i = 0; i < nw; ++i) xe[i] = std::exp(-0.5 * xw[i]);
+    for (int i = 0; i < nw; ++i) tmp[i] = xe[i] * ps[i];
+    const double md = trapz(tmp.data(), xw.data(), nw);
+    for (int i = 0; i < nw; ++i) { const double d = xe[i] - md; tmp[i] = d * d * ps[i]; }
+    const double sDL = std::sqrt(trapz(tmp.data(), xw.data(), nw)) / md;
+    bool finite = std::isfinite(norm) && norm != 0.0;
+    for (int i = 0; i < n_xi; ++i) {
+        P_out[i] = pall[(size_t)nw + i] / norm;
+        finite = finite && std::isfinite(P_out[i]);
+    }
+    if (meta) {
+        meta->nk_k = nk_k; meta->nk_g = nk_g; meta->n_kap = n_kap; meta->n_gam = n_gam;
+        meta->k_k_max = k_k_max; meta->k_g_max = k_g_max; meta->kap_min = kap_min; meta->kap_max = kap_max;
+        meta->gam_max = gam_max; meta->xi_min = xi_min; meta->xi_max = xi_max; meta->sigma = sigma;
+        meta->phi_at_k_cut = phic[0]; meta->phi_at_g_cut = phic[1];
+        meta->mean = mean; meta->var = var; meta->skew = skew; meta->sigmaDL = sDL; meta->norm = norm;
+        float a = 0, b = 0, cc = 0;
+        cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
+        cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]);
+        cudaEventElapsedTime(&cc, ctx->ev[2], ctx->ev[3]);
+        meta->ms_lambda = a; meta->ms_transform = b; meta->ms_path = cc;
+    }
+    if (!finite) return fail(ctx, SGL_ERR_NONFINITE, "PDF inversion returned non-finite values");
+    return SGL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,63 @@
+// Shared definitions for the sm_103a kernels of the lens-population characteristic function
+// and its inversion.  Host and device code.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <math.h>
+
+#include "sgl_gb300.h"
+
+namespace sgl {
+
+// ------------------------------------------------------------------ launch geometry
+constexpr int kNumSMs = 152;          // GB300: 2 dies x 76 SMs
+
+// ------------------------------------------------------------------ float-float helpers
+// A value v is carried as hi + lo with hi = (float)v, lo = (float)(v - hi): ~48 significant
+// bits on the FP32 pipes, which is what the phase k * kappa needs before range reduction.
+struct ff { float hi, lo; };
+
+__host__ __device__ inline ff ff_from_double(double v) {
+    ff r; r.hi = (float)v; r.lo = (float)(v - (double)r.hi); return r;
+}
+
+// ------------------------------------------------------------------ J0(x) - 1
+// Small-argument series below 1e-3 exactly as the reference forms it (-x^2/4 (1 - x^2/16));
+// above, CUDA's double-precision j0 minus 1.
+__device__ inline double j0m1_d(double x) {
+    if (x < 1e-3) { double x2 = x * x; return -x2 * 0.25 * (1.0 - x2 * (1.0 / 16.0)); }
+    return j0(x) - 1.0;
+}
+
+// ------------------------------------------------------------------ block reductions
+template <typename T>
+__device__ inline T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Deterministic block sum (fixed tree); every thread gets the total.  `sh` holds >= 32 T.
+template <typename T>
+__device__ inline T block_sum(T v, T* sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    T t = (threadIdx.x < nw) ? sh[threadIdx.x] : T(0);
+    if (wid == 0) t = warp_sum(t);
+    if (threadIdx.x == 0) sh[0] = t;
+    __syncthreads();
+    T r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// Number of kernels this library has launched (reported by sgl_stats_json).
+long long& launch_counter();
+#define SGL_COUNT(n) (::sgl::launch_counter() += (n))
+
+}  // namespace sgl

@@ -1,0 +1,189 @@
+// Composition of ln Phi on the full grid and the GEMM launchers.
+//
+// ln Phi(n, m) = [separable GEMM output](n, m) + A1[n] - 1/2 kk_n^2 V + Q(n, m)
+// where Q is the not-a-knot bicubic spline of the coarse-grid xi_lin term (reference:
+// Lam._Q_interpolated, sgl_full.py:2998-3022): with coefficients C = Mk Qc Mg^T on the knot
+// vectors of s = linspace(0, 1, n), Q(n, m) = sum_a sum_b Bk[n, a] C[lk + a, lg + b] Bg[m, b],
+// B the cubic B-spline basis (de Boor's recursion) at s = sqrt(clip(k / kmax, 0, 1)).
+#include "kernels.cuh"
+
+namespace sgl {
+
+long long& launch_counter() {
+    static long long n = 0;
+    return n;
+}
+
+// ------------------------------------------------------------------ GEMM launchers
+template <typename T>
+void launch_grouped_gemm(const GemmDesc<T>* d_descs, int nprob, int tiles, cudaStream_t st) {
+    if (tiles <= 0) return;
+    { grouped_gemm_kernel<T><<<tiles, 256, 0, st>>>(d_descs, nprob); SGL_COUNT(1); }
+}
+template void launch_grouped_gemm<double>(const GemmDesc<double>*, int, int, cudaStream_t);
+template void launch_grouped_gemm<float>(const GemmDesc<float>*, int, int, cudaStream_t);
+
+// out(i, j) = sum_s ws[s, i, j] (+ beta out(i, j)); ws slices are dense rows x cols, out has row stride ldo
+template <typename T>
+__global__ void k_sum_slices(const T* __restrict__ ws, int ns, int rows, int cols, T* __restrict__ out, long long ldo,
+                             T beta) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long n = (long long)rows * cols;
+    if (e >= n) return;
+    T acc = T(0);
+    for (int s = 0; s < ns; ++s) acc += ws[(long long)s * n + e];
+    T* o = out + (e / cols) * ldo + (e % cols);
+    *o = (beta != T(0)) ? acc + beta * *o : acc;
+}
+
+template <typename T>
+void launch_sum_slices(const T* ws, int ns, int rows, int cols, T* out, long long ldo, T beta, cudaStream_t st) {
+    { k_sum_slices<T><<<ceil_div((long long)rows * cols, 256), 256, 0, st>>>(ws, ns, rows, cols, out, ldo, beta); SGL_COUNT(1); }
+}
+template void launch_sum_slices<double>(const double*, int, int, int, double*, long long, double, cudaStream_t);
+template void launch_sum_slices<float>(const float*, int, int, int, float*, long long, float, cudaStream_t);
+
+// ------------------------------------------------------------------ spline basis
+// Knots t[0..ncoef+3]; find l in [3, ncoef-1] with t[l] <= s < t[l+1] (s = t[ncoef] -> last
+// interval), then the 4 nonzero cubic basis values B_{l-3..l}(s).
+__global__ void k_spline_basis(const double* __restrict__ x, int n, double xmax, const double* __restrict__ t,
+                               int ncoef, int* __restrict__ lout, double* __restrict__ bout) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = x[i] / xmax;
+    s = fmin(fmax(s, 0.0), 1.0);
+    s = sqrt(s);
+    int lo = 3, hi = ncoef - 1;          // search the interval
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (t[mid] <= s) lo = mid; else hi = mid - 1;
+    }
+    const int l = lo;
+    double N[4], left[4], right[4];
+    N[0] = 1.0;
+    for (int j = 1; j <= 3; ++j) {
+        left[j] = s - t[l + 1 - j];
+        right[j] = t[l + j] - s;
+        double saved = 0.0;
+        for (int r = 0; r < j; ++r) {
+            const double temp = N[r] / (right[r + 1] + left[j - r]);
+            N[r] = saved + right[r + 1] * temp;
+            saved = left[j - r] * temp;
+        }
+        N[j] = saved;
+    }
+    lout[i] = l - 3;
+    for (int a = 0; a < 4; ++a) bout[4 * i + a] = N[a];
+}
+
+void launch_spline_basis(const double* x, int n, double xmax, const double* knots, int ncoef, int* l, double* b,
+                         cudaStream_t st) {
+    { k_spline_basis<<<ceil_div(n, 128), 128, 0, st>>>(x, n, xmax, knots, ncoef, l, b); SGL_COUNT(1); }
+}
+
+// ------------------------------------------------------------------ finalize
+// G: GEMM output planes (rows 0..nk-1 real, nk..2nk-1 imaginary), ld = nkg.
+// write_phi = 0: out = ln Phi (double planes); 1: out = Phi = exp(ln Phi) (TT planes).
+template <typename TT, int WRITE_PHI>
+__global__ void k_finalize(const TT* __restrict__ G, int nk, int nkg, const double2* __restrict__ A1,
+                           const double* __restrict__ kk, double V, const double* __restrict__ Cre,
+                           const double* __restrict__ Cim, int ncg, SplineAxis sk, SplineAxis sg,
+                           void* __restrict__ out_re, void* __restrict__ out_im, long long ld_out) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = blockIdx.y;
+    if (m >= nkg) return;
+    const long long e = (long long)n * nkg + m;
+    const double k = kk[n];
+    double re = (double)G[e] + A1[n].x - 0.5 * (k * k * V);
+    double im = (double)G[(long long)nk * nkg + e] + A1[n].y;
+    if (Cre != nullptr) {
+        const int lk = sk.l[n], lg = sg.l[m];
+        double qr = 0.0, qi = 0.0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const double ba = sk.b[4 * n + a];
+            double rr = 0.0, ri = 0.0;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const double bb = sg.b[4 * m + b];
+                const long long ci = (long long)(lk + a) * ncg + (lg + b);
+                rr = fma(bb, Cre[ci], rr);
+                ri = fma(bb, Cim[ci], ri);
+            }
+            qr = fma(ba, rr, qr);
+            qi = fma(ba, ri, qi);
+        }
+        re += qr;
+        im += qi;
+    }
+    const long long eo = (long long)n * ld_out + m;
+    if (WRITE_PHI == 0) {
+        ((double*)out_re)[eo] = re;
+        ((double*)out_im)[eo] = im;
+    } else {
+        const double mag = exp(re);
+        double s, c;
+        sincos(im, &s, &c);
+        ((TT*)out_re)[eo] = (TT)(mag * c);
+        ((TT*)out_im)[eo] = (TT)(mag * s);
+    }
+}
+
+// Mixed path exp: the phase is reduced mod 2 pi in FP64, the rest is FP32.
+template <>
+__global__ void k_finalize<float, 1>(const float* __restrict__ G, int nk, int nkg, const double2* __restrict__ A1,
+                                     const double* __restrict__ kk, double V, const double* __restrict__ Cre,
+                                     const double* __restrict__ Cim, int ncg, SplineAxis sk, SplineAxis sg,
+                                     void* __restrict__ out_re, void* __restrict__ out_im, long long ld_out) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = blockIdx.y;
+    if (m >= nkg) return;
+    const long long e = (long long)n * nkg + m;
+    const double k = kk[n];
+    double re = (double)G[e] + A1[n].x - 0.5 * (k * k * V);
+    double im = (double)G[(long long)nk * nkg + e] + A1[n].y;
+    if (Cre != nullptr) {
+        const int lk = sk.l[n], lg = sg.l[m];
+        double qr = 0.0, qi = 0.0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const double ba = sk.b[4 * n + a];
+            double rr = 0.0, ri = 0.0;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const double bb = sg.b[4 * m + b];
+                const long long ci = (long long)(lk + a) * ncg + (lg + b);
+                rr = fma(bb, Cre[ci], rr);
+                ri = fma(bb, Cim[ci], ri);
+            }
+            qr = fma(ba, rr, qr);
+            qi = fma(ba, ri, qi);
+        }
+        re += qr;
+        im += qi;
+    }
+    const double two_pi = 6.283185307179586;
+    const double qn = rint(im * (1.0 / two_pi));
+    const float r = (float)fma(-qn, two_pi, im);
+    float s, c;
+    sincosf(r, &s, &c);
+    const float mag = expf((float)re);
+    const long long eo = (long long)n * ld_out + m;
+    ((float*)out_re)[eo] = mag * c;
+    ((float*)out_im)[eo] = mag * s;
+}
+
+void launch_finalize(int precision, int write_phi, const void* G, int nk, int nkg, const double2* A1, const double* kk,
+                     double V, const double* C_re, const double* C_im, int ncg, SplineAxis sk, SplineAxis sg,
+                     void* out_re, void* out_im, long long ld_out, cudaStream_t st) {
+    dim3 grid(ceil_div(nkg, 128), nk);
+    if (precision == SGL_FP64) {
+        if (write_phi) { k_finalize<double, 1><<<grid, 128, 0, st>>>((const double*)G, nk, nkg, A1, kk, V, C_re, C_im, ncg, sk, sg, out_re, out_im, ld_out); SGL_COUNT(1); }
+        else { k_finalize<double, 0><<<grid, 128, 0, st>>>((const double*)G, nk, nkg, A1, kk, V, C_re, C_im, ncg, sk, sg, out_re, out_im, ld_out); SGL_COUNT(1); }
+    } else {
+        if (write_phi) { k_finalize<float, 1><<<grid, 128, 0, st>>>((const float*)G, nk, nkg, A1, kk, V, C_re, C_im, ncg, sk, sg, out_re, out_im, ld_out); SGL_COUNT(1); }
+        else { k_finalize<float, 0><<<grid, 128, 0, st>>>((const float*)G, nk, nkg, A1, kk, V, C_re, C_im, ncg, sk, sg, out_re, out_im, ld_out); SGL_COUNT(1); }
+    }
+}
+
+}  // namespace sgl

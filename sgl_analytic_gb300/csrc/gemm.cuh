@@ -1,0 +1,117 @@
+// Grouped, register-tiled SIMT GEMM used by the separable Psi_1 products, the gauss Psi_2
+// coarse-grid contraction and the Hankel / kappa transforms.
+//
+// C(i, j) = alpha * sum_k A(i, k) B(k, j) + beta * C(i, j)
+// with arbitrary element strides for A and B (row- or column-major views) and a row-major C.
+// Several independent problems (e.g. the xi_lin groups) run in ONE launch: each CTA finds its
+// problem from a prefix sum of tile counts.  FP64 instances are FMA-pipe bound (GB300's FP64
+// rate is a small fraction of FP32); FP32 instances use 128x128 tiles with 8x8 per thread.
+#pragma once
+#include "common.cuh"
+
+namespace sgl {
+
+template <typename T>
+struct GemmDesc {
+    int M, N, K;
+    const T* A; long long a_rs, a_cs;   // A(i,k) = A[i*a_rs + k*a_cs]
+    const T* B; long long b_rs, b_cs;   // B(k,j) = B[k*b_rs + j*b_cs]
+    T* C; long long ldc;                // C(i,j) = C[i*ldc + j]
+    T alpha, beta;
+    int tile_begin;                     // first global tile of this problem
+    int tiles_n;                        // tiles along N
+};
+
+template <typename T> struct GemmCfg;
+template <> struct GemmCfg<double> { static constexpr int BM = 64, BN = 64, BK = 16, TM = 4, TN = 4; };
+template <> struct GemmCfg<float>  { static constexpr int BM = 128, BN = 128, BK = 8, TM = 8, TN = 8; };
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+grouped_gemm_kernel(const GemmDesc<T>* __restrict__ descs, int nprob) {
+    constexpr int BM = GemmCfg<T>::BM, BN = GemmCfg<T>::BN, BK = GemmCfg<T>::BK;
+    constexpr int TM = GemmCfg<T>::TM, TN = GemmCfg<T>::TN;
+    constexpr int NT = (BM / TM) * (BN / TN);
+    static_assert(NT == 256, "256 threads per CTA");
+    __shared__ T As[BK][BM + 1];
+    __shared__ T Bs[BK][BN + 1];
+
+    // locate the problem (nprob is small: linear scan from the top)
+    const int tile = blockIdx.x;
+    int p = nprob - 1;
+    while (p > 0 && descs[p].tile_begin > tile) --p;
+    const GemmDesc<T> d = descs[p];
+    const int local = tile - d.tile_begin;
+    const int tm = local / d.tiles_n, tn = local % d.tiles_n;
+    const int i0 = tm * BM, j0 = tn * BN;
+    if (i0 >= d.M) return;
+
+    const int tid = threadIdx.x;
+    const int tx = tid % (BN / TN), ty = tid / (BN / TN);
+    T acc[TM][TN];
+#pragma unroll
+    for (int a = 0; a < TM; ++a)
+#pragma unroll
+        for (int b = 0; b < TN; ++b) acc[a][b] = T(0);
+
+    const bool a_kcontig = (d.a_cs == 1);
+    const bool b_jcontig = (d.b_cs == 1);
+    for (int k0 = 0; k0 < d.K; k0 += BK) {
+        // A tile: BM x BK
+        for (int e = tid; e < BM * BK; e += NT) {
+            int i, k;
+            if (a_kcontig) { i = e / BK; k = e % BK; } else { k = e / BM; i = e % BM; }
+            const int gi = i0 + i, gk = k0 + k;
+            As[k][i] = (gi < d.M && gk < d.K) ? d.A[(long long)gi * d.a_rs + (long long)gk * d.a_cs] : T(0);
+        }
+        // B tile: BK x BN
+        for (int e = tid; e < BK * BN; e += NT) {
+            int k, j;
+            if (b_jcontig) { k = e / BN; j = e % BN; } else { j = e / BK; k = e % BK; }
+            const int gk = k0 + k, gj = j0 + j;
+            Bs[k][j] = (gk < d.K && gj < d.N) ? d.B[(long long)gk * d.b_rs + (long long)gj * d.b_cs] : T(0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < BK; ++k) {
+            T a[TM], b[TN];
+#pragma unroll
+            for (int r = 0; r < TM; ++r) a[r] = As[k][ty * TM + r];
+#pragma unroll
+            for (int c = 0; c < TN; ++c) b[c] = Bs[k][tx * TN + c];
+#pragma unroll
+            for (int r = 0; r < TM; ++r)
+#pragma unroll
+                for (int c = 0; c < TN; ++c) acc[r][c] = fma(a[r], b[c], acc[r][c]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int r = 0; r < TM; ++r) {
+        const int gi = i0 + ty * TM + r;
+        if (gi >= d.M) continue;
+#pragma unroll
+        for (int c = 0; c < TN; ++c) {
+            const int gj = j0 + tx * TN + c;
+            if (gj >= d.N) continue;
+            T* cp = d.C + (long long)gi * d.ldc + gj;
+            T v = d.alpha * acc[r][c];
+            if (d.beta != T(0)) v += d.beta * *cp;
+            *cp = v;
+        }
+    }
+}
+
+// Host helper: fills tile_begin / tiles_n and returns the total tile count.
+template <typename T>
+inline int gemm_plan(GemmDesc<T>* d, int nprob) {
+    int t = 0;
+    for (int p = 0; p < nprob; ++p) {
+        d[p].tiles_n = ceil_div(d[p].N, GemmCfg<T>::BN);
+        d[p].tile_begin = t;
+        t += ceil_div(d[p].M, GemmCfg<T>::BM) * d[p].tiles_n;
+    }
+    return t;
+}
+
+}  // namespace sgl

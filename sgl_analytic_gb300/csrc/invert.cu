@@ -1,0 +1,183 @@
+// Inversion Phi(k_kappa, k_gamma) -> P3(kappa, gamma) -> P_s(ln mu)
+// (reference: sgl.P_vector_joint sgl.py:1127-1156, sgl_full.invert sgl_full.py:272-360).
+//
+//   Hankel   F[n, j]   = sum_m Phi[n, m] k_g[m] w_g[m] J0(gam_j k_g[m])         (GEMM, M matrix)
+//   kappa    P3[i, j]  = 1/(2 pi^2) sum_n w_k[n] Re(e^{-i kap_i k_n} F[n, j])   (GEMM, CS matrix)
+//   E-M      P3       += a(kap) + b(kap) gam^2 from Phi[:, 0], Phi[:, 1]        (2 extra F columns)
+//   path     P_i(xi)   = pi / mu^2 int P3(kap, gam(kap; mu)) dkap  (+ gamma-parametrised tail)
+#include "kernels.cuh"
+
+namespace sgl {
+
+// M[m, j] = k_g[m] w_g[m] J0(gam_j k_g[m]),  w_g = dk_g (halved at both ends); row stride ld
+template <typename TT>
+__global__ void k_hankel_matrix(const double* __restrict__ kg, int nkg, double dkg, const double* __restrict__ gam,
+                                int ngam, int ld, TT* __restrict__ M) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)nkg * ngam) return;
+    const int m = (int)(e / ngam), j = (int)(e % ngam);
+    double w = dkg;
+    if (m == 0 || m == nkg - 1) w *= 0.5;
+    M[(long long)m * ld + j] = (TT)((kg[m] * w) * j0(gam[j] * kg[m]));
+}
+
+void launch_hankel_matrix(int precision, const double* kg, int nkg, double dkg, const double* gam, int ngam, int ld,
+                          void* M, cudaStream_t st) {
+    const long long tot = (long long)nkg * ngam;
+    if (precision == SGL_FP64) { k_hankel_matrix<double><<<ceil_div(tot, 256), 256, 0, st>>>(kg, nkg, dkg, gam, ngam, ld, (double*)M); SGL_COUNT(1); }
+    else { k_hankel_matrix<float><<<ceil_div(tot, 256), 256, 0, st>>>(kg, nkg, dkg, gam, ngam, ld, (float*)M); SGL_COUNT(1); }
+}
+
+// CS[i, n] = cos(kap_i k_n) w_k[n],  CS[i, nk + n] = sin(kap_i k_n) w_k[n]
+template <typename TT>
+__global__ void k_kappa_matrix(const double* __restrict__ kk, int nk, double dkk, const double* __restrict__ kap,
+                               int nkap, TT* __restrict__ CS) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)nkap * nk) return;
+    const int i = (int)(e / nk), n = (int)(e % nk);
+    double w = dkk;
+    if (n == 0 || n == nk - 1) w *= 0.5;
+    double s, c;
+    sincos(kap[i] * kk[n], &s, &c);
+    CS[(long long)i * 2 * nk + n] = (TT)(c * w);
+    CS[(long long)i * 2 * nk + nk + n] = (TT)(s * w);
+}
+
+void launch_kappa_matrix(int precision, const double* kk, int nk, double dkk, const double* kap, int nkap, void* CS,
+                         cudaStream_t st) {
+    const long long tot = (long long)nkap * nk;
+    if (precision == SGL_FP64) { k_kappa_matrix<double><<<ceil_div(tot, 256), 256, 0, st>>>(kk, nk, dkk, kap, nkap, (double*)CS); SGL_COUNT(1); }
+    else { k_kappa_matrix<float><<<ceil_div(tot, 256), 256, 0, st>>>(kk, nk, dkk, kap, nkap, (float*)CS); SGL_COUNT(1); }
+}
+
+// Euler-Maclaurin endpoint columns (sgl_full.py:277-298): from Phi0 = Phi[:, 0], Phi1 = Phi[:, 1],
+// Phi2 = (Phi1 - Phi0)/dkg^2, va = dkg^2/12 Phi0 - dkg^4/120 Phi2, vb = dkg^4/480 Phi0, written into
+// columns col (va) and col + 1 (vb) of F (real rows then imaginary rows).
+template <typename TT>
+__global__ void k_em_columns(const TT* __restrict__ Phi, int nk, int nkg, double dkg, TT* __restrict__ F, int ldF,
+                             int col) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nk) return;
+    const long long im_off = (long long)nk * nkg;
+    const double p0r = (double)Phi[(long long)n * nkg], p0i = (double)Phi[im_off + (long long)n * nkg];
+    const double p1r = (double)Phi[(long long)n * nkg + 1], p1i = (double)Phi[im_off + (long long)n * nkg + 1];
+    const double d2 = dkg * dkg, d4 = d2 * d2;
+    const double p2r = (p1r - p0r) / d2, p2i = (p1i - p0i) / d2;
+    F[(long long)n * ldF + col] = (TT)((d2 / 12.0) * p0r - (d4 / 120.0) * p2r);
+    F[(long long)(nk + n) * ldF + col] = (TT)((d2 / 12.0) * p0i - (d4 / 120.0) * p2i);
+    F[(long long)n * ldF + col + 1] = (TT)((d4 / 480.0) * p0r);
+    F[(long long)(nk + n) * ldF + col + 1] = (TT)((d4 / 480.0) * p0i);
+}
+
+void launch_em_columns(int precision, const void* Phi, int nk, int nkg, double dkg, void* F, int ldF, int col,
+                       cudaStream_t st) {
+    if (precision == SGL_FP64) { k_em_columns<double><<<ceil_div(nk, 128), 128, 0, st>>>((const double*)Phi, nk, nkg, dkg, (double*)F, ldF, col); SGL_COUNT(1); }
+    else { k_em_columns<float><<<ceil_div(nk, 128), 128, 0, st>>>((const float*)Phi, nk, nkg, dkg, (float*)F, ldF, col); SGL_COUNT(1); }
+}
+
+// P3[i, j] = P3ext[i, j] + P3ext[i, ngam] + P3ext[i, ngam + 1] gam_j^2  (already scaled by 1/(2 pi^2))
+template <typename TT>
+__global__ void k_p3_finish(const TT* __restrict__ P3ext, int nkap, int ngam, int ld, const double* __restrict__ gam,
+                            double* __restrict__ P3) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)nkap * ngam) return;
+    const int i = (int)(e / ngam), j = (int)(e % ngam);
+    const TT* row = P3ext + (long long)i * ld;
+    const double g = gam[j];
+    P3[e] = (double)row[j] + (double)row[ngam] + (double)row[ngam + 1] * (g * g);
+}
+
+void launch_p3_finish(int precision, const void* P3ext, int nkap, int ngam, int ld, const double* gam, double* P3,
+                      cudaStream_t st) {
+    const long long tot = (long long)nkap * ngam;
+    if (precision == SGL_FP64) { k_p3_finish<double><<<ceil_div(tot, 256), 256, 0, st>>>((const double*)P3ext, nkap, ngam, ld, gam, P3); SGL_COUNT(1); }
+    else { k_p3_finish<float><<<ceil_div(tot, 256), 256, 0, st>>>((const float*)P3ext, nkap, ngam, ld, gam, P3); SGL_COUNT(1); }
+}
+
+// ------------------------------------------------------------------ path integral
+// Uniform axis a_i = a0 + i h (i < n-1), a_{n-1} = a1 (numpy linspace).  Interval index as
+// RegularGridInterpolator: i = (#nodes < x) - 1 clipped to [0, n-2]; x outside [a0, a1] -> -1.
+struct Axis { double a0, a1, h; int n; };
+
+// numpy rounds i * step and + start separately: no FMA contraction here
+__device__ inline double axis_node(const Axis& A, int i) {
+    return (i == A.n - 1) ? A.a1 : __dadd_rn(__dmul_rn((double)i, A.h), A.a0);
+}
+
+__device__ inline int axis_find(const Axis& A, double x, double& t) {
+    if (!(x >= A.a0 && x <= A.a1)) return -1;
+    int i = (int)floor((x - A.a0) / A.h);
+    i = max(0, min(i, A.n - 1));
+    while (i + 1 < A.n && axis_node(A, i + 1) < x) ++i;   // largest i with node_i < x
+    while (i > 0 && !(axis_node(A, i) < x)) --i;
+    i = min(i, A.n - 2);
+    const double lo = axis_node(A, i), hi = axis_node(A, i + 1);
+    t = (x - lo) / (hi - lo);
+    return i;
+}
+
+__device__ inline double bilinear(const double* __restrict__ P3, const Axis& K, const Axis& G, double x, double y) {
+    double tx, ty;
+    const int i = axis_find(K, x, tx);
+    const int j = axis_find(G, y, ty);
+    if (i < 0 || j < 0) return 0.0;
+    const long long b = (long long)i * G.n + j;
+    const double v00 = P3[b], v01 = P3[b + 1], v10 = P3[b + G.n], v11 = P3[b + G.n + 1];
+    return (1.0 - tx) * (1.0 - ty) * v00 + (1.0 - tx) * ty * v01 + tx * (1.0 - ty) * v10 + tx * ty * v11;
+}
+
+__device__ inline double lin(double a, double b, int n, int i) {     // numpy linspace node
+    return (i == n - 1) ? b : __dadd_rn(__dmul_rn((double)i, (b - a) / (double)(n - 1)), a);
+}
+
+__global__ void __launch_bounds__(256)
+k_path_integral(const double* __restrict__ P3, Axis K, Axis G, const double* __restrict__ xi, double gmax,
+                double g_def, int n_k_int, double* __restrict__ out) {
+    __shared__ double sh[32];
+    const double x = xi[blockIdx.x];
+    const double mu = exp(x);
+    const double rm = 1.0 / sqrt(mu);
+    const double hi = 1.0 - rm;
+    const double lo = fmax(K.a0, 1.0 - sqrt(1.0 / mu + g_def * g_def));
+    const double pref = M_PI / (mu * mu);
+    double acc = 0.0;
+    const bool body = hi > lo;
+    if (body) {
+        for (int i = threadIdx.x; i < n_k_int - 1; i += blockDim.x) {
+            const double k0 = lin(lo, hi, n_k_int, i), k1 = lin(lo, hi, n_k_int, i + 1);
+            const double g0 = sqrt(fmax((hi - k0) * (1.0 - k0 + rm), 0.0));
+            const double g1 = sqrt(fmax((hi - k1) * (1.0 - k1 + rm), 0.0));
+            const double v0 = bilinear(P3, K, G, k0, g0), v1 = bilinear(P3, K, G, k1, g1);
+            acc += (k1 - k0) * (v0 + v1) / 2.0;
+        }
+    }
+    double total = pref * block_sum(acc, sh);
+    if (body && gmax > g_def && lo > K.a0) {
+        const double gb = fmin(gmax, sqrt(fmax((hi - K.a0) * (1.0 - K.a0 + rm), 0.0)));
+        if (gb > g_def) {
+            const double dgam = G.h;
+            const int n = (int)ceil((gb - g_def) / (0.5 * dgam)) + 1;
+            double acc2 = 0.0;
+            for (int i = threadIdx.x; i < n - 1; i += blockDim.x) {
+                const double ga = lin(g_def, gb, n, i), gc = lin(g_def, gb, n, i + 1);
+                const double ra = sqrt(1.0 / mu + ga * ga), rc = sqrt(1.0 / mu + gc * gc);
+                const double ka = fmin(fmax(1.0 - ra, K.a0), K.a1), kc = fmin(fmax(1.0 - rc, K.a0), K.a1);
+                const double va = bilinear(P3, K, G, ka, ga) * (ga / ra);
+                const double vc = bilinear(P3, K, G, kc, gc) * (gc / rc);
+                acc2 += (gc - ga) * (va + vc) / 2.0;
+            }
+            total += pref * block_sum(acc2, sh);
+        }
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = body ? total : 0.0;
+}
+
+void launch_path_integral(const double* P3, int nkap, int ngam, double kap0, double kap1, double gam1,
+                          const double* xi, int nxi, double gmax, double g_def, int n_k_int, double* out,
+                          cudaStream_t st) {
+    Axis K{kap0, kap1, (kap1 - kap0) / (nkap - 1), nkap};
+    Axis G{0.0, gam1, gam1 / (ngam - 1), ngam};
+    if (nxi > 0) { k_path_integral<<<nxi, 256, 0, st>>>(P3, K, G, xi, gmax, g_def, n_k_int, out); SGL_COUNT(1); }
+}
+
+}  // namespace sgl

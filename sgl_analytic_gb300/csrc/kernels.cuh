@@ -1,0 +1,105 @@
+// Internal launcher declarations shared by the .cu translation units.
+#pragma once
+#include "common.cuh"
+#include "gemm.cuh"
+
+namespace sgl {
+
+// Separable Psi_1 plan on the device (cells sorted by gamma-node group).
+struct SepDevice {
+    int n_cells = 0, n_groups = 0, n_cols = 0, n_cols_sep = 0, nchunks = 0;
+    const double* kap = nullptr;      // [n_cells] centroid kappa
+    const double* w = nullptr;        // [n_cells] weight
+    const double* wl = nullptr;       // [n_cells * 8] weight x Lagrange basis (direct cells: w, 0...)
+    const float* kap_hi = nullptr;    // float-float kappa (mixed path)
+    const float* kap_lo = nullptr;
+    const float* w_f = nullptr;
+    const float* wl_f = nullptr;
+    const int* grp = nullptr;         // [n_cells] group of each cell
+    const int* gcol0 = nullptr;       // [n_groups] first T column
+    const int* gncol = nullptr;       // [n_groups] 8 (Chebyshev nodes) or 1 (exact node)
+    const int* chunk_begin = nullptr; // [nchunks + 1] cell offsets (group aligned)
+};
+
+// ---- Psi_1
+void launch_psi1_direct(const double* kk, int nk, const double* kg, int nkg, const double* k0,
+                        const double* g0, const double* w0, int64_t nc, double* re, double* im,
+                        cudaStream_t st);
+void launch_sep_sweep(int precision, const double* kk, int nk, const SepDevice& s, void* Tt,
+                      double2* A_part, double2* A1, cudaStream_t st);
+void launch_j0m1_table(int precision, const double* nodes, int nn, const double* x, int nx, void* B,
+                       cudaStream_t st);
+void launch_cheb_matrix(int precision, double K, int N, const double* x, int nx, void* L, cudaStream_t st);
+void launch_cheb_points(double K, int N, double* t, cudaStream_t st);
+
+// ---- GEMM
+template <typename T>
+void launch_grouped_gemm(const GemmDesc<T>* d_descs, int nprob, int tiles, cudaStream_t st);
+template <typename T>
+void launch_sum_slices(const T* ws, int nslices, int rows, int cols, T* out, long long ldo, T beta, cudaStream_t st);
+
+// ---- xi_lin (gauss) Psi_2
+struct XiDevice {
+    int n_groups = 0, n_kmc = 0, n_gmc = 0;
+    const double* kmc = nullptr;       // [n_kmc] coarse kappa centres
+    const double* gmc = nullptr;       // [n_gmc] coarse gamma centres
+    // per group
+    const int* g_m = nullptr;
+    const int* g_r = nullptr;
+    const int* g_nP = nullptr;
+    const long long* g_p_off = nullptr;     // into idx_p / p_ptr rows
+    const long long* g_ent_off = nullptr;   // into ent_q / rows columns
+    const long long* g_row_off = nullptr;   // into rows / res / sum_rows (row units)
+    const int* idx_p = nullptr;        // global kappa-centre index of each local p
+    const int* p_ptr = nullptr;        // CSR over local p: entries [p_ptr[p], p_ptr[p+1]) (group relative)
+    const int* ent_qg = nullptr;       // global gamma-centre index of each entry
+    const double* rows = nullptr;      // rows: entry-major per group: rows[(ent_off + e) * r + rr]
+    const double* res = nullptr;       // [total rows]
+    const double* sum_rows = nullptr;  // [total rows]
+    // 1-D reach paths
+    int R0 = 0;
+    const double* W0 = nullptr;        // [R0 * n_kmc]
+    const double* res0 = nullptr;
+    const double* sum0 = nullptr;
+    int Rm[3] = {0, 0, 0};
+    const double* U[3] = {nullptr, nullptr, nullptr};    // [Rm * n_gmc]
+    const double* resm[3] = {nullptr, nullptr, nullptr};
+    const double* summ[3] = {nullptr, nullptr, nullptr};
+};
+
+void launch_xi_line_k(const XiDevice& x, const double* kk, int nk, double* out_re, double* out_im, cudaStream_t st);
+void launch_xi_line_g(const XiDevice& x, const double* kg, int nkg, double* out_re, double* out_im, cudaStream_t st);
+void launch_bessel_tables(int precision, const double* gmc, int n_gmc, const double* kg, int nkg, void* J, cudaStream_t st);
+void launch_xi_stageA(int precision, const XiDevice& x, const long long* h_p_prefix, int total_p, const long long* T_off,
+                      const void* J, int nkg, void* T, cudaStream_t st);
+void launch_xi_E(int precision, const XiDevice& x, const double* kk, int nk, const long long* E_off,
+                 const long long* h_p_prefix, int total_p, void* E, cudaStream_t st);
+void launch_xi_square(int precision, const XiDevice& x, const long long* G_off, const void* G, const double* kk, int nk,
+                      const double* kg, int nkg, double* out_re, double* out_im, cudaStream_t st);
+
+// ---- spline + composition
+struct SplineAxis {              // per evaluation point: interval l (first coefficient) + 4 weights
+    const int* l = nullptr;
+    const double* b = nullptr;   // [n * 4]
+};
+void launch_spline_basis(const double* x, int n, double xmax, const double* knots, int ncoef, int* l, double* b,
+                         cudaStream_t st);
+// out = G + A1[n] - 1/2 kk^2 V + spline(C) ; mode 0: write lnPhi (double planes), mode 1: write Phi (TT planes)
+void launch_finalize(int precision, int write_phi, const void* G, int nk, int nkg, const double2* A1, const double* kk,
+                     double V, const double* C_re, const double* C_im, int ncg, SplineAxis sk, SplineAxis sg,
+                     void* out_re, void* out_im, long long ld_out, cudaStream_t st);
+
+// ---- inversion
+void launch_hankel_matrix(int precision, const double* kg, int nkg, double dkg, const double* gam, int ngam, int ld,
+                          void* M, cudaStream_t st);
+void launch_kappa_matrix(int precision, const double* kk, int nk, double dkk, const double* kap, int nkap, void* CS,
+                         cudaStream_t st);
+void launch_em_columns(int precision, const void* Phi, int nk, int nkg, double dkg, void* F, int ldF, int col,
+                       cudaStream_t st);
+void launch_p3_finish(int precision, const void* P3ext, int nkap, int ngam, int ld, const double* gam, double* P3,
+                      cudaStream_t st);
+void launch_path_integral(const double* P3, int nkap, int ngam, double kap0, double kap1, double gam1,
+                          const double* xi, int nxi, double gmax, double g_def, int n_k_int, double* out,
+                          cudaStream_t st);
+
+}  // namespace sgl

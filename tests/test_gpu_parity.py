@@ -1,0 +1,160 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference's own outputs and the oracle.
+
+Tolerances (the benchmark spec): FP64 path max|d ln Phi| <= 1e-10 and max|dP|/peak <= 1e-9 (the
+reference's regression tolerance); mixed path PDF L1 <= 1e-4 and tail relative error <= 1e-3.
+"""
+import json
+
+import numpy as np
+import pytest
+
+from tests.conftest import FULL_FIXTURE, GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+TOL_LN = 1e-10
+TOL_PEAK = 1e-9
+KG_FULL = np.linspace(0.0, 808.3706243177588, 2687)
+KK16 = np.linspace(0.0, 1010.4632803971984, 1683)[::16]     # 106 rows: 106 x 2687 > 200000 points
+
+
+@pytest.fixture(scope="module")
+def lam1(pop_sub):
+    from sgl_analytic_gb300 import Lam
+    return Lam(pop_sub, xi=False)
+
+
+@pytest.fixture(scope="module")
+def lamx(pop_sub):
+    from sgl_analytic_gb300 import Lam
+    return Lam(pop_sub, xi=True)
+
+
+def test_sigma(lam1, lamx, ref_sub):
+    assert lam1.sigma() == pytest.approx(float(ref_sub["sigma1"]), rel=1e-13)
+    assert lamx.sigma() == pytest.approx(float(ref_sub["sigmax"]), rel=1e-13)
+
+
+def test_psi1_direct_small_grid(lam1, ref_sub):
+    L = lam1(ref_sub["kk"], ref_sub["kg"])            # 4452 points: direct sums
+    assert np.max(np.abs(L - ref_sub["psi1_grid"])) <= TOL_LN
+
+
+def _ln_close(a, b):
+    """max|d ln Phi| <= 1e-10 where |ln Phi| <= 100; beyond (|Phi| < e^-100, far past the k-reach)
+    the bar is 1e-12 relative: the FP64 roundoff of sums whose weights total 3.7e6 (ulp 4.7e-10)."""
+    tol = np.maximum(TOL_LN, 1e-12 * np.abs(b))
+    return bool(np.all(np.abs(a - b) <= tol))
+
+
+def test_psi1_probe_lines(lam1, ref_sub):
+    ks = ref_sub["probe_k"]
+    assert _ln_close(lam1(ks, np.zeros(1))[:, 0], ref_sub["psi1_line_k"])
+    assert _ln_close(lam1(np.zeros(1), ks)[0, :], ref_sub["psi1_line_g"])
+
+
+def test_psi1_separable_full_width(lam1, ref_sub):
+    # >= 200000 points: the separable sweep + Chebyshev GEMMs + direct-tail GEMM
+    L = lam1(KK16, KG_FULL)
+    assert L.shape == (KK16.size, KG_FULL.size)
+    assert np.max(np.abs(L[::2, ::32] - ref_sub["psi1_grid"])) <= TOL_LN
+
+
+def test_psi1_separable_mixed_precision(lam1, ref_sub):
+    from sgl_analytic_gb300._lib import SGL_MIXED
+    Lm = lam1.engine.lnphi(KK16, KG_FULL, SGL_MIXED)[::2, ::32]
+    Lr = ref_sub["psi1_grid"]
+    # Phi = exp(ln Phi) agrees to 1e-5 absolute; ln Phi to 1e-3 where |Phi| > 1e-6
+    assert np.max(np.abs(np.exp(Lm) - np.exp(Lr))) <= 1e-5
+    big = np.abs(np.exp(Lr)) > 1e-6
+    assert np.max(np.abs(Lm - Lr)[big]) <= 1e-3
+
+
+def test_xi_term_exact(lamx, ref_sub):
+    Q = lamx.engine.xi_term(ref_sub["kkc"], ref_sub["kgc"])
+    Qr = ref_sub["xi_coarse"]
+    assert np.max(np.abs(Q - Qr)) <= TOL_LN * max(1.0, np.max(np.abs(Qr)))
+    ks = ref_sub["probe_k"]
+    assert np.max(np.abs(lamx.engine.xi_term(ks, np.zeros(1))[:, 0] - ref_sub["xi_line_k"])) <= TOL_LN
+    assert np.max(np.abs(lamx.engine.xi_term(np.zeros(1), ks)[0, :] - ref_sub["xi_line_g"])) <= TOL_LN
+
+
+def test_lambda_with_xi_small_grid(lamx, ref_sub):
+    L = lamx(ref_sub["kk"][:20], ref_sub["kg"][:20])
+    assert np.max(np.abs(L - ref_sub["lamx_grid"])) <= TOL_LN
+
+
+def test_lambda_with_xi_interpolated_matches_oracle(lamx, pop_sub, ref_sub):
+    """Full-width grid: separable Psi_1 + 101^2 coarse xi term + not-a-knot bicubic spline."""
+    from oracle import lam_oracle as LO
+    X = LO.XiGroups(pop_sub.groups(), pop_sub.ce_k, pop_sub.ce_g)
+    orc = LO.OracleLam(pop_sub.w0, pop_sub.k0, pop_sub.g0, pop_sub.ig, pop_sub.fe_g, pop_sub.V, X)
+    kk = KK16
+    L = lamx(kk, KG_FULL)
+    Lo = orc(kk, KG_FULL)
+    assert np.max(np.abs(L - Lo)) <= TOL_LN
+
+
+def _pdf_errors(P, Pref, x):
+    peak = np.max(Pref)
+    l1 = np.trapezoid(np.abs(P - Pref), x)
+    tail = x > 1.0
+    sig = np.abs(Pref[tail]) > 1e-6 * peak
+    rel_tail = np.max(np.abs(P[tail][sig] - Pref[tail][sig]) / np.abs(Pref[tail][sig])) if sig.any() else 0.0
+    return np.max(np.abs(P - Pref)) / peak, l1, rel_tail
+
+
+@pytest.mark.parametrize("which", ["pdf1", "pdfx"])
+def test_pdf_fp64_matches_reference(which, lam1, lamx, ref_sub):
+    from sgl_analytic_gb300 import invert
+    lam = lam1 if which == "pdf1" else lamx
+    x = ref_sub["xi_out"]
+    _, P, meta = invert(lam, lam.sigma(), xi_out=x, tail_box=True, phi_tol=1e-8, n_xi_wide=500)
+    g = meta["grid"]
+    rg = ref_sub[which + "_grid"]
+    assert [g["nk_k"], g["nk_g"], g["n_kap"], g["n_gam"]] == [int(rg[i]) for i in (0, 1, 4, 5)]
+    assert g["k_k_max"] == pytest.approx(rg[2], rel=1e-14) and g["k_g_max"] == pytest.approx(rg[3], rel=1e-14)
+    dpeak, l1, _ = _pdf_errors(P, ref_sub[which + "_P"], x)
+    assert dpeak <= TOL_PEAK and l1 <= 1e-9
+    np.testing.assert_allclose([meta["mean"], meta["var"], meta["skew"], meta["sigmaDL"]],
+                               ref_sub[which + "_moments"], rtol=1e-8)
+
+
+def test_pdf_mixed_matches_reference(lamx, ref_sub):
+    from sgl_analytic_gb300 import invert
+    x = ref_sub["xi_out"]
+    _, P, _ = invert(lamx, lamx.sigma(), xi_out=x, tail_box=True, phi_tol=1e-8, precision="mixed")
+    dpeak, l1, rel_tail = _pdf_errors(P, ref_sub["pdfx_P"], x)
+    assert l1 <= 1e-4 and rel_tail <= 1e-3, (dpeak, l1, rel_tail)
+
+
+def test_pdf_is_deterministic(lamx, ref_sub):
+    from sgl_analytic_gb300 import invert
+    x = ref_sub["xi_out"][::50]
+    a = invert(lamx, lamx.sigma(), xi_out=x, phi_tol=1e-8)[1]
+    b = invert(lamx, lamx.sigma(), xi_out=x, phi_tol=1e-8)[1]
+    assert np.array_equal(a, b)
+
+
+def test_bad_input_raises_value_error(lam1):
+    with pytest.raises(ValueError):
+        lam1(np.array([np.nan, 1.0]), np.array([0.0, 1.0]))
+    with pytest.raises(ValueError):
+        lam1(np.array([1.0]), np.array([-1.0]))
+
+
+@pytest.mark.skipif(not FULL_FIXTURE.exists(), reason="full z_s=1 population (290 MB) not shipped")
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_full_chain_matches_stored_golden_pdf(precision):
+    """All 201 xi groups: GPU vs the reference's stored z_s=1 golden PDF."""
+    from sgl_analytic_gb300 import Lam, Population, invert
+    lam = Lam(Population.load(FULL_FIXTURE), xi=True)
+    ref = json.load(open(GOLDEN / "pdf_zs1.json"))
+    x = np.concatenate([ref["xi"], ref["xi_tail"]])
+    _, P, meta = invert(lam, lam.sigma(), xi_out=x, phi_tol=1e-8, precision=precision)
+    P0 = np.concatenate([ref["P_s"], ref["P_s_tail"]])
+    dpeak, l1, rel_tail = _pdf_errors(P, P0, x)
+    if precision == "fp64":
+        assert dpeak <= TOL_PEAK
+    else:
+        assert l1 <= 1e-4 and rel_tail <= 1e-3

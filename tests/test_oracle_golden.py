@@ -1,0 +1,91 @@
+"""The FP64 oracle (oracle/) pinned against the reference's own outputs.
+
+Golden vectors: tests/golden/ref_zs1_sub.npz, produced by the reference's NumPy code on the
+committed population (tests/golden/make_golden.py), and the reference's stored golden PDF
+tests/golden/pdf_zs1.json (its tests/reference/, checked by its tests/test_reference.py at
+max|dP|/peak <= 1e-9).
+"""
+import json
+
+import numpy as np
+import pytest
+
+from oracle import invert_oracle as IO
+from oracle import lam_oracle as LO
+from tests.conftest import FULL_FIXTURE, GOLDEN
+
+TOL_LN = 1e-10          # max |d ln Phi| (spec FP64 bar)
+TOL_PEAK = 1e-9         # max |dP| / peak (the reference's own regression tolerance)
+
+
+def oracle_for(pop, xi, method="sep"):
+    X = LO.XiGroups(pop.groups(), pop.ce_k, pop.ce_g) if xi else None
+    return LO.OracleLam(pop.w0, pop.k0, pop.g0, pop.ig, pop.fe_g, pop.V, X, method=method)
+
+
+def test_psi1_direct_matches_reference(pop_sub, ref_sub):
+    lam = oracle_for(pop_sub, False, "direct")
+    L = lam(ref_sub["kk"], ref_sub["kg"])
+    assert np.max(np.abs(L - ref_sub["psi1_grid"])) <= TOL_LN
+
+
+def test_psi1_separable_matches_reference_direct(pop_sub, ref_sub):
+    # the separable path depends on the full k_gamma extent (node placement): evaluate the
+    # sub-sampled k_kappa rows against the FULL k_gamma axis, compare every 32nd column
+    kg_full = np.linspace(0.0, 808.3706243177588, 2687)
+    lam = oracle_for(pop_sub, False, "sep")
+    L = lam.psi1_sep(ref_sub["kk"], kg_full)[:, ::32]
+    assert np.max(np.abs(L - ref_sub["psi1_grid"])) <= TOL_LN
+
+
+def test_probe_lines_and_sigma(pop_sub, ref_sub):
+    lam = oracle_for(pop_sub, False, "direct")
+    ks = ref_sub["probe_k"]
+    assert np.max(np.abs(lam(ks, np.zeros(1))[:, 0] - ref_sub["psi1_line_k"])) <= TOL_LN
+    assert np.max(np.abs(lam(np.zeros(1), ks)[0, :] - ref_sub["psi1_line_g"])) <= TOL_LN
+    assert lam.sigma() == pytest.approx(float(ref_sub["sigma1"]), rel=1e-14)
+    assert oracle_for(pop_sub, True).sigma() == pytest.approx(float(ref_sub["sigmax"]), rel=1e-14)
+
+
+def test_xi_term_matches_reference(pop_sub, ref_sub):
+    lam = oracle_for(pop_sub, True)
+    Q = lam.qxi(ref_sub["kkc"], ref_sub["kgc"])
+    Qr = ref_sub["xi_coarse"]
+    assert np.max(np.abs(Q - Qr)) <= TOL_LN * max(1.0, np.max(np.abs(Qr)))
+    ks = ref_sub["probe_k"]
+    assert np.max(np.abs(lam.qxi(ks, np.zeros(1))[:, 0] - ref_sub["xi_line_k"])) <= TOL_LN
+    assert np.max(np.abs(lam.qxi(np.zeros(1), ks)[0, :] - ref_sub["xi_line_g"])) <= TOL_LN
+    # full composition on a small grid (exact xi term)
+    L = lam(ref_sub["kk"][:20], ref_sub["kg"][:20])
+    assert np.max(np.abs(L - ref_sub["lamx_grid"])) <= TOL_LN
+
+
+def _check_pdf(P, Pref, x):
+    peak = np.max(Pref)
+    assert np.max(np.abs(P - Pref)) / peak <= TOL_PEAK
+    assert np.trapezoid(np.abs(P - Pref), x) <= 1e-9
+
+
+def test_invert_chain_matches_reference(pop_sub, ref_sub):
+    """Psi_1 + xi subset through the whole inversion (separable Lambda, as the reference's default)."""
+    lam = oracle_for(pop_sub, True, "sep")
+    x = ref_sub["xi_out"]
+    _, P, meta = IO.invert(lam, lam.sigma(), x)
+    g = meta["grid"]
+    ref_grid = ref_sub["pdfx_grid"]
+    assert [g["nk_k"], g["nk_g"], g["n_kap"], g["n_gam"]] == [int(ref_grid[i]) for i in (0, 1, 4, 5)]
+    _check_pdf(P, ref_sub["pdfx_P"], x)
+    np.testing.assert_allclose([meta["mean"], meta["var"], meta["skew"], meta["sigmaDL"]],
+                               ref_sub["pdfx_moments"], rtol=1e-8)
+
+
+@pytest.mark.skipif(not FULL_FIXTURE.exists(), reason="full z_s=1 population (290 MB) not present")
+def test_full_chain_matches_stored_golden_pdf():
+    """All 201 xi groups: the oracle reproduces the reference's stored z_s=1 PDF."""
+    lam = LO.oracle_from_npz(FULL_FIXTURE)
+    ref = json.load(open(GOLDEN / "pdf_zs1.json"))
+    x = np.concatenate([ref["xi"], ref["xi_tail"]])
+    _, P, meta = IO.invert(lam, lam.sigma(), x)
+    P0 = np.concatenate([ref["P_s"], ref["P_s_tail"]])
+    assert np.max(np.abs(P - P0)) / P0.max() <= TOL_PEAK
+    assert meta["grid"]["nk_k"] == ref["grid"]["nk_k"] and meta["grid"]["nk_g"] == ref["grid"]["nk_g"]
