@@ -131,6 +131,24 @@ void sgl_invert_opts_default(sgl_invert_opts* opts);
 sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_invert_opts* opts,
                    double* P_out, sgl_invert_meta* meta);
 
+/* Allocation-free entry point ------------------------------------------------------------
+ * No counterpart in the reference.  For callers that may not allocate device memory (a host that
+ * gives its whole device budget to its own pool or caching allocator, or that forbids third-party
+ * allocations on its streams): computes the kappa-axis Poisson exponent
+ *     out[n] = sum_c w0_c (e^{i kk_n k0_c} - 1 - i kk_n k0_c)      (FP64; = sgl_lnphi at k_gamma = 0
+ *                                                                   for cells with V = 0 and no xi)
+ * with no cudaMalloc / cudaFree and no context.  Partial sums live in one fixed 8 MiB file-scope
+ * device array (16 x 32768 double2) that every GPU loading the library holds until exit; nk is
+ * limited to 32768 and larger nk is rejected (SGL_ERR_VALUE).  kk, k0, w0, out_re, out_im are
+ * device-accessible pointers; stream is a cudaStream_t (NULL = legacy default stream); the call
+ * is asynchronous on that stream.  The first call on each device resolves the array's device
+ * address (cudaGetSymbolAddress) with that device current: make it before any stream capture.
+ * All calls share the array, so calls that overlap on the GPU (other streams, other threads)
+ * race; every partial the call reads is written by the same call, so nothing needs clearing.
+ * Errors: sgl_last_error(NULL, ...). */
+sgl_status sgl_cf_kappa_noalloc(const double* kk, int nk, const double* k0, const double* w0,
+                                int64_t n_cells, double* out_re, double* out_im, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

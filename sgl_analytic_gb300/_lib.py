@@ -20,7 +20,8 @@ PRECISIONS = {"fp64": SGL_FP64, "mixed": SGL_MIXED}
 # every symbol the header declares (checked by the CPU test suite)
 EXPORTS = ("sgl_abi_version", "sgl_ctx_create", "sgl_ctx_destroy", "sgl_last_error", "sgl_ctx_stream",
            "sgl_ctx_profile", "sgl_stats_json", "sgl_lam_set_cells",
-           "sgl_lam_set_xi", "sgl_lam_sigma", "sgl_lnphi", "sgl_xi_term", "sgl_invert_opts_default", "sgl_pdf")
+           "sgl_lam_set_xi", "sgl_lam_sigma", "sgl_lnphi", "sgl_xi_term", "sgl_invert_opts_default", "sgl_pdf",
+           "sgl_cf_kappa_noalloc")
 
 
 class InvertOpts(C.Structure):
@@ -67,6 +68,8 @@ def lib():
         L.sgl_lam_sigma.argtypes = [vp, dp]
         L.sgl_lnphi.argtypes = [vp, dp, C.c_int, dp, C.c_int, C.c_int, dp, dp]
         L.sgl_xi_term.argtypes = [vp, dp, C.c_int, dp, C.c_int, C.c_int, dp, dp]
+        L.sgl_cf_kappa_noalloc.argtypes = [vp, C.c_int, vp, vp, C.c_int64, vp, vp, vp]
+        L.sgl_cf_kappa_noalloc.restype = C.c_int
         L.sgl_invert_opts_default.argtypes = [C.POINTER(InvertOpts)]
         L.sgl_invert_opts_default.restype = None
         L.sgl_pdf.argtypes = [vp, dp, C.c_int, C.POINTER(InvertOpts), dp, C.POINTER(InvertMeta)]

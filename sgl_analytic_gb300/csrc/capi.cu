@@ -696,6 +696,9 @@ double trapz(const double* y, const double* x, int n) {
 
 }  // namespace
 
+// Message of the last failed call that has no context (sgl_ctx_create, sgl_cf_kappa_noalloc).
+std::string& sgl_noctx_error() { return g_create_error; }
+
 // ================================================================== C ABI
 extern "C" {
 
