@@ -58,7 +58,7 @@ struct SepHost {
 
 struct XiHost {
     bool on = false;
-    int n_groups = 0, n_kmc = 0, n_gmc = 0, total_p = 0;
+    int n_groups = 0, n_kmc = 0, n_gmc = 0, total_p = 0, total_rows = 0;
     std::vector<int> m, r, nP;
     std::vector<long long> p_prefix_rowel;   // p_prefix (n_groups+1) then rowel_off (n_groups)
     std::vector<double> kmc, gmc;
@@ -94,6 +94,10 @@ struct sgl_ctx {
     XiDevice xid;
     SplineHost spline;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // pinned staging ring for small uploads (pageable copies would serialise host and device);
+    // reset whenever the stream has been synchronised
+    char* pinned = nullptr;
+    size_t pinned_cap = 0, pinned_off = 0;
     // per-kernel statistics (sgl_ctx_profile)
     bool profiling = false;
     long long launches_at_enable = 0;
@@ -139,10 +143,24 @@ T* dbuf(sgl_ctx* ctx, const std::string& name, size_t count) {
     T* var = dbuf<T>(ctx, name, (size_t)(count));                                             \
     if (!var) return fail(ctx, SGL_ERR_CUDA, std::string("device allocation failed: ") + name)
 
+sgl_status sync_stream(sgl_ctx* ctx) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->pinned_off = 0;
+    return SGL_OK;
+}
+
 template <typename T>
 sgl_status upload(sgl_ctx* ctx, T* dst, const T* src, size_t n) {
     if (n == 0) return SGL_OK;
-    CK(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    const size_t bytes = n * sizeof(T);
+    if (ctx->pinned && ctx->pinned_off + bytes <= ctx->pinned_cap) {
+        char* stage = ctx->pinned + ctx->pinned_off;
+        std::memcpy(stage, src, bytes);
+        ctx->pinned_off += (bytes + 255) & ~(size_t)255;
+        CK(cudaMemcpyAsync(dst, stage, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        return SGL_OK;
+    }
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
     return SGL_OK;
 }
 
@@ -222,11 +240,14 @@ GemmDesc<T> gd(int M, int N, int K, const void* A, long long ars, long long acs,
 // One GEMM with split-K when it would under-fill the GPU: K slices write workspace slices,
 // then a fixed-order sum (deterministic).
 template <typename T>
-sgl_status gemm_splitk(sgl_ctx* ctx, GemmDesc<T> g, const std::string& tag) {
+sgl_status gemm_splitk(sgl_ctx* ctx, GemmDesc<T> g, const std::string& tag, int min_split = 1) {
     GemmDesc<T> tmp = g;
     const int tiles = gemm_plan(&tmp, 1);
     int split = 1;
     if (tiles < 2 * kNumSMs) split = std::min(ceil_div(2 * kNumSMs, tiles), std::max(1, g.K / 512));
+    // min_split > 1 (mixed-precision transforms): FP32 partial sums over at most K / min_split
+    // terms, combined in FP64 -- shorter FP32 accumulation chains for the oscillatory sums
+    split = std::max(split, std::min(min_split, std::max(1, g.K / 32)));
     if (split <= 1) { std::vector<GemmDesc<T>> v{g}; return run_gemms(ctx, v, tag); }
     const long long slice = (long long)g.M * g.N;
     DBUF(ws, T, "splitk_ws_" + tag, slice * split);
@@ -375,6 +396,7 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
     CKS(upload(ctx, d_cb, cb.data(), cb.size()));
     CKS(upload(ctx, d_nodes, nodes.data(), nodes.size()));
     CK(cudaStreamSynchronize(ctx->stream));   // host staging vectors go out of scope
+    ctx->pinned_off = 0;
     SepDevice& D = ctx->sepd;
     D.n_cells = (int)N; D.n_groups = n_groups; D.n_cols = S.n_cols; D.n_cols_sep = n_cols_sep;
     D.nchunks = (int)cb.size() - 1;
@@ -449,10 +471,12 @@ sgl_status xi_eval(sgl_ctx* ctx, int precision, const double* d_kk, const double
     XiHost& X = ctx->xi;
     const cudaStream_t st = ctx->stream;
     if (nkg == 1 && h_kg[0] == 0.0 && X.R0 > 0) {
-        launch_xi_line_k(ctx->xid, d_kk, nk, d_re, d_im, st); CKLAUNCH(); return SGL_OK;
+        DBUF(d_part, double, "xi_line_part", 2LL * kLineChunks * nk);
+        launch_xi_line_k(ctx->xid, d_kk, nk, d_re, d_im, d_part, st); CKLAUNCH(); return SGL_OK;
     }
     if (nk == 1 && h_kk[0] == 0.0 && (X.Rm[0] + X.Rm[1] + X.Rm[2]) > 0) {
-        launch_xi_line_g(ctx->xid, d_kg, nkg, d_re, d_im, st); CKLAUNCH(); return SGL_OK;
+        DBUF(d_part, double, "xi_line_part", 2LL * kLineChunks * nkg);
+        launch_xi_line_g(ctx->xid, d_kg, nkg, d_re, d_im, d_part, st); CKLAUNCH(); return SGL_OK;
     }
     const size_t es = elem_size(precision);
     // offsets
@@ -468,7 +492,7 @@ sgl_status xi_eval(sgl_ctx* ctx, int precision, const double* d_kk, const double
     CKS(upload(ctx, d_off, T_off.data(), X.n_groups));
     CKS(upload(ctx, d_off + X.n_groups, E_off.data(), X.n_groups));
     CKS(upload(ctx, d_off + 2 * X.n_groups, G_off.data(), X.n_groups));
-    void* J = ctx->arena.get("xi_J", 3ULL * X.n_gmc * nkg * es);
+    void* J = ctx->arena.get("xi_J", 4ULL * X.n_gmc * nkg * es);
     void* T = ctx->arena.get("xi_T", (size_t)tT * es);
     void* E = ctx->arena.get("xi_E", (size_t)tE * es);
     void* G = ctx->arena.get("xi_G", (size_t)tG * es);
@@ -498,9 +522,21 @@ sgl_status xi_eval(sgl_ctx* ctx, int precision, const double* d_kk, const double
         }
         CKS(run_gemms(ctx, v, "xi"));
     }
+    double* d_V = nullptr;
+    if (precision == SGL_MIXED) {
+        // compensated m = 0 form: V = U (J0 - 1) in FP64 from an FP64 J0 - 1 table
+        d_V = dbuf<double>(ctx, "xi_V", (size_t)X.total_rows * nkg);
+        DBUF(d_J64, double, "xi_J64", 4LL * X.n_gmc * nkg);
+        if (!d_V) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (xi V)");
+        launch_bessel_tables(SGL_FP64, ctx->xid.gmc, X.n_gmc, d_kg, nkg, d_J64, st); CKLAUNCH();
+        launch_xi_V(ctx->xid, d_J64 + 3LL * X.n_gmc * nkg, nkg, d_V, X.total_rows, st); CKLAUNCH();
+    }
     {
+        const int nsplit = std::max(1, std::min(X.n_groups, 16));
+        DBUF(d_part, double, "xi_sq_part", 2LL * nsplit * nk * nkg);
         Timed t(ctx, "xi_square", 0.0, (double)tG * es);
-        launch_xi_square(precision, ctx->xid, d_off + 2 * X.n_groups, G, d_kk, nk, d_kg, nkg, d_re, d_im, st);
+        launch_xi_square(precision, ctx->xid, d_off + 2 * X.n_groups, G, d_kk, nk, d_kg, nkg, d_V, nsplit, d_part,
+                         d_re, d_im, st);
     }
     CKLAUNCH();
     return SGL_OK;
@@ -516,6 +552,8 @@ sgl_status sep_gemms(sgl_ctx* ctx, int precision, const double* h_kg, const doub
     const double Kg = nkg ? h_kg[nkg - 1] : 0.0;
     const int Nch = (S.n_cols_sep > 0 && Kg > 0) ? (int)(0.65 * S.max_sep_node * Kg + 50.0) : 0;
     const long long ld = 2LL * nk;
+    // mixed path: FP32 partial sums over at most ~32 K-terms per slice, slices combined in FP64
+    const int msplit = precision == SGL_FP64 ? 1 : 64;
     const double* d_nodes = (const double*)ctx->arena.find("sep_nodes");
     if (S.n_cols_sep > 0) {
         if (nkg > 1 && Nch > 0 && Nch < 0.6 * nkg && h_kg[0] >= 0.0) {
@@ -527,13 +565,13 @@ sgl_status sep_gemms(sgl_ctx* ctx, int precision, const double* h_kg, const doub
             if (!Bc || !L || !U) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (cheb)");
             launch_j0m1_table(precision, d_nodes, S.n_cols_sep, d_t, Nch, Bc, st); CKLAUNCH();
             launch_cheb_matrix(precision, Kg, Nch, d_kg, nkg, L, st); CKLAUNCH();
-            CKS(gemm_splitk<TT>(ctx, gd<TT>((int)ld, Nch, S.n_cols_sep, Tt, 1, ld, Bc, Nch, 1, U, Nch), "sep1"));
-            CKS(gemm_splitk<TT>(ctx, gd<TT>((int)ld, nkg, Nch, U, Nch, 1, L, 1, Nch, Gout, nkg), "sep2"));
+            CKS(gemm_splitk<TT>(ctx, gd<TT>((int)ld, Nch, S.n_cols_sep, Tt, 1, ld, Bc, Nch, 1, U, Nch), "sep1", msplit));
+            CKS(gemm_splitk<TT>(ctx, gd<TT>((int)ld, nkg, Nch, U, Nch, 1, L, 1, Nch, Gout, nkg), "sep2", msplit));
         } else {
             void* Bn = ctx->arena.get("sep_Bn", (size_t)S.n_cols_sep * nkg * sizeof(TT));
             if (!Bn) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (Bn)");
             launch_j0m1_table(precision, d_nodes, S.n_cols_sep, d_kg, nkg, Bn, st); CKLAUNCH();
-            CKS(gemm_splitk<TT>(ctx, gd<TT>((int)ld, nkg, S.n_cols_sep, Tt, 1, ld, Bn, nkg, 1, Gout, nkg), "sep1"));
+            CKS(gemm_splitk<TT>(ctx, gd<TT>((int)ld, nkg, S.n_cols_sep, Tt, 1, ld, Bn, nkg, 1, Gout, nkg), "sep1", msplit));
         }
     } else {
         CK(cudaMemsetAsync(Gout, 0, (size_t)ld * nkg * sizeof(TT), st));
@@ -543,7 +581,7 @@ sgl_status sep_gemms(sgl_ctx* ctx, int precision, const double* h_kg, const doub
         if (!Bd) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (Bd)");
         launch_j0m1_table(precision, d_nodes + S.n_cols_sep, S.n_direct, d_kg, nkg, Bd, st); CKLAUNCH();
         const TT* Td = (const TT*)Tt + (long long)S.n_cols_sep * ld;
-        CKS(gemm_splitk<TT>(ctx, gd<TT>((int)ld, nkg, S.n_direct, Td, 1, ld, Bd, nkg, 1, Gout, nkg, 1.0, 1.0), "sep3"));
+        CKS(gemm_splitk<TT>(ctx, gd<TT>((int)ld, nkg, S.n_direct, Td, 1, ld, Bd, nkg, 1, Gout, nkg, 1.0, 1.0), "sep3", msplit));
     }
     return SGL_OK;
 }
@@ -596,7 +634,8 @@ sgl_status lambda_eval(sgl_ctx* ctx, int precision, const double* h_kk, int nk, 
         const double* d_k0 = (const double*)ctx->arena.find("cells_k0");
         const double* d_g0 = (const double*)ctx->arena.find("cells_g0");
         const double* d_w0 = (const double*)ctx->arena.find("cells_w0");
-        launch_psi1_direct(d_kk, nk, d_kg, nkg, d_k0, d_g0, d_w0, (int64_t)ctx->w0.size(), d_dir, d_dir + npt, st);
+        DBUF(d_dpart, double2, "direct_part", (long long)std::max(1, psi1_direct_chunks((int64_t)ctx->w0.size())) * npt);
+        launch_psi1_direct(d_kk, nk, d_kg, nkg, d_k0, d_g0, d_w0, (int64_t)ctx->w0.size(), d_dir, d_dir + npt, d_dpart, st);
         CKLAUNCH();
         CK(cudaMemsetAsync(d_zero, 0, (size_t)nk * sizeof(double2), st));
         G = d_dir; A1 = d_zero; fin_precision = SGL_FP64;
@@ -668,7 +707,8 @@ sgl_status lambda_direct(sgl_ctx* ctx, const double* h_kk, int nk, const double*
     const double* d_k0 = (const double*)ctx->arena.find("cells_k0");
     const double* d_g0 = (const double*)ctx->arena.find("cells_g0");
     const double* d_w0 = (const double*)ctx->arena.find("cells_w0");
-    launch_psi1_direct(d_kk, nk, d_kg, nkg, d_k0, d_g0, d_w0, (int64_t)ctx->w0.size(), d_out, d_out + npt, st);
+    DBUF(d_dpart, double2, "direct_part", (long long)std::max(1, psi1_direct_chunks((int64_t)ctx->w0.size())) * npt);
+    launch_psi1_direct(d_kk, nk, d_kg, nkg, d_k0, d_g0, d_w0, (int64_t)ctx->w0.size(), d_out, d_out + npt, d_dpart, st);
     CKLAUNCH();
     bool xi = false;
     if (ctx->xi.on) {
@@ -677,7 +717,7 @@ sgl_status lambda_direct(sgl_ctx* ctx, const double* h_kk, int nk, const double*
     }
     std::vector<double> h((size_t)(4 * npt));
     CK(cudaMemcpyAsync(h.data(), d_out, (size_t)(xi ? 4 : 2) * npt * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
+    CKS(sync_stream(ctx));
     for (long long e = 0; e < npt; ++e) {
         const int n = (int)(e / nkg);
         double r = h[(size_t)e] - 0.5 * (h_kk[n] * h_kk[n] * ctx->V);
@@ -722,6 +762,11 @@ sgl_status sgl_ctx_create(int device, sgl_ctx** out) {
         g_create_error = "stream creation failed"; delete ctx; return SGL_ERR_CUDA;
     }
     for (auto& ev : ctx->ev) cudaEventCreate(&ev);
+    ctx->pinned_cap = 16u << 20;
+    if (cudaHostAlloc((void**)&ctx->pinned, ctx->pinned_cap, cudaHostAllocDefault) != cudaSuccess) {
+        ctx->pinned = nullptr; ctx->pinned_cap = 0;
+        cudaGetLastError();
+    }
     *out = ctx;
     return SGL_OK;
 }
@@ -734,6 +779,7 @@ void sgl_ctx_destroy(sgl_ctx* ctx) {
     for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
     resolve_stats(ctx);
     for (auto& ev : ctx->ev_pool) cudaEventDestroy(ev);
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -857,8 +903,9 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
     }
     if (s0_override > 0) s0 = s0_override;
     // device staging
-    std::vector<int> g_m, g_r, g_nP, idx_p, p_ptr{0}, ent_qg;
-    std::vector<long long> g_p_off, g_ent_off, g_row_off, p_prefix{0}, rowel_off;
+    std::vector<int> g_m, g_r, g_nP, idx_p, p_ptr{0}, ent_qg, g_nQ, idx_q;
+    std::vector<long long> g_p_off, g_ent_off, g_row_off, p_prefix{0}, rowel_off, g_q_off, g_u_off;
+    std::vector<double> U0;
     std::vector<double> rows_t, res, sum_rows;
     std::vector<double> W0, res0, sum0, U[3], resm[3], summ[3];
     long long ent_total = 0, row_total = 0, rowel_total = 0;
@@ -931,6 +978,25 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
             }
             X.Rm[mg] += R;
         }
+        // unique q of the group and U = sum over p of the rows (compensated m = 0 form)
+        {
+            std::vector<int> qs(qg.begin(), qg.end());
+            std::sort(qs.begin(), qs.end());
+            qs.erase(std::unique(qs.begin(), qs.end()), qs.end());
+            std::vector<int> qpos(X.n_gmc, -1);
+            for (size_t i = 0; i < qs.size(); ++i) qpos[qs[i]] = (int)i;
+            g_q_off.push_back((long long)idx_q.size());
+            g_u_off.push_back((long long)U0.size());
+            g_nQ.push_back((int)qs.size());
+            idx_q.insert(idx_q.end(), qs.begin(), qs.end());
+            const size_t base = U0.size();
+            U0.resize(base + (size_t)R * qs.size(), 0.0);
+            if (mg == 0)
+                for (int rr = 0; rr < R; ++rr) {
+                    const double* row = rows + row_off[g] + (long long)keep[rr] * w;
+                    for (int e = 0; e < nidx[g]; ++e) U0[base + (size_t)rr * qs.size() + qpos[qg[e]]] += row[e];
+                }
+        }
         g_m.push_back(mg); g_r.push_back(R); g_nP.push_back(nP);
         g_p_off.push_back(p_prefix.back());
         g_ent_off.push_back(ent_total);
@@ -944,6 +1010,7 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
     }
     X.n_groups = (int)g_m.size();
     X.total_p = (int)p_prefix.back();
+    X.total_rows = (int)row_total;
     X.sigma_var = sigma_var;
     X.on = X.n_groups > 0;
     // upload
@@ -986,6 +1053,24 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         D.g_m = d_gm; D.g_r = d_gr; D.g_nP = d_gnP;
         D.g_p_off = d_goff; D.g_ent_off = d_goff + X.n_groups; D.g_row_off = d_goff + 2 * X.n_groups;
         D.idx_p = d_idxp; D.p_ptr = d_pptr; D.ent_qg = d_qg; D.rows = d_rows; D.res = d_res; D.sum_rows = d_sum;
+        {
+            std::vector<float> rf(rows_t.begin(), rows_t.end());
+            DBUF(d_rowsf, float, "xi_rows_f", rf.size());
+            CKS(upload(ctx, d_rowsf, rf.data(), rf.size()));
+            DBUF(d_gnQ, int, "xi_gnQ", g_nQ.size());
+            DBUF(d_qoff, long long, "xi_qoff", g_q_off.size());
+            DBUF(d_uoff, long long, "xi_uoff", g_u_off.size());
+            DBUF(d_idxq, int, "xi_idxq", idx_q.size());
+            DBUF(d_U0, double, "xi_Usum", U0.size());
+            CKS(upload(ctx, d_gnQ, g_nQ.data(), g_nQ.size()));
+            CKS(upload(ctx, d_qoff, g_q_off.data(), g_q_off.size()));
+            CKS(upload(ctx, d_uoff, g_u_off.data(), g_u_off.size()));
+            CKS(upload(ctx, d_idxq, idx_q.data(), idx_q.size()));
+            CKS(upload(ctx, d_U0, U0.data(), U0.size()));
+            CK(cudaStreamSynchronize(ctx->stream));   // rf is a local staging vector
+            D.rows_f = d_rowsf; D.g_nQ = d_gnQ; D.g_q_off = d_qoff; D.g_u_off = d_uoff; D.idx_q = d_idxq; D.U0 = d_U0;
+            D.r_max = *std::max_element(g_r.begin(), g_r.end());
+        }
         D.R0 = X.R0;
         if (X.R0 > 0) {
             DBUF(d_W0, double, "xi_W0", W0.size());
@@ -1041,7 +1126,7 @@ sgl_status sgl_lnphi(sgl_ctx* ctx, const double* kk, int nkk, const double* kg, 
     CKS(lambda_eval(ctx, precision, kk, nkk, kg, nkg, 0, d_re, d_im));
     CK(cudaMemcpyAsync(out_re, d_re, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(out_im, d_im, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+    CKS(sync_stream(ctx));
     for (long long e = 0; e < npt; ++e)
         if (!std::isfinite(out_re[e]) || !std::isfinite(out_im[e])) return fail(ctx, SGL_ERR_NONFINITE, "non-finite ln Phi");
     return SGL_OK;
@@ -1065,7 +1150,7 @@ sgl_status sgl_xi_term(sgl_ctx* ctx, const double* kk, int nkk, const double* kg
     CKS(xi_eval(ctx, precision, d_kk, kk, nkk, d_kg, kg, nkg, d_o, d_o + npt));
     CK(cudaMemcpyAsync(out_re, d_o, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(out_im, d_o + npt, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+    CKS(sync_stream(ctx));
     return SGL_OK;
 }
 
@@ -1092,6 +1177,7 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
         return fail(ctx, SGL_ERR_VALUE, "invalid inversion options");
     for (int i = 0; i < n_xi; ++i) if (!std::isfinite(xi_out[i])) return fail(ctx, SGL_ERR_VALUE, "non-finite xi_out");
     CK(cudaSetDevice(ctx->device));
+    CKS(sync_stream(ctx));
     const cudaStream_t st = ctx->stream;
     double sigma;
     CKS(sgl_lam_sigma(ctx, &sigma));
@@ -1183,13 +1269,13 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
     if (P == SGL_FP64) {
         CKS(gemm_splitk<double>(ctx, gd<double>(2 * nk, ngam, nkg, Phi, nkg, 1, M, ldF, 1, F, ldF), "hankel"));
     } else {
-        CKS(gemm_splitk<float>(ctx, gd<float>(2 * nk, ngam, nkg, Phi, nkg, 1, M, ldF, 1, F, ldF), "hankel"));
+        CKS(gemm_splitk<float>(ctx, gd<float>(2 * nk, ngam, nkg, Phi, nkg, 1, M, ldF, 1, F, ldF), "hankel", 128));
     }
     launch_em_columns(P, Phi, nk, nkg, dkg, F, ldF, ngam, st); CKLAUNCH();
     if (P == SGL_FP64) {
         CKS(gemm_splitk<double>(ctx, gd<double>(nkap, ldF, 2 * nk, CS, 2 * nk, 1, F, ldF, 1, P3e, ldF, c), "kappa"));
     } else {
-        CKS(gemm_splitk<float>(ctx, gd<float>(nkap, ldF, 2 * nk, CS, 2 * nk, 1, F, ldF, 1, P3e, ldF, c), "kappa"));
+        CKS(gemm_splitk<float>(ctx, gd<float>(nkap, ldF, 2 * nk, CS, 2 * nk, 1, F, ldF, 1, P3e, ldF, c), "kappa", 128));
     }
     launch_p3_finish(P, P3e, nkap, ngam, ldF, d_gam, d_P3, st); CKLAUNCH();
     cudaEventRecord(ctx->ev[2], st);
@@ -1211,7 +1297,7 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
     cudaEventRecord(ctx->ev[3], st);
     std::vector<double> pall(xall.size());
     CK(cudaMemcpyAsync(pall.data(), d_pi, pall.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
+    CKS(sync_stream(ctx));
     // ---- normalisation and moments (sgl_full.py:362-372)
     const double* pw = pall.data();
     const double norm = trapz(pw, xw.data(), nw);

@@ -30,10 +30,10 @@ __global__ void k_sum_slices(const T* __restrict__ ws, int ns, int rows, int col
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long n = (long long)rows * cols;
     if (e >= n) return;
-    T acc = T(0);
-    for (int s = 0; s < ns; ++s) acc += ws[(long long)s * n + e];
+    double acc = 0.0;                         // slices summed in FP64 in both precisions
+    for (int s = 0; s < ns; ++s) acc += (double)ws[(long long)s * n + e];
     T* o = out + (e / cols) * ldo + (e % cols);
-    *o = (beta != T(0)) ? acc + beta * *o : acc;
+    *o = (beta != T(0)) ? (T)(acc + (double)beta * (double)*o) : (T)acc;
 }
 
 template <typename T>

@@ -97,7 +97,7 @@ void launch_p3_finish(int precision, const void* P3ext, int nkap, int ngam, int 
 // ------------------------------------------------------------------ path integral
 // Uniform axis a_i = a0 + i h (i < n-1), a_{n-1} = a1 (numpy linspace).  Interval index as
 // RegularGridInterpolator: i = (#nodes < x) - 1 clipped to [0, n-2]; x outside [a0, a1] -> -1.
-struct Axis { double a0, a1, h; int n; };
+struct Axis { double a0, a1, h, inv_h; int n; };
 
 // numpy rounds i * step and + start separately: no FMA contraction here
 __device__ inline double axis_node(const Axis& A, int i) {
@@ -106,13 +106,14 @@ __device__ inline double axis_node(const Axis& A, int i) {
 
 __device__ inline int axis_find(const Axis& A, double x, double& t) {
     if (!(x >= A.a0 && x <= A.a1)) return -1;
-    int i = (int)floor((x - A.a0) / A.h);
+    int i = (int)((x - A.a0) * A.inv_h);                  // guess, then exact node comparisons
     i = max(0, min(i, A.n - 1));
-    while (i + 1 < A.n && axis_node(A, i + 1) < x) ++i;   // largest i with node_i < x
-    while (i > 0 && !(axis_node(A, i) < x)) --i;
-    i = min(i, A.n - 2);
-    const double lo = axis_node(A, i), hi = axis_node(A, i + 1);
-    t = (x - lo) / (hi - lo);
+    double lo = axis_node(A, i);
+    while (i > 0 && !(lo < x)) { --i; lo = axis_node(A, i); }
+    double nx = axis_node(A, min(i + 1, A.n - 1));
+    while (i + 1 < A.n && nx < x) { ++i; lo = nx; nx = axis_node(A, min(i + 1, A.n - 1)); }
+    if (i > A.n - 2) { i = A.n - 2; lo = axis_node(A, i); nx = axis_node(A, i + 1); }
+    t = (x - lo) / (nx - lo);
     return i;
 }
 
@@ -130,53 +131,78 @@ __device__ inline double lin(double a, double b, int n, int i) {     // numpy li
     return (i == n - 1) ? b : __dadd_rn(__dmul_rn((double)i, (b - a) / (double)(n - 1)), a);
 }
 
+constexpr int kPathSmem = 4096;      // path points kept in shared memory (larger paths: 2 evaluations)
+
+// One CTA per xi.  Body: n_k_int points kappa in [lo, hi], gamma = sqrt((hi - k)(1 - k + 1/sqrt(mu))),
+// trapezoid in kappa; tail (gamma in (g_def, gb]) parametrised in gamma with weight gamma / r.
 __global__ void __launch_bounds__(256)
 k_path_integral(const double* __restrict__ P3, Axis K, Axis G, const double* __restrict__ xi, double gmax,
                 double g_def, int n_k_int, double* __restrict__ out) {
     __shared__ double sh[32];
+    __shared__ double sv[kPathSmem];
     const double x = xi[blockIdx.x];
     const double mu = exp(x);
     const double rm = 1.0 / sqrt(mu);
     const double hi = 1.0 - rm;
     const double lo = fmax(K.a0, 1.0 - sqrt(1.0 / mu + g_def * g_def));
     const double pref = M_PI / (mu * mu);
-    double acc = 0.0;
     const bool body = hi > lo;
-    if (body) {
+    if (!body) { if (threadIdx.x == 0) out[blockIdx.x] = 0.0; return; }
+    double acc = 0.0;
+    if (n_k_int <= kPathSmem) {
+        for (int i = threadIdx.x; i < n_k_int; i += blockDim.x) {
+            const double k0 = lin(lo, hi, n_k_int, i);
+            const double g0 = sqrt(fmax((hi - k0) * (1.0 - k0 + rm), 0.0));
+            sv[i] = bilinear(P3, K, G, k0, g0);
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < n_k_int - 1; i += blockDim.x)
+            acc += (lin(lo, hi, n_k_int, i + 1) - lin(lo, hi, n_k_int, i)) * (sv[i] + sv[i + 1]) / 2.0;
+    } else {
         for (int i = threadIdx.x; i < n_k_int - 1; i += blockDim.x) {
             const double k0 = lin(lo, hi, n_k_int, i), k1 = lin(lo, hi, n_k_int, i + 1);
             const double g0 = sqrt(fmax((hi - k0) * (1.0 - k0 + rm), 0.0));
             const double g1 = sqrt(fmax((hi - k1) * (1.0 - k1 + rm), 0.0));
-            const double v0 = bilinear(P3, K, G, k0, g0), v1 = bilinear(P3, K, G, k1, g1);
-            acc += (k1 - k0) * (v0 + v1) / 2.0;
+            acc += (k1 - k0) * (bilinear(P3, K, G, k0, g0) + bilinear(P3, K, G, k1, g1)) / 2.0;
         }
     }
     double total = pref * block_sum(acc, sh);
-    if (body && gmax > g_def && lo > K.a0) {
+    if (gmax > g_def && lo > K.a0) {
         const double gb = fmin(gmax, sqrt(fmax((hi - K.a0) * (1.0 - K.a0 + rm), 0.0)));
         if (gb > g_def) {
-            const double dgam = G.h;
-            const int n = (int)ceil((gb - g_def) / (0.5 * dgam)) + 1;
+            const int n = (int)ceil((gb - g_def) / (0.5 * G.h)) + 1;
             double acc2 = 0.0;
-            for (int i = threadIdx.x; i < n - 1; i += blockDim.x) {
-                const double ga = lin(g_def, gb, n, i), gc = lin(g_def, gb, n, i + 1);
-                const double ra = sqrt(1.0 / mu + ga * ga), rc = sqrt(1.0 / mu + gc * gc);
-                const double ka = fmin(fmax(1.0 - ra, K.a0), K.a1), kc = fmin(fmax(1.0 - rc, K.a0), K.a1);
-                const double va = bilinear(P3, K, G, ka, ga) * (ga / ra);
-                const double vc = bilinear(P3, K, G, kc, gc) * (gc / rc);
-                acc2 += (gc - ga) * (va + vc) / 2.0;
+            if (n <= kPathSmem) {
+                __syncthreads();
+                for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                    const double ga = lin(g_def, gb, n, i);
+                    const double ra = sqrt(1.0 / mu + ga * ga);
+                    const double ka = fmin(fmax(1.0 - ra, K.a0), K.a1);
+                    sv[i] = bilinear(P3, K, G, ka, ga) * (ga / ra);
+                }
+                __syncthreads();
+                for (int i = threadIdx.x; i < n - 1; i += blockDim.x)
+                    acc2 += (lin(g_def, gb, n, i + 1) - lin(g_def, gb, n, i)) * (sv[i] + sv[i + 1]) / 2.0;
+            } else {
+                for (int i = threadIdx.x; i < n - 1; i += blockDim.x) {
+                    const double ga = lin(g_def, gb, n, i), gc = lin(g_def, gb, n, i + 1);
+                    const double ra = sqrt(1.0 / mu + ga * ga), rc = sqrt(1.0 / mu + gc * gc);
+                    const double ka = fmin(fmax(1.0 - ra, K.a0), K.a1), kc = fmin(fmax(1.0 - rc, K.a0), K.a1);
+                    acc2 += (gc - ga) * (bilinear(P3, K, G, ka, ga) * (ga / ra) + bilinear(P3, K, G, kc, gc) * (gc / rc)) / 2.0;
+                }
             }
             total += pref * block_sum(acc2, sh);
         }
     }
-    if (threadIdx.x == 0) out[blockIdx.x] = body ? total : 0.0;
+    if (threadIdx.x == 0) out[blockIdx.x] = total;
 }
 
 void launch_path_integral(const double* P3, int nkap, int ngam, double kap0, double kap1, double gam1,
                           const double* xi, int nxi, double gmax, double g_def, int n_k_int, double* out,
                           cudaStream_t st) {
-    Axis K{kap0, kap1, (kap1 - kap0) / (nkap - 1), nkap};
-    Axis G{0.0, gam1, gam1 / (ngam - 1), ngam};
+    const double hk = (kap1 - kap0) / (nkap - 1), hg = gam1 / (ngam - 1);
+    Axis K{kap0, kap1, hk, 1.0 / hk, nkap};
+    Axis G{0.0, gam1, hg, 1.0 / hg, ngam};
     if (nxi > 0) { k_path_integral<<<nxi, 256, 0, st>>>(P3, K, G, xi, gmax, g_def, n_k_int, out); SGL_COUNT(1); }
 }
 

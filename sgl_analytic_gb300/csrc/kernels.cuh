@@ -22,9 +22,10 @@ struct SepDevice {
 };
 
 // ---- Psi_1
+int psi1_direct_chunks(int64_t nc);
 void launch_psi1_direct(const double* kk, int nk, const double* kg, int nkg, const double* k0,
                         const double* g0, const double* w0, int64_t nc, double* re, double* im,
-                        cudaStream_t st);
+                        double2* part, cudaStream_t st);
 void launch_sep_sweep(int precision, const double* kk, int nk, const SepDevice& s, void* Tt,
                       double2* A_part, double2* A1, cudaStream_t st);
 void launch_j0m1_table(int precision, const double* nodes, int nn, const double* x, int nx, void* B,
@@ -54,6 +55,13 @@ struct XiDevice {
     const int* p_ptr = nullptr;        // CSR over local p: entries [p_ptr[p], p_ptr[p+1]) (group relative)
     const int* ent_qg = nullptr;       // global gamma-centre index of each entry
     const double* rows = nullptr;      // rows: entry-major per group: rows[(ent_off + e) * r + rr]
+    const float* rows_f = nullptr;     // float copy of rows (mixed path)
+    int r_max = 0;                     // largest group row count
+    const int* g_nQ = nullptr;         // unique gamma cells per group
+    const long long* g_q_off = nullptr;   // into idx_q
+    const long long* g_u_off = nullptr;   // into U0 (r x nQ per group)
+    const int* idx_q = nullptr;        // global gamma-centre index of each local q
+    const double* U0 = nullptr;        // sum over p of the rows (m = 0 groups; zeros otherwise)
     const double* res = nullptr;       // [total rows]
     const double* sum_rows = nullptr;  // [total rows]
     // 1-D reach paths
@@ -67,15 +75,20 @@ struct XiDevice {
     const double* summ[3] = {nullptr, nullptr, nullptr};
 };
 
-void launch_xi_line_k(const XiDevice& x, const double* kk, int nk, double* out_re, double* out_im, cudaStream_t st);
-void launch_xi_line_g(const XiDevice& x, const double* kg, int nkg, double* out_re, double* out_im, cudaStream_t st);
+void launch_xi_line_k(const XiDevice& x, const double* kk, int nk, double* out_re, double* out_im, double* part,
+                      cudaStream_t st);
+void launch_xi_line_g(const XiDevice& x, const double* kg, int nkg, double* out_re, double* out_im, double* part,
+                      cudaStream_t st);
+constexpr int kLineChunks = 32;   // row chunks of the 1-D reach paths (part: 3 * kLineChunks * points)
 void launch_bessel_tables(int precision, const double* gmc, int n_gmc, const double* kg, int nkg, void* J, cudaStream_t st);
 void launch_xi_stageA(int precision, const XiDevice& x, const long long* h_p_prefix, int total_p, const long long* T_off,
                       const void* J, int nkg, void* T, cudaStream_t st);
 void launch_xi_E(int precision, const XiDevice& x, const double* kk, int nk, const long long* E_off,
                  const long long* h_p_prefix, int total_p, void* E, cudaStream_t st);
 void launch_xi_square(int precision, const XiDevice& x, const long long* G_off, const void* G, const double* kk, int nk,
-                      const double* kg, int nkg, double* out_re, double* out_im, cudaStream_t st);
+                      const double* kg, int nkg, const double* V, int nsplit, double* part, double* out_re,
+                      double* out_im, cudaStream_t st);
+void launch_xi_V(const XiDevice& x, const double* J0m1, int nkg, double* V, int total_rows, cudaStream_t st);
 
 // ---- spline + composition
 struct SplineAxis {              // per evaluation point: interval l (first coefficient) + 4 weights

@@ -55,18 +55,22 @@ __device__ inline void halfangle_sincos_ff(ff k, ff kap, float& s, float& c, flo
 }
 
 // ------------------------------------------------------------------ direct sum
-// One CTA per output point (n, m); threads stride over the cells; deterministic block sum.
+// CTA (output point, cell chunk); threads stride over the chunk's cells; deterministic block sum
+// into part[chunk, point]; a second kernel sums the chunks in a fixed order.
+constexpr int kDirectChunkCells = 4096;
+
 __global__ void __launch_bounds__(256)
 k_psi1_direct(const double* __restrict__ kk, int nk, const double* __restrict__ kg, int nkg,
               const double* __restrict__ k0, const double* __restrict__ g0,
-              const double* __restrict__ w0, int64_t nc, double* __restrict__ out_re,
-              double* __restrict__ out_im) {
+              const double* __restrict__ w0, int64_t nc, double2* __restrict__ part) {
     __shared__ double sh[32];
     const int pt = blockIdx.x;
     const int n = pt / nkg, m = pt % nkg;
     const double k = kk[n], g = kg[m];
+    const int64_t c0 = (int64_t)blockIdx.y * kDirectChunkCells;
+    const int64_t c1 = c0 + kDirectChunkCells < nc ? c0 + kDirectChunkCells : nc;
     double re = 0.0, im = 0.0;
-    for (int64_t c = threadIdx.x; c < nc; c += blockDim.x) {
+    for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
         const double w = w0[c];
         const double ph = k * k0[c];
         const double x = g * g0[c];
@@ -82,14 +86,30 @@ k_psi1_direct(const double* __restrict__ kk, int nk, const double* __restrict__ 
     }
     re = block_sum(re, sh);
     im = block_sum(im, sh);
-    if (threadIdx.x == 0) { out_re[pt] = re; out_im[pt] = im; }
+    if (threadIdx.x == 0) part[(long long)blockIdx.y * gridDim.x + pt] = make_double2(re, im);
 }
+
+__global__ void k_direct_reduce(const double2* __restrict__ part, int nchunks, int npt, double* __restrict__ re,
+                                double* __restrict__ im) {
+    const int pt = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pt >= npt) return;
+    double r = 0.0, i = 0.0;
+    for (int c = 0; c < nchunks; ++c) { const double2 v = part[(long long)c * npt + pt]; r += v.x; i += v.y; }
+    re[pt] = r;
+    im[pt] = i;
+}
+
+int psi1_direct_chunks(int64_t nc) { return (int)((nc + kDirectChunkCells - 1) / kDirectChunkCells); }
 
 void launch_psi1_direct(const double* kk, int nk, const double* kg, int nkg, const double* k0,
                         const double* g0, const double* w0, int64_t nc, double* re, double* im,
-                        cudaStream_t st) {
-    if (nk * (long long)nkg == 0) return;
-    { k_psi1_direct<<<nk * nkg, 256, 0, st>>>(kk, nk, kg, nkg, k0, g0, w0, nc, re, im); SGL_COUNT(1); }
+                        double2* part, cudaStream_t st) {
+    const int npt = nk * nkg;
+    if (npt == 0) return;
+    const int nch = psi1_direct_chunks(nc) > 0 ? psi1_direct_chunks(nc) : 1;
+    dim3 grid(npt, nch);
+    { k_psi1_direct<<<grid, 256, 0, st>>>(kk, nk, kg, nkg, k0, g0, w0, nc, part); SGL_COUNT(1); }
+    { k_direct_reduce<<<ceil_div(npt, 256), 256, 0, st>>>(part, nch, npt, re, im); SGL_COUNT(1); }
 }
 
 // ------------------------------------------------------------------ separable sweep

@@ -28,21 +28,22 @@ __device__ inline double bessel_jm(int m, double x) {
     return m == 0 ? j0(x) : (m == 1 ? j1(x) : bessel_j2(x));
 }
 
-// J[m][q][j] = J_m(gmc[q] * kg[j]), m = 0, 1, 2
+// J[m][q][j] = J_m(gmc[q] * kg[j]) for m = 0, 1, 2 and, as table 3, J0 - 1 without cancellation
 template <typename TT>
 __global__ void k_bessel_tables(const double* __restrict__ gmc, int n_gmc, const double* __restrict__ kg, int nkg,
                                 TT* __restrict__ J) {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long per = (long long)n_gmc * nkg;
-    if (e >= 3 * per) return;
+    if (e >= 4 * per) return;
     const int m = (int)(e / per);
     const long long r = e % per;
     const int q = (int)(r / nkg), j = (int)(r % nkg);
-    J[e] = (TT)bessel_jm(m, gmc[q] * kg[j]);
+    const double x = gmc[q] * kg[j];
+    J[e] = (TT)(m < 3 ? bessel_jm(m, x) : j0m1_d(x));
 }
 
 void launch_bessel_tables(int precision, const double* gmc, int n_gmc, const double* kg, int nkg, void* J, cudaStream_t st) {
-    const long long tot = 3LL * n_gmc * nkg;
+    const long long tot = 4LL * n_gmc * nkg;
     if (precision == SGL_FP64) { k_bessel_tables<double><<<ceil_div(tot, 256), 256, 0, st>>>(gmc, n_gmc, kg, nkg, (double*)J); SGL_COUNT(1); }
     else { k_bessel_tables<float><<<ceil_div(tot, 256), 256, 0, st>>>(gmc, n_gmc, kg, nkg, (float*)J); SGL_COUNT(1); }
 }
@@ -56,11 +57,67 @@ __device__ inline int find_group(const long long* prefix, int ng, long long v) {
     return lo;
 }
 
-// stage A: one CTA per (group, local p); threads over (r, j)
+// stage A: one CTA per (group, local p); threads over (r, j).  The p-row's entries (their rows
+// and J_m rows) are staged in shared memory; accumulation in TT (FP64 path: double).
+constexpr int kStageAEnt = 32;
 template <typename TT>
 __global__ void __launch_bounds__(256)
 k_xi_stageA(XiDevice x, const long long* __restrict__ p_prefix, const long long* __restrict__ T_off,
             const long long* __restrict__ rowel_off, const TT* __restrict__ J, int nkg, TT* __restrict__ T) {
+    extern __shared__ unsigned char smraw[];
+    TT* s_rows = (TT*)smraw;                                  // [kStageAEnt][r]
+    const long long P = blockIdx.x;
+    const int g = find_group(p_prefix, x.n_groups, P);
+    const int p = (int)(P - p_prefix[g]);
+    const int r = x.g_r[g], m = x.g_m[g];
+    TT* s_J = s_rows + kStageAEnt * r;                        // [kStageAEnt][nkg]
+    const int e0 = x.p_ptr[P], e1 = x.p_ptr[P + 1];
+    const long long ent0 = x.g_ent_off[g];
+    const TT* Jm = J + (long long)m * x.n_gmc * nkg;
+    TT* Tg = T + T_off[g] + (long long)p * r * nkg;
+    const double* rows = x.rows + rowel_off[g];
+    const float* rows_f = x.rows_f ? x.rows_f + rowel_off[g] : nullptr;
+    constexpr int kMaxOut = 24;                               // outputs per thread (r * nkg <= 256 * 24)
+    TT acc[kMaxOut];
+#pragma unroll
+    for (int i = 0; i < kMaxOut; ++i) acc[i] = TT(0);
+    const int nout = r * nkg;
+    for (int eb = e0; eb < e1; eb += kStageAEnt) {
+        const int cnt = min(kStageAEnt, e1 - eb);
+        __syncthreads();
+        for (int t = threadIdx.x; t < cnt * r; t += blockDim.x) {
+            const int e = t / r, rr = t % r;
+            const long long el = (long long)(eb + e) - ent0;
+            s_rows[e * r + rr] = (sizeof(TT) == 4 && rows_f) ? (TT)rows_f[el * r + rr] : (TT)rows[el * r + rr];
+        }
+        for (int t = threadIdx.x; t < cnt * nkg; t += blockDim.x) {
+            const int e = t / nkg, j = t % nkg;
+            s_J[e * nkg + j] = Jm[(long long)x.ent_qg[eb + e] * nkg + j];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < kMaxOut; ++i) {
+            const int t = threadIdx.x + i * blockDim.x;
+            if (t < nout) {
+                const int rr = t / nkg, j = t % nkg;
+                TT a = acc[i];
+                for (int e = 0; e < cnt; ++e) a = fma(s_rows[e * r + rr], s_J[e * nkg + j], a);
+                acc[i] = a;
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < kMaxOut; ++i) {
+        const int t = threadIdx.x + i * blockDim.x;
+        if (t < nout) Tg[t] = acc[i];
+    }
+}
+
+// Generic stage A (any grid width): no staging, FP64 accumulation.
+template <typename TT>
+__global__ void __launch_bounds__(256)
+k_xi_stageA_generic(XiDevice x, const long long* __restrict__ p_prefix, const long long* __restrict__ T_off,
+                    const long long* __restrict__ rowel_off, const TT* __restrict__ J, int nkg, TT* __restrict__ T) {
     const long long P = blockIdx.x;
     const int g = find_group(p_prefix, x.n_groups, P);
     const int p = (int)(P - p_prefix[g]);
@@ -70,8 +127,8 @@ k_xi_stageA(XiDevice x, const long long* __restrict__ p_prefix, const long long*
     const TT* Jm = J + (long long)m * x.n_gmc * nkg;
     TT* Tg = T + T_off[g] + (long long)p * r * nkg;
     const double* rows = x.rows + rowel_off[g];
-    for (int t = threadIdx.x; t < r * nkg; t += blockDim.x) {
-        const int rr = t / nkg, j = t % nkg;
+    for (long long t = threadIdx.x; t < (long long)r * nkg; t += blockDim.x) {
+        const int rr = (int)(t / nkg), j = (int)(t % nkg);
         double acc = 0.0;
         for (int e = e0; e < e1; ++e) {
             const long long el = e - ent0;
@@ -85,25 +142,41 @@ void launch_xi_stageA(int precision, const XiDevice& x, const long long* d_p_pre
                       const void* J, int nkg, void* T, cudaStream_t st) {
     // rowel_off is stored right after p_prefix in the same device block (see capi)
     const long long* rowel_off = d_p_prefix + (x.n_groups + 1);
-    if (precision == SGL_FP64)
-        { k_xi_stageA<double><<<total_p, 256, 0, st>>>(x, d_p_prefix, T_off, rowel_off, (const double*)J, nkg, (double*)T); SGL_COUNT(1); }
-    else
-        { k_xi_stageA<float><<<total_p, 256, 0, st>>>(x, d_p_prefix, T_off, rowel_off, (const float*)J, nkg, (float*)T); SGL_COUNT(1); }
+    const int rmax = x.r_max;
+    if (nkg > 128 || (long long)rmax * nkg > 256LL * 24) {
+        if (precision == SGL_FP64) { k_xi_stageA_generic<double><<<total_p, 256, 0, st>>>(x, d_p_prefix, T_off, rowel_off, (const double*)J, nkg, (double*)T); SGL_COUNT(1); }
+        else { k_xi_stageA_generic<float><<<total_p, 256, 0, st>>>(x, d_p_prefix, T_off, rowel_off, (const float*)J, nkg, (float*)T); SGL_COUNT(1); }
+        return;
+    }
+    if (precision == SGL_FP64) {
+        const size_t sm = (size_t)kStageAEnt * (rmax + nkg) * sizeof(double);
+        k_xi_stageA<double><<<total_p, 256, sm, st>>>(x, d_p_prefix, T_off, rowel_off, (const double*)J, nkg, (double*)T);
+        SGL_COUNT(1);
+    } else {
+        const size_t sm = (size_t)kStageAEnt * (rmax + nkg) * sizeof(float);
+        k_xi_stageA<float><<<total_p, 256, sm, st>>>(x, d_p_prefix, T_off, rowel_off, (const float*)J, nkg, (float*)T);
+        SGL_COUNT(1);
+    }
 }
 
 // E_g[i, p] = cos(kk_i kap_p) (i < nk) / sin(kk_{i-nk} kap_p): one CTA per global p
+// comp = 1 (mixed path): m = 0 groups get cos - 1 = -2 sin^2(x/2) in place of cos, so that
+// G_r = sum (cos - 1) T + sum_q U (J0 - 1) carries no cancellation against sum_rows.
 template <typename TT>
 __global__ void k_xi_E(XiDevice x, const double* __restrict__ kk, int nk, const long long* __restrict__ E_off,
-                       const long long* __restrict__ p_prefix, TT* __restrict__ E) {
+                       const long long* __restrict__ p_prefix, TT* __restrict__ E, int comp) {
     const long long P = blockIdx.x;
     const int g = find_group(p_prefix, x.n_groups, P);
     const int p = (int)(P - p_prefix[g]);
     const int nP = x.g_nP[g];
+    const bool cm1 = comp && x.g_m[g] == 0;
     const double kap = x.kmc[x.idx_p[P]];
     TT* Eg = E + E_off[g];
     for (int i = threadIdx.x; i < nk; i += blockDim.x) {
         double s, c;
-        sincos(kk[i] * kap, &s, &c);
+        const double ph = kk[i] * kap;
+        sincos(ph, &s, &c);
+        if (cm1) { const double h = sin(0.5 * ph); c = -2.0 * h * h; }
         Eg[(long long)i * nP + p] = (TT)c;
         Eg[(long long)(nk + i) * nP + p] = (TT)s;
     }
@@ -111,55 +184,106 @@ __global__ void k_xi_E(XiDevice x, const double* __restrict__ kk, int nk, const 
 
 void launch_xi_E(int precision, const XiDevice& x, const double* kk, int nk, const long long* E_off,
                  const long long* d_p_prefix, int total_p, void* E, cudaStream_t st) {
-    if (precision == SGL_FP64) { k_xi_E<double><<<total_p, 128, 0, st>>>(x, kk, nk, E_off, d_p_prefix, (double*)E); SGL_COUNT(1); }
-    else { k_xi_E<float><<<total_p, 128, 0, st>>>(x, kk, nk, E_off, d_p_prefix, (float*)E); SGL_COUNT(1); }
+    if (precision == SGL_FP64) { k_xi_E<double><<<total_p, 128, 0, st>>>(x, kk, nk, E_off, d_p_prefix, (double*)E, 0); SGL_COUNT(1); }
+    else { k_xi_E<float><<<total_p, 128, 0, st>>>(x, kk, nk, E_off, d_p_prefix, (float*)E, 1); SGL_COUNT(1); }
 }
 
-// stage C: one thread per output (n, j); groups and rows in a fixed order (deterministic)
+// V[g, r, j] = sum_q U_g[r, q] (J0 - 1)(gam_q kg_j) for the m = 0 groups (compensated form),
+// U_g = sum over p of the group's rows; one CTA per (group row), threads over j.  FP64.
+__global__ void k_xi_V(XiDevice x, const double* __restrict__ J0m1, int nkg, double* __restrict__ V) {
+    const int R = blockIdx.x;                     // global row index
+    int g = 0;
+    {
+        int lo = 0, hi = x.n_groups - 1;
+        while (lo < hi) { const int mid = (lo + hi + 1) >> 1; if (x.g_row_off[mid] <= R) lo = mid; else hi = mid - 1; }
+        g = lo;
+    }
+    if (x.g_m[g] != 0) return;
+    const int rr = R - (int)x.g_row_off[g];
+    const int nQ = x.g_nQ[g];
+    const double* U = x.U0 + x.g_u_off[g] + (long long)rr * nQ;
+    const int* qs = x.idx_q + x.g_q_off[g];
+    for (int j = threadIdx.x; j < nkg; j += blockDim.x) {
+        double a = 0.0;
+        for (int q = 0; q < nQ; ++q) a = fma(U[q], J0m1[(long long)qs[q] * nkg + j], a);
+        V[(long long)R * nkg + j] = a;
+    }
+}
+
+void launch_xi_V(const XiDevice& x, const double* J0m1, int nkg, double* V, int total_rows, cudaStream_t st) {
+    if (total_rows > 0) { k_xi_V<<<total_rows, 128, 0, st>>>(x, J0m1, nkg, V); SGL_COUNT(1); }
+}
+
+// stage C: thread per output (n, j) and group chunk (blockIdx.y); groups and rows in a fixed
+// order; per-chunk partials then a fixed-order sum (deterministic).  Within a group the FP32 path
+// accumulates in FP32 (rows of one group), across groups in FP64.
+// V != nullptr: compensated m = 0 form (real part + V instead of - sum_rows).
 template <typename TT>
 __global__ void k_xi_square(XiDevice x, const long long* __restrict__ G_off, const TT* __restrict__ G,
                             const double* __restrict__ kk, int nk, const double* __restrict__ kg, int nkg,
-                            double* __restrict__ out_re, double* __restrict__ out_im) {
+                            const double* __restrict__ V, int nsplit, double* __restrict__ part) {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= (long long)nk * nkg) return;
+    const long long npt = (long long)nk * nkg;
+    if (e >= npt) return;
     const int n = (int)(e / nkg), j = (int)(e % nkg);
     const double k = kk[n], q = kg[j];
+    const int per = (x.n_groups + nsplit - 1) / nsplit;
+    const int g0 = blockIdx.y * per, g1 = min(x.n_groups, g0 + per);
     double re = 0.0, im = 0.0;
-    for (int g = 0; g < x.n_groups; ++g) {
+    for (int g = g0; g < g1; ++g) {
         const int r = x.g_r[g], m = x.g_m[g];
         const double sign = (m == 0) ? 1.0 : ((m & 1) ? -2.0 : 2.0);
-        const TT* Gg = G + G_off[g];
-        const long long ldg = (long long)r * nkg;
+        const TT* Gg = G + G_off[g] + (long long)n * r * nkg + j;
+        const TT* Gi = G + G_off[g] + (long long)(nk + n) * r * nkg + j;
         const double* res = x.res + x.g_row_off[g];
         const double* srow = x.sum_rows + x.g_row_off[g];
-        double gre = 0.0, gim = 0.0;
+        const double* Vg = V ? V + x.g_row_off[g] * (long long)nkg + j : nullptr;
+        TT gre = TT(0), gim = TT(0);
         for (int rr = 0; rr < r; ++rr) {
-            double a = (double)Gg[(long long)n * ldg + (long long)rr * nkg + j];
-            double b = (double)Gg[(long long)(nk + n) * ldg + (long long)rr * nkg + j];
-            if (m == 0) { a -= srow[rr]; b = fma(k, res[rr], b); }
-            else if (m == 1) { a = fma(0.5 * q, res[rr], a); }
-            gre += a * a - b * b;
-            gim += a * b;
+            TT a = Gg[(long long)rr * nkg];
+            TT b = Gi[(long long)rr * nkg];
+            if (m == 0) {
+                if (Vg) a += (TT)Vg[(long long)rr * nkg];
+                else a = (TT)((double)a - srow[rr]);
+                b = (TT)fma(k, res[rr], (double)b);
+            } else if (m == 1) {
+                a = (TT)fma(0.5 * q, res[rr], (double)a);
+            }
+            gre = fma(a, a, fma(-b, b, gre));
+            gim = fma(a, b, gim);
         }
-        re = fma(0.5 * sign, gre, re);
-        im = fma(0.5 * sign, 2.0 * gim, im);
+        re = fma(0.5 * sign, (double)gre, re);
+        im = fma(0.5 * sign, 2.0 * (double)gim, im);
     }
+    part[(long long)blockIdx.y * npt + e] = re;
+    part[(long long)(nsplit + blockIdx.y) * npt + e] = im;
+}
+
+__global__ void k_xi_square_sum(const double* __restrict__ part, int nsplit, long long npt, double* __restrict__ out_re,
+                                double* __restrict__ out_im) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= npt) return;
+    double re = 0.0, im = 0.0;
+    for (int s = 0; s < nsplit; ++s) { re += part[(long long)s * npt + e]; im += part[(long long)(nsplit + s) * npt + e]; }
     out_re[e] = re;
     out_im[e] = im;
 }
 
 void launch_xi_square(int precision, const XiDevice& x, const long long* G_off, const void* G, const double* kk, int nk,
-                      const double* kg, int nkg, double* out_re, double* out_im, cudaStream_t st) {
+                      const double* kg, int nkg, const double* V, int nsplit, double* part, double* out_re,
+                      double* out_im, cudaStream_t st) {
     const long long tot = (long long)nk * nkg;
-    if (precision == SGL_FP64)
-        { k_xi_square<double><<<ceil_div(tot, 128), 128, 0, st>>>(x, G_off, (const double*)G, kk, nk, kg, nkg, out_re, out_im); SGL_COUNT(1); }
-    else
-        { k_xi_square<float><<<ceil_div(tot, 128), 128, 0, st>>>(x, G_off, (const float*)G, kk, nk, kg, nkg, out_re, out_im); SGL_COUNT(1); }
+    dim3 grid(ceil_div(tot, 128), nsplit);
+    if (precision == SGL_FP64) { k_xi_square<double><<<grid, 128, 0, st>>>(x, G_off, (const double*)G, kk, nk, kg, nkg, V, nsplit, part); SGL_COUNT(1); }
+    else { k_xi_square<float><<<grid, 128, 0, st>>>(x, G_off, (const float*)G, kk, nk, kg, nkg, V, nsplit, part); SGL_COUNT(1); }
+    k_xi_square_sum<<<ceil_div(tot, 256), 256, 0, st>>>(part, nsplit, tot, out_re, out_im);
+    SGL_COUNT(1);
 }
 
 // ---- 1-D path along k_kappa (k_gamma = 0): G_R = sum_p e^{i k kap_p} W0[R, p] - sum0_R + i k res0_R
+// CTA (point, row chunk); partial sums part[chunk, point], then a fixed-order sum.
 __global__ void __launch_bounds__(256)
-k_xi_line_k(XiDevice x, const double* __restrict__ kk, double* __restrict__ out_re, double* __restrict__ out_im) {
+k_xi_line_k(XiDevice x, const double* __restrict__ kk, int nk, double* __restrict__ part) {
     extern __shared__ double sm[];
     double* ec = sm;
     double* es = sm + x.n_kmc;
@@ -168,8 +292,10 @@ k_xi_line_k(XiDevice x, const double* __restrict__ kk, double* __restrict__ out_
     const double k = kk[n];
     for (int p = threadIdx.x; p < x.n_kmc; p += blockDim.x) sincos(k * x.kmc[p], &es[p], &ec[p]);
     __syncthreads();
+    const int per = (x.R0 + kLineChunks - 1) / kLineChunks;
+    const int r0 = blockIdx.y * per, r1 = min(x.R0, r0 + per);
     double re = 0.0, im = 0.0;
-    for (int R = threadIdx.x; R < x.R0; R += blockDim.x) {
+    for (int R = r0 + threadIdx.x; R < r1; R += blockDim.x) {
         const double* w = x.W0 + (long long)R * x.n_kmc;
         double a = 0.0, b = 0.0;
         for (int p = 0; p < x.n_kmc; ++p) { a = fma(ec[p], w[p], a); b = fma(es[p], w[p], b); }
@@ -180,47 +306,73 @@ k_xi_line_k(XiDevice x, const double* __restrict__ kk, double* __restrict__ out_
     }
     re = block_sum(re, red);
     im = block_sum(im, red);
-    if (threadIdx.x == 0) { out_re[n] = 0.5 * re; out_im[n] = 0.5 * im; }
+    if (threadIdx.x == 0) {
+        part[(long long)blockIdx.y * nk + n] = 0.5 * re;
+        part[(long long)(kLineChunks + blockIdx.y) * nk + n] = 0.5 * im;
+    }
 }
 
-void launch_xi_line_k(const XiDevice& x, const double* kk, int nk, double* out_re, double* out_im, cudaStream_t st) {
+__global__ void k_line_reduce(const double* __restrict__ part, int nchunks, int npt, double* __restrict__ re,
+                              double* __restrict__ im) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npt) return;
+    double r = 0.0, m = 0.0;
+    for (int c = 0; c < nchunks; ++c) { r += part[(long long)c * npt + i]; m += part[(long long)(nchunks + c) * npt + i]; }
+    re[i] = r;
+    im[i] = m;
+}
+
+void launch_xi_line_k(const XiDevice& x, const double* kk, int nk, double* out_re, double* out_im, double* part,
+                      cudaStream_t st) {
     const size_t sm = (2 * (size_t)x.n_kmc + 32) * sizeof(double);
-    { k_xi_line_k<<<nk, 256, sm, st>>>(x, kk, out_re, out_im); SGL_COUNT(1); }
+    dim3 grid(nk, kLineChunks);
+    { k_xi_line_k<<<grid, 256, sm, st>>>(x, kk, nk, part); SGL_COUNT(1); }
+    { k_line_reduce<<<ceil_div(nk, 256), 256, 0, st>>>(part, kLineChunks, nk, out_re, out_im); SGL_COUNT(1); }
 }
 
 // ---- 1-D path along k_gamma (k_kappa = 0): per m, G_R = sum_q U_m[R, q] J_m(gam_q kg) (+ residuals)
+// CTA (point, chunk of the concatenated m = 0, 1, 2 rows); partials then a fixed-order sum.
 __global__ void __launch_bounds__(256)
-k_xi_line_g(XiDevice x, const double* __restrict__ kg, double* __restrict__ out_re, double* __restrict__ out_im) {
+k_xi_line_g(XiDevice x, const double* __restrict__ kg, int nkg, double* __restrict__ part) {
     extern __shared__ double sm[];
-    double* Jq = sm;                 // [n_gmc]
-    double* red = sm + x.n_gmc;
+    double* Jq = sm;                 // [3][n_gmc]
+    double* red = sm + 3 * x.n_gmc;
     const int j = blockIdx.x;
     const double q = kg[j];
-    double tot = 0.0;
-    for (int m = 0; m < 3; ++m) {
-        if (x.Rm[m] == 0) continue;
-        __syncthreads();
-        for (int c = threadIdx.x; c < x.n_gmc; c += blockDim.x) Jq[c] = bessel_jm(m, x.gmc[c] * q);
-        __syncthreads();
-        double acc = 0.0;
-        for (int R = threadIdx.x; R < x.Rm[m]; R += blockDim.x) {
-            const double* u = x.U[m] + (long long)R * x.n_gmc;
-            double a = 0.0;
-            for (int c = 0; c < x.n_gmc; ++c) a = fma(u[c], Jq[c], a);
-            if (m == 0) a -= x.summ[m][R];
-            else if (m == 1) a = fma(0.5 * q, x.resm[m][R], a);
-            acc += a * a;
-        }
-        acc = block_sum(acc, red);
-        const double sign = (m == 0) ? 1.0 : ((m & 1) ? -2.0 : 2.0);
-        tot += 0.5 * sign * acc;
+    for (int c = threadIdx.x; c < 3 * x.n_gmc; c += blockDim.x) {
+        const int m = c / x.n_gmc, qi = c % x.n_gmc;
+        Jq[c] = bessel_jm(m, x.gmc[qi] * q);
     }
-    if (threadIdx.x == 0) { out_re[j] = tot; out_im[j] = 0.0; }
+    __syncthreads();
+    const int Rtot = x.Rm[0] + x.Rm[1] + x.Rm[2];
+    const int per = (Rtot + kLineChunks - 1) / kLineChunks;
+    const int r0 = blockIdx.y * per, r1 = min(Rtot, r0 + per);
+    double tot = 0.0;
+    for (int Rg = r0 + threadIdx.x; Rg < r1; Rg += blockDim.x) {
+        int m = 0, R = Rg;
+        if (R >= x.Rm[0]) { R -= x.Rm[0]; m = 1; if (R >= x.Rm[1]) { R -= x.Rm[1]; m = 2; } }
+        const double* u = x.U[m] + (long long)R * x.n_gmc;
+        const double* J = Jq + m * x.n_gmc;
+        double a = 0.0;
+        for (int c = 0; c < x.n_gmc; ++c) a = fma(u[c], J[c], a);
+        if (m == 0) a -= x.summ[m][R];
+        else if (m == 1) a = fma(0.5 * q, x.resm[m][R], a);
+        const double sign = (m == 0) ? 1.0 : ((m & 1) ? -2.0 : 2.0);
+        tot += 0.5 * sign * (a * a);
+    }
+    tot = block_sum(tot, red);
+    if (threadIdx.x == 0) {
+        part[(long long)blockIdx.y * nkg + j] = tot;
+        part[(long long)(kLineChunks + blockIdx.y) * nkg + j] = 0.0;
+    }
 }
 
-void launch_xi_line_g(const XiDevice& x, const double* kg, int nkg, double* out_re, double* out_im, cudaStream_t st) {
-    const size_t sm = ((size_t)x.n_gmc + 32) * sizeof(double);
-    { k_xi_line_g<<<nkg, 256, sm, st>>>(x, kg, out_re, out_im); SGL_COUNT(1); }
+void launch_xi_line_g(const XiDevice& x, const double* kg, int nkg, double* out_re, double* out_im, double* part,
+                      cudaStream_t st) {
+    const size_t sm = (3 * (size_t)x.n_gmc + 32) * sizeof(double);
+    dim3 grid(nkg, kLineChunks);
+    { k_xi_line_g<<<grid, 256, sm, st>>>(x, kg, nkg, part); SGL_COUNT(1); }
+    { k_line_reduce<<<ceil_div(nkg, 256), 256, 0, st>>>(part, kLineChunks, nkg, out_re, out_im); SGL_COUNT(1); }
 }
 
 }  // namespace sgl

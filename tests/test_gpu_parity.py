@@ -79,6 +79,29 @@ def test_xi_term_exact(lamx, ref_sub):
     assert np.max(np.abs(lamx.engine.xi_term(np.zeros(1), ks)[0, :] - ref_sub["xi_line_g"])) <= TOL_LN
 
 
+def test_xi_term_mixed_vs_fp64(lamx, ref_sub):
+    """The mixed path's compensated m=0 form (sum (cos-1) T + U (J0-1)) in FP32 vs the FP64 term."""
+    from sgl_analytic_gb300._lib import SGL_MIXED
+    Q = lamx.engine.xi_term(ref_sub["kkc"], ref_sub["kgc"], SGL_MIXED)
+    Qr = ref_sub["xi_coarse"]
+    assert np.max(np.abs(Q - Qr)) <= 1e-5 * max(1.0, np.max(np.abs(Qr)))
+
+
+def test_lambda_full_grid_mixed_vs_fp64(lamx):
+    from sgl_analytic_gb300._lib import SGL_FP64, SGL_MIXED
+    L64 = lamx.engine.lnphi(KK16, KG_FULL, SGL_FP64)
+    Lmx = lamx.engine.lnphi(KK16, KG_FULL, SGL_MIXED)
+    assert np.max(np.abs(np.exp(Lmx) - np.exp(L64))) <= 1e-5
+
+
+def test_pdf_mixed_psi1_only(lam1, ref_sub):
+    from sgl_analytic_gb300 import invert
+    x = ref_sub["xi_out"]
+    _, P, _ = invert(lam1, lam1.sigma(), xi_out=x, tail_box=True, phi_tol=1e-8, precision="mixed")
+    dpeak, l1, rel_tail = _pdf_errors(P, ref_sub["pdf1_P"], x)
+    assert l1 <= 1e-4 and rel_tail <= 1e-3, (dpeak, l1, rel_tail)
+
+
 def test_lambda_with_xi_small_grid(lamx, ref_sub):
     L = lamx(ref_sub["kk"][:20], ref_sub["kg"][:20])
     assert np.max(np.abs(L - ref_sub["lamx_grid"])) <= TOL_LN
