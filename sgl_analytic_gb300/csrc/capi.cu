@@ -245,8 +245,8 @@ sgl_status gemm_splitk(sgl_ctx* ctx, GemmDesc<T> g, const std::string& tag, int 
     const int tiles = gemm_plan(&tmp, 1);
     int split = 1;
     if (tiles < 2 * kNumSMs) split = std::min(ceil_div(2 * kNumSMs, tiles), std::max(1, g.K / 512));
-    // min_split > 1 (mixed-precision transforms): FP32 partial sums over at most K / min_split
-    // terms, combined in FP64 -- shorter FP32 accumulation chains for the oscillatory sums
+    // min_split > 1 (mixed path): FP32 partial sums over at most K / min_split terms, combined in
+    // FP64 -- shorter FP32 accumulation chains
     split = std::max(split, std::min(min_split, std::max(1, g.K / 32)));
     if (split <= 1) { std::vector<GemmDesc<T>> v{g}; return run_gemms(ctx, v, tag); }
     const long long slice = (long long)g.M * g.N;
@@ -552,8 +552,9 @@ sgl_status sep_gemms(sgl_ctx* ctx, int precision, const double* h_kg, const doub
     const double Kg = nkg ? h_kg[nkg - 1] : 0.0;
     const int Nch = (S.n_cols_sep > 0 && Kg > 0) ? (int)(0.65 * S.max_sep_node * Kg + 50.0) : 0;
     const long long ld = 2LL * nk;
-    // mixed path: FP32 partial sums over at most ~32 K-terms per slice, slices combined in FP64
-    const int msplit = precision == SGL_FP64 ? 1 : 64;
+    // mixed path: at least 8 K-slices, FP32 within a slice, slices combined in FP64 (the PDF tail
+    // is sensitive to the FP32 accumulation length of these sums)
+    const int msplit = precision == SGL_FP64 ? 1 : 8;
     const double* d_nodes = (const double*)ctx->arena.find("sep_nodes");
     if (S.n_cols_sep > 0) {
         if (nkg > 1 && Nch > 0 && Nch < 0.6 * nkg && h_kg[0] >= 0.0) {
@@ -1256,7 +1257,7 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
     CKS(upload(ctx, d_kap, kap.data(), nkap));
     CKS(upload(ctx, d_gam, gam.data(), ngam));
     const int ldF = ngam + 2;
-    void* M = ctx->arena.get("inv_M", (size_t)nkg * ldF * es);
+    void* M = ctx->arena.get("inv_M", (size_t)nkg * ldF * es * (P == SGL_FP64 ? 1 : 2));
     void* F = ctx->arena.get("inv_F", 2ULL * nk * ldF * es);
     void* CS = ctx->arena.get("inv_CS", (size_t)nkap * 2 * nk * es);
     void* P3e = ctx->arena.get("inv_P3e", (size_t)nkap * ldF * es);
@@ -1269,13 +1270,16 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
     if (P == SGL_FP64) {
         CKS(gemm_splitk<double>(ctx, gd<double>(2 * nk, ngam, nkg, Phi, nkg, 1, M, ldF, 1, F, ldF), "hankel"));
     } else {
-        CKS(gemm_splitk<float>(ctx, gd<float>(2 * nk, ngam, nkg, Phi, nkg, 1, M, ldF, 1, F, ldF), "hankel", 128));
+        // F = Phi M_hi + Phi M_lo (split Hankel matrix)
+        CKS(gemm_splitk<float>(ctx, gd<float>(2 * nk, ngam, nkg, Phi, nkg, 1, M, ldF, 1, F, ldF), "hankel", 8));
+        CKS(gemm_splitk<float>(ctx, gd<float>(2 * nk, ngam, nkg, Phi, nkg, 1, (const float*)M + (size_t)nkg * ldF, ldF,
+                                              1, F, ldF, 1.0, 1.0), "hankel_lo", 8));
     }
     launch_em_columns(P, Phi, nk, nkg, dkg, F, ldF, ngam, st); CKLAUNCH();
     if (P == SGL_FP64) {
         CKS(gemm_splitk<double>(ctx, gd<double>(nkap, ldF, 2 * nk, CS, 2 * nk, 1, F, ldF, 1, P3e, ldF, c), "kappa"));
     } else {
-        CKS(gemm_splitk<float>(ctx, gd<float>(nkap, ldF, 2 * nk, CS, 2 * nk, 1, F, ldF, 1, P3e, ldF, c), "kappa", 128));
+        CKS(gemm_splitk<float>(ctx, gd<float>(nkap, ldF, 2 * nk, CS, 2 * nk, 1, F, ldF, 1, P3e, ldF, c), "kappa", 8));
     }
     launch_p3_finish(P, P3e, nkap, ngam, ldF, d_gam, d_P3, st); CKLAUNCH();
     cudaEventRecord(ctx->ev[2], st);

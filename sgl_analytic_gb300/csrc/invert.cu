@@ -9,7 +9,9 @@
 
 namespace sgl {
 
-// M[m, j] = k_g[m] w_g[m] J0(gam_j k_g[m]),  w_g = dk_g (halved at both ends); row stride ld
+// M[m, j] = k_g[m] w_g[m] J0(gam_j k_g[m]),  w_g = dk_g (halved at both ends); row stride ld.
+// FP32 (mixed path): M = M_hi + M_lo, both FP32, M_lo written nkg * ld elements after M_hi --
+// the Hankel sum's rounding of M would otherwise dominate the PDF tail error.
 template <typename TT>
 __global__ void k_hankel_matrix(const double* __restrict__ kg, int nkg, double dkg, const double* __restrict__ gam,
                                 int ngam, int ld, TT* __restrict__ M) {
@@ -18,7 +20,10 @@ __global__ void k_hankel_matrix(const double* __restrict__ kg, int nkg, double d
     const int m = (int)(e / ngam), j = (int)(e % ngam);
     double w = dkg;
     if (m == 0 || m == nkg - 1) w *= 0.5;
-    M[(long long)m * ld + j] = (TT)((kg[m] * w) * j0(gam[j] * kg[m]));
+    const double v = (kg[m] * w) * j0(gam[j] * kg[m]);
+    const TT hi = (TT)v;
+    M[(long long)m * ld + j] = hi;
+    if (sizeof(TT) == 4) M[(long long)nkg * ld + (long long)m * ld + j] = (TT)(v - (double)hi);
 }
 
 void launch_hankel_matrix(int precision, const double* kg, int nkg, double dkg, const double* gam, int ngam, int ld,
