@@ -181,3 +181,28 @@ def test_full_chain_matches_stored_golden_pdf(precision):
         assert dpeak <= TOL_PEAK
     else:
         assert l1 <= 1e-4 and rel_tail <= 1e-3
+
+
+def test_api_generate_pdf_lnmu_matches_reference(ref_sub):
+    """The drop-in API end to end (population given, GPU hot path) vs the reference's invert."""
+    from sgl_analytic_gb300 import generate_pdf_lnmu
+    from tests.conftest import GOLDEN
+    x = ref_sub["xi_out"]
+    xo, p, info = generate_pdf_lnmu(1.0, lnmu=x, population=GOLDEN / "pop_zs1_sub.npz", return_info=True)
+    np.testing.assert_array_equal(xo, x)
+    dpeak, l1, _ = _pdf_errors(p, ref_sub["pdfx_P"], x)
+    assert dpeak <= TOL_PEAK
+    assert info["grid"]["nk_k"] == int(ref_sub["pdfx_grid"][0])
+    assert {"diagnostics", "moment_interval", "t_stages", "sigma_kappa"} <= set(info)
+
+
+def test_cli_end_to_end(tmp_path, ref_sub):
+    import json as _json
+    from sgl_analytic_gb300 import cli
+    from tests.conftest import GOLDEN
+    dest = tmp_path / "pdf.json"
+    cli.main(["--z-s", "1", "--population", str(GOLDEN / "pop_zs1_sub.npz"), "--out", str(dest)])
+    d = _json.loads(dest.read_text())
+    P = np.array(d["P_s"] + d["P_s_tail"])
+    dpeak, _, _ = _pdf_errors(P, ref_sub["pdfx_P"], ref_sub["xi_out"])
+    assert dpeak <= TOL_PEAK
