@@ -120,6 +120,19 @@ sgl_status sgl_lnphi(sgl_ctx* ctx, const double* kk, int nkk, const double* kg, 
 sgl_status sgl_xi_term(sgl_ctx* ctx, const double* kk, int nkk, const double* kg, int nkg, int precision,
                        double* out_re, double* out_im);
 
+/* One-dimensional compensated CF sweep over an arbitrary cell list (the synthetic plane x mass x
+ * impact-parameter microbenchmark, 16.8M cells x 16384 k):
+ *     out[n] = sum_c w_c (e^{i kk_n kap_c} - 1 - i kk_n kap_c)
+ * the kappa part of the separable Psi_1 (A1 of _sep_lam_kernel, sgl_full.py:2596-2617).
+ * set_cells uploads the cells once (host pointers); eval runs on a k grid (host in/out). */
+sgl_status sgl_sweep_set_cells(sgl_ctx* ctx, int64_t n_cells, const double* kap, const double* w);
+sgl_status sgl_sweep_eval(sgl_ctx* ctx, const double* kk, int nk, int precision, double* out_re,
+                          double* out_im);
+
+/* Measured FMA throughput of this GPU (fp64 = 1: FP64, 0: FP32), TFLOP/s (2 flops per FMA):
+ * the denominator of the CF-sweep roofline.  No counterpart in the reference. */
+sgl_status sgl_measure_peak(sgl_ctx* ctx, int fp64, double* tflops);
+
 /* Fills opts with the pipeline defaults above. */
 void sgl_invert_opts_default(sgl_invert_opts* opts);
 

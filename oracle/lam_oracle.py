@@ -364,3 +364,22 @@ def oracle_from_npz(path, method="sep", xi=True, select=None):
     if xi:
         X = XiGroups(groups_from_npz(d, select), d["ce_k"], d["ce_g"])
     return OracleLam(d["w0"], d["k0"], d["g0"], d["ig"], d["fe_g"], float(d["V"]), X, method=method)
+
+
+def cf_sweep(kk, kap, w, chunk=8):
+    """sum_c w_c (e^{i k kap_c} - 1 - i k kap_c) per k, with the cancellation-free forms of
+    _sep_lam_kernel's A1 term (sgl_full.py:2596-2617); also returns sum_c w_c (|cos-1| + |sin-ph|),
+    the scale of the roundoff of any summation order."""
+    kk = np.asarray(kk, float)
+    out = np.empty(kk.size, complex)
+    mag = np.empty(kk.size)
+    for lo in range(0, kk.size, chunk):
+        hi = min(lo + chunk, kk.size)
+        ph = np.outer(kk[lo:hi], kap)
+        hs = np.sin(0.5 * ph)
+        cm1 = -2.0 * hs * hs
+        p2 = ph * ph
+        smp = np.where(np.abs(ph) < 1e-2, -ph * p2 / 6.0 * (1.0 - p2 / 20.0 * (1.0 - p2 / 42.0)), np.sin(ph) - ph)
+        out[lo:hi] = cm1 @ w + 1j * (smp @ w)
+        mag[lo:hi] = np.abs(cm1) @ w + np.abs(smp) @ w
+    return out, mag

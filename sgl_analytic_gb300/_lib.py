@@ -20,7 +20,8 @@ PRECISIONS = {"fp64": SGL_FP64, "mixed": SGL_MIXED}
 # every symbol the header declares (checked by the CPU test suite)
 EXPORTS = ("sgl_abi_version", "sgl_ctx_create", "sgl_ctx_destroy", "sgl_last_error", "sgl_ctx_stream",
            "sgl_ctx_profile", "sgl_stats_json", "sgl_lam_set_cells",
-           "sgl_lam_set_xi", "sgl_lam_sigma", "sgl_lnphi", "sgl_xi_term", "sgl_invert_opts_default", "sgl_pdf",
+           "sgl_lam_set_xi", "sgl_lam_sigma", "sgl_lnphi", "sgl_xi_term", "sgl_sweep_set_cells", "sgl_sweep_eval", "sgl_measure_peak",
+           "sgl_invert_opts_default", "sgl_pdf",
            "sgl_cf_kappa_noalloc")
 
 
@@ -68,6 +69,11 @@ def lib():
         L.sgl_lam_sigma.argtypes = [vp, dp]
         L.sgl_lnphi.argtypes = [vp, dp, C.c_int, dp, C.c_int, C.c_int, dp, dp]
         L.sgl_xi_term.argtypes = [vp, dp, C.c_int, dp, C.c_int, C.c_int, dp, dp]
+        L.sgl_sweep_set_cells.argtypes = [vp, C.c_int64, dp, dp]
+        L.sgl_sweep_eval.argtypes = [vp, dp, C.c_int, C.c_int, dp, dp]
+        L.sgl_measure_peak.argtypes = [vp, C.c_int, dp]
+        for name in ("sgl_sweep_set_cells", "sgl_sweep_eval", "sgl_measure_peak"):
+            getattr(L, name).restype = C.c_int
         L.sgl_cf_kappa_noalloc.argtypes = [vp, C.c_int, vp, vp, C.c_int64, vp, vp, vp]
         L.sgl_cf_kappa_noalloc.restype = C.c_int
         L.sgl_invert_opts_default.argtypes = [C.POINTER(InvertOpts)]
@@ -187,6 +193,26 @@ class Engine:
         self._check(self._L.sgl_xi_term(self._h, _ptr(kk), kk.size, _ptr(kg), kg.size, int(precision), _ptr(re),
                                         _ptr(im)), "sgl_xi_term")
         return re + 1j * im
+
+    def sweep_set_cells(self, kap, w):
+        kap = np.ascontiguousarray(kap, np.float64)
+        w = np.ascontiguousarray(w, np.float64)
+        if kap.size != w.size:
+            raise ValueError("kap and w must have equal length")
+        self._check(self._L.sgl_sweep_set_cells(self._h, kap.size, _ptr(kap), _ptr(w)), "sgl_sweep_set_cells")
+
+    def sweep(self, kk, precision=SGL_FP64):
+        kk = np.ascontiguousarray(np.atleast_1d(kk), np.float64)
+        re = np.empty(kk.size)
+        im = np.empty(kk.size)
+        self._check(self._L.sgl_sweep_eval(self._h, _ptr(kk), kk.size, int(precision), _ptr(re), _ptr(im)),
+                    "sgl_sweep_eval")
+        return re + 1j * im
+
+    def measure_peak(self, fp64=True):
+        t = C.c_double()
+        self._check(self._L.sgl_measure_peak(self._h, int(bool(fp64)), C.byref(t)), "sgl_measure_peak")
+        return t.value
 
     def pdf(self, xi_out, precision=SGL_FP64, tail_box=True, phi_tol=1e-8, n_xi_wide=500, n_k_int=2400,
             xi_reach=24.0):

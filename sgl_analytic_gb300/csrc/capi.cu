@@ -92,6 +92,7 @@ struct sgl_ctx {
     int sep_precision_ready = -1;
     XiHost xi;
     XiDevice xid;
+    long long sweep_n = -1;          // cells of the 1-D sweep (sgl_sweep_set_cells)
     SplineHost spline;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // pinned staging ring for small uploads (pageable copies would serialise host and device);
@@ -1152,6 +1153,79 @@ sgl_status sgl_xi_term(sgl_ctx* ctx, const double* kk, int nkk, const double* kg
     CK(cudaMemcpyAsync(out_re, d_o, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(out_im, d_o + npt, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CKS(sync_stream(ctx));
+    return SGL_OK;
+}
+
+sgl_status sgl_sweep_set_cells(sgl_ctx* ctx, int64_t n_cells, const double* kap, const double* w) {
+    if (!ctx) return SGL_ERR_VALUE;
+    if (n_cells < 1 || !kap || !w) return fail(ctx, SGL_ERR_VALUE, "empty cell list");
+    CK(cudaSetDevice(ctx->device));
+    std::vector<float> kh((size_t)n_cells), kl((size_t)n_cells), wf((size_t)n_cells);
+    for (int64_t c = 0; c < n_cells; ++c) {
+        if (!std::isfinite(kap[c]) || !std::isfinite(w[c])) return fail(ctx, SGL_ERR_VALUE, "non-finite cell");
+        const ff f = ff_from_double(kap[c]);
+        kh[(size_t)c] = f.hi; kl[(size_t)c] = f.lo; wf[(size_t)c] = (float)w[c];
+    }
+    DBUF(d_k, double, "sw_kap", n_cells);
+    DBUF(d_w, double, "sw_w", n_cells);
+    DBUF(d_kh, float, "sw_kh", n_cells);
+    DBUF(d_kl, float, "sw_kl", n_cells);
+    DBUF(d_wf, float, "sw_wf", n_cells);
+    CK(cudaMemcpyAsync(d_k, kap, (size_t)n_cells * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(d_w, w, (size_t)n_cells * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(d_kh, kh.data(), (size_t)n_cells * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(d_kl, kl.data(), (size_t)n_cells * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(d_wf, wf.data(), (size_t)n_cells * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CKS(sync_stream(ctx));
+    ctx->sweep_n = n_cells;
+    return SGL_OK;
+}
+
+sgl_status sgl_sweep_eval(sgl_ctx* ctx, const double* kk, int nk, int precision, double* out_re, double* out_im) {
+    if (!ctx) return SGL_ERR_VALUE;
+    if (ctx->sweep_n < 1) return fail(ctx, SGL_ERR_STATE, "sweep cells not set");
+    if (nk < 1 || !kk || !out_re || !out_im) return fail(ctx, SGL_ERR_VALUE, "empty k grid");
+    if (precision != SGL_FP64 && precision != SGL_MIXED) return fail(ctx, SGL_ERR_VALUE, "unknown precision");
+    for (int i = 0; i < nk; ++i) if (!std::isfinite(kk[i])) return fail(ctx, SGL_ERR_VALUE, "non-finite kk");
+    CK(cudaSetDevice(ctx->device));
+    const long long nc = ctx->sweep_n;
+    const int nch = sweep1d_chunks(nk, nc);
+    DBUF(d_kk, double, "sw_kk", nk);
+    DBUF(d_part, double2, "sw_part", (long long)nch * nk);
+    DBUF(d_out, double, "sw_out", 2LL * nk);
+    CKS(upload(ctx, d_kk, kk, nk));
+    {
+        Timed t(ctx, precision == SGL_FP64 ? "sweep1d_f64" : "sweep1d_mixed", (double)nk * nc, (double)nk * 0 + nc * 16.0);
+        launch_sweep1d(precision, d_kk, nk, (const double*)ctx->arena.find("sw_kap"), (const double*)ctx->arena.find("sw_w"),
+                       (const float*)ctx->arena.find("sw_kh"), (const float*)ctx->arena.find("sw_kl"),
+                       (const float*)ctx->arena.find("sw_wf"), nc, nch, d_part, d_out, d_out + nk, ctx->stream);
+    }
+    CKLAUNCH();
+    CK(cudaMemcpyAsync(out_re, d_out, (size_t)nk * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(out_im, d_out + nk, (size_t)nk * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CKS(sync_stream(ctx));
+    for (int i = 0; i < nk; ++i)
+        if (!std::isfinite(out_re[i]) || !std::isfinite(out_im[i])) return fail(ctx, SGL_ERR_NONFINITE, "non-finite sweep");
+    return SGL_OK;
+}
+
+sgl_status sgl_measure_peak(sgl_ctx* ctx, int fp64, double* tflops) {
+    if (!ctx || !tflops) return SGL_ERR_VALUE;
+    CK(cudaSetDevice(ctx->device));
+    const int blocks = kNumSMs * 8, iters = fp64 ? 512 : 8192;
+    DBUF(d_o, double, "peak_out", (long long)blocks * 256);
+    launch_fma_probe(fp64, d_o, blocks, iters, ctx->stream);     // warm-up
+    CKLAUNCH();
+    cudaEvent_t a, b;
+    cudaEventCreate(&a); cudaEventCreate(&b);
+    cudaEventRecord(a, ctx->stream);
+    for (int r = 0; r < 5; ++r) launch_fma_probe(fp64, d_o, blocks, iters, ctx->stream);
+    cudaEventRecord(b, ctx->stream);
+    CKS(sync_stream(ctx));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a); cudaEventDestroy(b);
+    *tflops = 5.0 * (double)blocks * 256 * iters * 8 * 2 / (ms * 1e-3) / 1e12;
     return SGL_OK;
 }
 

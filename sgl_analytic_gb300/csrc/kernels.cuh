@@ -115,4 +115,11 @@ void launch_path_integral(const double* P3, int nkap, int ngam, double kap0, dou
                           const double* xi, int nxi, double gmax, double g_def, int n_k_int, double* out,
                           cudaStream_t st);
 
+// ---- 1-D CF sweep and FMA probes
+int sweep1d_chunks(int nk, long long nc);
+void launch_sweep1d(int precision, const double* kk, int nk, const double* kap, const double* w, const float* kh,
+                    const float* kl, const float* wf, long long nc, int nchunks, double2* part, double* re,
+                    double* im, cudaStream_t st);
+void launch_fma_probe(int fp64, void* out, int blocks, int iters, cudaStream_t st);
+
 }  // namespace sgl

@@ -41,3 +41,53 @@ def zs1_population(golden: Path = GOLDEN) -> Population:
     pop.xg_rows = np.concatenate(rows)
     pop.xg_s0 = float(st["s0"])
     return pop
+
+
+def nfw_trunc_projected(x, c):
+    """Projected density shape F(x; c) of an NFW profile truncated at r = c r_s (Takada & Jain 2003,
+    MNRAS 340, 580, their eq. 27): Sigma(x) = 2 rho_s r_s F(x), x = R / r_s; zero beyond x = c."""
+    x, c = np.broadcast_arrays(np.asarray(x, float), np.asarray(c, float))
+    out = np.zeros_like(x)
+    inside = x < c
+    a = np.sqrt(np.maximum(c ** 2 - x ** 2, 0.0))
+    arg = (x ** 2 + c) / (x * (1.0 + c))
+    lo = inside & (x < 1.0 - 1e-6)
+    hi = inside & (x > 1.0 + 1e-6)
+    mid = inside & ~lo & ~hi
+    out[lo] = (-a[lo] / ((1 - x[lo] ** 2) * (1 + c[lo]))
+               + np.arccosh(arg[lo]) / (1 - x[lo] ** 2) ** 1.5)
+    out[hi] = (-a[hi] / ((1 - x[hi] ** 2) * (1 + c[hi]))
+               - np.arccos(np.clip(arg[hi], -1.0, 1.0)) / (x[hi] ** 2 - 1) ** 1.5)
+    out[mid] = np.sqrt(c[mid] ** 2 - 1) / (3 * (1 + c[mid])) * (1 + 1 / (c[mid] + 1))
+    return out
+
+
+def cf_sweep_problem(seed=0, nz=128, nm=256, nb=512, nk=16384, total_rate=3.7e6):
+    """The synthetic plane x mass x impact-parameter CF sweep (nz * nm * nb cells, nk k-points).
+
+    Lens planes z in (0, 1) for a source at z_s = 1; masses log-spaced 1e8-1e16 Msun/h;
+    impact parameters log-spaced 1e-3-1e2 r_s; concentration c = 5 (M / 1e12)^-0.1;
+    kappa = kappa_s(M, z) F(b; c) with kappa_s = 0.05 (M / 1e12)^0.3 * 4 z (1 - z) (a lensing
+    efficiency shaped amplitude); rates proportional to M^-0.9 exp(-M / 1e15) x Gaussian(z; 0.5, 0.3)
+    x 2 pi b db x dlnM x dz, with a seeded lognormal (sigma 0.1) jitter per (z, M), normalised to a
+    total expected count of total_rate; k log-spaced in [1e-2, 1e6].  Returns (kap, w, kk)."""
+    rng = np.random.default_rng(seed)
+    z = np.linspace(0.02, 0.98, nz)
+    M = np.geomspace(1e8, 1e16, nm)
+    b = np.geomspace(1e-3, 1e2, nb)
+    dlnb = np.log(b[1] / b[0])
+    dlnM = np.log(M[1] / M[0])
+    dz = z[1] - z[0]
+    c = 5.0 * (M / 1e12) ** -0.1
+    F = nfw_trunc_projected(b[None, :], c[:, None])                        # (nm, nb)
+    ks = 0.05 * (M / 1e12) ** 0.3                                           # (nm,)
+    eff = 4.0 * z * (1.0 - z)                                               # (nz,)
+    kap = eff[:, None, None] * ks[None, :, None] * F[None, :, :]            # (nz, nm, nb)
+    dn = M ** -0.9 * np.exp(-M / 1e15) * dlnM                               # (nm,)
+    gz = np.exp(-0.5 * ((z - 0.5) / 0.3) ** 2) * dz                         # (nz,)
+    jit = np.exp(0.1 * rng.standard_normal((nz, nm)))
+    area = 2 * np.pi * b * b * dlnb                                         # 2 pi b db with db = b dlnb
+    w = (gz[:, None] * dn[None, :] * jit)[:, :, None] * area[None, None, :]
+    w *= total_rate / w.sum()
+    kk = np.geomspace(1e-2, 1e6, nk)
+    return kap.ravel(), w.ravel(), kk
