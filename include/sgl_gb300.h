@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define SGL_ABI_VERSION 1
+#define SGL_ABI_VERSION 2
 
 typedef struct sgl_ctx sgl_ctx;
 
@@ -50,6 +50,9 @@ typedef struct {
     int n_xi_wide;        /* normalisation / moment grid points (500 for gauss) */
     int n_k_int;          /* points per constant-mu path (2400) */
     double xi_reach;      /* moment grid reach in sigma_xi = 2 sigma (24) */
+    int window;           /* box window _window_pd (sgl_full.py:83-94, 254-258): 0 off (gauss
+                             default), 1 always, 2 "auto" = only when |Phi| > phi_tol at a box
+                             edge (the vp closure's default, pipeline.py:227-231) */
 } sgl_invert_opts;
 
 /* Grid and moments of one inversion (the reference's meta["grid"] and meta moments,
@@ -60,6 +63,8 @@ typedef struct {
     double phi_at_k_cut, phi_at_g_cut;
     double mean, var, skew, sigmaDL, norm;
     double ms_lambda, ms_transform, ms_path;   /* device time of the three stages */
+    double window;                             /* 1 if the box window was applied */
+    double xi_coarse, xi_coarse_k;             /* vp closure's coarse grid (gamma, kappa); 0 otherwise */
 } sgl_invert_meta;
 
 /* Library / context ------------------------------------------------------------------- */
@@ -119,6 +124,32 @@ sgl_status sgl_lnphi(sgl_ctx* ctx, const double* kk, int nkk, const double* kg, 
  * (sgl_full.py:2863-2951).  Requires sgl_lam_set_xi with at least one group. */
 sgl_status sgl_xi_term(sgl_ctx* ctx, const double* kk, int nkk, const double* kg, int nkg, int precision,
                        double* out_re, double* out_im);
+
+/* Positive (vp) Cox closure ---------------------------------------------------------------
+ * Replaces the gauss xi_lin term by  q_xi = unwrap(ln R) - shear_var k_gamma^2 / 4  with
+ *     ln R(k, q) = ln E_U exp( sum_s sum_g (lam_g(U_s) - 1) Y_g(k, q) ),
+ *     Y_g = sum_{c in g} w_c (e_c J_c + J_c - 1),  e_c = expm1(i k kap_c),  J_c = J0(q gam_c)
+ * over a stationary chain of nstate = 48 latent states (Closure.qxi pos_closure.py:690-705,
+ * FusedVP.lnR_blocked pos_closure_fused.py:119-140, _chain_recursion pos_closure.py:184-240).
+ * Arguments are the closure the reference's pos_closure.install (pos_closure.py:708-733) builds:
+ * state nodes u and stationary weights w; n_shells - 1 transition matrices K[s][i][j] (row-major);
+ * n_unique cells (ku, gu); n_cells group members (cu index into the unique cells, weight cw);
+ * n_groups groups (members gstart[g] .. gstart[g+1]-1) in shells sh_g[s] .. sh_g[s+1]-1, each with
+ * FusedVP's rate interval lam_g(u_j) - 1 = c + a (u_j - anchor) + b on states lo..hi (c = 0: all
+ * states, anchor 0; c = -1: an interval reaching one end, anchor u_lo if hi = nstate-1, else u_hi;
+ * rate_intervals pos_closure_fused.py:18-48).  Once set, sgl_lnphi / sgl_xi_term / sgl_pdf use it
+ * (Lam._Qxi routed to the closure), sgl_pdf grows the coarse grid per axis with the box
+ * (sgl_full.py:226-238), and sigma keeps the gauss groups' variance (Lam.sigma).
+ * n_shells = 0 removes the closure. */
+sgl_status sgl_vp_set(sgl_ctx* ctx, int nstate, const double* u, const double* w, int n_shells, const double* K,
+                      int n_unique, const double* ku, const double* gu, int64_t n_cells, const int32_t* cu,
+                      const double* cw, int n_groups, const int64_t* gstart, const int32_t* sh_g, const double* ga,
+                      const double* gb, const double* gc, const int32_t* glo, const int32_t* ghi, double shear_var);
+
+/* ln R on the tensor grid kv x qv (nk x nq, row-major), principal branch, no shear term:
+ * FusedVP.lnR_blocked (pos_closure_fused.py:119-140). */
+sgl_status sgl_vp_lnR(sgl_ctx* ctx, const double* kv, int nk, const double* qv, int nq, int precision,
+                      double* out_re, double* out_im);
 
 /* One-dimensional compensated CF sweep over an arbitrary cell list (the synthetic plane x mass x
  * impact-parameter microbenchmark, 16.8M cells x 16384 k):

@@ -21,20 +21,21 @@ PRECISIONS = {"fp64": SGL_FP64, "mixed": SGL_MIXED}
 EXPORTS = ("sgl_abi_version", "sgl_ctx_create", "sgl_ctx_destroy", "sgl_last_error", "sgl_ctx_stream",
            "sgl_ctx_profile", "sgl_stats_json", "sgl_lam_set_cells",
            "sgl_lam_set_xi", "sgl_lam_sigma", "sgl_lnphi", "sgl_xi_term", "sgl_sweep_set_cells", "sgl_sweep_eval", "sgl_measure_peak",
-           "sgl_invert_opts_default", "sgl_pdf",
+           "sgl_vp_set", "sgl_vp_lnR", "sgl_invert_opts_default", "sgl_pdf",
            "sgl_cf_kappa_noalloc")
 
 
 class InvertOpts(C.Structure):
     _fields_ = [("precision", C.c_int), ("tail_box", C.c_int), ("phi_tol", C.c_double),
-                ("n_xi_wide", C.c_int), ("n_k_int", C.c_int), ("xi_reach", C.c_double)]
+                ("n_xi_wide", C.c_int), ("n_k_int", C.c_int), ("xi_reach", C.c_double), ("window", C.c_int)]
 
 
 class InvertMeta(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("nk_k", "nk_g", "n_kap", "n_gam")] + \
                [(n, C.c_double) for n in ("k_k_max", "k_g_max", "kap_min", "kap_max", "gam_max", "xi_min",
                                           "xi_max", "sigma", "phi_at_k_cut", "phi_at_g_cut", "mean", "var",
-                                          "skew", "sigmaDL", "norm", "ms_lambda", "ms_transform", "ms_path")]
+                                          "skew", "sigmaDL", "norm", "ms_lambda", "ms_transform", "ms_path",
+                                          "window", "xi_coarse", "xi_coarse_k")]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -72,6 +73,10 @@ def lib():
         L.sgl_sweep_set_cells.argtypes = [vp, C.c_int64, dp, dp]
         L.sgl_sweep_eval.argtypes = [vp, dp, C.c_int, C.c_int, dp, dp]
         L.sgl_measure_peak.argtypes = [vp, C.c_int, dp]
+        lp = C.POINTER(C.c_int64)
+        L.sgl_vp_set.argtypes = [vp, C.c_int, dp, dp, C.c_int, dp, C.c_int, dp, dp, C.c_int64, ip, dp, C.c_int, lp,
+                                 ip, dp, dp, dp, ip, ip, C.c_double]
+        L.sgl_vp_lnR.argtypes = [vp, dp, C.c_int, dp, C.c_int, C.c_int, dp, dp]
         for name in ("sgl_sweep_set_cells", "sgl_sweep_eval", "sgl_measure_peak"):
             getattr(L, name).restype = C.c_int
         L.sgl_cf_kappa_noalloc.argtypes = [vp, C.c_int, vp, vp, C.c_int64, vp, vp, vp]
@@ -80,9 +85,9 @@ def lib():
         L.sgl_invert_opts_default.restype = None
         L.sgl_pdf.argtypes = [vp, dp, C.c_int, C.POINTER(InvertOpts), dp, C.POINTER(InvertMeta)]
         for name in ("sgl_ctx_create", "sgl_ctx_stream", "sgl_ctx_profile", "sgl_lam_set_cells", "sgl_lam_set_xi", "sgl_lam_sigma", "sgl_lnphi",
-                     "sgl_xi_term", "sgl_pdf"):
+                     "sgl_xi_term", "sgl_pdf", "sgl_vp_set", "sgl_vp_lnR"):
             getattr(L, name).restype = C.c_int
-        if L.sgl_abi_version() != 1:
+        if L.sgl_abi_version() != 2:
             raise RuntimeError("libsgl_gb300.so ABI version mismatch; rebuild it")
         _lib = L
     return _lib
@@ -194,6 +199,37 @@ class Engine:
                                         _ptr(im)), "sgl_xi_term")
         return re + 1j * im
 
+    def set_vp(self, d):
+        """Installs the positive (vp) closure from a mapping with the arrays of sgl_vp_set (u, w, K, ku,
+        gu, cu, cw, gstart, sh_g, ga, gb, gc, glo, ghi, shear_var); None removes it."""
+        if d is None:
+            self._check(self._L.sgl_vp_set(self._h, 48, None, None, 0, None, 0, None, None, 0, None, None, 0, None,
+                                           None, None, None, None, None, None, 0.0), "sgl_vp_set")
+            return
+        f64 = lambda k: np.ascontiguousarray(d[k], np.float64)
+        i32 = lambda k: np.ascontiguousarray(d[k], np.int32)
+        u, w, ku, gu, cw, ga, gb, gc = (f64(k) for k in ("u", "w", "ku", "gu", "cw", "ga", "gb", "gc"))
+        K = np.ascontiguousarray(d["K"], np.float64).reshape(-1)
+        cu, sh_g, glo, ghi = (i32(k) for k in ("cu", "sh_g", "glo", "ghi"))
+        gstart = np.ascontiguousarray(d["gstart"], np.int64)
+        nsh, G = sh_g.size - 1, ga.size
+        if u.size != w.size or ku.size != gu.size or cu.size != cw.size or gstart.size != G + 1 or \
+                not (gb.size == gc.size == glo.size == ghi.size == G) or K.size != max(nsh - 1, 0) * u.size ** 2:
+            raise ValueError("vp closure arrays have inconsistent sizes")
+        self._check(self._L.sgl_vp_set(self._h, u.size, _ptr(u), _ptr(w), nsh, _ptr(K), ku.size, _ptr(ku), _ptr(gu),
+                                       cu.size, _ptr(cu, C.c_int32), _ptr(cw), G, _ptr(gstart, C.c_int64),
+                                       _ptr(sh_g, C.c_int32), _ptr(ga), _ptr(gb), _ptr(gc), _ptr(glo, C.c_int32),
+                                       _ptr(ghi, C.c_int32), float(d["shear_var"])), "sgl_vp_set")
+
+    def vp_lnR(self, kv, qv, precision=SGL_FP64):
+        kv = np.ascontiguousarray(np.atleast_1d(kv), np.float64)
+        qv = np.ascontiguousarray(np.atleast_1d(qv), np.float64)
+        re = np.empty((kv.size, qv.size))
+        im = np.empty((kv.size, qv.size))
+        self._check(self._L.sgl_vp_lnR(self._h, _ptr(kv), kv.size, _ptr(qv), qv.size, int(precision), _ptr(re),
+                                       _ptr(im)), "sgl_vp_lnR")
+        return re + 1j * im
+
     def sweep_set_cells(self, kap, w):
         kap = np.ascontiguousarray(kap, np.float64)
         w = np.ascontiguousarray(w, np.float64)
@@ -215,13 +251,16 @@ class Engine:
         return t.value
 
     def pdf(self, xi_out, precision=SGL_FP64, tail_box=True, phi_tol=1e-8, n_xi_wide=500, n_k_int=2400,
-            xi_reach=24.0):
+            xi_reach=24.0, window=False):
         x = np.ascontiguousarray(xi_out, np.float64)
         out = np.empty(x.size)
         o = InvertOpts()
         self._L.sgl_invert_opts_default(C.byref(o))
         o.precision, o.tail_box, o.phi_tol = int(precision), int(bool(tail_box)), float(phi_tol)
         o.n_xi_wide, o.n_k_int, o.xi_reach = int(n_xi_wide), int(n_k_int), float(xi_reach)
+        if window not in (True, False, "auto", None):
+            raise ValueError(f"window must be True, False or 'auto', got {window!r}")
+        o.window = 2 if window == "auto" else (1 if window is True else 0)
         meta = InvertMeta()
         self._check(self._L.sgl_pdf(self._h, _ptr(x), x.size, C.byref(o), _ptr(out), C.byref(meta)), "sgl_pdf")
         return out, meta.as_dict()

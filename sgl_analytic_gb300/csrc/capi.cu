@@ -93,7 +93,12 @@ struct sgl_ctx {
     XiHost xi;
     XiDevice xid;
     long long sweep_n = -1;          // cells of the 1-D sweep (sgl_sweep_set_cells)
-    SplineHost spline;
+    std::unordered_map<int, SplineHost> splines;   // not-a-knot collocation inverses by node count
+    // positive (vp) Cox closure replacing the gauss xi term (sgl_vp_set)
+    bool vp_on = false;
+    VpDevice vpd;
+    double vp_shear = 0.0;
+    int vp_xi_coarse = 101, vp_xi_coarse_k = 0;   // coarse grid (gamma, kappa); grown by sgl_pdf's rule
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // pinned staging ring for small uploads (pageable copies would serialise host and device);
     // reset whenever the stream has been synchronised
@@ -543,6 +548,68 @@ sgl_status xi_eval(sgl_ctx* ctx, int precision, const double* d_kk, const double
     return SGL_OK;
 }
 
+// numpy.unwrap along a strided line (period 2 pi, discontinuity pi)
+void unwrap_line(double* p, int n, long long stride) {
+    double corr = 0.0;
+    for (int i = 1; i < n; ++i) {
+        const double dd = p[(long long)i * stride] - (p[(long long)(i - 1) * stride] - corr);
+        double ddmod = std::fmod(dd + M_PI, 2.0 * M_PI);
+        if (ddmod < 0) ddmod += 2.0 * M_PI;
+        ddmod -= M_PI;
+        if (ddmod == -M_PI && dd > 0) ddmod = M_PI;
+        double pc = ddmod - dd;
+        if (std::fabs(dd) < M_PI) pc = 0.0;
+        corr += pc;
+        p[(long long)i * stride] += corr;
+    }
+}
+
+// ln R on kv x qv into device planes (tables, z buffer from the arena; rows in passes of <= 2 GiB z)
+sgl_status vp_lnR_device(sgl_ctx* ctx, int precision, const double* d_kv, int nk, const double* d_qv, int nq,
+                         double* d_re, double* d_im) {
+    const VpDevice& D = ctx->vpd;
+    void* tables = ctx->arena.get("vp_tables", vp_table_bytes(precision, D.U, nk, nq));
+    const int rows = vp_rows_per_pass(D.nsh, nk, nq, (size_t)2 << 30);
+    void* zb = ctx->arena.get("vp_z", (size_t)D.nsh * 49 * 16 * (size_t)rows * nq);
+    if (!tables || !zb) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (vp)");
+    const double pts = (double)nk * nq;
+    Timed t(ctx, precision == SGL_FP64 ? "vp_lnR_f64" : "vp_lnR_mixed", pts * (double)D.ncells * 12.0,
+            pts * D.nsh * 49 * 16.0 * 2);
+    launch_vp_lnR(precision, D, d_kv, nk, d_qv, nq, tables, (double2*)zb, rows, d_re, d_im, ctx->stream);
+    CKLAUNCH();
+    return SGL_OK;
+}
+
+// vp closure term on kk x kg (Closure.qxi, pos_closure.py:690-705): ln R, its imaginary part
+// unwrapped along k_kappa at the first k_gamma column and then along k_gamma, minus
+// shear_var kg^2 / 4.  Device planes out.
+sgl_status vp_qxi(sgl_ctx* ctx, int precision, const double* d_kk, int nk, const double* d_kg, const double* h_kg,
+                  int nkg, double* d_re, double* d_im) {
+    const cudaStream_t st = ctx->stream;
+    CKS(vp_lnR_device(ctx, precision, d_kk, nk, d_kg, nkg, d_re, d_im));
+    const long long npt = (long long)nk * nkg;
+    std::vector<double> im((size_t)npt), re((size_t)npt);
+    CK(cudaMemcpyAsync(im.data(), d_im, npt * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(re.data(), d_re, npt * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CKS(sync_stream(ctx));
+    unwrap_line(im.data(), nk, nkg);                              // first column along k_kappa
+    for (int i = 0; i < nk; ++i) unwrap_line(im.data() + (long long)i * nkg, nkg, 1);
+    for (long long e2 = 0; e2 < npt; ++e2) {
+        const double q = h_kg[e2 % nkg];
+        re[(size_t)e2] -= 0.25 * ctx->vp_shear * q * q;
+    }
+    CKS(upload(ctx, d_re, re.data(), (size_t)npt));
+    CKS(upload(ctx, d_im, im.data(), (size_t)npt));
+    CKS(sync_stream(ctx));
+    return SGL_OK;
+}
+
+sgl_status xi_any(sgl_ctx* ctx, int precision, const double* d_kk, const double* h_kk, int nk, const double* d_kg,
+                  const double* h_kg, int nkg, double* d_re, double* d_im) {
+    if (ctx->vp_on) return vp_qxi(ctx, precision, d_kk, nk, d_kg, h_kg, nkg, d_re, d_im);
+    return xi_eval(ctx, precision, d_kk, h_kk, nk, d_kg, h_kg, nkg, d_re, d_im);
+}
+
 // ------------------------------------------------------------------ Lambda on a grid
 // Separable Psi_1 GEMM stage: writes the (2nk x nkg) plane pair of TT into Gout.
 template <typename TT>
@@ -603,10 +670,12 @@ sgl_status lambda_eval(sgl_ctx* ctx, int precision, const double* h_kk, int nk, 
     CKS(upload(ctx, d_kk, h_kk, nk));
     CKS(upload(ctx, d_kg, h_kg, nkg));
     const bool use_sep = npt >= kSepMinPoints && nkg > 1;
-    const int n = kXiCoarse;
-    const bool use_interp = ctx->xi.on && npt > (long long)n * n && nk > 1 && nkg > 1 && h_kk[nk - 1] > 0 &&
+    const int n = ctx->vp_on ? ctx->vp_xi_coarse : kXiCoarse;                       // gamma nodes
+    const int nkc = (ctx->vp_on && ctx->vp_xi_coarse_k > 0) ? ctx->vp_xi_coarse_k : n;  // kappa nodes
+    const bool xi_active = ctx->xi.on || ctx->vp_on;
+    const bool use_interp = xi_active && npt > (long long)n * n && nk > 1 && nkg > 1 && h_kk[nk - 1] > 0 &&
                             h_kg[nkg - 1] > 0;
-    const bool exact_xi = ctx->xi.on && !use_interp;
+    const bool exact_xi = xi_active && !use_interp;
     if (exact_xi && write_phi) return fail(ctx, SGL_ERR_UNSUPPORTED, "exact xi term on an inversion grid");
 
     const void* G = nullptr;
@@ -647,38 +716,46 @@ sgl_status lambda_eval(sgl_ctx* ctx, int precision, const double* h_kk, int nk, 
     SplineAxis sk, sg;
     int ncg = 0;
     if (use_interp) {
-        if (!spline_setup(ctx->spline, n)) return fail(ctx, SGL_ERR_VALUE, "singular spline collocation");
-        const std::vector<double> s = linspace(0.0, 1.0, n);
-        std::vector<double> kkc(n), kgc(n);
+        SplineHost& Sg = ctx->splines[n];
+        SplineHost& Sk = ctx->splines[nkc];
+        if (!spline_setup(Sg, n) || !spline_setup(Sk, nkc)) return fail(ctx, SGL_ERR_VALUE, "singular spline collocation");
+        const std::vector<double> s = linspace(0.0, 1.0, n), s_k = linspace(0.0, 1.0, nkc);
+        std::vector<double> kkc(nkc), kgc(n);
         const double kkm = h_kk[nk - 1], kgm = h_kg[nkg - 1];
-        for (int i = 0; i < n; ++i) { kkc[i] = kkm * (s[i] * s[i]); kgc[i] = kgm * (s[i] * s[i]); }
-        DBUF(d_kkc, double, "xi_kkc", n);
+        for (int i = 0; i < nkc; ++i) kkc[i] = kkm * (s_k[i] * s_k[i]);
+        for (int i = 0; i < n; ++i) kgc[i] = kgm * (s[i] * s[i]);
+        DBUF(d_kkc, double, "xi_kkc", nkc);
         DBUF(d_kgc, double, "xi_kgc", n);
-        CKS(upload(ctx, d_kkc, kkc.data(), n));
+        CKS(upload(ctx, d_kkc, kkc.data(), nkc));
         CKS(upload(ctx, d_kgc, kgc.data(), n));
-        DBUF(d_Q, double, "xi_Qc", 2 * n * n);
-        CKS(xi_eval(ctx, precision, d_kkc, kkc.data(), n, d_kgc, kgc.data(), n, d_Q, d_Q + n * n));
-        // C = Minv Qc Minv^T for the real and imaginary parts (FP64)
-        DBUF(d_M, double, "spl_minv", n * n);
-        DBUF(d_knots, double, "spl_knots", n + 4);
-        CKS(upload(ctx, d_M, ctx->spline.minv.data(), (size_t)n * n));
-        CKS(upload(ctx, d_knots, ctx->spline.knots.data(), (size_t)n + 4));
-        DBUF(d_tmp, double, "spl_tmp", 2 * n * n);
-        DBUF(d_C, double, "spl_C", 2 * n * n);
-        std::vector<GemmDesc<double>> a{gd<double>(n, n, n, d_M, n, 1, d_Q, n, 1, d_tmp, n),
-                                        gd<double>(n, n, n, d_M, n, 1, d_Q + n * n, n, 1, d_tmp + n * n, n)};
+        const long long nq = (long long)nkc * n;
+        DBUF(d_Q, double, "xi_Qc", 2 * nq);
+        CKS(xi_any(ctx, precision, d_kkc, kkc.data(), nkc, d_kgc, kgc.data(), n, d_Q, d_Q + nq));
+        // C = Mk Qc Mg^T for the real and imaginary parts (FP64)
+        DBUF(d_Mk, double, "spl_mk", (long long)nkc * nkc);
+        DBUF(d_Mg, double, "spl_mg", (long long)n * n);
+        DBUF(d_knk, double, "spl_knots_k", nkc + 4);
+        DBUF(d_kng, double, "spl_knots_g", n + 4);
+        CKS(upload(ctx, d_Mk, Sk.minv.data(), (size_t)nkc * nkc));
+        CKS(upload(ctx, d_Mg, Sg.minv.data(), (size_t)n * n));
+        CKS(upload(ctx, d_knk, Sk.knots.data(), (size_t)nkc + 4));
+        CKS(upload(ctx, d_kng, Sg.knots.data(), (size_t)n + 4));
+        DBUF(d_tmp, double, "spl_tmp", 2 * nq);
+        DBUF(d_C, double, "spl_C", 2 * nq);
+        std::vector<GemmDesc<double>> a{gd<double>(nkc, n, nkc, d_Mk, nkc, 1, d_Q, n, 1, d_tmp, n),
+                                        gd<double>(nkc, n, nkc, d_Mk, nkc, 1, d_Q + nq, n, 1, d_tmp + nq, n)};
         CKS(run_gemms(ctx, a, "spl_a"));
-        std::vector<GemmDesc<double>> b{gd<double>(n, n, n, d_tmp, n, 1, d_M, 1, n, d_C, n),
-                                        gd<double>(n, n, n, d_tmp + n * n, n, 1, d_M, 1, n, d_C + n * n, n)};
+        std::vector<GemmDesc<double>> b{gd<double>(nkc, n, n, d_tmp, n, 1, d_Mg, 1, n, d_C, n),
+                                        gd<double>(nkc, n, n, d_tmp + nq, n, 1, d_Mg, 1, n, d_C + nq, n)};
         CKS(run_gemms(ctx, b, "spl_b"));
         DBUF(d_lk, int, "spl_lk", nk);
         DBUF(d_bk, double, "spl_bk", 4 * nk);
         DBUF(d_lg, int, "spl_lg", nkg);
         DBUF(d_bg, double, "spl_bg", 4 * nkg);
-        launch_spline_basis(d_kk, nk, kkm, d_knots, n, d_lk, d_bk, st); CKLAUNCH();
-        launch_spline_basis(d_kg, nkg, kgm, d_knots, n, d_lg, d_bg, st); CKLAUNCH();
+        launch_spline_basis(d_kk, nk, kkm, d_knk, nkc, d_lk, d_bk, st); CKLAUNCH();
+        launch_spline_basis(d_kg, nkg, kgm, d_kng, n, d_lg, d_bg, st); CKLAUNCH();
         sk.l = d_lk; sk.b = d_bk; sg.l = d_lg; sg.b = d_bg;
-        Cre = d_C; Cim = d_C + n * n; ncg = n;
+        Cre = d_C; Cim = d_C + nq; ncg = n;
     }
     if (write_phi && fin_precision != precision) return fail(ctx, SGL_ERR_UNSUPPORTED, "inversion grid below 2e5 points");
     {
@@ -689,7 +766,7 @@ sgl_status lambda_eval(sgl_ctx* ctx, int precision, const double* h_kk, int nk, 
     CKLAUNCH();
     if (exact_xi) {
         DBUF(d_qr, double, "xi_full", 2 * npt);
-        CKS(xi_eval(ctx, precision, d_kk, h_kk, nk, d_kg, h_kg, nkg, d_qr, d_qr + npt));
+        CKS(xi_any(ctx, precision, d_kk, h_kk, nk, d_kg, h_kg, nkg, d_qr, d_qr + npt));
         launch_sum_slices<double>(d_qr, 1, nk, nkg, (double*)out_re, nkg, 1.0, st); CKLAUNCH();
         launch_sum_slices<double>(d_qr + npt, 1, nk, nkg, (double*)out_im, nkg, 1.0, st); CKLAUNCH();
     }
@@ -713,8 +790,8 @@ sgl_status lambda_direct(sgl_ctx* ctx, const double* h_kk, int nk, const double*
     launch_psi1_direct(d_kk, nk, d_kg, nkg, d_k0, d_g0, d_w0, (int64_t)ctx->w0.size(), d_out, d_out + npt, d_dpart, st);
     CKLAUNCH();
     bool xi = false;
-    if (ctx->xi.on) {
-        CKS(xi_eval(ctx, SGL_FP64, d_kk, h_kk, nk, d_kg, h_kg, nkg, d_out + 2 * npt, d_out + 3 * npt));
+    if (ctx->xi.on || ctx->vp_on) {
+        CKS(xi_any(ctx, SGL_FP64, d_kk, h_kk, nk, d_kg, h_kg, nkg, d_out + 2 * npt, d_out + 3 * npt));
         xi = true;
     }
     std::vector<double> h((size_t)(4 * npt));
@@ -1134,10 +1211,169 @@ sgl_status sgl_lnphi(sgl_ctx* ctx, const double* kk, int nkk, const double* kg, 
     return SGL_OK;
 }
 
+sgl_status sgl_vp_set(sgl_ctx* ctx, int nstate, const double* u, const double* w, int n_shells, const double* K,
+                      int n_unique, const double* ku, const double* gu, int64_t n_cells, const int32_t* cu,
+                      const double* cw, int n_groups, const int64_t* gstart, const int32_t* sh_g, const double* ga,
+                      const double* gb, const double* gc, const int32_t* glo, const int32_t* ghi, double shear_var) {
+    if (!ctx) return SGL_ERR_VALUE;
+    if (n_shells == 0) { ctx->vp_on = false; return SGL_OK; }
+    if (nstate != 48) return fail(ctx, SGL_ERR_UNSUPPORTED, "vp closure: only the 48-state chain is built");
+    if (n_shells < 0 || n_unique < 1 || n_cells < 0 || n_groups < 0 || !u || !w || !ku || !gu || !gstart || !sh_g ||
+        (n_shells > 1 && !K) || (n_cells > 0 && (!cu || !cw)) || (n_groups > 0 && (!ga || !gb || !gc || !glo || !ghi)))
+        return fail(ctx, SGL_ERR_VALUE, "vp closure: missing arrays");
+    if (!std::isfinite(shear_var) || shear_var < 0) return fail(ctx, SGL_ERR_VALUE, "vp closure: shear_var must be finite, >= 0");
+    for (int j = 0; j < nstate; ++j)
+        if (!std::isfinite(u[j]) || !std::isfinite(w[j]) || (j > 0 && !(u[j] > u[j - 1])))
+            return fail(ctx, SGL_ERR_VALUE, "vp closure: state nodes must be finite and increasing");
+    for (long long e = 0; e < (long long)(n_shells - 1) * nstate * nstate; ++e)
+        if (!std::isfinite(K[e])) return fail(ctx, SGL_ERR_VALUE, "vp closure: non-finite transition matrix");
+    for (int i = 0; i < n_unique; ++i)
+        if (!std::isfinite(ku[i]) || !std::isfinite(gu[i])) return fail(ctx, SGL_ERR_VALUE, "vp closure: non-finite cell");
+    for (int64_t c = 0; c < n_cells; ++c)
+        if (cu[c] < 0 || cu[c] >= n_unique || !std::isfinite(cw[c]))
+            return fail(ctx, SGL_ERR_VALUE, "vp closure: cell index out of range or non-finite weight");
+    if (sh_g[0] != 0 || sh_g[n_shells] != n_groups) return fail(ctx, SGL_ERR_VALUE, "vp closure: shell offsets must span the groups");
+    for (int s = 0; s < n_shells; ++s)
+        if (sh_g[s + 1] < sh_g[s]) return fail(ctx, SGL_ERR_VALUE, "vp closure: shell offsets must be non-decreasing");
+    if (gstart[0] != 0 || gstart[n_groups] != n_cells) return fail(ctx, SGL_ERR_VALUE, "vp closure: group offsets must span the cells");
+    for (int g = 0; g < n_groups; ++g) {
+        if (gstart[g + 1] < gstart[g]) return fail(ctx, SGL_ERR_VALUE, "vp closure: group offsets must be non-decreasing");
+        if (!std::isfinite(ga[g]) || !std::isfinite(gb[g])) return fail(ctx, SGL_ERR_VALUE, "vp closure: non-finite rate");
+        if (glo[g] < 0 || ghi[g] >= nstate || glo[g] > ghi[g]) return fail(ctx, SGL_ERR_VALUE, "vp closure: bad rate interval");
+        // rate intervals (pos_closure_fused.py:18-48): c = 0 on all states, or c = -1 on an interval
+        // that reaches one end of the state grid
+        if (gc[g] == -1.0) {
+            if (ghi[g] != nstate - 1 && glo[g] != 0)
+                return fail(ctx, SGL_ERR_VALUE, "vp closure: clipped rate support must reach an end of the state grid");
+        } else if (gc[g] != 0.0) {
+            return fail(ctx, SGL_ERR_VALUE, "vp closure: rate offset c must be 0 or -1");
+        }
+    }
+    // zero stationary mean of every rate (pos_closure.py:15): the kernels rely on it
+    for (int g = 0; g < n_groups; ++g) {
+        double m = 0.0, mx = 0.0;
+        for (int j = 0; j < nstate; ++j) {
+            double D;
+            if (gc[g] == 0.0) D = ga[g] * u[j] + gb[g];
+            else if (j < glo[g] || j > ghi[g]) D = -1.0;
+            else D = -1.0 + (u[j] - u[ghi[g] == nstate - 1 ? glo[g] : ghi[g]]) * ga[g] + gb[g];
+            m += w[j] * D;
+            mx = std::max(mx, std::fabs(D));
+        }
+        if (std::fabs(m) > 1e-11 * std::max(mx, 1e-300) && mx > 0)
+            return fail(ctx, SGL_ERR_VALUE, "vp closure: a group's rate does not keep the mean (E_w[lam] != 1)");
+    }
+    // runs: per shell, groups ordered linear first, then by the first state they change
+    // (left: lo, right: hi + 1); cells concatenated with weights (w a, w b)
+    std::vector<int> cu_s, run_kind, run_bound, sh_run{0};
+    std::vector<double2> wab;
+    std::vector<float2> wabf;
+    std::vector<long long> run_cell{0};
+    cu_s.reserve((size_t)n_cells); wab.reserve((size_t)n_cells); wabf.reserve((size_t)n_cells);
+    for (int sh = 0; sh < n_shells; ++sh) {
+        std::vector<std::pair<int, int>> keyed;        // (sort key, group)
+        for (int g = sh_g[sh]; g < sh_g[sh + 1]; ++g) {
+            if (ga[g] == 0.0 && gb[g] == 0.0 && gc[g] == 0.0) continue;
+            if (gstart[g + 1] == gstart[g]) continue;
+            int key;
+            if (gc[g] == 0.0) key = -1;
+            else if (ghi[g] == nstate - 1) key = 2 * glo[g];            // left
+            else key = 2 * (ghi[g] + 1) + 1;                            // right
+            keyed.emplace_back(key, g);
+        }
+        std::stable_sort(keyed.begin(), keyed.end(), [](const std::pair<int, int>& x, const std::pair<int, int>& y) {
+            return x.first < y.first;
+        });
+        int cur_key = INT32_MIN;
+        for (const auto& kg : keyed) {
+            const int g = kg.second;
+            if (kg.first != cur_key) {
+                if (cur_key != INT32_MIN) run_cell.push_back((long long)cu_s.size());
+                cur_key = kg.first;
+                run_kind.push_back(gc[g] == 0.0 ? 0 : (ghi[g] == nstate - 1 ? 1 : 2));
+                run_bound.push_back(gc[g] == 0.0 ? 0 : (ghi[g] == nstate - 1 ? glo[g] : ghi[g]));
+            }
+            for (int64_t c = gstart[g]; c < gstart[g + 1]; ++c) {
+                cu_s.push_back(cu[c]);
+                const double2 v = make_double2(cw[c] * ga[g], cw[c] * gb[g]);
+                wab.push_back(v);
+                wabf.push_back(make_float2((float)v.x, (float)v.y));
+            }
+        }
+        if (cur_key != INT32_MIN) run_cell.push_back((long long)cu_s.size());
+        sh_run.push_back((int)run_kind.size());
+    }
+    const int nruns = (int)run_kind.size();
+    const long long ncs = (long long)cu_s.size();
+    CK(cudaSetDevice(ctx->device));
+    VpDevice D;
+    D.nsh = n_shells; D.U = n_unique; D.nruns = nruns; D.ncells = ncs;
+    DBUF(d_u, double, "vp_u", nstate);
+    DBUF(d_w, double, "vp_w", nstate);
+    DBUF(d_K, double, "vp_K", std::max<long long>(1, (long long)(n_shells - 1) * nstate * nstate));
+    DBUF(d_ku, double, "vp_ku", n_unique);
+    DBUF(d_gu, double, "vp_gu", n_unique);
+    DBUF(d_cu, int, "vp_cu", std::max<long long>(1, ncs));
+    DBUF(d_wab, double2, "vp_wab", std::max<long long>(1, ncs));
+    DBUF(d_wabf, float2, "vp_wabf", std::max<long long>(1, ncs));
+    DBUF(d_rc, long long, "vp_run_cell", nruns + 1);
+    DBUF(d_rk, int, "vp_run_kind", 2 * std::max(1, nruns));
+    DBUF(d_sr, int, "vp_sh_run", n_shells + 1);
+    CKS(upload(ctx, d_u, u, nstate));
+    CKS(upload(ctx, d_w, w, nstate));
+    if (n_shells > 1) CKS(upload(ctx, d_K, K, (size_t)(n_shells - 1) * nstate * nstate));
+    CKS(upload(ctx, d_ku, ku, n_unique));
+    CKS(upload(ctx, d_gu, gu, n_unique));
+    if (ncs > 0) {
+        CKS(upload(ctx, d_cu, cu_s.data(), (size_t)ncs));
+        CKS(upload(ctx, d_wab, wab.data(), (size_t)ncs));
+        CKS(upload(ctx, d_wabf, wabf.data(), (size_t)ncs));
+    }
+    CKS(upload(ctx, d_rc, run_cell.data(), run_cell.size()));
+    if (nruns > 0) {
+        CKS(upload(ctx, d_rk, run_kind.data(), (size_t)nruns));
+        CKS(upload(ctx, d_rk + nruns, run_bound.data(), (size_t)nruns));
+    }
+    CKS(upload(ctx, d_sr, sh_run.data(), sh_run.size()));
+    CKS(sync_stream(ctx));
+    D.u = d_u; D.w = d_w; D.K = d_K; D.ku = d_ku; D.gu = d_gu; D.cu = d_cu; D.wab = d_wab; D.wabf = d_wabf;
+    D.run_cell = d_rc; D.run_kind = d_rk; D.run_bound = d_rk + nruns; D.sh_run = d_sr;
+    ctx->vpd = D;
+    ctx->vp_shear = shear_var;
+    ctx->vp_xi_coarse = kXiCoarse;
+    ctx->vp_xi_coarse_k = 0;
+    ctx->vp_on = true;
+    return SGL_OK;
+}
+
+sgl_status sgl_vp_lnR(sgl_ctx* ctx, const double* kv, int nk, const double* qv, int nq, int precision,
+                      double* out_re, double* out_im) {
+    if (!ctx) return SGL_ERR_VALUE;
+    if (!ctx->vp_on) return fail(ctx, SGL_ERR_STATE, "vp closure not set");
+    if (nk < 1 || nq < 1 || !kv || !qv || !out_re || !out_im) return fail(ctx, SGL_ERR_VALUE, "empty grid");
+    if (precision != SGL_FP64 && precision != SGL_MIXED) return fail(ctx, SGL_ERR_VALUE, "unknown precision");
+    for (int i = 0; i < nk; ++i) if (!std::isfinite(kv[i])) return fail(ctx, SGL_ERR_VALUE, "non-finite k_kappa");
+    for (int i = 0; i < nq; ++i) if (!std::isfinite(qv[i])) return fail(ctx, SGL_ERR_VALUE, "non-finite k_gamma");
+    CK(cudaSetDevice(ctx->device));
+    const long long npt = (long long)nk * nq;
+    DBUF(d_kv, double, "vpr_k", nk);
+    DBUF(d_qv, double, "vpr_q", nq);
+    DBUF(d_o, double, "vpr_out", 2 * npt);
+    CKS(upload(ctx, d_kv, kv, nk));
+    CKS(upload(ctx, d_qv, qv, nq));
+    CKS(vp_lnR_device(ctx, precision, d_kv, nk, d_qv, nq, d_o, d_o + npt));
+    CK(cudaMemcpyAsync(out_re, d_o, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(out_im, d_o + npt, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CKS(sync_stream(ctx));
+    for (long long p = 0; p < npt; ++p)
+        if (!std::isfinite(out_re[p]) || !std::isfinite(out_im[p])) return fail(ctx, SGL_ERR_NONFINITE, "non-finite ln R");
+    return SGL_OK;
+}
+
 sgl_status sgl_xi_term(sgl_ctx* ctx, const double* kk, int nkk, const double* kg, int nkg, int precision,
                        double* out_re, double* out_im) {
     if (!ctx) return SGL_ERR_VALUE;
-    if (!ctx->xi.on) return fail(ctx, SGL_ERR_STATE, "xi groups not set");
+    if (!ctx->xi.on && !ctx->vp_on) return fail(ctx, SGL_ERR_STATE, "xi groups not set");
     if (nkk < 1 || nkg < 1 || !kk || !kg || !out_re || !out_im) return fail(ctx, SGL_ERR_VALUE, "empty grid");
     if (precision != SGL_FP64 && precision != SGL_MIXED) return fail(ctx, SGL_ERR_VALUE, "unknown precision");
     for (int i = 0; i < nkk; ++i) if (!std::isfinite(kk[i])) return fail(ctx, SGL_ERR_VALUE, "non-finite kk");
@@ -1149,7 +1385,7 @@ sgl_status sgl_xi_term(sgl_ctx* ctx, const double* kk, int nkk, const double* kg
     DBUF(d_o, double, "xt_out", 2 * npt);
     CKS(upload(ctx, d_kk, kk, nkk));
     CKS(upload(ctx, d_kg, kg, nkg));
-    CKS(xi_eval(ctx, precision, d_kk, kk, nkk, d_kg, kg, nkg, d_o, d_o + npt));
+    CKS(xi_any(ctx, precision, d_kk, kk, nkk, d_kg, kg, nkg, d_o, d_o + npt));
     CK(cudaMemcpyAsync(out_re, d_o, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(out_im, d_o + npt, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CKS(sync_stream(ctx));
@@ -1237,6 +1473,7 @@ void sgl_invert_opts_default(sgl_invert_opts* o) {
     o->n_xi_wide = 500;
     o->n_k_int = 2400;
     o->xi_reach = 24.0;
+    o->window = 0;
 }
 
 sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_invert_opts* opts, double* P_out,
@@ -1248,7 +1485,7 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
     sgl_invert_opts_default(&o);
     if (opts) o = *opts;
     if (o.precision != SGL_FP64 && o.precision != SGL_MIXED) return fail(ctx, SGL_ERR_VALUE, "unknown precision");
-    if (o.n_xi_wide < 2 || o.n_k_int < 2 || !(o.phi_tol > 0) || !(o.xi_reach > 0))
+    if (o.n_xi_wide < 2 || o.n_k_int < 2 || !(o.phi_tol > 0) || !(o.xi_reach > 0) || o.window < 0 || o.window > 2)
         return fail(ctx, SGL_ERR_VALUE, "invalid inversion options");
     for (int i = 0; i < n_xi; ++i) if (!std::isfinite(xi_out[i])) return fail(ctx, SGL_ERR_VALUE, "non-finite xi_out");
     CK(cudaSetDevice(ctx->device));
@@ -1302,6 +1539,14 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
     k_k_max = reach[0]; k_g_max = reach[1];
     const long long nk_k = (long long)std::ceil(k_k_max / dk_k) + 1;
     const long long nk_g = (long long)std::ceil(k_g_max / dk_g) + 1;
+    if (ctx->vp_on) {
+        // the positive closure's coarse grid follows ln R as the box grows, per axis
+        // (sgl_full.py:226-238); persistent, like the reference's Lam attributes
+        const double kks = k_k_max * sigma, kgs = k_g_max * sigma;
+        ctx->vp_xi_coarse = (int)std::min(401.0, std::max((double)ctx->vp_xi_coarse, 1.0 + std::ceil(12.65 * std::sqrt(kgs))));
+        ctx->vp_xi_coarse_k = (int)std::min(4001.0, std::max({(double)ctx->vp_xi_coarse_k, (double)ctx->vp_xi_coarse,
+                                                              1.0 + std::ceil(66.7 * std::sqrt(kks))}));
+    }
     if ((double)n_kap * (double)n_gam > kOutGridMax)
         return fail(ctx, SGL_ERR_UNSUPPORTED, "geometric output grid (n_kap * n_gam > OUT_GRID_MAX) not implemented");
     if ((double)nk_k * (double)nk_g > kInvertBlockPts)
@@ -1320,6 +1565,25 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
     void* Phi = ctx->arena.get("phi", 2ULL * nk * nkg * es);
     if (!Phi) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (phi)");
     CKS(lambda_eval(ctx, P, kk.data(), nk, kg.data(), nkg, 1, Phi, (char*)Phi + (size_t)nk * nkg * es));
+    // window (sgl_full.py:254-258): 1 always, 2 ("auto") only when the reach did not converge
+    const bool use_win = o.window == 1 || (o.window == 2 && std::max(phic[0], phic[1]) > o.phi_tol);
+    if (use_win) {
+        std::vector<double> wk(nk), wg(nkg);
+        for (int i = 0; i < nk; ++i) {
+            const double x = std::fabs(kk[i]) * 2.0 / k_k_max;
+            const double v = x < 1 ? 2.0 / 3.0 - x * x + x * x * x / 2 : (x < 2 ? (2 - x) * (2 - x) * (2 - x) / 6 : 0.0);
+            wk[i] = v / (2.0 / 3.0);
+        }
+        for (int j = 0; j < nkg; ++j) {
+            const double r = std::min(1.0, std::max(0.0, std::fabs(kg[j]) / k_g_max));
+            wg[j] = std::pow(1 - r, 4) * (4 * r + 1);
+        }
+        DBUF(d_wk, double, "win_k", nk);
+        DBUF(d_wg, double, "win_g", nkg);
+        CKS(upload(ctx, d_wk, wk.data(), nk));
+        CKS(upload(ctx, d_wg, wg.data(), nkg));
+        launch_window(P, Phi, nk, nkg, d_wk, d_wg, st); CKLAUNCH();
+    }
     cudaEventRecord(ctx->ev[1], st);
     // ---- transforms: F = Phi @ M (Hankel), P3ext = c CS @ [F | va | vb]
     DBUF(d_kk, double, "inv_kk", nk);
@@ -1409,6 +1673,9 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
         cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]);
         cudaEventElapsedTime(&cc, ctx->ev[2], ctx->ev[3]);
         meta->ms_lambda = a; meta->ms_transform = b; meta->ms_path = cc;
+        meta->window = use_win ? 1.0 : 0.0;
+        meta->xi_coarse = ctx->vp_on ? ctx->vp_xi_coarse : 0.0;
+        meta->xi_coarse_k = ctx->vp_on ? ctx->vp_xi_coarse_k : 0.0;
     }
     if (!finite) return fail(ctx, SGL_ERR_NONFINITE, "PDF inversion returned non-finite values");
     return SGL_OK;

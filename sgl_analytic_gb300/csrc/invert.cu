@@ -80,6 +80,24 @@ void launch_em_columns(int precision, const void* Phi, int nk, int nkg, double d
     else { k_em_columns<float><<<ceil_div(nk, 128), 128, 0, st>>>((const float*)Phi, nk, nkg, dkg, (float*)F, ldF, col); SGL_COUNT(1); }
 }
 
+// Phi[i, j] *= wk[i] wg[j] on both planes (positive-definite box window, sgl_full.py:83-94)
+template <typename TT>
+__global__ void k_window(TT* __restrict__ Phi, int nk, int nkg, const double* __restrict__ wk,
+                         const double* __restrict__ wg) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long npt = (long long)nk * nkg;
+    if (e >= npt) return;
+    const double w = wk[e / nkg] * wg[e % nkg];
+    Phi[e] = (TT)((double)Phi[e] * w);
+    Phi[npt + e] = (TT)((double)Phi[npt + e] * w);
+}
+
+void launch_window(int precision, void* Phi, int nk, int nkg, const double* wk, const double* wg, cudaStream_t st) {
+    const long long tot = (long long)nk * nkg;
+    if (precision == SGL_FP64) { k_window<double><<<ceil_div(tot, 256), 256, 0, st>>>((double*)Phi, nk, nkg, wk, wg); SGL_COUNT(1); }
+    else { k_window<float><<<ceil_div(tot, 256), 256, 0, st>>>((float*)Phi, nk, nkg, wk, wg); SGL_COUNT(1); }
+}
+
 // P3[i, j] = P3ext[i, j] + P3ext[i, ngam] + P3ext[i, ngam + 1] gam_j^2  (already scaled by 1/(2 pi^2))
 template <typename TT>
 __global__ void k_p3_finish(const TT* __restrict__ P3ext, int nkap, int ngam, int ld, const double* __restrict__ gam,

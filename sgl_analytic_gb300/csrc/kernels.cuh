@@ -109,11 +109,36 @@ void launch_kappa_matrix(int precision, const double* kk, int nk, double dkk, co
                          cudaStream_t st);
 void launch_em_columns(int precision, const void* Phi, int nk, int nkg, double dkg, void* F, int ldF, int col,
                        cudaStream_t st);
+void launch_window(int precision, void* Phi, int nk, int nkg, const double* wk, const double* wg, cudaStream_t st);
 void launch_p3_finish(int precision, const void* P3ext, int nkap, int ngam, int ld, const double* gam, double* P3,
                       cudaStream_t st);
 void launch_path_integral(const double* P3, int nkap, int ngam, double kap0, double kap1, double gam1,
                           const double* xi, int nxi, double gmax, double g_def, int n_k_int, double* out,
                           cudaStream_t st);
+
+// ---- positive (vp) Cox closure
+// Cells sorted per shell into runs (one kind and interval bound; runs ordered linear first, then by
+// the first state they change: lo for left runs, hi + 1 for right runs), per-cell weights (w a, w b).
+struct VpDevice {
+    int nsh = 0, U = 0, nruns = 0;
+    long long ncells = 0;
+    const double* u = nullptr;          // [48] Gauss-Hermite nodes
+    const double* w = nullptr;          // [48] stationary weights
+    const double* K = nullptr;          // [(nsh - 1) * 48 * 48] transition matrices K[s][i][j]
+    const double* ku = nullptr;         // [U] unique cell kappa
+    const double* gu = nullptr;         // [U] unique cell gamma
+    const int* cu = nullptr;            // [ncells] unique-cell index, run-sorted
+    const double2* wab = nullptr;       // [ncells] (w a, w b)
+    const float2* wabf = nullptr;       // [ncells] the same, rounded to FP32
+    const long long* run_cell = nullptr;   // [nruns + 1] cell offsets
+    const int* run_kind = nullptr;      // [nruns] 0 linear, 1 left (states lo..47), 2 right (states 0..hi)
+    const int* run_bound = nullptr;     // [nruns] lo (left) or hi (right)
+    const int* sh_run = nullptr;        // [nsh + 1] run offsets
+};
+size_t vp_table_bytes(int precision, int U, int nk, int nq);
+int vp_rows_per_pass(int nsh, int nk, int nq, size_t z_cap_bytes);
+void launch_vp_lnR(int precision, const VpDevice& d, const double* kv, int nk, const double* qv, int nq, void* tables,
+                   double2* zbuf, int rows_per_pass, double* out_re, double* out_im, cudaStream_t st);
 
 // ---- 1-D CF sweep and FMA probes
 int sweep1d_chunks(int nk, long long nc);

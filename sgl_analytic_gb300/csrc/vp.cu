@@ -1,0 +1,320 @@
+// Positive (vp) Cox closure: ln R(k, q) = ln E_U exp( sum_s z_s(U_s; k, q) ),
+//   z_s(u_j) = sum_{g in shell s} D_g(u_j) Y_g,   Y_g = sum_{c in g} w_c F_c,
+//   F_c(k, q) = e_c J_c + J_c - 1,  e = expm1(i k kap_c), J = J0(q gam_c)
+// (reference: FusedVP.lnR_blocked pos_closure_fused.py:119-140 = _fused_groups :51-105 +
+//  _chain_recursion pos_closure.py:184-240).
+//
+// D_g(u) = lam_g(u) - 1 is, per group, c + a (u - anchor) + b on an interval of states that reaches
+// an end of the state grid (rate_intervals pos_closure_fused.py:18-48), and E_w[D_g] = 0 exactly
+// (the rates keep the mean, pos_closure.py:15).  The host sorts each shell's groups into RUNS of
+// one kind and one interval bound (linear; "left" = states lo..47; "right" = states 0..hi) and
+// stores per-cell weights (w a, w b).  Then
+//   z_s(u_j) = u_j A_lin + sum_{left runs, lo <= j} [(u_j - u_lo) A_r + B_r]
+//            + sum_{right runs, j <= hi} [(u_j - u_hi) A_r + B_r] + const,
+//   A_r = sum_{c in r} (w a)_c F_c,  B_r = sum_{c in r} (w b)_c F_c.
+// The constant (c = -1 offsets, linear intercepts) is not formed: z_s has zero stationary mean, so
+// z_s = z_partial - E_w[z_partial] exactly, and that projection also removes the common-mode part
+// of the rounding error (what keeps the mixed path within 1e-8 of FP64).
+//
+// Phase 1 (k_vp_z): one CTA per (shell, 16 k x 32 q tile); each thread owns 2 x 2 points.  Cells of
+// a run stream through shared memory in chunks of 32 (table rows e[u][k], (J, J - 1)[u][q] gathered
+// by cell index, coalesced along k / q); per point 4 FMAs + 2 for F.  Mixed: FP32 chunk sums folded
+// into float-float run totals (TwoSum); FP64: FP64 throughout.  Run totals go to FP64 running sums
+// over the sorted bounds and each state's z is written once (FP64, [shell][state][point]).
+// Phase 2 (k_vp_chain): one thread per point walks the shells: projection, alpha' = K^T alpha (or the
+// stationary weights at s = 0) times exp(z - max Re z), renormalisation by max |alpha|, log scale;
+// FP64 in both precisions.  Thread-private shared memory, no barriers.
+#include "kernels.cuh"
+
+namespace sgl {
+
+constexpr int kVpNS = 48;                 // latent states (Gauss-Hermite nodes)
+constexpr int kZK = 16, kZQ = 32;         // phase-1 point tile (k x q)
+constexpr int kZThreads = 128;            // 2 x 2 points per thread
+constexpr int kZCh = 32;                  // cells per staged chunk
+constexpr int kChPts = 64;                // phase-2 points per CTA
+
+template <typename TT> struct V2;
+template <> struct V2<float> { using T = float2; };
+template <> struct V2<double> { using T = double2; };
+
+// e[u][i] = (cos - 1, sin)(k_i kap_u) from the half angle (no cancellation); Jt[u][j] = (J0, J0 - 1)
+template <typename TT>
+__global__ void k_vp_tables(const double* __restrict__ ku, const double* __restrict__ gu, int U,
+                            const double* __restrict__ kv, int nk, const double* __restrict__ qv, int nq,
+                            typename V2<TT>::T* __restrict__ e, typename V2<TT>::T* __restrict__ Jt) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long ne = (long long)U * nk;
+    if (t < ne) {
+        const int u = (int)(t / nk), i = (int)(t % nk);
+        const double ph = kv[i] * ku[u];
+        double s, c;
+        sincos(0.5 * ph, &s, &c);
+        e[t].x = (TT)(-2.0 * s * s);
+        e[t].y = (TT)(2.0 * s * c);
+    } else if (t < ne + (long long)U * nq) {
+        const long long r = t - ne;
+        const int u = (int)(r / nq), j = (int)(r % nq);
+        const double jm = j0m1_d(qv[j] * gu[u]);
+        Jt[r].x = (TT)(1.0 + jm);
+        Jt[r].y = (TT)jm;
+    }
+}
+
+// hi + lo += p  (Knuth TwoSum; no FMA contraction applies to additions)
+__device__ __forceinline__ void ff_acc(float& hi, float& lo, float p) {
+    const float s = hi + p;
+    const float bb = s - hi;
+    const float err = (hi - (s - bb)) + (p - bb);
+    hi = s;
+    lo += err;
+}
+
+template <typename TT>
+__global__ void __launch_bounds__(kZThreads)
+k_vp_z(VpDevice d, const typename V2<TT>::T* __restrict__ e, const typename V2<TT>::T* __restrict__ Jt, int nk,
+       int nq, int kb, int nkc, double2* __restrict__ zp, double2* __restrict__ alin, long long NP) {
+    using T2 = typename V2<TT>::T;
+    __shared__ T2 s_e[kZCh][kZK];
+    __shared__ T2 s_J[kZCh][kZQ];
+    __shared__ T2 s_w[kZCh];
+    constexpr bool MIX = sizeof(TT) == 4;
+    const int s = blockIdx.z;
+    const int q0 = blockIdx.x * kZQ, k0 = kb + blockIdx.y * kZK, kend = kb + nkc;
+    const int t = threadIdx.x, tq = t % 16, tk = t / 16;
+    // my points: (k0 + tk + 8 m, q0 + tq + 16 i), index P = 2 m + i
+    double SAr[4], SAi[4], SBr[4], SBi[4], ALr[4], ALi[4];
+#pragma unroll
+    for (int P = 0; P < 4; ++P) { SAr[P] = SAi[P] = SBr[P] = SBi[P] = ALr[P] = ALi[P] = 0.0; }
+    long long pidx[4];
+    bool live[4];
+#pragma unroll
+    for (int P = 0; P < 4; ++P) {
+        const int k = k0 + tk + 8 * (P >> 1), q = q0 + tq + 16 * (P & 1);
+        live[P] = k < kend && q < nq;
+        pidx[P] = (long long)(k - kb) * nq + q;
+    }
+    int jcur = 0;
+    auto emit_to = [&](int jend) {
+        for (; jcur < jend; ++jcur) {
+            const double uj = d.u[jcur];
+            double2* row = zp + ((long long)s * kVpNS + jcur) * NP;
+#pragma unroll
+            for (int P = 0; P < 4; ++P)
+                if (live[P]) row[pidx[P]] = make_double2(fma(uj, SAr[P], SBr[P]), fma(uj, SAi[P], SBi[P]));
+        }
+    };
+    const int r0 = d.sh_run[s], r1 = d.sh_run[s + 1];
+    for (int r = r0; r < r1; ++r) {
+        const long long c0 = d.run_cell[r], c1 = d.run_cell[r + 1];
+        // run totals: mixed = float-float (hi, lo), FP64 = plain
+        TT hi[4][4], lo[4][4];
+#pragma unroll
+        for (int P = 0; P < 4; ++P)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) { hi[P][v] = TT(0); lo[P][v] = TT(0); }
+        for (long long base = c0; base < c1; base += kZCh) {
+            const int cnt = (int)((c1 - base) < kZCh ? (c1 - base) : kZCh);
+            __syncthreads();
+            for (int idx = t; idx < kZCh * kZK; idx += kZThreads) {
+                const int c = idx / kZK, rr = idx % kZK, k = k0 + rr;
+                T2 v; v.x = TT(0); v.y = TT(0);
+                if (c < cnt && k < kend) v = e[(long long)d.cu[base + c] * nk + k];
+                s_e[c][rr] = v;
+            }
+            for (int idx = t; idx < kZCh * kZQ; idx += kZThreads) {
+                const int c = idx / kZQ, rr = idx % kZQ, q = q0 + rr;
+                T2 v; v.x = TT(0); v.y = TT(0);
+                if (c < cnt && q < nq) v = Jt[(long long)d.cu[base + c] * nq + q];
+                s_J[c][rr] = v;
+            }
+            if (t < kZCh) {
+                T2 v; v.x = TT(0); v.y = TT(0);
+                if (t < cnt) {
+                    if constexpr (MIX) { const float2 f = d.wabf[base + t]; v.x = f.x; v.y = f.y; }
+                    else { const double2 f = d.wab[base + t]; v.x = f.x; v.y = f.y; }
+                }
+                s_w[t] = v;
+            }
+            __syncthreads();
+            TT p[4][4];
+#pragma unroll
+            for (int P = 0; P < 4; ++P)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) p[P][v] = TT(0);
+            for (int c = 0; c < cnt; ++c) {
+                const T2 wv = s_w[c];
+                const T2 ev[2] = {s_e[c][tk], s_e[c][tk + 8]};
+                const T2 jv[2] = {s_J[c][tq], s_J[c][tq + 16]};
+#pragma unroll
+                for (int P = 0; P < 4; ++P) {
+                    const T2 ee = ev[P >> 1], jj = jv[P & 1];
+                    const TT Fr = ee.x * jj.x + jj.y;          // (cos - 1) J + (J - 1)
+                    const TT Fi = ee.y * jj.x;                 // sin J
+                    p[P][0] += wv.x * Fr; p[P][1] += wv.x * Fi;
+                    p[P][2] += wv.y * Fr; p[P][3] += wv.y * Fi;
+                }
+            }
+#pragma unroll
+            for (int P = 0; P < 4; ++P)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    if constexpr (MIX) ff_acc(hi[P][v], lo[P][v], p[P][v]);
+                    else hi[P][v] += p[P][v];
+                }
+        }
+        const int kind = d.run_kind[r], bound = d.run_bound[r];
+        if (kind == 0) {                                   // linear: u_j A (intercept dropped)
+#pragma unroll
+            for (int P = 0; P < 4; ++P) {
+                ALr[P] += (double)hi[P][0] + (double)lo[P][0];
+                ALi[P] += (double)hi[P][1] + (double)lo[P][1];
+            }
+        } else if (kind == 1) {                            // left: states >= lo, anchored at u_lo
+            emit_to(bound);
+            const double ub = d.u[bound];
+#pragma unroll
+            for (int P = 0; P < 4; ++P) {
+                const double Ar = (double)hi[P][0] + (double)lo[P][0], Ai = (double)hi[P][1] + (double)lo[P][1];
+                const double Br = (double)hi[P][2] + (double)lo[P][2], Bi = (double)hi[P][3] + (double)lo[P][3];
+                SAr[P] += Ar; SAi[P] += Ai;
+                SBr[P] += fma(-ub, Ar, Br); SBi[P] += fma(-ub, Ai, Bi);
+            }
+        } else {                                           // right: states <= hi, anchored at u_hi
+            // = u_j A on every state (+ a dropped constant) minus [(u_j - u_hi) A + B] on states > hi
+            emit_to(bound + 1);
+            const double ub = d.u[bound];
+#pragma unroll
+            for (int P = 0; P < 4; ++P) {
+                const double Ar = (double)hi[P][0] + (double)lo[P][0], Ai = (double)hi[P][1] + (double)lo[P][1];
+                const double Br = (double)hi[P][2] + (double)lo[P][2], Bi = (double)hi[P][3] + (double)lo[P][3];
+                ALr[P] += Ar; ALi[P] += Ai;
+                SAr[P] -= Ar; SAi[P] -= Ai;
+                SBr[P] += fma(ub, Ar, -Br); SBi[P] += fma(ub, Ai, -Bi);
+            }
+        }
+    }
+    emit_to(kVpNS);
+#pragma unroll
+    for (int P = 0; P < 4; ++P)
+        if (live[P]) alin[(long long)s * NP + pidx[P]] = make_double2(ALr[P], ALi[P]);
+}
+
+__global__ void __launch_bounds__(kChPts)
+k_vp_chain(VpDevice d, const double2* __restrict__ zp, const double2* __restrict__ alin, long long NP, int nq, int kb,
+           double* __restrict__ out_re, double* __restrict__ out_im) {
+    extern __shared__ __align__(16) unsigned char vsm[];
+    double (*ar)[kChPts] = (double (*)[kChPts])vsm;                       // alpha (normalised)
+    double (*ai)[kChPts] = (double (*)[kChPts])(vsm + 1 * kVpNS * kChPts * 8);
+    double (*br)[kChPts] = (double (*)[kChPts])(vsm + 2 * kVpNS * kChPts * 8);   // z, then alpha'
+    double (*bi)[kChPts] = (double (*)[kChPts])(vsm + 3 * kVpNS * kChPts * 8);
+    const int t = threadIdx.x;
+    const long long p = (long long)blockIdx.x * kChPts + t;
+    if (p >= NP) return;                       // each thread touches only its own column
+    double scale = 0.0;
+    for (int s = 0; s < d.nsh; ++s) {
+        const double2 al = alin[(long long)s * NP + p];
+        double mr = 0.0, mi = 0.0;
+        for (int j = 0; j < kVpNS; ++j) {
+            const double2 zz = zp[((long long)s * kVpNS + j) * NP + p];
+            const double uj = d.u[j], wj = d.w[j];
+            const double zr = fma(uj, al.x, zz.x), zi = fma(uj, al.y, zz.y);
+            br[j][t] = zr; bi[j][t] = zi;
+            mr = fma(wj, zr, mr); mi = fma(wj, zi, mi);
+        }
+        double mx = -1e300;
+        for (int j = 0; j < kVpNS; ++j) {
+            const double zr = br[j][t] - mr;
+            br[j][t] = zr; bi[j][t] -= mi;
+            mx = fmax(mx, zr);
+        }
+        double nrm = 0.0;
+        const double* Ks = d.K + (long long)(s > 0 ? s - 1 : 0) * kVpNS * kVpNS;
+        for (int j0 = 0; j0 < kVpNS; j0 += 4) {
+            double gr[4], gi[4];
+            if (s == 0) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) { gr[q] = d.w[j0 + q]; gi[q] = 0.0; }
+            } else {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) { gr[q] = 0.0; gi[q] = 0.0; }
+                for (int i = 0; i < kVpNS; ++i) {
+                    const double xr = ar[i][t], xi = ai[i][t];
+                    const double2 k01 = *(const double2*)(Ks + i * kVpNS + j0);
+                    const double2 k23 = *(const double2*)(Ks + i * kVpNS + j0 + 2);
+                    gr[0] = fma(k01.x, xr, gr[0]); gi[0] = fma(k01.x, xi, gi[0]);
+                    gr[1] = fma(k01.y, xr, gr[1]); gi[1] = fma(k01.y, xi, gi[1]);
+                    gr[2] = fma(k23.x, xr, gr[2]); gi[2] = fma(k23.x, xi, gi[2]);
+                    gr[3] = fma(k23.y, xr, gr[3]); gi[3] = fma(k23.y, xi, gi[3]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int j = j0 + q;
+                const double m = exp(br[j][t] - mx);
+                double sn, cs;
+                sincos(bi[j][t], &sn, &cs);
+                const double er = m * cs, ei = m * sn;
+                const double nr = gr[q] * er - gi[q] * ei, ni = gr[q] * ei + gi[q] * er;
+                br[j][t] = nr; bi[j][t] = ni;
+                nrm = fmax(nrm, nr * nr + ni * ni);
+            }
+        }
+        nrm = sqrt(nrm);
+        const double inv = 1.0 / nrm;
+        for (int j = 0; j < kVpNS; ++j) { ar[j][t] = br[j][t] * inv; ai[j][t] = bi[j][t] * inv; }
+        scale += mx + log(nrm);
+    }
+    double sr = 0.0, si = 0.0;
+    for (int j = 0; j < kVpNS; ++j) { sr += ar[j][t]; si += ai[j][t]; }
+    const long long o = (long long)kb * nq + p;
+    out_re[o] = scale + 0.5 * log(sr * sr + si * si);
+    out_im[o] = atan2(si, sr);
+}
+
+size_t vp_table_bytes(int precision, int U, int nk, int nq) {
+    const size_t es = precision == SGL_FP64 ? 8 : 4;
+    return 2 * es * ((size_t)U * nk + (size_t)U * nq) + 256;
+}
+
+int vp_rows_per_pass(int nsh, int nk, int nq, size_t z_cap_bytes) {
+    const size_t per_row = (size_t)nsh * (kVpNS + 1) * 16 * (size_t)nq;
+    long long rows = (long long)(z_cap_bytes / (per_row > 0 ? per_row : 1));
+    if (rows < 1) rows = 1;
+    if (rows > nk) rows = nk;
+    return (int)rows;
+}
+
+void launch_vp_lnR(int precision, const VpDevice& d, const double* kv, int nk, const double* qv, int nq, void* tables,
+                   double2* zbuf, int rows_per_pass, double* out_re, double* out_im, cudaStream_t st) {
+    const long long tot = (long long)d.U * (nk + nq);
+    const size_t es = precision == SGL_FP64 ? 8 : 4;
+    void* e = tables;
+    void* Jt = (char*)tables + 2 * es * (size_t)d.U * nk;
+    if (precision == SGL_FP64) {
+        k_vp_tables<double><<<ceil_div(tot, 256), 256, 0, st>>>(d.ku, d.gu, d.U, kv, nk, qv, nq, (double2*)e, (double2*)Jt);
+        SGL_COUNT(1);
+    } else {
+        k_vp_tables<float><<<ceil_div(tot, 256), 256, 0, st>>>(d.ku, d.gu, d.U, kv, nk, qv, nq, (float2*)e, (float2*)Jt);
+        SGL_COUNT(1);
+    }
+    const size_t chain_smem = 4 * (size_t)kVpNS * kChPts * sizeof(double);
+    cudaFuncSetAttribute(k_vp_chain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chain_smem);
+    for (int kb = 0; kb < nk; kb += rows_per_pass) {
+        const int nkc = nk - kb < rows_per_pass ? nk - kb : rows_per_pass;
+        const long long NP = (long long)nkc * nq;
+        double2* zp = zbuf;
+        double2* al = zbuf + (long long)d.nsh * kVpNS * NP;
+        dim3 g1(ceil_div(nq, kZQ), ceil_div(nkc, kZK), d.nsh);
+        if (precision == SGL_FP64) {
+            k_vp_z<double><<<g1, kZThreads, 0, st>>>(d, (const double2*)e, (const double2*)Jt, nk, nq, kb, nkc, zp, al, NP);
+            SGL_COUNT(1);
+        } else {
+            k_vp_z<float><<<g1, kZThreads, 0, st>>>(d, (const float2*)e, (const float2*)Jt, nk, nq, kb, nkc, zp, al, NP);
+            SGL_COUNT(1);
+        }
+        { k_vp_chain<<<ceil_div(NP, kChPts), kChPts, chain_smem, st>>>(d, zp, al, NP, nq, kb, out_re, out_im); SGL_COUNT(1); }
+    }
+}
+
+}  // namespace sgl

@@ -7,7 +7,10 @@ import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
 GOLDEN = ROOT / "tests" / "golden"
-FULL_FIXTURE = ROOT / "_work" / "fixtures" / "cells_zs1_gauss_full.npz"
+# full-size fixtures made by tests/golden/make_fixtures.py / make_vp_fixtures.py (git-ignored)
+FULL_DIR = GOLDEN / "full"
+FULL_FIXTURE = FULL_DIR / "cells_zs1_gauss_full.npz"
+VP_FULL = FULL_DIR / "vp_zs1_full.npz"
 if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
 

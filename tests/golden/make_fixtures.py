@@ -6,12 +6,12 @@ installable here, so this script puts ``oracle/numba_standin`` (``njit`` = ident
 
 Stage ``build`` (slow, ~30 min per z_s on 8 cores): replicates ``pipeline.run`` up to the
 population build (sgl_analytic/pipeline.py:165-192) and pickles the reference's own
-``Cells`` object into ``_work/big/`` (large, never committed).
+``Cells`` object into ``tests/golden/full/`` (large, git-ignored, never committed).
 
 Stage ``extract``: from the pickle, constructs the reference ``Lam`` (sgl_full.py:2728) and
 writes the compact inputs of the hot path -- the occupied fine cells (w0, k0, g0, fine gamma
 bin), the weak-arm variance, the xi_lin groups and the coarse lattice centres -- plus
-the reference's sigma.  Output: ``_work/fixtures/cells_zs<z>_<closure>_full.npz`` (all xi groups;
+the reference's sigma.  Output: ``tests/golden/full/cells_zs<z>_<closure>_full.npz`` (all xi groups;
 ~290 MB at z_s=1, not committed; the committed subset is made by ``make_golden.py``).
 
 Usage (from the repository root)::
@@ -33,8 +33,8 @@ import numpy as np
 REPO = Path(__file__).resolve().parents[2]
 REF_SRC = Path("/root/reference/src")
 STANDIN = REPO / "oracle" / "numba_standin"
-WORK = REPO / "_work" / "big"
-FULL = REPO / "_work" / "fixtures"
+FULL = REPO / "tests" / "golden" / "full"          # large, git-ignored
+WORK = FULL
 GOLDEN = REPO / "tests" / "golden"
 
 

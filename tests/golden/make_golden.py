@@ -31,8 +31,8 @@ import numpy as np
 REPO = Path(__file__).resolve().parents[2]
 REF = Path("/root/reference")
 GOLDEN = REPO / "tests" / "golden"
-WORK = REPO / "_work" / "big"
-FULL = REPO / "_work" / "fixtures"
+FULL = REPO / "tests" / "golden" / "full"          # large, git-ignored
+WORK = FULL
 SHELL = 30
 
 

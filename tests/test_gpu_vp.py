@@ -1,0 +1,174 @@
+"""GPU parity of the positive (vp) Cox closure: ln R through the C ABI against the reference's own
+outputs (tests/golden/make_vp_fixtures.py) and the NumPy oracle (oracle/vp_oracle.py).
+
+Tolerances: FP64 ln R within 1e-14 + 1e-10 |ln R| of the reference; mixed ln R within
+2e-8 (1 + |ln R|) of FP64 (FP32 cell sums in chunks of 32, float-float run totals, FP64 chain);
+the vp PDF through the whole chain within
+1e-5 of peak of the stored golden (whose closure was built with the reference's pinned numpy /
+scipy: 0.03% of its groups differ from the rebuild used here) and the mixed PDF within L1 1e-4 of
+the FP64 one.
+"""
+import json
+
+import numpy as np
+import pytest
+
+from tests.conftest import GOLDEN, VP_FULL
+
+pytestmark = pytest.mark.gpu
+
+KV = np.array([0.0, 1.5, 9.0, 40.0, 123.0, 250.0, 610.0, 900.0, 1010.0])            # 9 rows (tile 4)
+QV = np.concatenate([[0.0], np.geomspace(2.0, 800.0, 36)])                           # 37 columns (tile 16)
+
+
+@pytest.fixture(scope="module")
+def vp_sub():
+    return dict(np.load(GOLDEN / "vp_zs1_sub.npz"))
+
+
+@pytest.fixture(scope="module")
+def eng_sub(vp_sub):
+    from sgl_analytic_gb300._lib import Engine
+    e = Engine(0)
+    e.set_vp(vp_sub)
+    return e
+
+
+def mirrored(d):
+    """The same closure with the states relabelled j -> 47 - j (u -> -u on the symmetric nodes):
+    every clipped "left" rate (states lo..47) becomes a "right" one (states 0..47-lo, slope -a,
+    anchored at its upper end) and linear slopes change sign; ln R is unchanged."""
+    m = dict(d)
+    ns = d["u"].size
+    m["K"] = d["K"][:, ::-1, ::-1].copy()
+    m["w"] = d["w"][::-1].copy()
+    m["ga"] = -d["ga"]
+    clipped = d["gc"] != 0
+    m["glo"] = np.where(clipped, ns - 1 - d["ghi"], d["glo"]).astype(np.int32)
+    m["ghi"] = np.where(clipped, ns - 1 - d["glo"], d["ghi"]).astype(np.int32)
+    return m
+
+
+def _close(a, b, atol, rtol):
+    return np.abs(a - b) <= atol + rtol * np.abs(b)
+
+
+def test_lnR_matches_reference_golden(eng_sub, vp_sub):
+    """Sub-closure (shells 0-5): the reference's _fused_groups + _chain_recursion on 5 x 4 points."""
+    L = eng_sub.vp_lnR(vp_sub["kv"], vp_sub["qv"])
+    assert _close(L, vp_sub["lnR"], 1e-14, 1e-10).all(), np.abs(L - vp_sub["lnR"]).max()
+
+
+def test_lnR_matches_oracle_on_ragged_grid(eng_sub, vp_sub):
+    """9 x 37 points: partial tiles on both axes."""
+    from oracle.vp_oracle import lnR
+    kv, qv = KV[::2], QV[::3]
+    L = eng_sub.vp_lnR(kv, qv)
+    Lo = lnR(vp_sub, kv, qv)
+    assert _close(L, Lo, 1e-14, 1e-10).all(), np.abs(L - Lo).max()
+
+
+def test_right_clipped_rates_mirror(vp_sub):
+    """Right-clipped runs (states 0..hi): the mirrored closure gives the same ln R."""
+    from oracle.vp_oracle import lnR
+    from sgl_analytic_gb300._lib import SGL_MIXED, Engine
+    m = mirrored(vp_sub)
+    e = Engine(0)
+    e.set_vp(m)
+    kv, qv = KV[::2], QV[::3]
+    L = e.vp_lnR(kv, qv)
+    Lo = lnR(vp_sub, kv, qv)
+    assert _close(L, Lo, 1e-14, 1e-10).all(), np.abs(L - Lo).max()
+    Lm = e.vp_lnR(kv, qv, SGL_MIXED)
+    assert (np.abs(Lm - L) / (1 + np.abs(L))).max() <= 2e-8
+
+
+def test_lnR_mixed_vs_fp64(eng_sub):
+    from sgl_analytic_gb300._lib import SGL_MIXED
+    L64 = eng_sub.vp_lnR(KV, QV)
+    Lm = eng_sub.vp_lnR(KV, QV, SGL_MIXED)
+    err = np.abs(Lm - L64) / (1.0 + np.abs(L64))
+    assert err.max() <= 2e-8, err.max()
+
+
+def test_qxi_unwrap_and_shear_match_oracle(eng_sub, vp_sub):
+    """sgl_xi_term with the closure installed = Closure.qxi: ln R, unwrapped phase, - shear kg^2 / 4."""
+    from oracle.vp_oracle import qxi
+    kv, qv = KV[::2], QV[::3]
+    Q = eng_sub.xi_term(kv, qv)
+    Qo = qxi(vp_sub, kv, qv)
+    assert _close(Q, Qo, 1e-14, 1e-10).all(), np.abs(Q - Qo).max()
+
+
+def test_vp_set_rejects_bad_closures(vp_sub):
+    from sgl_analytic_gb300._lib import Engine
+    e = Engine(0)
+    bad = dict(vp_sub)
+    bad["cu"] = vp_sub["cu"].copy()
+    bad["cu"][3] = vp_sub["ku"].size           # index past the unique cells
+    with pytest.raises(ValueError):
+        e.set_vp(bad)
+    bad = dict(vp_sub)
+    bad["gc"] = vp_sub["gc"].copy()
+    bad["gc"][0] = 0.5                          # neither linear nor clipped
+    with pytest.raises(ValueError):
+        e.set_vp(bad)
+    bad = dict(vp_sub)
+    bad["u"] = np.zeros(47)
+    bad["w"] = np.zeros(47)
+    with pytest.raises((ValueError, NotImplementedError)):
+        e.set_vp(bad)
+    with pytest.raises(RuntimeError):           # no closure installed
+        e.vp_lnR([1.0], [1.0])
+
+
+@pytest.mark.skipif(not VP_FULL.exists(), reason="full z_s=1 vp closure (34 MB) not shipped")
+def test_full_closure_lnR_matches_reference_probe():
+    from sgl_analytic_gb300._lib import SGL_MIXED, Engine
+    full = dict(np.load(VP_FULL))
+    probe = np.load(GOLDEN / "vp_zs1_full_lnR_probe.npz")
+    e = Engine(0)
+    e.set_vp(full)
+    L = e.vp_lnR(probe["kv"], probe["qv"])
+    assert _close(L, probe["fused"], 1e-13, 1e-10).all(), np.abs(L - probe["fused"]).max()
+    Lm = e.vp_lnR(probe["kv"], probe["qv"], SGL_MIXED)
+    assert (np.abs(Lm - L) / (1 + np.abs(L))).max() <= 2e-8
+
+
+def _sigma_equivalent_population(full):
+    """The committed z_s=1 cells with the xi groups replaced by one m=0 group of the same sigma
+    contribution: under the vp closure the gauss groups only enter sigma (Lam.sigma)."""
+    from sgl_analytic_gb300 import Population
+    pop = Population.load(GOLDEN / "pop_zs1_sub.npz")
+    v_xi = float(full["sigma"]) ** 2 - float(np.sum(pop.w0 * pop.k0 ** 2)) - float(pop.V)
+    pop.xg_m = np.array([0], np.int32)
+    pop.xg_nrow = np.array([1], np.int32)
+    pop.xg_nidx = np.array([1], np.int32)
+    pop.xg_idx = np.array([0], np.int32)
+    pop.xg_rows = np.array([0.0, np.sqrt(v_xi)])
+    pop.xg_s0 = 0.0
+    return pop
+
+
+@pytest.mark.skipif(not VP_FULL.exists(), reason="full z_s=1 vp closure (34 MB) not shipped")
+def test_full_vp_pdf_matches_stored_golden():
+    """Whole chain with the vp closure (pipeline.run xi_closure="vp": window "auto", n_xi_wide 4000,
+    the per-axis coarse-grid rule) against the reference's stored z_s=1 vp PDF."""
+    from sgl_analytic_gb300 import Lam, invert
+    full = dict(np.load(VP_FULL))
+    lam = Lam(_sigma_equivalent_population(full), xi=True)
+    lam.install_vp(full)
+    assert lam.sigma() == pytest.approx(float(full["sigma"]), rel=1e-12)
+    ref = json.load(open(GOLDEN / "pdf_zs1_vp.json"))
+    x = np.concatenate([ref["xi"], ref["xi_tail"]])
+    P0 = np.concatenate([ref["P_s"], ref["P_s_tail"]])
+    _, P, meta = invert(lam, lam.sigma(), xi_out=x, phi_tol=1e-8, window="auto", n_xi_wide=4000)
+    g, rg = meta["grid"], ref["grid"]
+    for k in ("nk_k", "nk_g", "n_kap", "n_gam", "xi_coarse", "xi_coarse_k", "window"):
+        assert g[k] == rg[k], k
+    peak = P0.max()
+    assert np.abs(P - P0).max() / peak <= 1e-5
+    _, Pm, _ = invert(lam, lam.sigma(), xi_out=x, phi_tol=1e-8, window="auto", n_xi_wide=4000, precision="mixed")
+    assert np.trapezoid(np.abs(Pm - P), x) <= 1e-4
+    tail = (x > 1.0) & (np.abs(P) > 1e-6 * peak)
+    assert np.max(np.abs(Pm[tail] - P[tail]) / np.abs(P[tail])) <= 1e-3

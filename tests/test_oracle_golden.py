@@ -12,7 +12,8 @@ import pytest
 
 from oracle import invert_oracle as IO
 from oracle import lam_oracle as LO
-from tests.conftest import FULL_FIXTURE, GOLDEN
+from oracle import vp_oracle as VO
+from tests.conftest import FULL_FIXTURE, GOLDEN, VP_FULL
 
 TOL_LN = 1e-10          # max |d ln Phi| (spec FP64 bar)
 TOL_PEAK = 1e-9         # max |dP| / peak (the reference's own regression tolerance)
@@ -89,3 +90,41 @@ def test_full_chain_matches_stored_golden_pdf():
     P0 = np.concatenate([ref["P_s"], ref["P_s_tail"]])
     assert np.max(np.abs(P - P0)) / P0.max() <= TOL_PEAK
     assert meta["grid"]["nk_k"] == ref["grid"]["nk_k"] and meta["grid"]["nk_g"] == ref["grid"]["nk_g"]
+
+
+def test_vp_oracle_matches_reference_sub_golden():
+    """vp closure, shells 0-5: the oracle's ln R against the reference's _fused_groups +
+    _chain_recursion on the same sub-closure (5 x 4 points)."""
+    d = dict(np.load(GOLDEN / "vp_zs1_sub.npz"))
+    L = VO.lnR(d, d["kv"], d["qv"])
+    assert np.all(np.abs(L - d["lnR"]) <= 1e-15 + 1e-12 * np.abs(d["lnR"]))
+
+
+def test_vp_oracle_unwraps_like_numpy():
+    """q_xi's phase is unwrapped along k_kappa at the first k_gamma column, then along k_gamma."""
+    d = dict(np.load(GOLDEN / "vp_zs1_sub.npz"))
+    kv, qv = np.array([0.0, 300.0, 900.0]), np.array([0.0, 100.0])
+    Q = VO.qxi(d, kv, qv)
+    L = VO.lnR(d, kv, qv)
+    assert np.allclose(np.exp(1j * Q.imag), np.exp(1j * L.imag), atol=1e-12)
+    assert np.allclose(Q.real, L.real - 0.25 * float(d["shear_var"]) * qv[None, :] ** 2, rtol=0, atol=1e-15)
+
+
+@pytest.mark.skipif(not VP_FULL.exists(), reason="full z_s=1 vp closure (34 MB) not present")
+def test_vp_oracle_matches_reference_full_closure_probe():
+    """All 67 shells: the oracle against FusedVP.lnR_blocked and Closure.lnR_ref on 3 x 3 points."""
+    d = dict(np.load(VP_FULL))
+    p = np.load(GOLDEN / "vp_zs1_full_lnR_probe.npz")
+    L = VO.lnR(d, p["kv"], p["qv"])
+    for key in ("fused", "ref"):
+        assert np.all(np.abs(L - p[key]) <= 1e-13 + 1e-10 * np.abs(p[key])), key
+
+
+def test_vp_oracle_mirrored_closure_gives_same_lnR():
+    """Right-clipped rates: relabelling the states j -> 47 - j leaves ln R unchanged."""
+    from tests.test_gpu_vp import mirrored
+    d = dict(np.load(GOLDEN / "vp_zs1_sub.npz"))
+    kv, qv = np.array([0.0, 40.0, 900.0]), np.array([0.0, 150.0, 600.0])
+    L = VO.lnR(d, kv, qv)
+    Lm = VO.lnR(mirrored(d), kv, qv)
+    assert np.all(np.abs(L - Lm) <= 1e-14 + 1e-11 * np.abs(L))
