@@ -6,7 +6,7 @@ measured k-reach probes, ln Phi on the 1688 x 2150 k-grid (separable Psi_1 over 
 201 xi_lin groups on the 101^2 coarse grid + bicubic spline), exp, Hankel and kappa transforms,
 Euler-Maclaurin term, constant-mu path integrals on 500 + 3201 ln mu points, normalisation.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64] [--impl ours|reference]
 
 * value    PDFs/s with the population resident in HBM, device-timed with CUDA events on the
            engine's stream (max over ranks; N ranks run N independent replicas: weak scaling).
@@ -15,7 +15,8 @@ Euler-Maclaurin term, constant-mu path integrals on 500 + 3201 ln mu points, nor
 * roofline the kernel with the largest device time in the timed region: its algorithmic FLOPs
            (or bytes) per launch / its event-timed duration, against the measured peak.
 * accuracy every PDF of the timed arm is checked against the FP64 oracle-pinned GPU path:
-           PDF L1 over ln mu in [-1, 9] (bar 1e-4).
+           PDF L1 over ln mu in [-1, 9] (bar 1e-4) and the tail relative error (bar 1e-3).
+* fp64_path the parity path (max |d ln Phi| <= 1e-10 vs the reference) timed the same way.
 * --impl reference  the reference algorithm on the host CPU cores (the FP64 NumPy oracle that
            restates sgl_full.Lam / invert; the reference itself is Python and cannot be shipped).
 """
@@ -40,6 +41,9 @@ WORKLOAD = ("z_s=1 default flat LCDM PDF: reference z_s=1 population (79,574 fin
             "groups with the reference's z_s=1 shapes (shell-30 groups scaled to each shell's row norm), "
             "gauss closure, CLI ln mu grids (1601 + 1600 points), FP64 oracle-pinned")
 XI_OUT = np.concatenate([np.linspace(-1.0, 1.0, 1601), np.linspace(1.005, 9.0, 1600)])
+# DRAM bytes (read + write) per launch of the dominant kernels, from one ncu capture of this
+# workload (profiles/ holds the summaries and the commands)
+TRAFFIC = {"gemm_f32_xi": 1.2079e9}        # profiles/gemm_f32_xi_zs1.md
 
 
 def dist_env():
@@ -211,7 +215,8 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--precision", default="fp64", choices=("fp64", "mixed"))
+    ap.add_argument("--precision", default="mixed", choices=("fp64", "mixed"))
+    ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
@@ -278,6 +283,18 @@ def main():
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
+    # ---- the FP64 parity path, same timing method (outside the headline region)
+    fp64_line = None
+    if args.fp64_steps > 0 and args.precision != "fp64":
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.fp64_steps):
+            invert(lam, sig, xi_out=XI_OUT, phi_tol=1e-8, precision="fp64")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = e0.elapsed_time(e1)
+        fp64_line = {"value": args.fp64_steps / (ms64 / 1e3), "unit": "PDF/s", "ms_per_pdf": ms64 / args.fp64_steps,
+                     "steps": args.fp64_steps}
     value = world * args.steps / (ms / 1e3)
     l1 = float(np.trapezoid(np.abs(P - P64), XI_OUT))
     tail = (XI_OUT > 1.0) & (np.abs(P64) > 1e-6 * np.max(P64))
@@ -306,14 +323,19 @@ def main():
             peak_v = float(pk.get("fp64_tflops", 1.25)) if fp64 else float(pk["bf16_tflops_sustained"])
             ach = r["flops"] / r["launches"] / (per_ms / 1e3) / 1e12
             roof = {"kernel": top, "bound": "fp64" if fp64 else "tensor", "achieved": ach, "peak": peak_v,
-                    "unit": "TFLOP/s", "frac": ach / peak_v, "traffic": None,
+                    "unit": "TFLOP/s", "frac": ach / peak_v, "traffic": TRAFFIC.get(top),
                     "peak_source": ("nominal GB300 FP64 (1.25 TFLOP/s): no measured FP64 peak in "
-                                    "MEASURED_PEAKS.json") if fp64 else f"{pk_src} bf16 sustained",
-                    "launches": r["launches"], "ms_per_launch": per_ms}
+                                    "MEASURED_PEAKS.json") if fp64 else f"{pk_src} bf16 sustained (of measured)",
+                    "launches": r["launches"], "ms_per_launch": per_ms,
+                    "flops_per_launch": r["flops"] / r["launches"]}
+            if top.startswith("gemm_f32"):
+                # the kernel runs on the FP32 FMA pipe (SIMT): its own ceiling is the FMA probe
+                f32 = eng.measure_peak(False)
+                roof["simt_fp32"] = {"peak": f32, "frac": ach / f32, "peak_source": "FP32 FMA probe, this run"}
         else:
             ach = r["bytes"] / r["launches"] / (per_ms / 1e3) / 1e9
             roof = {"kernel": top, "bound": "hbm", "achieved": ach, "peak": float(pk["hbm_gbs"]), "unit": "GB/s",
-                    "frac": ach / float(pk["hbm_gbs"]), "traffic": None, "peak_source": pk_src,
+                    "frac": ach / float(pk["hbm_gbs"]), "traffic": TRAFFIC.get(top), "peak_source": pk_src,
                     "launches": r["launches"], "ms_per_launch": per_ms}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -333,6 +355,7 @@ def main():
                            "parallelism": f"replicas x{world}",
                            "l2": "per-PDF working set > L2 (Psi_2 intermediates ~2.5 GB, T 190 MB)"},
                 "accuracy": {"pdf_l1_vs_fp64": l1, "bar": 1e-4, "tail_rel_vs_fp64": tail_rel, "tail_bar": 1e-3},
+                "fp64_path": fp64_line,
                 "e2e": {"value": e2e, "unit": "PDF/s", "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(XI_OUT.size * 8)},
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches * 1,
