@@ -100,6 +100,7 @@ struct sgl_ctx {
     double vp_shear = 0.0;
     int vp_xi_coarse = 101, vp_xi_coarse_k = 0;   // coarse grid (gamma, kappa); grown by sgl_pdf's rule
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    int* dev_err = nullptr;          // raised by kernels whose bounded waits ran out
     // pinned staging ring for small uploads (pageable copies would serialise host and device);
     // reset whenever the stream has been synchronised
     char* pinned = nullptr;
@@ -226,6 +227,51 @@ sgl_status run_gemms(sgl_ctx* ctx, std::vector<GemmDesc<T>>& d, const std::strin
     {
         Timed t(ctx, std::string(sizeof(T) == 8 ? "gemm_f64_" : "gemm_f32_") + tag, fl, 0.0);
         launch_grouped_gemm<T>(dd, (int)d.size(), tiles, ctx->stream);
+    }
+    CKLAUNCH();
+    return SGL_OK;
+}
+
+// device error flag of this context (zeroed on first use)
+int* dev_err_flag(sgl_ctx* ctx) {
+    if (!ctx->dev_err) {
+        ctx->dev_err = (int*)ctx->arena.get("dev_err", sizeof(int));
+        if (ctx->dev_err) cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), ctx->stream);
+    }
+    return ctx->dev_err;
+}
+
+// reads (and clears) the flag; call after the stream has work queued that may raise it
+sgl_status check_dev_err(sgl_ctx* ctx) {
+    if (!ctx->dev_err) return SGL_OK;
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CKS(sync_stream(ctx));
+    if (h) {
+        CK(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), ctx->stream));
+        return fail(ctx, SGL_ERR_CUDA, "tensor-core GEMM: a bounded mbarrier wait ran out");
+    }
+    return SGL_OK;
+}
+
+sgl_status run_tc_gemms(sgl_ctx* ctx, std::vector<TcGemmDesc>& d, const std::string& tag) {
+    if (d.empty()) return SGL_OK;
+    std::vector<TcPackDesc> pk(2 * d.size());
+    int tiles = 0;
+    long long quads = 0;
+    const long long pfl = tc_gemm_plan(d.data(), (int)d.size(), pk.data(), &tiles, &quads);
+    DBUF(dd, TcGemmDesc, "tc_desc_" + tag, d.size());
+    DBUF(dp, TcPackDesc, "tc_pack_" + tag, pk.size());
+    DBUF(packed, float, "tc_packed", std::max<long long>(pfl, 1));
+    CKS(upload(ctx, dd, d.data(), d.size()));
+    CKS(upload(ctx, dp, pk.data(), pk.size()));
+    int* err = dev_err_flag(ctx);
+    if (!err) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (error flag)");
+    double fl = 0.0;
+    for (auto& g : d) fl += 2.0 * g.M * (double)g.N * g.K;
+    {
+        Timed t(ctx, "gemm_tc_" + tag, fl, (double)pfl * 4.0);
+        launch_tc_gemm(dd, (int)d.size(), tiles, dp, quads, packed, err, ctx->stream);
     }
     CKLAUNCH();
     return SGL_OK;
@@ -520,13 +566,19 @@ sgl_status xi_eval(sgl_ctx* ctx, int precision, const double* d_kk, const double
         }
         CKS(run_gemms(ctx, v, "xi"));
     } else {
-        std::vector<GemmDesc<float>> v;
+        // tensor cores, transposed so that the 2 nk rows of E fit one tile width:
+        // G^T (N x 2nk) = T^T (N x nP) E^T (nP x 2nk)
+        std::vector<TcGemmDesc> v;
         for (int g = 0; g < X.n_groups; ++g) {
             const int N = X.r[g] * nkg;
-            v.push_back(gd<float>(2 * nk, N, X.nP[g], (const float*)E + E_off[g], X.nP[g], 1,
-                                  (const float*)T + T_off[g], N, 1, (float*)G + G_off[g], N));
+            TcGemmDesc t{};
+            t.M = N; t.N = 2 * nk; t.K = X.nP[g];
+            t.A = (const float*)T + T_off[g]; t.a_rs = 1; t.a_cs = N;
+            t.B = (const float*)E + E_off[g]; t.b_rs = 1; t.b_cs = X.nP[g];
+            t.C = (float*)G + G_off[g]; t.c_rs = 1; t.c_cs = N;
+            v.push_back(t);
         }
-        CKS(run_gemms(ctx, v, "xi"));
+        CKS(run_tc_gemms(ctx, v, "xi"));
     }
     double* d_V = nullptr;
     if (precision == SGL_MIXED) {
@@ -1206,6 +1258,7 @@ sgl_status sgl_lnphi(sgl_ctx* ctx, const double* kk, int nkk, const double* kg, 
     CK(cudaMemcpyAsync(out_re, d_re, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(out_im, d_im, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CKS(sync_stream(ctx));
+    CKS(check_dev_err(ctx));
     for (long long e = 0; e < npt; ++e)
         if (!std::isfinite(out_re[e]) || !std::isfinite(out_im[e])) return fail(ctx, SGL_ERR_NONFINITE, "non-finite ln Phi");
     return SGL_OK;
@@ -1389,6 +1442,7 @@ sgl_status sgl_xi_term(sgl_ctx* ctx, const double* kk, int nkk, const double* kg
     CK(cudaMemcpyAsync(out_re, d_o, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(out_im, d_o + npt, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CKS(sync_stream(ctx));
+    CKS(check_dev_err(ctx));
     return SGL_OK;
 }
 
@@ -1640,6 +1694,7 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
     std::vector<double> pall(xall.size());
     CK(cudaMemcpyAsync(pall.data(), d_pi, pall.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
     CKS(sync_stream(ctx));
+    CKS(check_dev_err(ctx));
     // ---- normalisation and moments (sgl_full.py:362-372)
     const double* pw = pall.data();
     const double norm = trapz(pw, xw.data(), nw);

@@ -36,10 +36,13 @@ grouped_gemm_kernel(const GemmDesc<T>* __restrict__ descs, int nprob) {
     __shared__ T As[BK][BM + 1];
     __shared__ T Bs[BK][BN + 1];
 
-    // locate the problem (nprob is small: linear scan from the top)
+    // locate the problem (binary search over the tile prefix)
     const int tile = blockIdx.x;
-    int p = nprob - 1;
-    while (p > 0 && descs[p].tile_begin > tile) --p;
+    int p = 0, ph = nprob - 1;                       // last problem with tile_begin <= tile
+    while (p < ph) {
+        const int mid = (p + ph + 1) >> 1;
+        if (descs[mid].tile_begin <= tile) p = mid; else ph = mid - 1;
+    }
     const GemmDesc<T> d = descs[p];
     const int local = tile - d.tile_begin;
     const int tm = local / d.tiles_n, tn = local % d.tiles_n;
@@ -112,8 +115,11 @@ grouped_gemm_kernel<float>(const GemmDesc<float>* __restrict__ descs, int nprob)
     __shared__ __align__(16) float As[2][BK][BM + PAD];
     __shared__ __align__(16) float Bs[2][BK][BN + PAD];
     const int tile = blockIdx.x;
-    int p = nprob - 1;
-    while (p > 0 && descs[p].tile_begin > tile) --p;
+    int p = 0, ph = nprob - 1;                       // last problem with tile_begin <= tile
+    while (p < ph) {
+        const int mid = (p + ph + 1) >> 1;
+        if (descs[mid].tile_begin <= tile) p = mid; else ph = mid - 1;
+    }
     const GemmDesc<float> d = descs[p];
     const int local = tile - d.tile_begin;
     const int i0 = (local / d.tiles_n) * BM, j0 = (local % d.tiles_n) * BN;

@@ -116,6 +116,26 @@ void launch_path_integral(const double* P3, int nkap, int ngam, double kap0, dou
                           const double* xi, int nxi, double gmax, double g_def, int n_k_int, double* out,
                           cudaStream_t st);
 
+// ---- tcgen05 grouped GEMM (TF32 hi/lo split, FP32 accumulation in TMEM)
+struct TcGemmDesc {
+    int M, N, K;
+    const float* A; long long a_rs, a_cs;   // A(i,k) = A[i*a_rs + k*a_cs]
+    const float* B; long long b_rs, b_cs;   // B(k,j) = B[k*b_rs + j*b_cs]
+    float* C; long long c_rs, c_cs;         // C(i,j) = C[i*c_rs + j*c_cs]
+    // filled by tc_gemm_plan
+    int tile_begin, tiles_n, bn, Mpad, Npad;
+    long long a_off, b_off;                 // packed operands (floats into the packed buffer)
+};
+struct TcPackDesc {                         // one operand to pack: X(r, k) = X[r*x_rs + k*x_cs]
+    const float* X; long long x_rs, x_cs;
+    int R, K, Rpad, nkb;
+    long long out_off, quad_begin;
+};
+// fills tiles / packing descriptors (pk: 2 n entries); returns the packed buffer size in floats
+long long tc_gemm_plan(TcGemmDesc* d, int n, TcPackDesc* pk, int* tiles, long long* quads);
+void launch_tc_gemm(const TcGemmDesc* d_descs, int nprob, int tiles, const TcPackDesc* d_pack, long long quads,
+                    float* packed, int* err, cudaStream_t st);
+
 // ---- positive (vp) Cox closure
 // Cells sorted per shell into runs (one kind and interval bound; runs ordered linear first, then by
 // the first state they change: lo for left runs, hi + 1 for right runs), per-cell weights (w a, w b).

@@ -1,0 +1,298 @@
+// Grouped FP32 GEMM on the 5th-generation tensor cores (tcgen05), at FP32-level accuracy:
+//   C(i, j) = sum_k A(i, k) B(k, j)
+//
+// Operands are first PACKED (k_tc_pack): every element is split into TF32 parts hi = rna(x),
+// lo = rna(x - hi) and written in the tensor core's canonical K-major no-swizzle layout, K in
+// blocks of 16:
+//   packed[kb][part][row][16 k]  with  row-group stride 512 B (8 rows) and K-chunk stride 128 B
+//   (core matrices of 8 rows x 16 bytes),
+// so the 16 K-columns of any 8-row-aligned run of rows are one contiguous span in global memory.
+// The GEMM (k_tc_gemm) then moves each operand tile with one bulk copy per part
+// (cp.async.bulk ... mbarrier::complete_tx::bytes: the TMA engine, no register staging) through a
+// 4-stage shared-memory ring; one thread produces (copies), one thread issues
+//   D += A_hi B_hi + A_hi B_lo + A_lo B_hi      (3 x tcgen05.mma.kind::tf32 per K-step of 8)
+// into an FP32 accumulator in tensor memory (128 lanes x bn columns) and commits each stage's MMAs
+// to that stage's "empty" mbarrier; the epilogue (4 warps, warp w owns TMEM lanes 32w..32w+31)
+// reads TMEM with tcgen05.ld and stores C with arbitrary strides.  The dropped lo * lo term and
+// the TF32 rounding of lo are ~2^-22 of each product; accumulation is FP32 in TMEM.
+//
+// Every mbarrier wait is bounded (~2 s); a wait that runs out raises *err, the CTA skips the rest
+// of its work, waits (bounded) for its own MMAs and frees its TMEM before returning.
+#include "kernels.cuh"
+
+namespace sgl {
+
+constexpr int kTcBM = 128;                 // tile rows = TMEM lanes
+constexpr int kTcBNmax = 256;              // tile columns = TMEM columns allocated
+constexpr int kTcBK = 16;                  // K per stage: two MMA k-steps of 8 (TF32)
+constexpr int kTcStages = 4;
+constexpr int kTcThreads = 128;
+constexpr int kTcLBO = 128;                // bytes between core matrices along K
+constexpr int kTcSBO = 512;                // bytes between 8-row groups
+constexpr int kTcAbytes = kTcBM * kTcBK * 4;          // 8 KB per TF32 part
+constexpr int kTcBbytes = kTcBNmax * kTcBK * 4;       // 16 KB per TF32 part (bn <= 256)
+constexpr int kTcStageBytes = 2 * kTcAbytes + 2 * kTcBbytes;   // 48 KB
+constexpr int kTcBarOff = kTcStages * kTcStageBytes;           // mbarriers after the ring
+constexpr int kTcSmemBytes = kTcBarOff + 128;
+constexpr long long kTcWaitCycles = 4000000000LL;              // ~2 s at 2 GHz
+
+// shared-memory matrix descriptor: start >> 4 [0,14), LBO >> 4 [16,30), SBO >> 4 [32,46),
+// descriptor version 1 [46,48), base offset 0, no swizzle (layout type 0 in [61,64))
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)(kTcLBO >> 4) << 16;
+    d |= (uint64_t)(kTcSBO >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// instruction descriptor, kind::tf32: D f32 [4,6) = 1, A tf32 [7,10) = 2, B tf32 [10,13) = 2,
+// both K-major (bits 15, 16 = 0), N >> 3 at [17,23), M >> 4 at [24,29)
+__device__ __forceinline__ uint32_t tc_idesc_tf32(int M, int N) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ float tf32_rna(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n"
+                 :: "r"(tmem_d), "l"(a), "l"(b), "r"(idesc), "r"(acc) : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(mbar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(mbar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(dst), "l"(src), "r"(bytes), "r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.b32 %0, 1, 0, p;\n\t}\n" : "=r"(ok) : "r"(mbar), "r"(parity) : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try(mbar, parity))
+        if (clock64() - t0 > kTcWaitCycles) return false;
+    return true;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = __uint_as_float(r[q]);
+}
+
+// ------------------------------------------------------------------ packing
+// One thread per (row, 4 consecutive k): reads X(r, k..k+3), writes the hi and lo float4 rows of
+// its core matrix.  Rows >= R and k >= K are zero.
+__global__ void __launch_bounds__(256)
+k_tc_pack(const TcPackDesc* __restrict__ descs, int nprob, float* __restrict__ base) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int lo = 0, hi = nprob - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (descs[mid].quad_begin <= t) lo = mid; else hi = mid - 1;
+    }
+    const TcPackDesc d = descs[lo];
+    const long long q = t - d.quad_begin;
+    const long long nq = (long long)d.Rpad * d.nkb * 4;
+    if (q < 0 || q >= nq) return;
+    // quads ordered (kb, chunk, row): consecutive threads take consecutive rows
+    const int r = (int)(q % d.Rpad);
+    const long long rest = q / d.Rpad;
+    const int c = (int)(rest % 4), kb = (int)(rest / 4);
+    float v[4], h[4], l[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const int k = kb * kTcBK + c * 4 + e;
+        v[e] = (r < d.R && k < d.K) ? __ldg(d.X + (long long)r * d.x_rs + (long long)k * d.x_cs) : 0.f;
+        h[e] = tf32_rna(v[e]);
+        l[e] = tf32_rna(v[e] - h[e]);
+    }
+    float* out = base + d.out_off;
+    const long long o = (long long)(r >> 3) * 128 + c * 32 + (r & 7) * 4;     // floats
+    const long long part = (long long)d.Rpad * kTcBK;                          // floats per (kb, part)
+    *(float4*)(out + (2LL * kb) * part + o) = make_float4(h[0], h[1], h[2], h[3]);
+    *(float4*)(out + (2LL * kb + 1) * part + o) = make_float4(l[0], l[1], l[2], l[3]);
+}
+
+// ------------------------------------------------------------------ GEMM
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_tc_gemm(const TcGemmDesc* __restrict__ descs, int nprob, const float* __restrict__ packed, int* __restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char tsm[];
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(tsm);
+    const uint32_t bar = sbase + kTcBarOff;             // full[4], empty[4], done
+    const uint32_t tslot = bar + 9 * 8;
+    volatile int* s_fail = (volatile int*)(tsm + kTcBarOff + 80);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    const int tile = blockIdx.x;
+    int lo = 0, hi = nprob - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (descs[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+    }
+    const TcGemmDesc d = descs[lo];
+    const int local = tile - d.tile_begin;
+    const int i0 = (local / d.tiles_n) * kTcBM, bn = d.bn, j0 = (local % d.tiles_n) * bn;
+    const int nkb = (d.K + kTcBK - 1) / kTcBK;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(tslot), "r"(kTcBNmax) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < 2 * kTcStages + 1; ++s) mbar_init(bar + 8 * s, 1);
+        *s_fail = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *(volatile uint32_t*)(tsm + kTcBarOff + 72);
+
+    const float* Ap = packed + d.a_off;       // [nkb][2][Mpad][16]
+    const float* Bp = packed + d.b_off;       // [nkb][2][Npad][16]
+    const long long a_part = (long long)d.Mpad * kTcBK, b_part = (long long)d.Npad * kTcBK;
+    const uint32_t a_bytes = kTcAbytes, b_bytes = (uint32_t)bn * kTcBK * 4;
+
+    if (tid == 0 && nkb > 0) {
+        // producer: bulk copies of A (hi, lo) and B (hi, lo) for each K block
+        for (int kb = 0; kb < nkb; ++kb) {
+            const int s = kb % kTcStages;
+            if (kb >= kTcStages && !mbar_wait_bounded(bar + 8 * (kTcStages + s), (uint32_t)(((kb / kTcStages) - 1) & 1))) {
+                *s_fail = 1;
+                break;
+            }
+            const uint32_t st = sbase + s * kTcStageBytes;
+            mbar_expect_tx(bar + 8 * s, 2 * a_bytes + 2 * b_bytes);
+            const float* a = Ap + (2LL * kb) * a_part + (long long)(i0 >> 3) * 128;
+            const float* b = Bp + (2LL * kb) * b_part + (long long)(j0 >> 3) * 128;
+            bulk_g2s(st, a, a_bytes, bar + 8 * s);
+            bulk_g2s(st + kTcAbytes, a + a_part, a_bytes, bar + 8 * s);
+            bulk_g2s(st + 2 * kTcAbytes, b, b_bytes, bar + 8 * s);
+            bulk_g2s(st + 2 * kTcAbytes + kTcBbytes, b + b_part, b_bytes, bar + 8 * s);
+        }
+    } else if (tid == 32 && nkb > 0) {
+        // MMA issuer
+        const uint32_t idesc = tc_idesc_tf32(kTcBM, bn);
+        int kb = 0;
+        for (; kb < nkb; ++kb) {
+            const int s = kb % kTcStages;
+            if (*s_fail || !mbar_wait_bounded(bar + 8 * s, (uint32_t)((kb / kTcStages) & 1))) { *s_fail = 1; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t a_hi = sbase + s * kTcStageBytes, a_lo = a_hi + kTcAbytes;
+            const uint32_t b_hi = a_hi + 2 * kTcAbytes, b_lo = b_hi + kTcBbytes;
+#pragma unroll
+            for (int ks = 0; ks < kTcBK / 8; ++ks) {
+                const uint32_t o = ks * 2 * kTcLBO;
+                tc_mma(tmem, tc_desc(a_hi + o), tc_desc(b_hi + o), idesc, (kb | ks) ? 1u : 0u);
+                tc_mma(tmem, tc_desc(a_hi + o), tc_desc(b_lo + o), idesc, 1u);
+                tc_mma(tmem, tc_desc(a_lo + o), tc_desc(b_hi + o), idesc, 1u);
+            }
+            tc_commit(bar + 8 * (kTcStages + s));
+        }
+        tc_commit(bar + 8 * (2 * kTcStages));    // "done": every MMA issued above has completed
+    }
+    // epilogue: all threads wait for the done barrier (bounded), then read TMEM
+    bool ok = true;
+    if (nkb > 0) ok = mbar_wait_bounded(bar + 8 * (2 * kTcStages), 0u);
+    const int all_ok = __syncthreads_and((ok && !*s_fail) ? 1 : 0);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int row = warp * 32 + lane, gi = i0 + row;
+    if (all_ok) {
+        for (int c0 = 0; c0 < bn; c0 += 16) {
+            float v[16];
+            if (nkb > 0) tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            else {
+#pragma unroll
+                for (int q = 0; q < 16; ++q) v[q] = 0.f;
+            }
+            if (gi < d.M) {
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const int gj = j0 + c0 + q;
+                    if (gj < d.N) d.C[(long long)gi * d.c_rs + (long long)gj * d.c_cs] = v[q];
+                }
+            }
+        }
+    } else if (tid == 0) {
+        atomicExch(err, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kTcBNmax) : "memory");
+    }
+}
+
+// ------------------------------------------------------------------ host planning / launch
+long long tc_gemm_plan(TcGemmDesc* d, int n, TcPackDesc* pk, int* tiles_out, long long* quads_out) {
+    long long off = 0, quads = 0;
+    int tiles = 0;
+    for (int i = 0; i < n; ++i) {
+        TcGemmDesc& g = d[i];
+        const int bn = g.N <= kTcBNmax ? ((g.N + 15) / 16) * 16 : kTcBNmax;
+        g.bn = bn < 16 ? 16 : bn;
+        g.tiles_n = (g.N + g.bn - 1) / g.bn;
+        g.tile_begin = tiles;
+        tiles += g.tiles_n * ((g.M + kTcBM - 1) / kTcBM);
+        const int nkb = (g.K + kTcBK - 1) / kTcBK;
+        g.Mpad = ((g.M + kTcBM - 1) / kTcBM) * kTcBM;
+        g.Npad = g.tiles_n * g.bn;
+        g.a_off = off;
+        off += 2LL * nkb * g.Mpad * kTcBK;
+        g.b_off = off;
+        off += 2LL * nkb * g.Npad * kTcBK;
+        // A(i, k) rows = i; B(k, j) is packed as rows j
+        TcPackDesc& pa = pk[2 * i];
+        pa.X = g.A; pa.x_rs = g.a_rs; pa.x_cs = g.a_cs; pa.R = g.M; pa.K = g.K; pa.Rpad = g.Mpad; pa.nkb = nkb;
+        pa.out_off = g.a_off; pa.quad_begin = quads;
+        quads += 4LL * g.Mpad * nkb;
+        TcPackDesc& pb = pk[2 * i + 1];
+        pb.X = g.B; pb.x_rs = g.b_cs; pb.x_cs = g.b_rs; pb.R = g.N; pb.K = g.K; pb.Rpad = g.Npad; pb.nkb = nkb;
+        pb.out_off = g.b_off; pb.quad_begin = quads;
+        quads += 4LL * g.Npad * nkb;
+    }
+    *tiles_out = tiles;
+    *quads_out = quads;
+    return off;
+}
+
+void launch_tc_gemm(const TcGemmDesc* d_descs, int nprob, int tiles, const TcPackDesc* d_pack, long long quads,
+                    float* packed, int* err, cudaStream_t st) {
+    if (quads > 0) {
+        k_tc_pack<<<ceil_div(quads, 256), 256, 0, st>>>(d_pack, 2 * nprob, packed);
+        SGL_COUNT(1);
+    }
+    cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes);
+    k_tc_gemm<<<tiles, kTcThreads, kTcSmemBytes, st>>>(d_descs, nprob, packed, err);
+    SGL_COUNT(1);
+}
+
+}  // namespace sgl
