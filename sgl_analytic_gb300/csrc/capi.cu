@@ -254,12 +254,13 @@ sgl_status check_dev_err(sgl_ctx* ctx) {
     return SGL_OK;
 }
 
-sgl_status run_tc_gemms(sgl_ctx* ctx, std::vector<TcGemmDesc>& d, const std::string& tag) {
+// parts = 2: operands to ~22 bits (3 MMAs per K-step); parts = 3: FP32 operands exactly (6 MMAs)
+sgl_status run_tc_gemms(sgl_ctx* ctx, std::vector<TcGemmDesc>& d, const std::string& tag, int parts) {
     if (d.empty()) return SGL_OK;
     std::vector<TcPackDesc> pk(2 * d.size());
     int tiles = 0;
     long long quads = 0;
-    const long long pfl = tc_gemm_plan(d.data(), (int)d.size(), pk.data(), &tiles, &quads);
+    const long long pfl = tc_gemm_plan(d.data(), (int)d.size(), parts, pk.data(), &tiles, &quads);
     DBUF(dd, TcGemmDesc, "tc_desc_" + tag, d.size());
     DBUF(dp, TcPackDesc, "tc_pack_" + tag, pk.size());
     DBUF(packed, float, "tc_packed", std::max<long long>(pfl, 1));
@@ -271,7 +272,7 @@ sgl_status run_tc_gemms(sgl_ctx* ctx, std::vector<TcGemmDesc>& d, const std::str
     for (auto& g : d) fl += 2.0 * g.M * (double)g.N * g.K;
     {
         Timed t(ctx, "gemm_tc_" + tag, fl, (double)pfl * 4.0);
-        launch_tc_gemm(dd, (int)d.size(), tiles, dp, quads, packed, err, ctx->stream);
+        launch_tc_gemm(parts, dd, (int)d.size(), tiles, dp, quads, packed, err, ctx->stream);
     }
     CKLAUNCH();
     return SGL_OK;
@@ -290,9 +291,9 @@ GemmDesc<T> gd(int M, int N, int K, const void* A, long long ars, long long acs,
 }
 
 // One GEMM with split-K when it would under-fill the GPU: K slices write workspace slices,
-// then a fixed-order sum (deterministic).
+// then a fixed-order sum (deterministic).  SIMT kernels (FP64, and FP32 where chosen below).
 template <typename T>
-sgl_status gemm_splitk(sgl_ctx* ctx, GemmDesc<T> g, const std::string& tag, int min_split = 1) {
+sgl_status gemm_splitk_simt(sgl_ctx* ctx, GemmDesc<T> g, const std::string& tag, int min_split = 1) {
     GemmDesc<T> tmp = g;
     const int tiles = gemm_plan(&tmp, 1);
     int split = 1;
@@ -321,6 +322,57 @@ sgl_status gemm_splitk(sgl_ctx* ctx, GemmDesc<T> g, const std::string& tag, int 
     launch_sum_slices<T>(ws, (int)v.size(), g.M, g.N, g.C, g.ldc, g.beta, ctx->stream);
     CKLAUNCH();
     return SGL_OK;
+}
+
+// FP32 on the tensor cores.  K split into >= min_split slices (FP32 accumulation in TMEM within a
+// slice), slices combined in FP64 by the fixed-order sum.
+sgl_status gemm_splitk_tc(sgl_ctx* ctx, GemmDesc<float> g, const std::string& tag, int min_split) {
+    int split = std::max(1, std::min(min_split, std::max(1, g.K / 32)));
+    const long long slice = (long long)g.M * g.N;
+    const bool direct = split == 1 && g.beta == 0.f;
+    float* ws = nullptr;
+    if (!direct) {
+        ws = dbuf<float>(ctx, "splitk_ws_" + tag, (size_t)(slice * split));
+        if (!ws) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (split-K workspace)");
+    }
+    std::vector<TcGemmDesc> v;
+    const int kc = ceil_div(g.K, split);
+    for (int s = 0; s < split; ++s) {
+        const int k0 = s * kc, k1 = std::min(g.K, k0 + kc);
+        if (k1 <= k0) continue;
+        TcGemmDesc t{};
+        t.M = g.M; t.N = g.N; t.K = k1 - k0;
+        t.A = g.A + (long long)k0 * g.a_cs; t.a_rs = g.a_rs; t.a_cs = g.a_cs;
+        t.B = g.B + (long long)k0 * g.b_rs; t.b_rs = g.b_rs; t.b_cs = g.b_cs;
+        if (direct) { t.C = g.C; t.c_rs = g.ldc; t.c_cs = 1; }
+        else { t.C = ws + (long long)v.size() * slice; t.c_rs = g.N; t.c_cs = 1; }
+        t.alpha = g.alpha;
+        v.push_back(t);
+    }
+    CKS(run_tc_gemms(ctx, v, tag, 3));
+    if (!direct) {
+        launch_sum_slices<float>(ws, (int)v.size(), g.M, g.N, g.C, g.ldc, g.beta, ctx->stream);
+        CKLAUNCH();
+    }
+    return SGL_OK;
+}
+
+// Mixed-path GEMMs that run on the tensor cores.  Measured at z_s = 1 (tail relative error of the
+// mixed PDF against the FP64 path, bar 1e-3): with every FP32 GEMM on the SIMT path 3.6e-4; moving
+// sep2 + sep3 keeps 3.5e-4, while kappa (6.4e-4), the Hankel pair (5.0e-4) and sep1 (2.0e-3) each
+// raise it, and more K-slices do not help (3x: 1.2e-3, 6x: 1.8e-3 with all six moved) -- the
+// tensor core's FP32 accumulation has a per-instruction bias that the Fourier sums do not cancel,
+// where SIMT FMAs round to nearest.  Those stay on the SIMT FP32 kernel.
+bool tc_for(const std::string& tag) {
+    return tag == "sep2" || tag == "sep3";
+}
+
+template <typename T>
+sgl_status gemm_splitk(sgl_ctx* ctx, GemmDesc<T> g, const std::string& tag, int min_split = 1) {
+    if constexpr (sizeof(T) == 4) {
+        if (tc_for(tag)) return gemm_splitk_tc(ctx, g, tag, min_split);
+    }
+    return gemm_splitk_simt<T>(ctx, g, tag, min_split);
 }
 
 // ------------------------------------------------------------------ separable plan
@@ -576,9 +628,10 @@ sgl_status xi_eval(sgl_ctx* ctx, int precision, const double* d_kk, const double
             t.A = (const float*)T + T_off[g]; t.a_rs = 1; t.a_cs = N;
             t.B = (const float*)E + E_off[g]; t.b_rs = 1; t.b_cs = X.nP[g];
             t.C = (float*)G + G_off[g]; t.c_rs = 1; t.c_cs = N;
+            t.alpha = 1.f;
             v.push_back(t);
         }
-        CKS(run_tc_gemms(ctx, v, "xi"));
+        CKS(run_tc_gemms(ctx, v, "xi", 2));
     }
     double* d_V = nullptr;
     if (precision == SGL_MIXED) {

@@ -118,103 +118,65 @@ void launch_p3_finish(int precision, const void* P3ext, int nkap, int ngam, int 
 }
 
 // ------------------------------------------------------------------ path integral
-// Uniform axis a_i = a0 + i h (i < n-1), a_{n-1} = a1 (numpy linspace).  Interval index as
-// RegularGridInterpolator: i = (#nodes < x) - 1 clipped to [0, n-2]; x outside [a0, a1] -> -1.
+// Uniform axis a_i = a0 + i h (numpy linspace); RegularGridInterpolator linear semantics: cell
+// i = floor((x - a0) / h) clipped to [0, n-2], weight t = (x - a0) / h - i, and 0 outside [a0, a1].
+// GB300's FP64 pipe is ~1/74 of FP32, so the per-point work is kept to a few FP64 operations:
+// no divisions (reciprocal steps precomputed), one sqrt per path point, and the blend written
+// as v00 + t_x (v10 - v00) + t_y (v01 - v00 + t_x (v11 - v10 - v01 + v00)).  Against the
+// reference's node-exact interval search this moves P by ~1e-16 relative.
 struct Axis { double a0, a1, h, inv_h; int n; };
 
-// numpy rounds i * step and + start separately: no FMA contraction here
-__device__ inline double axis_node(const Axis& A, int i) {
-    return (i == A.n - 1) ? A.a1 : __dadd_rn(__dmul_rn((double)i, A.h), A.a0);
+__device__ __forceinline__ double bilinear(const double* __restrict__ P3, const Axis& K, const Axis& G, double x,
+                                           double y) {
+    if (!(x >= K.a0 && x <= K.a1 && y >= G.a0 && y <= G.a1)) return 0.0;
+    const double fx = (x - K.a0) * K.inv_h, fy = (y - G.a0) * G.inv_h;
+    const int i = min(max((int)fx, 0), K.n - 2), j = min(max((int)fy, 0), G.n - 2);
+    const double tx = fx - (double)i, ty = fy - (double)j;
+    const double* p = P3 + (long long)i * G.n + j;
+    const double v00 = __ldg(p), v01 = __ldg(p + 1), v10 = __ldg(p + G.n), v11 = __ldg(p + G.n + 1);
+    const double d10 = v10 - v00, d01 = v01 - v00;
+    return fma(tx, d10, v00) + ty * fma(tx, (v11 - v10) - d01, d01);
 }
-
-__device__ inline int axis_find(const Axis& A, double x, double& t) {
-    if (!(x >= A.a0 && x <= A.a1)) return -1;
-    int i = (int)((x - A.a0) * A.inv_h);                  // guess, then exact node comparisons
-    i = max(0, min(i, A.n - 1));
-    double lo = axis_node(A, i);
-    while (i > 0 && !(lo < x)) { --i; lo = axis_node(A, i); }
-    double nx = axis_node(A, min(i + 1, A.n - 1));
-    while (i + 1 < A.n && nx < x) { ++i; lo = nx; nx = axis_node(A, min(i + 1, A.n - 1)); }
-    if (i > A.n - 2) { i = A.n - 2; lo = axis_node(A, i); nx = axis_node(A, i + 1); }
-    t = (x - lo) / (nx - lo);
-    return i;
-}
-
-__device__ inline double bilinear(const double* __restrict__ P3, const Axis& K, const Axis& G, double x, double y) {
-    double tx, ty;
-    const int i = axis_find(K, x, tx);
-    const int j = axis_find(G, y, ty);
-    if (i < 0 || j < 0) return 0.0;
-    const long long b = (long long)i * G.n + j;
-    const double v00 = P3[b], v01 = P3[b + 1], v10 = P3[b + G.n], v11 = P3[b + G.n + 1];
-    return (1.0 - tx) * (1.0 - ty) * v00 + (1.0 - tx) * ty * v01 + tx * (1.0 - ty) * v10 + tx * ty * v11;
-}
-
-__device__ inline double lin(double a, double b, int n, int i) {     // numpy linspace node
-    return (i == n - 1) ? b : __dadd_rn(__dmul_rn((double)i, (b - a) / (double)(n - 1)), a);
-}
-
-constexpr int kPathSmem = 4096;      // path points kept in shared memory (larger paths: 2 evaluations)
 
 // One CTA per xi.  Body: n_k_int points kappa in [lo, hi], gamma = sqrt((hi - k)(1 - k + 1/sqrt(mu))),
-// trapezoid in kappa; tail (gamma in (g_def, gb]) parametrised in gamma with weight gamma / r.
+// trapezoid in kappa (uniform step: endpoints halved); tail (gamma in (g_def, gb]) parametrised in
+// gamma with weight gamma / r.
 __global__ void __launch_bounds__(256)
 k_path_integral(const double* __restrict__ P3, Axis K, Axis G, const double* __restrict__ xi, double gmax,
                 double g_def, int n_k_int, double* __restrict__ out) {
     __shared__ double sh[32];
-    __shared__ double sv[kPathSmem];
     const double x = xi[blockIdx.x];
     const double mu = exp(x);
     const double rm = 1.0 / sqrt(mu);
     const double hi = 1.0 - rm;
     const double lo = fmax(K.a0, 1.0 - sqrt(1.0 / mu + g_def * g_def));
     const double pref = M_PI / (mu * mu);
-    const bool body = hi > lo;
-    if (!body) { if (threadIdx.x == 0) out[blockIdx.x] = 0.0; return; }
+    if (!(hi > lo)) { if (threadIdx.x == 0) out[blockIdx.x] = 0.0; return; }
+    const double step = (hi - lo) / (double)(n_k_int - 1);
+    const double c1 = 1.0 + rm;
     double acc = 0.0;
-    if (n_k_int <= kPathSmem) {
-        for (int i = threadIdx.x; i < n_k_int; i += blockDim.x) {
-            const double k0 = lin(lo, hi, n_k_int, i);
-            const double g0 = sqrt(fmax((hi - k0) * (1.0 - k0 + rm), 0.0));
-            sv[i] = bilinear(P3, K, G, k0, g0);
-        }
-        __syncthreads();
-        for (int i = threadIdx.x; i < n_k_int - 1; i += blockDim.x)
-            acc += (lin(lo, hi, n_k_int, i + 1) - lin(lo, hi, n_k_int, i)) * (sv[i] + sv[i + 1]) / 2.0;
-    } else {
-        for (int i = threadIdx.x; i < n_k_int - 1; i += blockDim.x) {
-            const double k0 = lin(lo, hi, n_k_int, i), k1 = lin(lo, hi, n_k_int, i + 1);
-            const double g0 = sqrt(fmax((hi - k0) * (1.0 - k0 + rm), 0.0));
-            const double g1 = sqrt(fmax((hi - k1) * (1.0 - k1 + rm), 0.0));
-            acc += (k1 - k0) * (bilinear(P3, K, G, k0, g0) + bilinear(P3, K, G, k1, g1)) / 2.0;
-        }
+    for (int i = threadIdx.x; i < n_k_int; i += blockDim.x) {
+        const double k0 = (i == n_k_int - 1) ? hi : fma((double)i, step, lo);
+        const double g0 = sqrt(fmax((hi - k0) * (c1 - k0), 0.0));
+        const double v = bilinear(P3, K, G, k0, g0);
+        acc += (i == 0 || i == n_k_int - 1) ? 0.5 * v : v;
     }
-    double total = pref * block_sum(acc, sh);
+    double total = pref * step * block_sum(acc, sh);
     if (gmax > g_def && lo > K.a0) {
-        const double gb = fmin(gmax, sqrt(fmax((hi - K.a0) * (1.0 - K.a0 + rm), 0.0)));
+        const double gb = fmin(gmax, sqrt(fmax((hi - K.a0) * (c1 - K.a0), 0.0)));
         if (gb > g_def) {
             const int n = (int)ceil((gb - g_def) / (0.5 * G.h)) + 1;
+            const double gstep = (gb - g_def) / (double)(n - 1);
+            const double imu = 1.0 / mu;
             double acc2 = 0.0;
-            if (n <= kPathSmem) {
-                __syncthreads();
-                for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                    const double ga = lin(g_def, gb, n, i);
-                    const double ra = sqrt(1.0 / mu + ga * ga);
-                    const double ka = fmin(fmax(1.0 - ra, K.a0), K.a1);
-                    sv[i] = bilinear(P3, K, G, ka, ga) * (ga / ra);
-                }
-                __syncthreads();
-                for (int i = threadIdx.x; i < n - 1; i += blockDim.x)
-                    acc2 += (lin(g_def, gb, n, i + 1) - lin(g_def, gb, n, i)) * (sv[i] + sv[i + 1]) / 2.0;
-            } else {
-                for (int i = threadIdx.x; i < n - 1; i += blockDim.x) {
-                    const double ga = lin(g_def, gb, n, i), gc = lin(g_def, gb, n, i + 1);
-                    const double ra = sqrt(1.0 / mu + ga * ga), rc = sqrt(1.0 / mu + gc * gc);
-                    const double ka = fmin(fmax(1.0 - ra, K.a0), K.a1), kc = fmin(fmax(1.0 - rc, K.a0), K.a1);
-                    acc2 += (gc - ga) * (bilinear(P3, K, G, ka, ga) * (ga / ra) + bilinear(P3, K, G, kc, gc) * (gc / rc)) / 2.0;
-                }
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                const double ga = (i == n - 1) ? gb : fma((double)i, gstep, g_def);
+                const double ra = sqrt(fma(ga, ga, imu));
+                const double ka = fmin(fmax(1.0 - ra, K.a0), K.a1);
+                const double v = bilinear(P3, K, G, ka, ga) * (ga / ra);
+                acc2 += (i == 0 || i == n - 1) ? 0.5 * v : v;
             }
-            total += pref * block_sum(acc2, sh);
+            total += pref * gstep * block_sum(acc2, sh);
         }
     }
     if (threadIdx.x == 0) out[blockIdx.x] = total;

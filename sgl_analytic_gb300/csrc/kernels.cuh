@@ -121,7 +121,8 @@ struct TcGemmDesc {
     int M, N, K;
     const float* A; long long a_rs, a_cs;   // A(i,k) = A[i*a_rs + k*a_cs]
     const float* B; long long b_rs, b_cs;   // B(k,j) = B[k*b_rs + j*b_cs]
-    float* C; long long c_rs, c_cs;         // C(i,j) = C[i*c_rs + j*c_cs]
+    float* C; long long c_rs, c_cs;         // C(i,j) = alpha * sum_k A(i,k) B(k,j) at C[i*c_rs + j*c_cs]
+    float alpha;
     // filled by tc_gemm_plan
     int tile_begin, tiles_n, bn, Mpad, Npad;
     long long a_off, b_off;                 // packed operands (floats into the packed buffer)
@@ -131,10 +132,11 @@ struct TcPackDesc {                         // one operand to pack: X(r, k) = X[
     int R, K, Rpad, nkb;
     long long out_off, quad_begin;
 };
-// fills tiles / packing descriptors (pk: 2 n entries); returns the packed buffer size in floats
-long long tc_gemm_plan(TcGemmDesc* d, int n, TcPackDesc* pk, int* tiles, long long* quads);
-void launch_tc_gemm(const TcGemmDesc* d_descs, int nprob, int tiles, const TcPackDesc* d_pack, long long quads,
-                    float* packed, int* err, cudaStream_t st);
+// fills tiles / packing descriptors (pk: 2 n entries) for operands split into `parts` (2 or 3)
+// TF32 parts; returns the packed buffer size in floats
+long long tc_gemm_plan(TcGemmDesc* d, int n, int parts, TcPackDesc* pk, int* tiles, long long* quads);
+void launch_tc_gemm(int parts, const TcGemmDesc* d_descs, int nprob, int tiles, const TcPackDesc* d_pack,
+                    long long quads, float* packed, int* err, cudaStream_t st);
 
 // ---- positive (vp) Cox closure
 // Cells sorted per shell into runs (one kind and interval bound; runs ordered linear first, then by

@@ -1,20 +1,23 @@
 // Grouped FP32 GEMM on the 5th-generation tensor cores (tcgen05), at FP32-level accuracy:
 //   C(i, j) = sum_k A(i, k) B(k, j)
 //
-// Operands are first PACKED (k_tc_pack): every element is split into TF32 parts hi = rna(x),
-// lo = rna(x - hi) and written in the tensor core's canonical K-major no-swizzle layout, K in
-// blocks of 16:
+// Operands are first PACKED (k_tc_pack): every element is split into NP TF32 parts
+// t0 = rna(x), t1 = rna(x - t0) (, t2 = rna(x - t0 - t1)) and written in the tensor core's
+// canonical K-major no-swizzle layout, K in blocks of 16:
 //   packed[kb][part][row][16 k]  with  row-group stride 512 B (8 rows) and K-chunk stride 128 B
 //   (core matrices of 8 rows x 16 bytes),
 // so the 16 K-columns of any 8-row-aligned run of rows are one contiguous span in global memory.
 // The GEMM (k_tc_gemm) then moves each operand tile with one bulk copy per part
 // (cp.async.bulk ... mbarrier::complete_tx::bytes: the TMA engine, no register staging) through a
-// 4-stage shared-memory ring; one thread produces (copies), one thread issues
-//   D += A_hi B_hi + A_hi B_lo + A_lo B_hi      (3 x tcgen05.mma.kind::tf32 per K-step of 8)
-// into an FP32 accumulator in tensor memory (128 lanes x bn columns) and commits each stage's MMAs
-// to that stage's "empty" mbarrier; the epilogue (4 warps, warp w owns TMEM lanes 32w..32w+31)
-// reads TMEM with tcgen05.ld and stores C with arbitrary strides.  The dropped lo * lo term and
-// the TF32 rounding of lo are ~2^-22 of each product; accumulation is FP32 in TMEM.
+// shared-memory ring (4 stages for NP = 2, 3 for NP = 3); one thread produces (copies), one thread
+// issues the part products into an FP32 accumulator in tensor memory (128 lanes x bn columns):
+//   NP = 2:  A0 B0 + A0 B1 + A1 B0                         (3 tcgen05.mma.kind::tf32 per K-step)
+//            operands carried to ~22 bits: product error ~2^-21
+//   NP = 3:  A0 B0 + A0 B1 + A1 B0 + A0 B2 + A2 B0 + A1 B1  (6 per K-step)
+//            FP32 operands carried exactly (3 x 11 bits): product error ~2^-32
+// and commits each stage's MMAs to that stage's "empty" mbarrier; the epilogue (4 warps, warp w owns
+// TMEM lanes 32w..32w+31) reads TMEM with tcgen05.ld and stores alpha * C with arbitrary strides.
+// Accumulation is FP32 in TMEM; callers bound its length by splitting K.
 //
 // Every mbarrier wait is bounded (~2 s); a wait that runs out raises *err, the CTA skips the rest
 // of its work, waits (bounded) for its own MMAs and frees its TMEM before returning.
@@ -25,16 +28,19 @@ namespace sgl {
 constexpr int kTcBM = 128;                 // tile rows = TMEM lanes
 constexpr int kTcBNmax = 256;              // tile columns = TMEM columns allocated
 constexpr int kTcBK = 16;                  // K per stage: two MMA k-steps of 8 (TF32)
-constexpr int kTcStages = 4;
 constexpr int kTcThreads = 128;
 constexpr int kTcLBO = 128;                // bytes between core matrices along K
 constexpr int kTcSBO = 512;                // bytes between 8-row groups
 constexpr int kTcAbytes = kTcBM * kTcBK * 4;          // 8 KB per TF32 part
 constexpr int kTcBbytes = kTcBNmax * kTcBK * 4;       // 16 KB per TF32 part (bn <= 256)
-constexpr int kTcStageBytes = 2 * kTcAbytes + 2 * kTcBbytes;   // 48 KB
-constexpr int kTcBarOff = kTcStages * kTcStageBytes;           // mbarriers after the ring
-constexpr int kTcSmemBytes = kTcBarOff + 128;
-constexpr long long kTcWaitCycles = 4000000000LL;              // ~2 s at 2 GHz
+constexpr long long kTcWaitCycles = 4000000000LL;     // ~2 s at 2 GHz
+
+template <int NP> struct TcCfg {
+    static constexpr int kStages = NP == 2 ? 4 : 3;
+    static constexpr int kStageBytes = NP * (kTcAbytes + kTcBbytes);      // 48 / 72 KB
+    static constexpr int kBarOff = kStages * kStageBytes;                  // mbarriers after the ring
+    static constexpr int kSmem = kBarOff + 128;
+};
 
 // shared-memory matrix descriptor: start >> 4 [0,14), LBO >> 4 [16,30), SBO >> 4 [32,46),
 // descriptor version 1 [46,48), base offset 0, no swizzle (layout type 0 in [61,64))
@@ -107,8 +113,9 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 }
 
 // ------------------------------------------------------------------ packing
-// One thread per (row, 4 consecutive k): reads X(r, k..k+3), writes the hi and lo float4 rows of
-// its core matrix.  Rows >= R and k >= K are zero.
+// One thread per (row, 4 consecutive k): reads X(r, k..k+3), writes the NP float4 rows of its core
+// matrix.  Rows >= R and k >= K are zero.
+template <int NP>
 __global__ void __launch_bounds__(256)
 k_tc_pack(const TcPackDesc* __restrict__ descs, int nprob, float* __restrict__ base) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -125,29 +132,37 @@ k_tc_pack(const TcPackDesc* __restrict__ descs, int nprob, float* __restrict__ b
     const int r = (int)(q % d.Rpad);
     const long long rest = q / d.Rpad;
     const int c = (int)(rest % 4), kb = (int)(rest / 4);
-    float v[4], h[4], l[4];
+    float part[NP][4];
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
         const int k = kb * kTcBK + c * 4 + e;
-        v[e] = (r < d.R && k < d.K) ? __ldg(d.X + (long long)r * d.x_rs + (long long)k * d.x_cs) : 0.f;
-        h[e] = tf32_rna(v[e]);
-        l[e] = tf32_rna(v[e] - h[e]);
+        float v = (r < d.R && k < d.K) ? __ldg(d.X + (long long)r * d.x_rs + (long long)k * d.x_cs) : 0.f;
+#pragma unroll
+        for (int pp = 0; pp < NP; ++pp) {
+            const float tv = tf32_rna(v);
+            part[pp][e] = tv;
+            v -= tv;
+        }
     }
     float* out = base + d.out_off;
     const long long o = (long long)(r >> 3) * 128 + c * 32 + (r & 7) * 4;     // floats
-    const long long part = (long long)d.Rpad * kTcBK;                          // floats per (kb, part)
-    *(float4*)(out + (2LL * kb) * part + o) = make_float4(h[0], h[1], h[2], h[3]);
-    *(float4*)(out + (2LL * kb + 1) * part + o) = make_float4(l[0], l[1], l[2], l[3]);
+    const long long pstride = (long long)d.Rpad * kTcBK;                       // floats per (kb, part)
+#pragma unroll
+    for (int pp = 0; pp < NP; ++pp)
+        *(float4*)(out + ((long long)NP * kb + pp) * pstride + o) = make_float4(part[pp][0], part[pp][1], part[pp][2], part[pp][3]);
 }
 
 // ------------------------------------------------------------------ GEMM
+template <int NP>
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_tc_gemm(const TcGemmDesc* __restrict__ descs, int nprob, const float* __restrict__ packed, int* __restrict__ err) {
+    using Cfg = TcCfg<NP>;
+    constexpr int S = Cfg::kStages;
     extern __shared__ __align__(1024) unsigned char tsm[];
     const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(tsm);
-    const uint32_t bar = sbase + kTcBarOff;             // full[4], empty[4], done
-    const uint32_t tslot = bar + 9 * 8;
-    volatile int* s_fail = (volatile int*)(tsm + kTcBarOff + 80);
+    const uint32_t bar = sbase + Cfg::kBarOff;          // full[S], empty[S], done
+    const uint32_t tslot = bar + 72;
+    volatile int* s_fail = (volatile int*)(tsm + Cfg::kBarOff + 80);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     const int tile = blockIdx.x;
@@ -166,61 +181,64 @@ k_tc_gemm(const TcGemmDesc* __restrict__ descs, int nprob, const float* __restri
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        for (int s = 0; s < 2 * kTcStages + 1; ++s) mbar_init(bar + 8 * s, 1);
+        for (int s = 0; s < 2 * S + 1; ++s) mbar_init(bar + 8 * s, 1);
         *s_fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const uint32_t tmem = *(volatile uint32_t*)(tsm + kTcBarOff + 72);
+    const uint32_t tmem = *(volatile uint32_t*)(tsm + Cfg::kBarOff + 72);
 
-    const float* Ap = packed + d.a_off;       // [nkb][2][Mpad][16]
-    const float* Bp = packed + d.b_off;       // [nkb][2][Npad][16]
+    const float* Ap = packed + d.a_off;       // [nkb][NP][Mpad][16]
+    const float* Bp = packed + d.b_off;       // [nkb][NP][Npad][16]
     const long long a_part = (long long)d.Mpad * kTcBK, b_part = (long long)d.Npad * kTcBK;
     const uint32_t a_bytes = kTcAbytes, b_bytes = (uint32_t)bn * kTcBK * 4;
 
     if (tid == 0 && nkb > 0) {
-        // producer: bulk copies of A (hi, lo) and B (hi, lo) for each K block
+        // producer: one bulk copy per operand part and K block
         for (int kb = 0; kb < nkb; ++kb) {
-            const int s = kb % kTcStages;
-            if (kb >= kTcStages && !mbar_wait_bounded(bar + 8 * (kTcStages + s), (uint32_t)(((kb / kTcStages) - 1) & 1))) {
+            const int s = kb % S;
+            if (kb >= S && !mbar_wait_bounded(bar + 8 * (S + s), (uint32_t)(((kb / S) - 1) & 1))) {
                 *s_fail = 1;
                 break;
             }
-            const uint32_t st = sbase + s * kTcStageBytes;
-            mbar_expect_tx(bar + 8 * s, 2 * a_bytes + 2 * b_bytes);
-            const float* a = Ap + (2LL * kb) * a_part + (long long)(i0 >> 3) * 128;
-            const float* b = Bp + (2LL * kb) * b_part + (long long)(j0 >> 3) * 128;
-            bulk_g2s(st, a, a_bytes, bar + 8 * s);
-            bulk_g2s(st + kTcAbytes, a + a_part, a_bytes, bar + 8 * s);
-            bulk_g2s(st + 2 * kTcAbytes, b, b_bytes, bar + 8 * s);
-            bulk_g2s(st + 2 * kTcAbytes + kTcBbytes, b + b_part, b_bytes, bar + 8 * s);
+            const uint32_t st = sbase + s * Cfg::kStageBytes;
+            mbar_expect_tx(bar + 8 * s, NP * (a_bytes + b_bytes));
+            const float* a = Ap + ((long long)NP * kb) * a_part + (long long)(i0 >> 3) * 128;
+            const float* b = Bp + ((long long)NP * kb) * b_part + (long long)(j0 >> 3) * 128;
+#pragma unroll
+            for (int pp = 0; pp < NP; ++pp) {
+                bulk_g2s(st + pp * kTcAbytes, a + pp * a_part, a_bytes, bar + 8 * s);
+                bulk_g2s(st + NP * kTcAbytes + pp * kTcBbytes, b + pp * b_part, b_bytes, bar + 8 * s);
+            }
         }
     } else if (tid == 32 && nkb > 0) {
-        // MMA issuer
+        // MMA issuer: part products, larger terms first
+        constexpr int NPROD = NP == 2 ? 3 : 6;
+        constexpr int PA[6] = {0, 0, 1, 0, 2, 1};
+        constexpr int PB[6] = {0, 1, 0, 2, 0, 1};
         const uint32_t idesc = tc_idesc_tf32(kTcBM, bn);
-        int kb = 0;
-        for (; kb < nkb; ++kb) {
-            const int s = kb % kTcStages;
-            if (*s_fail || !mbar_wait_bounded(bar + 8 * s, (uint32_t)((kb / kTcStages) & 1))) { *s_fail = 1; break; }
+        for (int kb = 0; kb < nkb; ++kb) {
+            const int s = kb % S;
+            if (*s_fail || !mbar_wait_bounded(bar + 8 * s, (uint32_t)((kb / S) & 1))) { *s_fail = 1; break; }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t a_hi = sbase + s * kTcStageBytes, a_lo = a_hi + kTcAbytes;
-            const uint32_t b_hi = a_hi + 2 * kTcAbytes, b_lo = b_hi + kTcBbytes;
+            const uint32_t a0 = sbase + s * Cfg::kStageBytes, b0 = a0 + NP * kTcAbytes;
 #pragma unroll
             for (int ks = 0; ks < kTcBK / 8; ++ks) {
                 const uint32_t o = ks * 2 * kTcLBO;
-                tc_mma(tmem, tc_desc(a_hi + o), tc_desc(b_hi + o), idesc, (kb | ks) ? 1u : 0u);
-                tc_mma(tmem, tc_desc(a_hi + o), tc_desc(b_lo + o), idesc, 1u);
-                tc_mma(tmem, tc_desc(a_lo + o), tc_desc(b_hi + o), idesc, 1u);
+#pragma unroll
+                for (int t = 0; t < NPROD; ++t)
+                    tc_mma(tmem, tc_desc(a0 + PA[t] * kTcAbytes + o), tc_desc(b0 + PB[t] * kTcBbytes + o), idesc,
+                           (kb | ks | t) ? 1u : 0u);
             }
-            tc_commit(bar + 8 * (kTcStages + s));
+            tc_commit(bar + 8 * (S + s));
         }
-        tc_commit(bar + 8 * (2 * kTcStages));    // "done": every MMA issued above has completed
+        tc_commit(bar + 8 * (2 * S));    // "done": every MMA issued above has completed
     }
     // epilogue: all threads wait for the done barrier (bounded), then read TMEM
     bool ok = true;
-    if (nkb > 0) ok = mbar_wait_bounded(bar + 8 * (2 * kTcStages), 0u);
+    if (nkb > 0) ok = mbar_wait_bounded(bar + 8 * (2 * S), 0u);
     const int all_ok = __syncthreads_and((ok && !*s_fail) ? 1 : 0);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const int row = warp * 32 + lane, gi = i0 + row;
@@ -236,7 +254,7 @@ k_tc_gemm(const TcGemmDesc* __restrict__ descs, int nprob, const float* __restri
 #pragma unroll
                 for (int q = 0; q < 16; ++q) {
                     const int gj = j0 + c0 + q;
-                    if (gj < d.N) d.C[(long long)gi * d.c_rs + (long long)gj * d.c_cs] = v[q];
+                    if (gj < d.N) d.C[(long long)gi * d.c_rs + (long long)gj * d.c_cs] = d.alpha * v[q];
                 }
             }
         }
@@ -252,7 +270,7 @@ k_tc_gemm(const TcGemmDesc* __restrict__ descs, int nprob, const float* __restri
 }
 
 // ------------------------------------------------------------------ host planning / launch
-long long tc_gemm_plan(TcGemmDesc* d, int n, TcPackDesc* pk, int* tiles_out, long long* quads_out) {
+long long tc_gemm_plan(TcGemmDesc* d, int n, int parts, TcPackDesc* pk, int* tiles_out, long long* quads_out) {
     long long off = 0, quads = 0;
     int tiles = 0;
     for (int i = 0; i < n; ++i) {
@@ -266,9 +284,9 @@ long long tc_gemm_plan(TcGemmDesc* d, int n, TcPackDesc* pk, int* tiles_out, lon
         g.Mpad = ((g.M + kTcBM - 1) / kTcBM) * kTcBM;
         g.Npad = g.tiles_n * g.bn;
         g.a_off = off;
-        off += 2LL * nkb * g.Mpad * kTcBK;
+        off += (long long)parts * nkb * g.Mpad * kTcBK;
         g.b_off = off;
-        off += 2LL * nkb * g.Npad * kTcBK;
+        off += (long long)parts * nkb * g.Npad * kTcBK;
         // A(i, k) rows = i; B(k, j) is packed as rows j
         TcPackDesc& pa = pk[2 * i];
         pa.X = g.A; pa.x_rs = g.a_rs; pa.x_cs = g.a_cs; pa.R = g.M; pa.K = g.K; pa.Rpad = g.Mpad; pa.nkb = nkb;
@@ -284,15 +302,19 @@ long long tc_gemm_plan(TcGemmDesc* d, int n, TcPackDesc* pk, int* tiles_out, lon
     return off;
 }
 
-void launch_tc_gemm(const TcGemmDesc* d_descs, int nprob, int tiles, const TcPackDesc* d_pack, long long quads,
-                    float* packed, int* err, cudaStream_t st) {
-    if (quads > 0) {
-        k_tc_pack<<<ceil_div(quads, 256), 256, 0, st>>>(d_pack, 2 * nprob, packed);
+void launch_tc_gemm(int parts, const TcGemmDesc* d_descs, int nprob, int tiles, const TcPackDesc* d_pack,
+                    long long quads, float* packed, int* err, cudaStream_t st) {
+    if (parts == 3) {
+        if (quads > 0) { k_tc_pack<3><<<ceil_div(quads, 256), 256, 0, st>>>(d_pack, 2 * nprob, packed); SGL_COUNT(1); }
+        cudaFuncSetAttribute(k_tc_gemm<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcCfg<3>::kSmem);
+        k_tc_gemm<3><<<tiles, kTcThreads, TcCfg<3>::kSmem, st>>>(d_descs, nprob, packed, err);
+        SGL_COUNT(1);
+    } else {
+        if (quads > 0) { k_tc_pack<2><<<ceil_div(quads, 256), 256, 0, st>>>(d_pack, 2 * nprob, packed); SGL_COUNT(1); }
+        cudaFuncSetAttribute(k_tc_gemm<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcCfg<2>::kSmem);
+        k_tc_gemm<2><<<tiles, kTcThreads, TcCfg<2>::kSmem, st>>>(d_descs, nprob, packed, err);
         SGL_COUNT(1);
     }
-    cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes);
-    k_tc_gemm<<<tiles, kTcThreads, kTcSmemBytes, st>>>(d_descs, nprob, packed, err);
-    SGL_COUNT(1);
 }
 
 }  // namespace sgl
