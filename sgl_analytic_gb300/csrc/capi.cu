@@ -3,10 +3,13 @@
 // Mirrors the control flow of the reference's Lam (sgl_full.py:2711-3452) and invert
 // (sgl_full.py:159-375) for the default gauss chain.
 #include <algorithm>
+#include <atomic>
+#include <functional>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -105,6 +108,9 @@ struct sgl_ctx {
     // reset whenever the stream has been synchronised
     char* pinned = nullptr;
     size_t pinned_cap = 0, pinned_off = 0;
+    // pinned host buffer for the large per-population arrays built on the host (grow-only)
+    char* big_pinned = nullptr;
+    size_t big_cap = 0;
     // per-kernel statistics (sgl_ctx_profile)
     bool profiling = false;
     long long launches_at_enable = 0;
@@ -169,6 +175,21 @@ sgl_status upload(sgl_ctx* ctx, T* dst, const T* src, size_t n) {
     }
     CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
     return SGL_OK;
+}
+
+// pinned host buffer of at least `bytes` (grow-only; the stream is synchronised before it grows)
+char* big_pinned(sgl_ctx* ctx, size_t bytes) {
+    if (bytes <= ctx->big_cap) return ctx->big_pinned;
+    cudaStreamSynchronize(ctx->stream);
+    if (ctx->big_pinned) cudaFreeHost(ctx->big_pinned);
+    ctx->big_pinned = nullptr; ctx->big_cap = 0;
+    const size_t cap = std::max(bytes, (size_t)64 << 20);
+    if (cudaHostAlloc((void**)&ctx->big_pinned, cap, cudaHostAllocDefault) != cudaSuccess) {
+        ctx->big_pinned = nullptr;
+        return nullptr;
+    }
+    ctx->big_cap = cap;
+    return ctx->big_pinned;
 }
 
 // numpy.linspace: a + i * step (separately rounded), last point = b exactly
@@ -596,20 +617,64 @@ sgl_status xi_eval(sgl_ctx* ctx, int precision, const double* d_kk, const double
     CKS(upload(ctx, d_off, T_off.data(), X.n_groups));
     CKS(upload(ctx, d_off + X.n_groups, E_off.data(), X.n_groups));
     CKS(upload(ctx, d_off + 2 * X.n_groups, G_off.data(), X.n_groups));
+    // mixed path: stage A writes the tensor-core GEMM's packed A operand directly
+    const bool fused = precision == SGL_MIXED && xi_stageA_pack_fits(ctx->xid.r_max, nkg);
     void* J = ctx->arena.get("xi_J", 4ULL * X.n_gmc * nkg * es);
-    void* T = ctx->arena.get("xi_T", (size_t)tT * es);
+    void* T = fused ? nullptr : ctx->arena.get("xi_T", (size_t)tT * es);
     void* E = ctx->arena.get("xi_E", (size_t)tE * es);
     void* G = ctx->arena.get("xi_G", (size_t)tG * es);
-    if (!J || !T || !E || !G) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (xi)");
+    if (!J || (!T && !fused) || !E || !G) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (xi)");
     const long long* d_pp = (const long long*)ctx->arena.find("xi_pprefix");
     launch_bessel_tables(precision, ctx->xid.gmc, X.n_gmc, d_kg, nkg, J, st); CKLAUNCH();
-    {
+    if (!fused) {
         Timed t(ctx, "xi_stageA", 0.0, (double)tT * es);
         launch_xi_stageA(precision, ctx->xid, d_pp, X.total_p, d_off, J, nkg, T, st);
     }
     CKLAUNCH();
     launch_xi_E(precision, ctx->xid, d_kk, nk, d_off + X.n_groups, d_pp, X.total_p, E, st); CKLAUNCH();
-    if (precision == SGL_FP64) {
+    if (fused) {
+        // G^T (N x 2nk) = T^T (N x nP) E^T (nP x 2nk); T^T produced packed by stage A
+        std::vector<TcGemmDesc> v;
+        std::vector<long long> chunk_prefix;
+        long long nchunks = 0;
+        for (int g = 0; g < X.n_groups; ++g) {
+            const int N = X.r[g] * nkg;
+            TcGemmDesc t{};
+            t.M = N; t.N = 2 * nk; t.K = X.nP[g];
+            t.A = nullptr; t.a_rs = 1; t.a_cs = N;
+            t.B = (const float*)E + E_off[g]; t.b_rs = 1; t.b_cs = X.nP[g];
+            t.C = (float*)G + G_off[g]; t.c_rs = 1; t.c_cs = N;
+            t.alpha = 1.f;
+            v.push_back(t);
+            chunk_prefix.push_back(nchunks);
+            nchunks += 4LL * ((X.nP[g] + 15) / 16);
+        }
+        std::vector<TcPackDesc> pk(2 * v.size());
+        int tiles = 0;
+        long long quads = 0;
+        const long long pfl = tc_gemm_plan(v.data(), (int)v.size(), 2, pk.data(), &tiles, &quads, false);
+        DBUF(dd, TcGemmDesc, "tc_desc_xi", v.size());
+        DBUF(dpk, TcPackDesc, "tc_pack_xi", pk.size());
+        DBUF(dcp, long long, "xi_chunk_prefix", chunk_prefix.size());
+        DBUF(packed, float, "tc_packed", std::max<long long>(pfl, 1));
+        CKS(upload(ctx, dd, v.data(), v.size()));
+        CKS(upload(ctx, dpk, pk.data(), pk.size()));
+        CKS(upload(ctx, dcp, chunk_prefix.data(), chunk_prefix.size()));
+        int* err = dev_err_flag(ctx);
+        if (!err) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (error flag)");
+        {
+            Timed t(ctx, "xi_stageA", 0.0, (double)pfl * 4.0);
+            launch_xi_stageA_pack(ctx->xid, d_pp, (const float*)J, nkg, dcp, nchunks, dd, packed, st);
+        }
+        CKLAUNCH();
+        double fl = 0.0;
+        for (auto& g : v) fl += 2.0 * g.M * (double)g.N * g.K;
+        {
+            Timed t(ctx, "gemm_tc_xi", fl, 0.0);
+            launch_tc_gemm(2, dd, (int)v.size(), tiles, dpk, quads, packed, err, st);
+        }
+        CKLAUNCH();
+    } else if (precision == SGL_FP64) {
         std::vector<GemmDesc<double>> v;
         for (int g = 0; g < X.n_groups; ++g) {
             const int N = X.r[g] * nkg;
@@ -964,6 +1029,7 @@ void sgl_ctx_destroy(sgl_ctx* ctx) {
     resolve_stats(ctx);
     for (auto& ev : ctx->ev_pool) cudaEventDestroy(ev);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->big_pinned) cudaFreeHost(ctx->big_pinned);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -1073,124 +1139,154 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         idx_off[g + 1] = idx_off[g] + nidx[g];
         row_off[g + 1] = row_off[g] + (long long)nrow[g] * (nidx[g] + 1);
     }
+    // The host side runs in three passes, the data-heavy ones in parallel over groups (each
+    // group writes disjoint, precomputed slices; the results do not depend on the thread count):
+    //   1. row norms (prune threshold)        2. per-group index structure (serial, index-only)
+    //   3. transposed kept rows, sums, 1-D reach stacks, U sums
+    const int nthr = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), 32));
+    auto parallel_groups = [&](const std::function<void(int)>& fn) {
+        std::vector<std::thread> th;
+        std::atomic<int> next{0};
+        for (int t = 0; t < nthr; ++t)
+            th.emplace_back([&]() { for (int g; (g = next.fetch_add(1)) < n_groups;) fn(g); });
+        for (auto& t : th) t.join();
+    };
     std::vector<std::vector<double>> norms(n_groups);
-    double s0 = 0.0;
-    for (int g = 0; g < n_groups; ++g) {
+    parallel_groups([&](int g) {
         const int w = nidx[g] + 1;
+        norms[g].resize(nrow[g]);
         for (int r = 0; r < nrow[g]; ++r) {
             double s = 0.0;
             const double* row = rows + row_off[g] + (long long)r * w;
             for (int e = 0; e < w; ++e) s += row[e] * row[e];
-            norms[g].push_back(std::sqrt(s));
-            s0 = std::max(s0, std::sqrt(s));
+            norms[g][r] = std::sqrt(s);
         }
-    }
+    });
+    double s0 = 0.0;
+    for (int g = 0; g < n_groups; ++g)
+        for (double v : norms[g]) s0 = std::max(s0, v);
     if (s0_override > 0) s0 = s0_override;
-    // device staging
+    for (int g = 0; g < n_groups; ++g) {
+        if (m[g] < 0 || m[g] > 2) return fail(ctx, SGL_ERR_UNSUPPORTED, "xi harmonic m must be 0, 1 or 2");
+        const int32_t* id = idx + idx_off[g];
+        for (int e = 0; e < nidx[g]; ++e)
+            if (id[e] < 0 || id[e] >= X.n_kmc * ngc) return fail(ctx, SGL_ERR_VALUE, "coarse index out of range");
+    }
+    // pass 2: keep lists, entry order by p, unique p / q, and every output offset
+    struct GPlan {
+        std::vector<int> keep, order, pg, qg, qs, qpos;
+        int nP = 0;
+        long long ent0 = 0, rowel0 = 0, row0 = 0, u0 = 0, w0 = 0, um0 = 0;
+    };
+    std::vector<GPlan> plan(n_groups);
     std::vector<int> g_m, g_r, g_nP, idx_p, p_ptr{0}, ent_qg, g_nQ, idx_q;
     std::vector<long long> g_p_off, g_ent_off, g_row_off, p_prefix{0}, rowel_off, g_q_off, g_u_off;
-    std::vector<double> U0;
-    std::vector<double> rows_t, res, sum_rows;
-    std::vector<double> W0, res0, sum0, U[3], resm[3], summ[3];
-    long long ent_total = 0, row_total = 0, rowel_total = 0;
-    double sigma_var = 0.0;
+    std::vector<int> kept;                      // groups with rows left after pruning
+    long long ent_total = 0, row_total = 0, rowel_total = 0, u_total = 0, w0_total = 0, um_total[3] = {0, 0, 0};
     for (int g = 0; g < n_groups; ++g) {
-        const int w = nidx[g] + 1;
-        std::vector<int> keep;
+        GPlan& P = plan[g];
         for (int r = 0; r < nrow[g]; ++r)
-            if (!(prune > 0) || norms[g][(size_t)r] > prune * s0) keep.push_back(r);
-        if (keep.empty()) continue;
-        const int R = (int)keep.size(), mg = m[g];
-        if (mg < 0 || mg > 2) return fail(ctx, SGL_ERR_UNSUPPORTED, "xi harmonic m must be 0, 1 or 2");
+            if (!(prune > 0) || norms[g][(size_t)r] > prune * s0) P.keep.push_back(r);
+        if (P.keep.empty()) continue;
+        const int R = (int)P.keep.size(), mg = m[g];
         const int32_t* id = idx + idx_off[g];
-        std::vector<int> pg(nidx[g]), qg(nidx[g]);
-        for (int e = 0; e < nidx[g]; ++e) {
-            if (id[e] < 0 || id[e] >= X.n_kmc * ngc) return fail(ctx, SGL_ERR_VALUE, "coarse index out of range");
-            pg[e] = id[e] / ngc; qg[e] = id[e] % ngc;
-        }
-        // unique p (sorted) and CSR of entries by p
-        std::vector<int> order(nidx[g]);
-        for (int e = 0; e < nidx[g]; ++e) order[e] = e;
-        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pg[a] < pg[b]; });
-        int nP = 0;
+        P.pg.resize(nidx[g]); P.qg.resize(nidx[g]);
+        for (int e = 0; e < nidx[g]; ++e) { P.pg[e] = id[e] / ngc; P.qg[e] = id[e] % ngc; }
+        P.order.resize(nidx[g]);
+        for (int e = 0; e < nidx[g]; ++e) P.order[e] = e;
+        std::stable_sort(P.order.begin(), P.order.end(), [&](int a, int b) { return P.pg[a] < P.pg[b]; });
         for (int i = 0; i < nidx[g]; ++i) {
-            const int e = order[i];
-            if (i == 0 || pg[e] != pg[order[i - 1]]) {
+            const int e = P.order[i];
+            if (i == 0 || P.pg[e] != P.pg[P.order[i - 1]]) {
                 if (i > 0) p_ptr.push_back((int)(ent_total + i));
-                idx_p.push_back(pg[e]);
-                ++nP;
+                idx_p.push_back(P.pg[e]);
+                ++P.nP;
             }
+            ent_qg.push_back(P.qg[e]);
         }
         p_ptr.push_back((int)(ent_total + nidx[g]));
-        // entries in p-order: global q index and rows (entry-major, R values each)
-        for (int i = 0; i < nidx[g]; ++i) {
-            const int e = order[i];
-            ent_qg.push_back(qg[e]);
-            for (int rr = 0; rr < R; ++rr) rows_t.push_back(rows[row_off[g] + (long long)keep[rr] * w + e]);
-        }
-        std::vector<double> resg(R), sumg(R);
-        for (int rr = 0; rr < R; ++rr) {
-            const double* row = rows + row_off[g] + (long long)keep[rr] * w;
-            double s = 0.0;
-            for (int e = 0; e < nidx[g]; ++e) s += row[e];
-            resg[rr] = row[nidx[g]];
-            sumg[rr] = s;
-            res.push_back(resg[rr]);
-            sum_rows.push_back(s);
-        }
-        // 1-D reach stacks (sgl_full.py:2846-2861) and the sigma term (sgl_full.py:3441-3447)
-        if (mg == 0) {
-            for (int rr = 0; rr < R; ++rr) {
-                std::vector<double> wrow(X.n_kmc, 0.0);
-                const double* row = rows + row_off[g] + (long long)keep[rr] * w;
-                double dot = 0.0;
-                for (int e = 0; e < nidx[g]; ++e) { wrow[pg[e]] += row[e]; dot += row[e] * X.kmc[pg[e]]; }
-                W0.insert(W0.end(), wrow.begin(), wrow.end());
-                res0.push_back(resg[rr]); sum0.push_back(sumg[rr]);
-                const double v = dot + resg[rr];
-                sigma_var += v * v;
-            }
-            X.R0 += R;
-        }
-        {
-            for (int rr = 0; rr < R; ++rr) {
-                std::vector<double> urow(X.n_gmc, 0.0);
-                const double* row = rows + row_off[g] + (long long)keep[rr] * w;
-                for (int e = 0; e < nidx[g]; ++e) urow[qg[e]] += row[e];
-                U[mg].insert(U[mg].end(), urow.begin(), urow.end());
-                resm[mg].push_back(resg[rr]); summ[mg].push_back(sumg[rr]);
-            }
-            X.Rm[mg] += R;
-        }
-        // unique q of the group and U = sum over p of the rows (compensated m = 0 form)
-        {
-            std::vector<int> qs(qg.begin(), qg.end());
-            std::sort(qs.begin(), qs.end());
-            qs.erase(std::unique(qs.begin(), qs.end()), qs.end());
-            std::vector<int> qpos(X.n_gmc, -1);
-            for (size_t i = 0; i < qs.size(); ++i) qpos[qs[i]] = (int)i;
-            g_q_off.push_back((long long)idx_q.size());
-            g_u_off.push_back((long long)U0.size());
-            g_nQ.push_back((int)qs.size());
-            idx_q.insert(idx_q.end(), qs.begin(), qs.end());
-            const size_t base = U0.size();
-            U0.resize(base + (size_t)R * qs.size(), 0.0);
-            if (mg == 0)
-                for (int rr = 0; rr < R; ++rr) {
-                    const double* row = rows + row_off[g] + (long long)keep[rr] * w;
-                    for (int e = 0; e < nidx[g]; ++e) U0[base + (size_t)rr * qs.size() + qpos[qg[e]]] += row[e];
-                }
-        }
-        g_m.push_back(mg); g_r.push_back(R); g_nP.push_back(nP);
+        P.qs.assign(P.qg.begin(), P.qg.end());
+        std::sort(P.qs.begin(), P.qs.end());
+        P.qs.erase(std::unique(P.qs.begin(), P.qs.end()), P.qs.end());
+        P.qpos.assign(X.n_gmc, -1);
+        for (size_t i = 0; i < P.qs.size(); ++i) P.qpos[P.qs[i]] = (int)i;
+        g_q_off.push_back((long long)idx_q.size());
+        g_u_off.push_back(u_total);
+        g_nQ.push_back((int)P.qs.size());
+        idx_q.insert(idx_q.end(), P.qs.begin(), P.qs.end());
+        P.ent0 = ent_total; P.rowel0 = rowel_total; P.row0 = row_total; P.u0 = u_total;
+        P.w0 = w0_total; P.um0 = um_total[mg];
+        if (mg == 0) { w0_total += (long long)R * X.n_kmc; X.R0 += R; }
+        um_total[mg] += (long long)R * X.n_gmc;
+        X.Rm[mg] += R;
+        u_total += (long long)R * P.qs.size();
+        g_m.push_back(mg); g_r.push_back(R); g_nP.push_back(P.nP);
         g_p_off.push_back(p_prefix.back());
         g_ent_off.push_back(ent_total);
         g_row_off.push_back(row_total);
         rowel_off.push_back(rowel_total);
-        p_prefix.push_back(p_prefix.back() + nP);
+        p_prefix.push_back(p_prefix.back() + P.nP);
         ent_total += nidx[g];
         row_total += R;
         rowel_total += (long long)R * nidx[g];
-        X.m.push_back(mg); X.r.push_back(R); X.nP.push_back(nP);
+        X.m.push_back(mg); X.r.push_back(R); X.nP.push_back(P.nP);
+        kept.push_back(g);
+    }
+    // pass 3: data, in parallel over groups
+    std::vector<double> res((size_t)row_total), sum_rows((size_t)row_total);
+    // the transposed rows (FP64 and FP32 copies) are written straight into pinned memory
+    CKS(sync_stream(ctx));
+    char* bp = big_pinned(ctx, (size_t)rowel_total * 12 + 256);
+    if (!bp) return fail(ctx, SGL_ERR_CUDA, "pinned host allocation failed (xi rows)");
+    double* rows_t_p = (double*)bp;
+    float* rows_tf_p = (float*)(bp + ((size_t)rowel_total * 8 + 255) / 256 * 256);
+    std::vector<double> U0((size_t)u_total, 0.0), W0((size_t)w0_total, 0.0), res0, sum0;
+    std::vector<double> U[3], resm[3], summ[3];
+    for (int k = 0; k < 3; ++k) U[k].assign((size_t)um_total[k], 0.0);
+    std::vector<double> sig_v((size_t)row_total, 0.0);     // (rows . kc + res) per m = 0 row
+    parallel_groups([&](int g) {
+        const GPlan& P = plan[g];
+        if (P.keep.empty()) return;
+        const int R = (int)P.keep.size(), mg = m[g], w = nidx[g] + 1, ne = nidx[g];
+        double* rt = rows_t_p + P.rowel0;
+        float* rtf = rows_tf_p + P.rowel0;
+        for (int rr = 0; rr < R; ++rr) {                     // rows_t[i][rr] = row_rr[order[i]]
+            const double* row = rows + row_off[g] + (long long)P.keep[rr] * w;
+            for (int i = 0; i < ne; ++i) {
+                const double v = row[P.order[i]];
+                rt[(long long)i * R + rr] = v;
+                rtf[(long long)i * R + rr] = (float)v;
+            }
+            double sm = 0.0;
+            for (int e = 0; e < ne; ++e) sm += row[e];
+            res[(size_t)(P.row0 + rr)] = row[ne];
+            sum_rows[(size_t)(P.row0 + rr)] = sm;
+            if (mg == 0) {
+                double* wrow = W0.data() + P.w0 + (long long)rr * X.n_kmc;
+                double dot = 0.0;
+                for (int e = 0; e < ne; ++e) { wrow[P.pg[e]] += row[e]; dot += row[e] * X.kmc[P.pg[e]]; }
+                sig_v[(size_t)(P.row0 + rr)] = dot + row[ne];
+                double* u0 = U0.data() + P.u0 + (long long)rr * P.qs.size();
+                for (int e = 0; e < ne; ++e) u0[P.qpos[P.qg[e]]] += row[e];
+            }
+            double* urow = U[mg].data() + P.um0 + (long long)rr * X.n_gmc;
+            for (int e = 0; e < ne; ++e) urow[P.qg[e]] += row[e];
+        }
+    });
+    double sigma_var = 0.0;
+    for (int g : kept) {
+        const GPlan& P = plan[g];
+        const int R = (int)P.keep.size();
+        for (int rr = 0; rr < R; ++rr) {
+            if (m[g] == 0) {
+                const double v = sig_v[(size_t)(P.row0 + rr)];
+                sigma_var += v * v;
+                res0.push_back(res[(size_t)(P.row0 + rr)]);
+                sum0.push_back(sum_rows[(size_t)(P.row0 + rr)]);
+            }
+            resm[m[g]].push_back(res[(size_t)(P.row0 + rr)]);
+            summ[m[g]].push_back(sum_rows[(size_t)(P.row0 + rr)]);
+        }
     }
     X.n_groups = (int)g_m.size();
     X.total_p = (int)p_prefix.back();
@@ -1214,7 +1310,7 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         DBUF(d_idxp, int, "xi_idxp", idx_p.size());
         DBUF(d_pptr, int, "xi_pptr", p_ptr.size());
         DBUF(d_qg, int, "xi_entq", ent_qg.size());
-        DBUF(d_rows, double, "xi_rows", rows_t.size());
+        DBUF(d_rows, double, "xi_rows", rowel_total);
         DBUF(d_res, double, "xi_res", res.size());
         DBUF(d_sum, double, "xi_sum", sum_rows.size());
         std::vector<long long> goff;
@@ -1231,16 +1327,17 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         CKS(upload(ctx, d_idxp, idx_p.data(), idx_p.size()));
         CKS(upload(ctx, d_pptr, p_ptr.data(), p_ptr.size()));
         CKS(upload(ctx, d_qg, ent_qg.data(), ent_qg.size()));
-        CKS(upload(ctx, d_rows, rows_t.data(), rows_t.size()));
+        if (rowel_total > 0)
+            CK(cudaMemcpyAsync(d_rows, rows_t_p, (size_t)rowel_total * 8, cudaMemcpyHostToDevice, ctx->stream));
         CKS(upload(ctx, d_res, res.data(), res.size()));
         CKS(upload(ctx, d_sum, sum_rows.data(), sum_rows.size()));
         D.g_m = d_gm; D.g_r = d_gr; D.g_nP = d_gnP;
         D.g_p_off = d_goff; D.g_ent_off = d_goff + X.n_groups; D.g_row_off = d_goff + 2 * X.n_groups;
         D.idx_p = d_idxp; D.p_ptr = d_pptr; D.ent_qg = d_qg; D.rows = d_rows; D.res = d_res; D.sum_rows = d_sum;
         {
-            std::vector<float> rf(rows_t.begin(), rows_t.end());
-            DBUF(d_rowsf, float, "xi_rows_f", rf.size());
-            CKS(upload(ctx, d_rowsf, rf.data(), rf.size()));
+            DBUF(d_rowsf, float, "xi_rows_f", rowel_total);
+            if (rowel_total > 0)
+                CK(cudaMemcpyAsync(d_rowsf, rows_tf_p, (size_t)rowel_total * 4, cudaMemcpyHostToDevice, ctx->stream));
             DBUF(d_gnQ, int, "xi_gnQ", g_nQ.size());
             DBUF(d_qoff, long long, "xi_qoff", g_q_off.size());
             DBUF(d_uoff, long long, "xi_uoff", g_u_off.size());
@@ -1251,7 +1348,7 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
             CKS(upload(ctx, d_uoff, g_u_off.data(), g_u_off.size()));
             CKS(upload(ctx, d_idxq, idx_q.data(), idx_q.size()));
             CKS(upload(ctx, d_U0, U0.data(), U0.size()));
-            CK(cudaStreamSynchronize(ctx->stream));   // rf is a local staging vector
+            CK(cudaStreamSynchronize(ctx->stream));   // host vectors are local
             D.rows_f = d_rowsf; D.g_nQ = d_gnQ; D.g_q_off = d_qoff; D.g_u_off = d_uoff; D.idx_q = d_idxq; D.U0 = d_U0;
             D.r_max = *std::max_element(g_r.begin(), g_r.end());
         }

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <math.h>
+#include <atomic>
 
 #include "sgl_gb300.h"
 
@@ -57,7 +58,7 @@ __device__ inline T block_sum(T v, T* sh) {
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
 // Number of kernels this library has launched (reported by sgl_stats_json).
-long long& launch_counter();
+std::atomic<long long>& launch_counter();
 #define SGL_COUNT(n) (::sgl::launch_counter() += (n))
 
 }  // namespace sgl

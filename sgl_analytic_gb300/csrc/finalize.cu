@@ -9,8 +9,8 @@
 
 namespace sgl {
 
-long long& launch_counter() {
-    static long long n = 0;
+std::atomic<long long>& launch_counter() {
+    static std::atomic<long long> n{0};      // contexts may run on several host threads
     return n;
 }
 

@@ -134,9 +134,16 @@ struct TcPackDesc {                         // one operand to pack: X(r, k) = X[
 };
 // fills tiles / packing descriptors (pk: 2 n entries) for operands split into `parts` (2 or 3)
 // TF32 parts; returns the packed buffer size in floats
-long long tc_gemm_plan(TcGemmDesc* d, int n, int parts, TcPackDesc* pk, int* tiles, long long* quads);
+long long tc_gemm_plan(TcGemmDesc* d, int n, int parts, TcPackDesc* pk, int* tiles, long long* quads,
+                       bool pack_a = true);
 void launch_tc_gemm(int parts, const TcGemmDesc* d_descs, int nprob, int tiles, const TcPackDesc* d_pack,
                     long long quads, float* packed, int* err, cudaStream_t st);
+
+// gauss stage A of the mixed path written as the packed (2-part TF32) A operand of the xi GEMM
+bool xi_stageA_pack_fits(int r_max, int nkg);
+void launch_xi_stageA_pack(const XiDevice& x, const long long* d_p_prefix, const float* J, int nkg,
+                           const long long* d_chunk_prefix, long long nchunks, const TcGemmDesc* d_descs,
+                           float* packed, cudaStream_t st);
 
 // ---- positive (vp) Cox closure
 // Cells sorted per shell into runs (one kind and interval bound; runs ordered linear first, then by

@@ -159,6 +159,138 @@ void launch_xi_stageA(int precision, const XiDevice& x, const long long* d_p_pre
     }
 }
 
+// Mixed-path stage A written straight into the xi GEMM's packed A operand
+//   A'(i', p) = T_g[p, i'],  i' = rr * nkg + j,  packed [kb][part][Mpad][16], 2 TF32 parts,
+// so the GEMM's bulk copies read it as is (no FP32 T in HBM, no separate pack pass).
+// One CTA per (group, 4 consecutive p): for each p, its entries (rows and J_m rows) stream through
+// shared memory in chunks of 32 and each thread accumulates 4 rr x 4 j tiles (FP32, float4 operand
+// reads); the 4 p results are staged in shared memory and written as (hi, lo) float4 rows of the
+// core matrices, with zeros in the padded rows and columns.
+constexpr int kSAEnt = 32, kSAThreads = 256, kSAMaxTasks = 2;
+
+bool xi_stageA_pack_fits(int r_max, int nkg) {
+    const int tasks = ((r_max + 3) / 4) * ((nkg + 3) / 4);
+    const size_t sm = (4ULL * r_max * nkg + (size_t)kSAEnt * (((r_max + 3) & ~3) + ((nkg + 3) & ~3))) * 4;
+    return tasks <= kSAThreads * kSAMaxTasks && sm <= 200 * 1024;
+}
+
+__device__ __forceinline__ float tf32_rna_sa(float v) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
+    return __uint_as_float(r);
+}
+
+__global__ void __launch_bounds__(kSAThreads)
+k_xi_stageA_pack(XiDevice x, const long long* __restrict__ p_prefix, const long long* __restrict__ rowel_off,
+                 const float* __restrict__ J, int nkg, const long long* __restrict__ chunk_prefix,
+                 const TcGemmDesc* __restrict__ descs, float* __restrict__ packed) {
+    extern __shared__ __align__(16) float sa_sm[];
+    const int rmax = x.r_max;
+    const int rpm = (rmax + 3) & ~3, nkp = (nkg + 3) & ~3;
+    float* s_out = sa_sm;                                   // [4][r * nkg]
+    float* s_rows = s_out + 4LL * rmax * nkg;               // [kSAEnt][rp]
+    float* s_J = s_rows + kSAEnt * rpm;                     // [kSAEnt][nkp]
+    const long long cidx = blockIdx.x;
+    const int g = find_group(chunk_prefix, x.n_groups, cidx);
+    const int c4 = (int)(cidx - chunk_prefix[g]);
+    const TcGemmDesc d = descs[g];
+    const int r = x.g_r[g], m = x.g_m[g], nP = x.g_nP[g];
+    const int rp = (r + 3) & ~3;
+    const int M = r * nkg;
+    const int nrb = rp / 4, njb = nkp / 4, ntask = nrb * njb;
+    const long long gp0 = p_prefix[g], ent0 = x.g_ent_off[g];
+    const float* rowsg = x.rows_f + rowel_off[g];
+    const float* Jm = J + (long long)m * x.n_gmc * nkg;
+    const int tid = threadIdx.x;
+    for (int pp = 0; pp < 4; ++pp) {
+        const int p = 4 * c4 + pp;
+        float* so = s_out + (long long)pp * M;
+        if (p >= nP) {
+            for (int i = tid; i < M; i += kSAThreads) so[i] = 0.f;
+            continue;
+        }
+        const long long P = gp0 + p;
+        const int e0 = x.p_ptr[P], e1 = x.p_ptr[P + 1];
+        float acc[kSAMaxTasks][16];
+#pragma unroll
+        for (int a = 0; a < kSAMaxTasks; ++a)
+#pragma unroll
+            for (int b = 0; b < 16; ++b) acc[a][b] = 0.f;
+        for (int eb = e0; eb < e1; eb += kSAEnt) {
+            const int cnt = min(kSAEnt, e1 - eb);
+            __syncthreads();
+            for (int t = tid; t < kSAEnt * rp; t += kSAThreads) {
+                const int e = t / rp, rr = t % rp;
+                s_rows[e * rp + rr] = (e < cnt && rr < r) ? rowsg[((long long)(eb + e) - ent0) * r + rr] : 0.f;
+            }
+            for (int t = tid; t < kSAEnt * nkp; t += kSAThreads) {
+                const int e = t / nkp, j = t % nkp;
+                s_J[e * nkp + j] = (e < cnt && j < nkg) ? Jm[(long long)x.ent_qg[eb + e] * nkg + j] : 0.f;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int a = 0; a < kSAMaxTasks; ++a) {
+                const int task = tid + a * kSAThreads;
+                if (task < ntask) {
+                    const int rb = task / njb, jb = task % njb;
+                    for (int e = 0; e < cnt; ++e) {
+                        const float4 ra = *(const float4*)(s_rows + e * rp + 4 * rb);
+                        const float4 jv = *(const float4*)(s_J + e * nkp + 4 * jb);
+                        const float av[4] = {ra.x, ra.y, ra.z, ra.w}, bv[4] = {jv.x, jv.y, jv.z, jv.w};
+#pragma unroll
+                        for (int u = 0; u < 4; ++u)
+#pragma unroll
+                            for (int w = 0; w < 4; ++w) acc[a][u * 4 + w] = fmaf(av[u], bv[w], acc[a][u * 4 + w]);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < kSAMaxTasks; ++a) {
+            const int task = tid + a * kSAThreads;
+            if (task < ntask) {
+                const int rb = task / njb, jb = task % njb;
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int w = 0; w < 4; ++w) {
+                        const int rr = 4 * rb + u, j = 4 * jb + w;
+                        if (rr < r && j < nkg) so[rr * nkg + j] = acc[a][u * 4 + w];
+                    }
+            }
+        }
+    }
+    __syncthreads();
+    // packed rows: chunk c of K block kb holds p = 16 kb + 4 c .. + 3
+    const int kb = c4 / 4, c = c4 % 4;
+    float* Ap = packed + d.a_off;
+    const long long pstride = (long long)d.Mpad * 16;
+    for (int i = tid; i < d.Mpad; i += kSAThreads) {
+        float hv[4], lv[4];
+#pragma unroll
+        for (int pp = 0; pp < 4; ++pp) {
+            const float v = i < M ? s_out[(long long)pp * M + i] : 0.f;
+            hv[pp] = tf32_rna_sa(v);
+            lv[pp] = tf32_rna_sa(v - hv[pp]);
+        }
+        const long long o = (long long)(i >> 3) * 128 + c * 32 + (i & 7) * 4;
+        *(float4*)(Ap + (2LL * kb) * pstride + o) = make_float4(hv[0], hv[1], hv[2], hv[3]);
+        *(float4*)(Ap + (2LL * kb + 1) * pstride + o) = make_float4(lv[0], lv[1], lv[2], lv[3]);
+    }
+}
+
+void launch_xi_stageA_pack(const XiDevice& x, const long long* d_p_prefix, const float* J, int nkg,
+                           const long long* d_chunk_prefix, long long nchunks, const TcGemmDesc* d_descs,
+                           float* packed, cudaStream_t st) {
+    const long long* rowel_off = d_p_prefix + (x.n_groups + 1);
+    const int rmax = x.r_max;
+    const size_t sm = (4ULL * rmax * nkg + (size_t)kSAEnt * (((rmax + 3) & ~3) + ((nkg + 3) & ~3))) * 4;
+    cudaFuncSetAttribute(k_xi_stageA_pack, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_xi_stageA_pack<<<(unsigned)nchunks, kSAThreads, sm, st>>>(x, d_p_prefix, rowel_off, J, nkg, d_chunk_prefix,
+                                                                d_descs, packed);
+    SGL_COUNT(1);
+}
+
 // E_g[i, p] = cos(kk_i kap_p) (i < nk) / sin(kk_{i-nk} kap_p): one CTA per global p
 // comp = 1 (mixed path): m = 0 groups get cos - 1 = -2 sin^2(x/2) in place of cos, so that
 // G_r = sum (cos - 1) T + sum_q U (J0 - 1) carries no cancellation against sum_rows.

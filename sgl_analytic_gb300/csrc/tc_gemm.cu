@@ -270,7 +270,8 @@ k_tc_gemm(const TcGemmDesc* __restrict__ descs, int nprob, const float* __restri
 }
 
 // ------------------------------------------------------------------ host planning / launch
-long long tc_gemm_plan(TcGemmDesc* d, int n, int parts, TcPackDesc* pk, int* tiles_out, long long* quads_out) {
+long long tc_gemm_plan(TcGemmDesc* d, int n, int parts, TcPackDesc* pk, int* tiles_out, long long* quads_out,
+                       bool pack_a) {
     long long off = 0, quads = 0;
     int tiles = 0;
     for (int i = 0; i < n; ++i) {
@@ -291,7 +292,8 @@ long long tc_gemm_plan(TcGemmDesc* d, int n, int parts, TcPackDesc* pk, int* til
         TcPackDesc& pa = pk[2 * i];
         pa.X = g.A; pa.x_rs = g.a_rs; pa.x_cs = g.a_cs; pa.R = g.M; pa.K = g.K; pa.Rpad = g.Mpad; pa.nkb = nkb;
         pa.out_off = g.a_off; pa.quad_begin = quads;
-        quads += 4LL * g.Mpad * nkb;
+        if (pack_a) quads += 4LL * g.Mpad * nkb;
+        else pa.nkb = 0;                               // A written packed by its producer
         TcPackDesc& pb = pk[2 * i + 1];
         pb.X = g.B; pb.x_rs = g.b_cs; pb.x_cs = g.b_rs; pb.R = g.N; pb.K = g.K; pb.Rpad = g.Npad; pb.nkb = nkb;
         pb.out_off = g.b_off; pb.quad_begin = quads;
