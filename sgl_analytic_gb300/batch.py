@@ -1,0 +1,70 @@
+"""Batched plain solver: many independent PDFs in flight on one GPU.
+
+Each slot is one engine context (its own CUDA stream and device arena) holding one resident
+population; host threads drive the slots, and the C calls release the GIL, so the slots' kernels
+overlap on the device.  A PDF is independent of every other PDF, so there is no exchange between
+slots.  With the z_s = 1 workload the device is already ~97% busy with one PDF in flight; four
+slots add about 20% throughput by filling the gaps between kernels and the host-side steps of
+each inversion.
+"""
+from __future__ import annotations
+
+import threading
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+from ._lib import Engine
+from .lam import Lam, invert
+
+
+class BatchSolver:
+    """slots: number of contexts (streams) kept busy at once."""
+
+    def __init__(self, slots=4, device=0, precision="mixed"):
+        if slots < 1:
+            raise ValueError("slots must be >= 1")
+        self.slots = int(slots)
+        self.precision = precision
+        self.engines = [Engine(device) for _ in range(self.slots)]
+        self.lams = [None] * self.slots
+        self._pool = ThreadPoolExecutor(max_workers=self.slots)
+        self._lock = threading.Lock()
+
+    def load(self, populations, xi=True):
+        """Makes populations resident, one per slot (len(populations) <= slots)."""
+        if len(populations) > self.slots:
+            raise ValueError("more populations than slots")
+        futs = [self._pool.submit(Lam, p, xi=xi, engine=self.engines[i], precision=self.precision)
+                for i, p in enumerate(populations)]
+        for i, f in enumerate(futs):
+            self.lams[i] = f.result()
+        return self
+
+    @property
+    def streams(self):
+        return [e.stream for e in self.engines]
+
+    def solve(self, xi_out, repeats=1, **invert_kw):
+        """Runs `repeats` PDFs on every loaded slot concurrently; returns the last (xi, P, meta) of
+        each slot."""
+        xi_out = np.asarray(xi_out, float)
+        live = [i for i in range(self.slots) if self.lams[i] is not None]
+        if not live:
+            raise RuntimeError("no population loaded")
+
+        def run(i):
+            lam = self.lams[i]
+            s = lam.sigma()
+            out = None
+            for _ in range(repeats):
+                out = invert(lam, s, xi_out=xi_out, **invert_kw)
+            return out
+
+        futs = [self._pool.submit(run, i) for i in live]
+        return [f.result() for f in futs]
+
+    def close(self):
+        self._pool.shutdown(wait=True)
+        for e in self.engines:
+            e.close()
