@@ -43,7 +43,9 @@ WORKLOAD = ("z_s=1 default flat LCDM PDF: reference z_s=1 population (79,574 fin
 XI_OUT = np.concatenate([np.linspace(-1.0, 1.0, 1601), np.linspace(1.005, 9.0, 1600)])
 # DRAM bytes (read + write) per launch of the dominant kernels, from one ncu capture of this
 # workload (profiles/ holds the summaries and the commands)
-TRAFFIC = {"gemm_f32_xi": 1.2079e9}        # profiles/gemm_f32_xi_zs1.md
+TRAFFIC = {"gemm_f32_xi": 1.2079e9,         # profiles/gemm_f32_xi_zs1.md
+           "xi_stageA": 1.4768e9,          # profiles/xi_stageA_pack_zs1.md
+           "gemm_tc_sep3": 2.140e8}        # profiles/tc_gemm_sep3_zs1.md
 
 
 def dist_env():
@@ -210,6 +212,93 @@ def run_cf_sweep(args, rank, world, local):
         print(json.dumps(line))
 
 
+def run_surrogate(args, rank, world, local):
+    """Learned per-plane log-CF surrogate: 2e6 training samples (3907 planes x 512 ln k) and 1e5
+    held-out samples (196 planes x 512) from the FP64 GPU solver over the cosmology box; a
+    two-member ensemble of 8 -> 6 x 256 SiLU -> 2 BF16 MLPs trained by the engine's tensor-core
+    kernels; accuracy against the FP64 solver and the judge's fallback fraction."""
+    import torch
+    from sgl_analytic_gb300 import surrogate as S
+    from sgl_analytic_gb300._lib import Engine
+    torch.cuda.set_device(local)
+    eng = Engine(local)
+    stream = torch.cuda.ExternalStream(eng.stream, device=torch.device("cuda", local))
+    model = S.PlaneModel()
+    n_tr, n_te, nk = 3907, 196, 512
+    th, zl, lnk = S.sample_inputs(n_tr, nk, seed=11 + rank)
+    t0 = time.perf_counter()
+    L = S.solve_planes(eng, model, th, zl, lnk)
+    t_solve = time.perf_counter() - t0
+    th2, zl2, lnk2 = S.sample_inputs(n_te, nk, seed=1000 + rank)
+    L2 = S.solve_planes(eng, model, th2, zl2, lnk2)
+    X, Y, X2 = S.features(th, zl, lnk), S.targets(L), S.features(th2, zl2, lnk2)
+    sur = S.Surrogate(eng, members=2, seed=rank)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    hist = sur.train(X, Y, epochs=args.sur_epochs, batch=16384, lr=2e-3)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_train = e0.elapsed_time(e1) / 1e3
+    steps = args.sur_epochs * (X.shape[0] // 16384) * len(sur.mlps)
+    sizes = sur.mlps[0].sizes
+    gemm_flops = 3 * 2.0 * 16384 * sum(a * c for a, c in zip(sizes[:-1], sizes[1:]))    # fwd, dX, dW
+    # inference throughput (device time, after warm-up) and accuracy on the held-out planes
+    (X2d,) = S.to_device(eng, X2)
+    for _ in range(3):
+        sur.mlps[0].predict(X2d)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    reps = 10
+    for _ in range(reps):
+        sur.mlps[0].predict(X2d)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_inf = e0.elapsed_time(e1) / 1e3 / reps
+    lam_s, dis = sur.log_cf(X2)
+    lam_x = L2.ravel()
+    d = np.abs(lam_s - lam_x)
+    rel = d / np.maximum(np.abs(lam_x), 1e-300)
+    fb = {f"{t:g}": float(np.mean(dis.reshape(n_te, nk).max(1) > t)) for t in (1e-5, 1e-3, 1e-1, 1.0)}
+    pk, pk_src = peaks()
+    ach = gemm_flops * steps / t_train / 1e12
+    # surrogate + judge PDF sweep (z_s = 1 instances, 64 planes each) against the plain solver
+    sw_thetas = S.sample_inputs(args.sweep_instances, 1, seed=5000 + rank)[0]
+    sw = S.pdf_sweep(eng, model, sur, sw_thetas, threshold=1e-5)
+    lnmu = sw["lnmu"]
+    l1s = [float(np.trapezoid(np.abs(a - b), lnmu)) for a, b in zip(sw["P_sur"], sw["P_plain"])]
+    sw_nojudge = S.pdf_sweep(eng, model, sur, sw_thetas[:2], threshold=np.inf)
+    l1_raw = [float(np.trapezoid(np.abs(a - b), lnmu)) for a, b in zip(sw_nojudge["P_sur"], sw_nojudge["P_plain"])]
+    if rank == 0:
+        line = {"metric": "surrogate per-plane log-CF evaluations/sec (BF16 MLP inference, 1 member)",
+                "value": X2.shape[0] / t_inf, "unit": "samples/s", "n_gpus": world, "steps": reps, "warmup": 3,
+                "ms_per_step": 1e3 * t_inf, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "bf16+f32", "data": "synthetic (seeded cosmology-dependent lens planes)",
+                "config": {"workload": "per-plane log-CF surrogate: 8 -> 6 x 256 SiLU -> 2 BF16 MLP, 2 members, "
+                                       "2e6 training / 1e5 held-out samples from the FP64 GPU solver",
+                           "train_samples": int(X.shape[0]), "heldout_samples": int(X2.shape[0]),
+                           "epochs": args.sur_epochs, "batch": 16384},
+                "solver_samples_per_s": X.shape[0] / t_solve,
+                "gain_vs_solver": (X2.shape[0] / t_inf) / (X.shape[0] / t_solve),
+                "training": {"seconds": t_train, "samples_per_s": steps * 16384 / t_train,
+                             "final_loss": [h[-1] for h in hist], "first_loss": [h[0] for h in hist]},
+                "accuracy": {"abs_dlncf_median": float(np.median(d)), "abs_dlncf_p90": float(np.quantile(d, 0.9)),
+                             "rel_median": float(np.median(rel)), "rel_p90": float(np.quantile(rel, 0.9))},
+                "judge_fallback_fraction": fb,
+                "pdf_sweep": {"instances": int(len(sw_thetas)), "planes_per_instance": 64, "k_points": 2048,
+                              "lnmu_points": int(lnmu.size), "judge_threshold_lncf": 1e-5,
+                              "fallback_fraction": float(np.mean(sw["fallback"])),
+                              "pdf_per_s_surrogate_judge": len(sw_thetas) / sw["t_sur"],
+                              "pdf_per_s_plain_solver": len(sw_thetas) / sw["t_plain"],
+                              "pdf_l1_vs_plain_max": max(l1s),
+                              "pdf_l1_surrogate_without_judge": l1_raw},
+                "roofline": {"kernel": "k_tc_gemm<1> (BF16) during training", "bound": "tensor", "achieved": ach,
+                             "peak": float(pk["bf16_tflops"]), "unit": "TFLOP/s", "frac": ach / float(pk["bf16_tflops"]),
+                             "traffic": None, "peak_source": f"{pk_src} bf16 burst",
+                             "note": "whole training step time, including host-side launch overhead"}}
+        print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -222,7 +311,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--workload", default="zs1_pdf", choices=("zs1_pdf", "cf_sweep"))
+    ap.add_argument("--workload", default="zs1_pdf", choices=("zs1_pdf", "cf_sweep", "surrogate"))
+    ap.add_argument("--sur-epochs", type=int, default=20)
+    ap.add_argument("--sweep-instances", type=int, default=8)
     args = ap.parse_args()
     rank, world, local = dist_env()
     if world > 1:
@@ -235,8 +326,8 @@ def main():
             dist.destroy_process_group()
         return
 
-    if args.workload == "cf_sweep":
-        run_cf_sweep(args, rank, world, local)
+    if args.workload in ("cf_sweep", "surrogate"):
+        (run_cf_sweep if args.workload == "cf_sweep" else run_surrogate)(args, rank, world, local)
         if world > 1:
             import torch.distributed as dist
             dist.destroy_process_group()

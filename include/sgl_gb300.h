@@ -160,7 +160,29 @@ sgl_status sgl_sweep_set_cells(sgl_ctx* ctx, int64_t n_cells, const double* kap,
 sgl_status sgl_sweep_eval(sgl_ctx* ctx, const double* kk, int nk, int precision, double* out_re,
                           double* out_im);
 
-/* Measured FMA throughput of this GPU (fp64 = 1: FP64, 0: FP32), TFLOP/s (2 flops per FMA):
+/* Surrogate MLP building blocks --------------------------------------------------------------
+ * No counterpart in the reference: the learned per-plane log-CF model of the BF16 surrogate.
+ * Device pointers; every call is asynchronous on the context's stream except sgl_mlp_mse.
+ * sgl_gemm_bf16: C(i,j) = alpha sum_k A(i,k) B(k,j) with A(i,k) = A[i*a_rs + k*a_cs],
+ *   B(k,j) = B[k*b_rs + j*b_cs], C(i,j) = C[i*c_rs + j*c_cs]; operands rounded to BF16 and packed for
+ *   the tensor cores (tcgen05.mma.kind::f16, FP32 accumulation in TMEM).
+ * sgl_mlp_bias_act: Zb = Z + bias[col], A = silu(Zb) (silu = 1) or Zb (silu = 0); M x N row-major.
+ * sgl_mlp_act_grad: dZ = dA * silu'(Zb).   sgl_mlp_col_sum: out[j] = sum_i X[i, j] (FP64 sums).
+ * sgl_mlp_mse: dpred = 2 (pred - target) / n and *loss = mean (pred - target)^2 (host, synchronous).
+ * sgl_mlp_adamw: AdamW step `step` (>= 1) with bias-corrected moments, decoupled weight decay. */
+sgl_status sgl_gemm_bf16(sgl_ctx* ctx, int M, int N, int K, const float* A, int64_t a_rs, int64_t a_cs,
+                         const float* B, int64_t b_rs, int64_t b_cs, float* C, int64_t c_rs, int64_t c_cs,
+                         float alpha);
+sgl_status sgl_mlp_bias_act(sgl_ctx* ctx, int M, int N, const float* Z, const float* bias, float* Zb,
+                            float* A, int silu);
+sgl_status sgl_mlp_act_grad(sgl_ctx* ctx, int M, int N, const float* dA, const float* Zb, float* dZ);
+sgl_status sgl_mlp_col_sum(sgl_ctx* ctx, int M, int N, const float* X, float* out);
+sgl_status sgl_mlp_mse(sgl_ctx* ctx, int64_t n, const float* pred, const float* target, float* dpred,
+                       double* loss);
+sgl_status sgl_mlp_adamw(sgl_ctx* ctx, int64_t n, float* w, const float* g, float* m, float* v, float lr,
+                         float b1, float b2, float eps, float wd, int step);
+
+/* Measured FMA throughput of this GPU/* Measured FMA throughput of this GPU (fp64 = 1: FP64, 0: FP32), TFLOP/s (2 flops per FMA):
  * the denominator of the CF-sweep roofline.  No counterpart in the reference. */
 sgl_status sgl_measure_peak(sgl_ctx* ctx, int fp64, double* tflops);
 

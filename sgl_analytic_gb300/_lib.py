@@ -22,6 +22,7 @@ EXPORTS = ("sgl_abi_version", "sgl_ctx_create", "sgl_ctx_destroy", "sgl_last_err
            "sgl_ctx_profile", "sgl_stats_json", "sgl_lam_set_cells",
            "sgl_lam_set_xi", "sgl_lam_sigma", "sgl_lnphi", "sgl_xi_term", "sgl_sweep_set_cells", "sgl_sweep_eval", "sgl_measure_peak",
            "sgl_vp_set", "sgl_vp_lnR", "sgl_invert_opts_default", "sgl_pdf",
+           "sgl_gemm_bf16", "sgl_mlp_bias_act", "sgl_mlp_act_grad", "sgl_mlp_col_sum", "sgl_mlp_mse", "sgl_mlp_adamw",
            "sgl_cf_kappa_noalloc")
 
 
@@ -78,6 +79,16 @@ def lib():
                                  ip, dp, dp, dp, ip, ip, C.c_double]
         L.sgl_vp_lnR.argtypes = [vp, dp, C.c_int, dp, C.c_int, C.c_int, dp, dp]
         for name in ("sgl_sweep_set_cells", "sgl_sweep_eval", "sgl_measure_peak"):
+            getattr(L, name).restype = C.c_int
+        i64, f32 = C.c_int64, C.c_float
+        L.sgl_gemm_bf16.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, i64, i64, vp, i64, i64, vp, i64, i64, f32]
+        L.sgl_mlp_bias_act.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, vp, C.c_int]
+        L.sgl_mlp_act_grad.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp]
+        L.sgl_mlp_col_sum.argtypes = [vp, C.c_int, C.c_int, vp, vp]
+        L.sgl_mlp_mse.argtypes = [vp, i64, vp, vp, vp, dp]
+        L.sgl_mlp_adamw.argtypes = [vp, i64, vp, vp, vp, vp, f32, f32, f32, f32, f32, C.c_int]
+        for name in ("sgl_gemm_bf16", "sgl_mlp_bias_act", "sgl_mlp_act_grad", "sgl_mlp_col_sum", "sgl_mlp_mse",
+                     "sgl_mlp_adamw"):
             getattr(L, name).restype = C.c_int
         L.sgl_cf_kappa_noalloc.argtypes = [vp, C.c_int, vp, vp, C.c_int64, vp, vp, vp]
         L.sgl_cf_kappa_noalloc.restype = C.c_int

@@ -1596,6 +1596,70 @@ sgl_status sgl_xi_term(sgl_ctx* ctx, const double* kk, int nkk, const double* kg
     return SGL_OK;
 }
 
+// ------------------------------------------------------------------ surrogate MLP building blocks
+sgl_status sgl_gemm_bf16(sgl_ctx* ctx, int M, int N, int K, const float* A, int64_t a_rs, int64_t a_cs, const float* B,
+                         int64_t b_rs, int64_t b_cs, float* C, int64_t c_rs, int64_t c_cs, float alpha) {
+    if (!ctx) return SGL_ERR_VALUE;
+    if (M < 0 || N < 0 || K < 0 || (M > 0 && N > 0 && (!A || !B || !C))) return fail(ctx, SGL_ERR_VALUE, "invalid GEMM arguments");
+    if (M == 0 || N == 0) return SGL_OK;
+    CK(cudaSetDevice(ctx->device));
+    std::vector<TcGemmDesc> v(1);
+    TcGemmDesc& t = v[0];
+    t = TcGemmDesc{};
+    t.M = M; t.N = N; t.K = K;
+    t.A = A; t.a_rs = a_rs; t.a_cs = a_cs;
+    t.B = B; t.b_rs = b_rs; t.b_cs = b_cs;
+    t.C = C; t.c_rs = c_rs; t.c_cs = c_cs;
+    t.alpha = alpha;
+    return run_tc_gemms(ctx, v, "bf16", 1);
+}
+
+sgl_status sgl_mlp_bias_act(sgl_ctx* ctx, int M, int N, const float* Z, const float* bias, float* Zb, float* A, int silu) {
+    if (!ctx || M < 0 || N < 0) return SGL_ERR_VALUE;
+    launch_bias_act(M, N, Z, bias, Zb, A, silu, ctx->stream);
+    CKLAUNCH();
+    return SGL_OK;
+}
+
+sgl_status sgl_mlp_act_grad(sgl_ctx* ctx, int M, int N, const float* dA, const float* Zb, float* dZ) {
+    if (!ctx || M < 0 || N < 0) return SGL_ERR_VALUE;
+    launch_act_grad(M, N, dA, Zb, dZ, ctx->stream);
+    CKLAUNCH();
+    return SGL_OK;
+}
+
+sgl_status sgl_mlp_col_sum(sgl_ctx* ctx, int M, int N, const float* X, float* out) {
+    if (!ctx || M < 0 || N < 0) return SGL_ERR_VALUE;
+    launch_col_sum(M, N, X, out, ctx->stream);
+    CKLAUNCH();
+    return SGL_OK;
+}
+
+sgl_status sgl_mlp_mse(sgl_ctx* ctx, int64_t n, const float* pred, const float* target, float* dpred, double* loss) {
+    if (!ctx || n < 1 || !pred || !target || !dpred || !loss) return SGL_ERR_VALUE;
+    const int nb = mse_blocks(n);
+    DBUF(part, double, "mse_part", nb);
+    launch_mse(n, pred, target, dpred, part, ctx->stream);
+    CKLAUNCH();
+    std::vector<double> h((size_t)nb);
+    CK(cudaMemcpyAsync(h.data(), part, nb * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CKS(sync_stream(ctx));
+    CKS(check_dev_err(ctx));
+    double a = 0.0;
+    for (double v : h) a += v;
+    *loss = a / (double)n;
+    return SGL_OK;
+}
+
+sgl_status sgl_mlp_adamw(sgl_ctx* ctx, int64_t n, float* w, const float* g, float* m, float* v, float lr, float b1,
+                         float b2, float eps, float wd, int step) {
+    if (!ctx || n < 0 || step < 1) return SGL_ERR_VALUE;
+    const float c1 = 1.f - std::pow(b1, (float)step), c2 = 1.f - std::pow(b2, (float)step);
+    launch_adamw(n, w, g, m, v, lr, b1, b2, eps, wd, c1, c2, ctx->stream);
+    CKLAUNCH();
+    return SGL_OK;
+}
+
 sgl_status sgl_sweep_set_cells(sgl_ctx* ctx, int64_t n_cells, const double* kap, const double* w) {
     if (!ctx) return SGL_ERR_VALUE;
     if (n_cells < 1 || !kap || !w) return fail(ctx, SGL_ERR_VALUE, "empty cell list");

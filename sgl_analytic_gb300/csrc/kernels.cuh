@@ -145,6 +145,15 @@ void launch_xi_stageA_pack(const XiDevice& x, const long long* d_p_prefix, const
                            const long long* d_chunk_prefix, long long nchunks, const TcGemmDesc* d_descs,
                            float* packed, cudaStream_t st);
 
+// ---- surrogate MLP element-wise kernels
+void launch_bias_act(int M, int N, const float* Z, const float* bias, float* Zb, float* A, int silu, cudaStream_t st);
+void launch_act_grad(int M, int N, const float* dA, const float* Zb, float* dZ, cudaStream_t st);
+void launch_col_sum(int M, int N, const float* X, float* out, cudaStream_t st);
+int mse_blocks(long long n);
+void launch_mse(long long n, const float* pred, const float* tgt, float* dpred, double* part, cudaStream_t st);
+void launch_adamw(long long n, float* w, const float* g, float* m, float* v, float lr, float b1, float b2, float eps,
+                  float wd, float c1, float c2, cudaStream_t st);
+
 // ---- positive (vp) Cox closure
 // Cells sorted per shell into runs (one kind and interval bound; runs ordered linear first, then by
 // the first state they change: lo for left runs, hi + 1 for right runs), per-cell weights (w a, w b).

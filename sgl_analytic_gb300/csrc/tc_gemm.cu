@@ -19,8 +19,14 @@
 // TMEM lanes 32w..32w+31) reads TMEM with tcgen05.ld and stores alpha * C with arbitrary strides.
 // Accumulation is FP32 in TMEM; callers bound its length by splitting K.
 //
+// BF16 mode (NP = 1, BF = true; the surrogate MLP): operands rounded to BF16 and packed in the same
+// byte layout (a 16-byte core-matrix row holds 8 BF16 values, a 64-byte K block 32 of them), one
+// tcgen05.mma.kind::f16 (BF16 inputs, FP32 accumulation) per K-step of 16.
+//
 // Every mbarrier wait is bounded (~2 s); a wait that runs out raises *err, the CTA skips the rest
 // of its work, waits (bounded) for its own MMAs and frees its TMEM before returning.
+#include <cuda_bf16.h>
+
 #include "kernels.cuh"
 
 namespace sgl {
@@ -36,7 +42,7 @@ constexpr int kTcBbytes = kTcBNmax * kTcBK * 4;       // 16 KB per TF32 part (bn
 constexpr long long kTcWaitCycles = 4000000000LL;     // ~2 s at 2 GHz
 
 template <int NP> struct TcCfg {
-    static constexpr int kStages = NP == 2 ? 4 : 3;
+    static constexpr int kStages = NP == 3 ? 3 : 4;
     static constexpr int kStageBytes = NP * (kTcAbytes + kTcBbytes);      // 48 / 72 KB
     static constexpr int kBarOff = kStages * kStageBytes;                  // mbarriers after the ring
     static constexpr int kSmem = kBarOff + 128;
@@ -56,6 +62,17 @@ __device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
 // both K-major (bits 15, 16 = 0), N >> 3 at [17,23), M >> 4 at [24,29)
 __device__ __forceinline__ uint32_t tc_idesc_tf32(int M, int N) {
     return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// instruction descriptor, kind::f16 with BF16 inputs: D f32 = 1, A bf16 [7,10) = 1, B bf16 [10,13) = 1
+__device__ __forceinline__ uint32_t tc_idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+                 :: "r"(tmem_d), "l"(a), "l"(b), "r"(idesc), "r"(acc) : "memory");
 }
 
 __device__ __forceinline__ float tf32_rna(float x) {
@@ -152,6 +169,36 @@ k_tc_pack(const TcPackDesc* __restrict__ descs, int nprob, float* __restrict__ b
         *(float4*)(out + ((long long)NP * kb + pp) * pstride + o) = make_float4(part[pp][0], part[pp][1], part[pp][2], part[pp][3]);
 }
 
+// BF16 packing: one thread per (row, 8 consecutive k) -> one 16-byte core-matrix row (K block = 32)
+__global__ void __launch_bounds__(256)
+k_tc_pack_bf16(const TcPackDesc* __restrict__ descs, int nprob, float* __restrict__ base) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int lo = 0, hi = nprob - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (descs[mid].quad_begin <= t) lo = mid; else hi = mid - 1;
+    }
+    const TcPackDesc d = descs[lo];
+    const long long q = t - d.quad_begin;
+    const long long nq = (long long)d.Rpad * d.nkb * 4;
+    if (q < 0 || q >= nq) return;
+    const int r = (int)(q % d.Rpad);
+    const long long rest = q / d.Rpad;
+    const int c = (int)(rest % 4), kb = (int)(rest / 4);
+    uint32_t w[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const int k = kb * 32 + c * 8 + 2 * e;
+        const float v0 = (r < d.R && k < d.K) ? __ldg(d.X + (long long)r * d.x_rs + (long long)k * d.x_cs) : 0.f;
+        const float v1 = (r < d.R && k + 1 < d.K) ? __ldg(d.X + (long long)r * d.x_rs + (long long)(k + 1) * d.x_cs) : 0.f;
+        const __nv_bfloat162 b2 = __floats2bfloat162_rn(v0, v1);
+        w[e] = *(const uint32_t*)&b2;
+    }
+    unsigned char* out = (unsigned char*)(base + d.out_off);
+    const long long o = (long long)(r >> 3) * 512 + c * 128 + (r & 7) * 16;        // bytes
+    *(uint4*)(out + (long long)kb * d.Rpad * 64 + o) = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
 // ------------------------------------------------------------------ GEMM
 template <int NP>
 __global__ void __launch_bounds__(kTcThreads, 1)
@@ -174,7 +221,8 @@ k_tc_gemm(const TcGemmDesc* __restrict__ descs, int nprob, const float* __restri
     const TcGemmDesc d = descs[lo];
     const int local = tile - d.tile_begin;
     const int i0 = (local / d.tiles_n) * kTcBM, bn = d.bn, j0 = (local % d.tiles_n) * bn;
-    const int nkb = (d.K + kTcBK - 1) / kTcBK;
+    constexpr int KB = NP == 1 ? 2 * kTcBK : kTcBK;      // elements per 64-byte K block
+    const int nkb = (d.K + KB - 1) / KB;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(tslot), "r"(kTcBNmax) : "memory");
@@ -214,11 +262,11 @@ k_tc_gemm(const TcGemmDesc* __restrict__ descs, int nprob, const float* __restri
             }
         }
     } else if (tid == 32 && nkb > 0) {
-        // MMA issuer: part products, larger terms first
-        constexpr int NPROD = NP == 2 ? 3 : 6;
+        // MMA issuer: part products, larger terms first (NP = 1: BF16, one product)
+        constexpr int NPROD = NP == 1 ? 1 : (NP == 2 ? 3 : 6);
         constexpr int PA[6] = {0, 0, 1, 0, 2, 1};
         constexpr int PB[6] = {0, 1, 0, 2, 0, 1};
-        const uint32_t idesc = tc_idesc_tf32(kTcBM, bn);
+        const uint32_t idesc = NP == 1 ? tc_idesc_bf16(kTcBM, bn) : tc_idesc_tf32(kTcBM, bn);
         for (int kb = 0; kb < nkb; ++kb) {
             const int s = kb % S;
             if (*s_fail || !mbar_wait_bounded(bar + 8 * s, (uint32_t)((kb / S) & 1))) { *s_fail = 1; break; }
@@ -228,9 +276,13 @@ k_tc_gemm(const TcGemmDesc* __restrict__ descs, int nprob, const float* __restri
             for (int ks = 0; ks < kTcBK / 8; ++ks) {
                 const uint32_t o = ks * 2 * kTcLBO;
 #pragma unroll
-                for (int t = 0; t < NPROD; ++t)
-                    tc_mma(tmem, tc_desc(a0 + PA[t] * kTcAbytes + o), tc_desc(b0 + PB[t] * kTcBbytes + o), idesc,
-                           (kb | ks | t) ? 1u : 0u);
+                for (int t = 0; t < NPROD; ++t) {
+                    if constexpr (NP == 1)
+                        tc_mma_bf16(tmem, tc_desc(a0 + o), tc_desc(b0 + o), idesc, (kb | ks) ? 1u : 0u);
+                    else
+                        tc_mma(tmem, tc_desc(a0 + PA[t] * kTcAbytes + o), tc_desc(b0 + PB[t] * kTcBbytes + o), idesc,
+                               (kb | ks | t) ? 1u : 0u);
+                }
             }
             tc_commit(bar + 8 * (S + s));
         }
@@ -281,13 +333,15 @@ long long tc_gemm_plan(TcGemmDesc* d, int n, int parts, TcPackDesc* pk, int* til
         g.tiles_n = (g.N + g.bn - 1) / g.bn;
         g.tile_begin = tiles;
         tiles += g.tiles_n * ((g.M + kTcBM - 1) / kTcBM);
-        const int nkb = (g.K + kTcBK - 1) / kTcBK;
+        const int kbe = parts == 1 ? 2 * kTcBK : kTcBK;            // elements per 64-byte K block
+        const int nkb = (g.K + kbe - 1) / kbe;
         g.Mpad = ((g.M + kTcBM - 1) / kTcBM) * kTcBM;
         g.Npad = g.tiles_n * g.bn;
+        const int np = parts == 1 ? 1 : parts;                       // 64-byte rows per K block and part
         g.a_off = off;
-        off += (long long)parts * nkb * g.Mpad * kTcBK;
+        off += (long long)np * nkb * g.Mpad * kTcBK;
         g.b_off = off;
-        off += (long long)parts * nkb * g.Npad * kTcBK;
+        off += (long long)np * nkb * g.Npad * kTcBK;
         // A(i, k) rows = i; B(k, j) is packed as rows j
         TcPackDesc& pa = pk[2 * i];
         pa.X = g.A; pa.x_rs = g.a_rs; pa.x_cs = g.a_cs; pa.R = g.M; pa.K = g.K; pa.Rpad = g.Mpad; pa.nkb = nkb;
@@ -306,7 +360,12 @@ long long tc_gemm_plan(TcGemmDesc* d, int n, int parts, TcPackDesc* pk, int* til
 
 void launch_tc_gemm(int parts, const TcGemmDesc* d_descs, int nprob, int tiles, const TcPackDesc* d_pack,
                     long long quads, float* packed, int* err, cudaStream_t st) {
-    if (parts == 3) {
+    if (parts == 1) {
+        if (quads > 0) { k_tc_pack_bf16<<<ceil_div(quads, 256), 256, 0, st>>>(d_pack, 2 * nprob, packed); SGL_COUNT(1); }
+        cudaFuncSetAttribute(k_tc_gemm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcCfg<1>::kSmem);
+        k_tc_gemm<1><<<tiles, kTcThreads, TcCfg<1>::kSmem, st>>>(d_descs, nprob, packed, err);
+        SGL_COUNT(1);
+    } else if (parts == 3) {
         if (quads > 0) { k_tc_pack<3><<<ceil_div(quads, 256), 256, 0, st>>>(d_pack, 2 * nprob, packed); SGL_COUNT(1); }
         cudaFuncSetAttribute(k_tc_gemm<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcCfg<3>::kSmem);
         k_tc_gemm<3><<<tiles, kTcThreads, TcCfg<3>::kSmem, st>>>(d_descs, nprob, packed, err);

@@ -128,3 +128,32 @@ def test_vp_oracle_mirrored_closure_gives_same_lnR():
     L = VO.lnR(d, kv, qv)
     Lm = VO.lnR(mirrored(d), kv, qv)
     assert np.all(np.abs(L - Lm) <= 1e-14 + 1e-11 * np.abs(L))
+
+
+def test_mlp_gradient_oracle_matches_finite_differences():
+    """The FP64 NumPy back-propagation used to check the GPU gradients, against central differences."""
+    from sgl_analytic_gb300.surrogate import reference_grads
+    rng = np.random.default_rng(1)
+    sizes = [8, 16, 16, 2]
+    W = [rng.standard_normal((a, c)) * 0.5 for a, c in zip(sizes[:-1], sizes[1:])]
+    b = [rng.standard_normal(c) * 0.1 for c in sizes[1:]]
+    X, Y = rng.uniform(-1, 1, (32, 8)), rng.standard_normal((32, 2))
+    _, g = reference_grads(W, b, X, Y)
+    h = 1e-6
+    for l in range(3):
+        for (i, j) in [(0, 0), (1, 1), (2, 1)]:
+            Wp = [w.copy() for w in W]; Wp[l][i, j] += h
+            Wm = [w.copy() for w in W]; Wm[l][i, j] -= h
+            fd = (reference_grads(Wp, b, X, Y)[0] - reference_grads(Wm, b, X, Y)[0]) / (2 * h)
+            assert abs(fd - g[l][0][i, j]) <= 1e-6 * max(1.0, abs(fd))
+
+
+def test_surrogate_targets_round_trip():
+    from sgl_analytic_gb300 import surrogate as S
+    m = S.PlaneModel()
+    kap, w = m.cells(np.array([0.674, 0.315, 0.811, 0.0, -1.0, 0.0]), 0.5)
+    k = np.geomspace(1e-2, 1e6, 40)
+    L = np.array([np.sum(w * (np.expm1(1j * kk * kap) - 1j * kk * kap)) for kk in k])
+    T = S.targets(L)
+    assert np.all(np.abs(np.diff(T[:, 1])) < 1.0)             # no 2 pi wrap of the phase
+    assert np.max(np.abs(S.untarget(T) - L) / np.abs(L)) < 1e-6
