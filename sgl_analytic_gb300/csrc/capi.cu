@@ -4,6 +4,7 @@
 // (sgl_full.py:159-375) for the default gauss chain.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <functional>
 #include <cmath>
 #include <cstdio>
@@ -176,6 +177,21 @@ sgl_status upload(sgl_ctx* ctx, T* dst, const T* src, size_t n) {
     CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
     return SGL_OK;
 }
+
+// host-side phase timing, recorded in the context's statistics as "host_<tag>" while profiling
+struct HostTimer {
+    sgl_ctx* c; std::chrono::steady_clock::time_point t0;
+    explicit HostTimer(sgl_ctx* c_) : c(c_), t0(std::chrono::steady_clock::now()) {}
+    void lap(const char* tag) {
+        const auto t1 = std::chrono::steady_clock::now();
+        if (c->profiling) {
+            StatRow& r = c->stats[std::string("host_") + tag];
+            r.launches += 1;
+            r.ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
+        }
+        t0 = t1;
+    }
+};
 
 // pinned host buffer of at least `bytes` (grow-only; the stream is synchronised before it grows)
 char* big_pinned(sgl_ctx* ctx, size_t bytes) {
@@ -400,6 +416,7 @@ sgl_status gemm_splitk(sgl_ctx* ctx, GemmDesc<T> g, const std::string& tag, int 
 // Restates _sep_gamma_nodes (sgl_full.py:2631-2661) for kg_max = key.
 sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
     if (ctx->sep.key == key && ctx->sep_precision_ready >= 0) return SGL_OK;
+    HostTimer ht(ctx);
     const long long N = (long long)ctx->w0.size();
     const double* fe = ctx->fe_g.data();
     double t[kSepMg];
@@ -422,13 +439,18 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
         sh[(size_t)c] = lo + (double)(j + 1) * wd / (double)ns;
         keyv[(size_t)c] = (long long)b * (kSepSmax + 1) + j;
     }
-    // order: sep cells by (bin, sub-bin) (stable), then direct cells in original order
-    std::vector<long long> order;
-    order.reserve((size_t)N);
-    for (long long c = 0; c < N; ++c) if (!direct[(size_t)c]) order.push_back(c);
-    std::stable_sort(order.begin(), order.end(), [&](long long a, long long b) { return keyv[(size_t)a] < keyv[(size_t)b]; });
-    const long long n_sep = (long long)order.size();
-    for (long long c = 0; c < N; ++c) if (direct[(size_t)c]) order.push_back(c);
+    // order: sep cells by (bin, sub-bin) (stable counting sort over the small key range), then
+    // direct cells in original order
+    long long kmax = -1;
+    for (long long c = 0; c < N; ++c) kmax = std::max(kmax, keyv[(size_t)c]);
+    std::vector<long long> cnt((size_t)(kmax + 2), 0), order((size_t)N);
+    long long n_sep = 0;
+    for (long long c = 0; c < N; ++c) if (!direct[(size_t)c]) { ++cnt[(size_t)keyv[(size_t)c] + 1]; ++n_sep; }
+    for (size_t i = 1; i < cnt.size(); ++i) cnt[i] += cnt[i - 1];
+    for (long long c = 0, d = n_sep; c < N; ++c) {
+        if (direct[(size_t)c]) order[(size_t)d++] = c;
+        else order[(size_t)cnt[(size_t)keyv[(size_t)c]]++] = c;
+    }
     const long long n_dir = N - n_sep;
 
     std::vector<double> kap((size_t)N), w((size_t)N), wl((size_t)N * 8, 0.0), nodes;
@@ -450,14 +472,25 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
             }
         }
         grp[(size_t)i] = ng;
-        const double lo_s = sl[(size_t)c], hi_s = sh[(size_t)c];
-        const double u = ((2.0 * ctx->g0[(size_t)c] - lo_s) - hi_s) / (hi_s - lo_s);
-        for (int a = 0; a < kSepMg; ++a) {
-            double L = 1.0;
-            for (int b2 = 0; b2 < kSepMg; ++b2)
-                if (b2 != a) L = L * ((u - t[b2]) / (t[a] - t[b2]));
-            wl[(size_t)i * 8 + a] = ctx->w0[(size_t)c] * L;
-        }
+    }
+    {   // Lagrange weights of each separable cell at its sub-bin's Chebyshev nodes (threads over cells)
+        const int nthr = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), 16));
+        std::vector<std::thread> th;
+        for (int tix = 0; tix < nthr; ++tix)
+            th.emplace_back([&, tix]() {
+                for (long long i = tix; i < n_sep; i += nthr) {
+                    const long long c = order[(size_t)i];
+                    const double lo_s = sl[(size_t)c], hi_s = sh[(size_t)c];
+                    const double u = ((2.0 * ctx->g0[(size_t)c] - lo_s) - hi_s) / (hi_s - lo_s);
+                    for (int a = 0; a < kSepMg; ++a) {
+                        double L = 1.0;
+                        for (int b2 = 0; b2 < kSepMg; ++b2)
+                            if (b2 != a) L = L * ((u - t[b2]) / (t[a] - t[b2]));
+                        wl[(size_t)i * 8 + a] = ctx->w0[(size_t)c] * L;
+                    }
+                }
+            });
+        for (auto& x : th) x.join();
     }
     const int n_sep_groups = ng + 1;
     const int n_cols_sep = n_sep_groups * kSepMg;
@@ -528,6 +561,7 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
     D.kap = d_kap; D.w = d_w; D.wl = d_wl; D.kap_hi = d_kh; D.kap_lo = d_kl; D.w_f = d_wf; D.wl_f = d_wlf;
     D.grp = d_grp; D.gcol0 = d_gc0; D.gncol = d_gnc; D.chunk_begin = d_cb;
     ctx->sep_precision_ready = 1;
+    ht.lap("sep_plan");
     return SGL_OK;
 }
 
@@ -1151,6 +1185,7 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
             th.emplace_back([&]() { for (int g; (g = next.fetch_add(1)) < n_groups;) fn(g); });
         for (auto& t : th) t.join();
     };
+    HostTimer ht(ctx);
     std::vector<std::vector<double>> norms(n_groups);
     parallel_groups([&](int g) {
         const int w = nidx[g] + 1;
@@ -1172,6 +1207,7 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         for (int e = 0; e < nidx[g]; ++e)
             if (id[e] < 0 || id[e] >= X.n_kmc * ngc) return fail(ctx, SGL_ERR_VALUE, "coarse index out of range");
     }
+    ht.lap("xi_norms");
     // pass 2: keep lists, entry order by p, unique p / q, and every output offset
     struct GPlan {
         std::vector<int> keep, order, pg, qg, qs, qpos;
@@ -1183,18 +1219,29 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
     std::vector<long long> g_p_off, g_ent_off, g_row_off, p_prefix{0}, rowel_off, g_q_off, g_u_off;
     std::vector<int> kept;                      // groups with rows left after pruning
     long long ent_total = 0, row_total = 0, rowel_total = 0, u_total = 0, w0_total = 0, um_total[3] = {0, 0, 0};
-    for (int g = 0; g < n_groups; ++g) {
+    // per-group index work in parallel (keep list, entry order by p, unique q), then the serial
+    // concatenation in group order
+    parallel_groups([&](int g) {
         GPlan& P = plan[g];
         for (int r = 0; r < nrow[g]; ++r)
             if (!(prune > 0) || norms[g][(size_t)r] > prune * s0) P.keep.push_back(r);
-        if (P.keep.empty()) continue;
-        const int R = (int)P.keep.size(), mg = m[g];
+        if (P.keep.empty()) return;
         const int32_t* id = idx + idx_off[g];
         P.pg.resize(nidx[g]); P.qg.resize(nidx[g]);
         for (int e = 0; e < nidx[g]; ++e) { P.pg[e] = id[e] / ngc; P.qg[e] = id[e] % ngc; }
         P.order.resize(nidx[g]);
         for (int e = 0; e < nidx[g]; ++e) P.order[e] = e;
         std::stable_sort(P.order.begin(), P.order.end(), [&](int a, int b) { return P.pg[a] < P.pg[b]; });
+        P.qs.assign(P.qg.begin(), P.qg.end());
+        std::sort(P.qs.begin(), P.qs.end());
+        P.qs.erase(std::unique(P.qs.begin(), P.qs.end()), P.qs.end());
+        P.qpos.assign(X.n_gmc, -1);
+        for (size_t i = 0; i < P.qs.size(); ++i) P.qpos[P.qs[i]] = (int)i;
+    });
+    for (int g = 0; g < n_groups; ++g) {
+        GPlan& P = plan[g];
+        if (P.keep.empty()) continue;
+        const int R = (int)P.keep.size(), mg = m[g];
         for (int i = 0; i < nidx[g]; ++i) {
             const int e = P.order[i];
             if (i == 0 || P.pg[e] != P.pg[P.order[i - 1]]) {
@@ -1205,11 +1252,6 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
             ent_qg.push_back(P.qg[e]);
         }
         p_ptr.push_back((int)(ent_total + nidx[g]));
-        P.qs.assign(P.qg.begin(), P.qg.end());
-        std::sort(P.qs.begin(), P.qs.end());
-        P.qs.erase(std::unique(P.qs.begin(), P.qs.end()), P.qs.end());
-        P.qpos.assign(X.n_gmc, -1);
-        for (size_t i = 0; i < P.qs.size(); ++i) P.qpos[P.qs[i]] = (int)i;
         g_q_off.push_back((long long)idx_q.size());
         g_u_off.push_back(u_total);
         g_nQ.push_back((int)P.qs.size());
@@ -1232,6 +1274,7 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         X.m.push_back(mg); X.r.push_back(R); X.nP.push_back(P.nP);
         kept.push_back(g);
     }
+    ht.lap("xi_plan");
     // pass 3: data, in parallel over groups
     std::vector<double> res((size_t)row_total), sum_rows((size_t)row_total);
     // the transposed rows (FP64 and FP32 copies) are written straight into pinned memory
@@ -1250,13 +1293,20 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         const int R = (int)P.keep.size(), mg = m[g], w = nidx[g] + 1, ne = nidx[g];
         double* rt = rows_t_p + P.rowel0;
         float* rtf = rows_tf_p + P.rowel0;
-        for (int rr = 0; rr < R; ++rr) {                     // rows_t[i][rr] = row_rr[order[i]]
-            const double* row = rows + row_off[g] + (long long)P.keep[rr] * w;
-            for (int i = 0; i < ne; ++i) {
-                const double v = row[P.order[i]];
-                rt[(long long)i * R + rr] = v;
-                rtf[(long long)i * R + rr] = (float)v;
+        // rows_t[i][rr] = row_rr[order[i]], in blocks of entries so the strided writes stay in cache
+        for (int i0 = 0; i0 < ne; i0 += 128) {
+            const int i1 = std::min(ne, i0 + 128);
+            for (int rr = 0; rr < R; ++rr) {
+                const double* row = rows + row_off[g] + (long long)P.keep[rr] * w;
+                for (int i = i0; i < i1; ++i) {
+                    const double v = row[P.order[i]];
+                    rt[(long long)i * R + rr] = v;
+                    rtf[(long long)i * R + rr] = (float)v;
+                }
             }
+        }
+        for (int rr = 0; rr < R; ++rr) {
+            const double* row = rows + row_off[g] + (long long)P.keep[rr] * w;
             double sm = 0.0;
             for (int e = 0; e < ne; ++e) sm += row[e];
             res[(size_t)(P.row0 + rr)] = row[ne];
@@ -1273,6 +1323,7 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
             for (int e = 0; e < ne; ++e) urow[P.qg[e]] += row[e];
         }
     });
+    ht.lap("xi_data");
     double sigma_var = 0.0;
     for (int g : kept) {
         const GPlan& P = plan[g];
@@ -1349,6 +1400,7 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
             CKS(upload(ctx, d_idxq, idx_q.data(), idx_q.size()));
             CKS(upload(ctx, d_U0, U0.data(), U0.size()));
             CK(cudaStreamSynchronize(ctx->stream));   // host vectors are local
+            ht.lap("xi_upload");
             D.rows_f = d_rowsf; D.g_nQ = d_gnQ; D.g_q_off = d_qoff; D.g_u_off = d_uoff; D.idx_q = d_idxq; D.U0 = d_U0;
             D.r_max = *std::max_element(g_r.begin(), g_r.end());
         }
