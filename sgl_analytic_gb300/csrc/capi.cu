@@ -768,12 +768,12 @@ void unwrap_line(double* p, int n, long long stride) {
     }
 }
 
-// ln R on kv x qv into device planes (tables, z buffer from the arena; rows in passes of <= 2 GiB z)
+// ln R on kv x qv into device planes (tables, z buffer from the arena; rows in passes of <= 8 GiB z)
 sgl_status vp_lnR_device(sgl_ctx* ctx, int precision, const double* d_kv, int nk, const double* d_qv, int nq,
                          double* d_re, double* d_im) {
     const VpDevice& D = ctx->vpd;
     void* tables = ctx->arena.get("vp_tables", vp_table_bytes(precision, D.U, nk, nq));
-    const int rows = vp_rows_per_pass(D.nsh, nk, nq, (size_t)2 << 30);
+    const int rows = vp_rows_per_pass(D.nsh, nk, nq, (size_t)8 << 30);
     void* zb = ctx->arena.get("vp_z", (size_t)D.nsh * 49 * 16 * (size_t)rows * nq);
     if (!tables || !zb) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (vp)");
     const double pts = (double)nk * nq;

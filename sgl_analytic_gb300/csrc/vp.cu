@@ -32,7 +32,7 @@ constexpr int kVpNS = 48;                 // latent states (Gauss-Hermite nodes)
 constexpr int kZK = 16, kZQ = 32;         // phase-1 point tile (k x q)
 constexpr int kZThreads = 128;            // 2 x 2 points per thread
 constexpr int kZCh = 32;                  // cells per staged chunk
-constexpr int kChPts = 64;                // phase-2 points per CTA
+constexpr int kChPts = 56;                // phase-2 points per CTA (2 CTAs per SM with K staged)
 
 template <typename TT> struct V2;
 template <> struct V2<float> { using T = float2; };
@@ -208,11 +208,19 @@ k_vp_chain(VpDevice d, const double2* __restrict__ zp, const double2* __restrict
     double (*ai)[kChPts] = (double (*)[kChPts])(vsm + 1 * kVpNS * kChPts * 8);
     double (*br)[kChPts] = (double (*)[kChPts])(vsm + 2 * kVpNS * kChPts * 8);   // z, then alpha'
     double (*bi)[kChPts] = (double (*)[kChPts])(vsm + 3 * kVpNS * kChPts * 8);
+    double* sK = (double*)(vsm + 4 * kVpNS * kChPts * 8);                    // K[s-1], 48 x 48
     const int t = threadIdx.x;
     const long long p = (long long)blockIdx.x * kChPts + t;
-    if (p >= NP) return;                       // each thread touches only its own column
+    const bool live = p < NP;                  // dead threads only help stage K
     double scale = 0.0;
     for (int s = 0; s < d.nsh; ++s) {
+        if (s > 0) {
+            __syncthreads();
+            const double* Ks = d.K + (long long)(s - 1) * kVpNS * kVpNS;
+            for (int e = t; e < kVpNS * kVpNS; e += kChPts) sK[e] = Ks[e];
+            __syncthreads();
+        }
+        if (!live) continue;
         const double2 al = alin[(long long)s * NP + p];
         double mr = 0.0, mi = 0.0;
         for (int j = 0; j < kVpNS; ++j) {
@@ -229,7 +237,6 @@ k_vp_chain(VpDevice d, const double2* __restrict__ zp, const double2* __restrict
             mx = fmax(mx, zr);
         }
         double nrm = 0.0;
-        const double* Ks = d.K + (long long)(s > 0 ? s - 1 : 0) * kVpNS * kVpNS;
         for (int j0 = 0; j0 < kVpNS; j0 += 4) {
             double gr[4], gi[4];
             if (s == 0) {
@@ -238,10 +245,11 @@ k_vp_chain(VpDevice d, const double2* __restrict__ zp, const double2* __restrict
             } else {
 #pragma unroll
                 for (int q = 0; q < 4; ++q) { gr[q] = 0.0; gi[q] = 0.0; }
+#pragma unroll 4
                 for (int i = 0; i < kVpNS; ++i) {
                     const double xr = ar[i][t], xi = ai[i][t];
-                    const double2 k01 = *(const double2*)(Ks + i * kVpNS + j0);
-                    const double2 k23 = *(const double2*)(Ks + i * kVpNS + j0 + 2);
+                    const double2 k01 = *(const double2*)(sK + i * kVpNS + j0);
+                    const double2 k23 = *(const double2*)(sK + i * kVpNS + j0 + 2);
                     gr[0] = fma(k01.x, xr, gr[0]); gi[0] = fma(k01.x, xi, gi[0]);
                     gr[1] = fma(k01.y, xr, gr[1]); gi[1] = fma(k01.y, xi, gi[1]);
                     gr[2] = fma(k23.x, xr, gr[2]); gi[2] = fma(k23.x, xi, gi[2]);
@@ -265,6 +273,7 @@ k_vp_chain(VpDevice d, const double2* __restrict__ zp, const double2* __restrict
         for (int j = 0; j < kVpNS; ++j) { ar[j][t] = br[j][t] * inv; ai[j][t] = bi[j][t] * inv; }
         scale += mx + log(nrm);
     }
+    if (!live) return;
     double sr = 0.0, si = 0.0;
     for (int j = 0; j < kVpNS; ++j) { sr += ar[j][t]; si += ai[j][t]; }
     const long long o = (long long)kb * nq + p;
@@ -282,7 +291,8 @@ int vp_rows_per_pass(int nsh, int nk, int nq, size_t z_cap_bytes) {
     long long rows = (long long)(z_cap_bytes / (per_row > 0 ? per_row : 1));
     if (rows < 1) rows = 1;
     if (rows > nk) rows = nk;
-    return (int)rows;
+    const long long passes = (nk + rows - 1) / rows;            // balanced passes (no thin last pass)
+    return (int)((nk + passes - 1) / passes);
 }
 
 void launch_vp_lnR(int precision, const VpDevice& d, const double* kv, int nk, const double* qv, int nq, void* tables,
@@ -298,7 +308,7 @@ void launch_vp_lnR(int precision, const VpDevice& d, const double* kv, int nk, c
         k_vp_tables<float><<<ceil_div(tot, 256), 256, 0, st>>>(d.ku, d.gu, d.U, kv, nk, qv, nq, (float2*)e, (float2*)Jt);
         SGL_COUNT(1);
     }
-    const size_t chain_smem = 4 * (size_t)kVpNS * kChPts * sizeof(double);
+    const size_t chain_smem = (4 * (size_t)kVpNS * kChPts + (size_t)kVpNS * kVpNS) * sizeof(double);
     cudaFuncSetAttribute(k_vp_chain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chain_smem);
     for (int kb = 0; kb < nk; kb += rows_per_pass) {
         const int nkc = nk - kb < rows_per_pass ? nk - kb : rows_per_pass;
