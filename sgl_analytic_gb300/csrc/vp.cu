@@ -70,15 +70,30 @@ __device__ __forceinline__ void ff_acc(float& hi, float& lo, float p) {
     lo += err;
 }
 
+// asynchronous global -> shared copies (zero-filled when !pred; the source address is then unused)
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem, bool pred) {
+    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+    const int n = pred ? BYTES : 0;
+    if constexpr (BYTES == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" :: "r"(sa), "l"(gmem), "r"(n) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" :: "r"(sa), "l"(gmem), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" :: "n"(N) : "memory"); }
+
 template <typename TT>
 __global__ void __launch_bounds__(kZThreads)
 k_vp_z(VpDevice d, const typename V2<TT>::T* __restrict__ e, const typename V2<TT>::T* __restrict__ Jt, int nk,
        int nq, int kb, int nkc, double2* __restrict__ zp, double2* __restrict__ alin, long long NP) {
     using T2 = typename V2<TT>::T;
-    __shared__ T2 s_e[kZCh][kZK];
-    __shared__ T2 s_J[kZCh][kZQ];
-    __shared__ T2 s_w[kZCh];
+    __shared__ __align__(16) T2 s_e[2][kZCh][kZK];
+    __shared__ __align__(16) T2 s_J[2][kZCh][kZQ];
+    __shared__ __align__(16) T2 s_w[2][kZCh];
     constexpr bool MIX = sizeof(TT) == 4;
+    constexpr int EB = (int)sizeof(T2);
     const int s = blockIdx.z;
     const int q0 = blockIdx.x * kZQ, k0 = kb + blockIdx.y * kZK, kend = kb + nkc;
     const int t = threadIdx.x, tq = t % 16, tk = t / 16;
@@ -104,7 +119,30 @@ k_vp_z(VpDevice d, const typename V2<TT>::T* __restrict__ e, const typename V2<T
                 if (live[P]) row[pidx[P]] = make_double2(fma(uj, SAr[P], SBr[P]), fma(uj, SAi[P], SBi[P]));
         }
     };
+    // chunks of <= 32 cells never straddle a run; the next chunk is copied (cp.async) into the other
+    // buffer while the current one is summed
+    auto issue = [&](int buf, long long base, long long c1) {
+        const int cnt = (int)((c1 - base) < kZCh ? (c1 - base) : kZCh);
+        for (int idx = t; idx < kZCh * kZK; idx += kZThreads) {
+            const int c = idx / kZK, rr = idx % kZK, k = k0 + rr;
+            const bool ok = c < cnt && k < kend;
+            cp_async<EB>(&s_e[buf][c][rr], ok ? (const void*)(e + (long long)d.cu[base + c] * nk + k) : (const void*)e, ok);
+        }
+        for (int idx = t; idx < kZCh * kZQ; idx += kZThreads) {
+            const int c = idx / kZQ, rr = idx % kZQ, q = q0 + rr;
+            const bool ok = c < cnt && q < nq;
+            cp_async<EB>(&s_J[buf][c][rr], ok ? (const void*)(Jt + (long long)d.cu[base + c] * nq + q) : (const void*)Jt, ok);
+        }
+        if (t < kZCh) {
+            const bool ok = t < cnt;
+            if constexpr (MIX) cp_async<EB>(&s_w[buf][t], ok ? (const void*)(d.wabf + base + t) : (const void*)d.wabf, ok);
+            else cp_async<EB>(&s_w[buf][t], ok ? (const void*)(d.wab + base + t) : (const void*)d.wab, ok);
+        }
+        cp_async_commit();
+    };
     const int r0 = d.sh_run[s], r1 = d.sh_run[s + 1];
+    int buf = 0;
+    if (r0 < r1) issue(0, d.run_cell[r0], d.run_cell[r0 + 1]);
     for (int r = r0; r < r1; ++r) {
         const long long c0 = d.run_cell[r], c1 = d.run_cell[r + 1];
         // run totals: mixed = float-float (hi, lo), FP64 = plain
@@ -115,26 +153,15 @@ k_vp_z(VpDevice d, const typename V2<TT>::T* __restrict__ e, const typename V2<T
             for (int v = 0; v < 4; ++v) { hi[P][v] = TT(0); lo[P][v] = TT(0); }
         for (long long base = c0; base < c1; base += kZCh) {
             const int cnt = (int)((c1 - base) < kZCh ? (c1 - base) : kZCh);
-            __syncthreads();
-            for (int idx = t; idx < kZCh * kZK; idx += kZThreads) {
-                const int c = idx / kZK, rr = idx % kZK, k = k0 + rr;
-                T2 v; v.x = TT(0); v.y = TT(0);
-                if (c < cnt && k < kend) v = e[(long long)d.cu[base + c] * nk + k];
-                s_e[c][rr] = v;
-            }
-            for (int idx = t; idx < kZCh * kZQ; idx += kZThreads) {
-                const int c = idx / kZQ, rr = idx % kZQ, q = q0 + rr;
-                T2 v; v.x = TT(0); v.y = TT(0);
-                if (c < cnt && q < nq) v = Jt[(long long)d.cu[base + c] * nq + q];
-                s_J[c][rr] = v;
-            }
-            if (t < kZCh) {
-                T2 v; v.x = TT(0); v.y = TT(0);
-                if (t < cnt) {
-                    if constexpr (MIX) { const float2 f = d.wabf[base + t]; v.x = f.x; v.y = f.y; }
-                    else { const double2 f = d.wab[base + t]; v.x = f.x; v.y = f.y; }
-                }
-                s_w[t] = v;
+            // prefetch the next chunk (this run's, or the next run's first)
+            const long long nb = base + kZCh;
+            const bool has_next = nb < c1 || r + 1 < r1;
+            if (has_next) {
+                if (nb < c1) issue(buf ^ 1, nb, c1);
+                else issue(buf ^ 1, d.run_cell[r + 1], d.run_cell[r + 2]);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
             }
             __syncthreads();
             TT p[4][4];
@@ -143,9 +170,9 @@ k_vp_z(VpDevice d, const typename V2<TT>::T* __restrict__ e, const typename V2<T
 #pragma unroll
                 for (int v = 0; v < 4; ++v) p[P][v] = TT(0);
             for (int c = 0; c < cnt; ++c) {
-                const T2 wv = s_w[c];
-                const T2 ev[2] = {s_e[c][tk], s_e[c][tk + 8]};
-                const T2 jv[2] = {s_J[c][tq], s_J[c][tq + 16]};
+                const T2 wv = s_w[buf][c];
+                const T2 ev[2] = {s_e[buf][c][tk], s_e[buf][c][tk + 8]};
+                const T2 jv[2] = {s_J[buf][c][tq], s_J[buf][c][tq + 16]};
 #pragma unroll
                 for (int P = 0; P < 4; ++P) {
                     const T2 ee = ev[P >> 1], jj = jv[P & 1];
@@ -162,6 +189,8 @@ k_vp_z(VpDevice d, const typename V2<TT>::T* __restrict__ e, const typename V2<T
                     if constexpr (MIX) ff_acc(hi[P][v], lo[P][v], p[P][v]);
                     else hi[P][v] += p[P][v];
                 }
+            __syncthreads();                  // buffer `buf` is refilled by the next prefetch
+            buf ^= 1;
         }
         const int kind = d.run_kind[r], bound = d.run_bound[r];
         if (kind == 0) {                                   // linear: u_j A (intercept dropped)
