@@ -1305,22 +1305,35 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
                 }
             }
         }
+        // one pass per kept row for its sums and the 1-D reach / compensation stacks (the same
+        // per-output summation order as separate passes)
         for (int rr = 0; rr < R; ++rr) {
             const double* row = rows + row_off[g] + (long long)P.keep[rr] * w;
+            double* urow = U[mg].data() + P.um0 + (long long)rr * X.n_gmc;
             double sm = 0.0;
-            for (int e = 0; e < ne; ++e) sm += row[e];
-            res[(size_t)(P.row0 + rr)] = row[ne];
-            sum_rows[(size_t)(P.row0 + rr)] = sm;
             if (mg == 0) {
                 double* wrow = W0.data() + P.w0 + (long long)rr * X.n_kmc;
-                double dot = 0.0;
-                for (int e = 0; e < ne; ++e) { wrow[P.pg[e]] += row[e]; dot += row[e] * X.kmc[P.pg[e]]; }
-                sig_v[(size_t)(P.row0 + rr)] = dot + row[ne];
                 double* u0 = U0.data() + P.u0 + (long long)rr * P.qs.size();
-                for (int e = 0; e < ne; ++e) u0[P.qpos[P.qg[e]]] += row[e];
+                double dot = 0.0;
+                for (int e = 0; e < ne; ++e) {
+                    const double v = row[e];
+                    const int pe = P.pg[e], qe = P.qg[e];
+                    sm += v;
+                    wrow[pe] += v;
+                    dot += v * X.kmc[pe];
+                    u0[P.qpos[qe]] += v;
+                    urow[qe] += v;
+                }
+                sig_v[(size_t)(P.row0 + rr)] = dot + row[ne];
+            } else {
+                for (int e = 0; e < ne; ++e) {
+                    const double v = row[e];
+                    sm += v;
+                    urow[P.qg[e]] += v;
+                }
             }
-            double* urow = U[mg].data() + P.um0 + (long long)rr * X.n_gmc;
-            for (int e = 0; e < ne; ++e) urow[P.qg[e]] += row[e];
+            res[(size_t)(P.row0 + rr)] = row[ne];
+            sum_rows[(size_t)(P.row0 + rr)] = sm;
         }
     });
     ht.lap("xi_data");
