@@ -105,6 +105,7 @@ struct sgl_ctx {
     int vp_xi_coarse = 101, vp_xi_coarse_k = 0;   // coarse grid (gamma, kappa); grown by sgl_pdf's rule
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     int* dev_err = nullptr;          // raised by kernels whose bounded waits ran out
+    bool coherent_host = false;      // the GPU reads pageable host memory through the host page tables
     // pinned staging ring for small uploads (pageable copies would serialise host and device);
     // reset whenever the stream has been synchronised
     char* pinned = nullptr;
@@ -1045,6 +1046,13 @@ sgl_status sgl_ctx_create(int device, sgl_ctx** out) {
         g_create_error = "stream creation failed"; delete ctx; return SGL_ERR_CUDA;
     }
     for (auto& ev : ctx->ev) cudaEventCreate(&ev);
+    {
+        int pa = 0, pt = 0;
+        cudaDeviceGetAttribute(&pa, cudaDevAttrPageableMemoryAccess, device);
+        cudaDeviceGetAttribute(&pt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
+        ctx->coherent_host = pa == 1 && pt == 1;
+        cudaGetLastError();
+    }
     ctx->pinned_cap = 16u << 20;
     if (cudaHostAlloc((void**)&ctx->pinned, ctx->pinned_cap, cudaHostAllocDefault) != cudaSuccess) {
         ctx->pinned = nullptr; ctx->pinned_cap = 0;
@@ -1186,17 +1194,38 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         for (auto& t : th) t.join();
     };
     HostTimer ht(ctx);
+    // coherent access: the GPU reads the caller's rows in place (norms here, the data in pass 3)
+    const bool coherent = ctx->coherent_host && !std::getenv("SGL_XI_HOST_PREP");
     std::vector<std::vector<double>> norms(n_groups);
-    parallel_groups([&](int g) {
-        const int w = nidx[g] + 1;
-        norms[g].resize(nrow[g]);
-        for (int r = 0; r < nrow[g]; ++r) {
-            double s = 0.0;
-            const double* row = rows + row_off[g] + (long long)r * w;
-            for (int e = 0; e < w; ++e) s += row[e] * row[e];
-            norms[g][r] = std::sqrt(s);
-        }
-    });
+    if (coherent) {
+        std::vector<long long> rs;
+        std::vector<int> rl;
+        for (int g = 0; g < n_groups; ++g)
+            for (int r = 0; r < nrow[g]; ++r) { rs.push_back(row_off[g] + (long long)r * (nidx[g] + 1)); rl.push_back(nidx[g] + 1); }
+        const int nr = (int)rs.size();
+        DBUF(d_rs, long long, "xi_prep_rs", std::max(1, nr));
+        DBUF(d_rl, int, "xi_prep_rl", std::max(1, nr));
+        DBUF(d_nrm, double, "xi_prep_norm", std::max(1, nr));
+        CKS(upload(ctx, d_rs, rs.data(), rs.size()));
+        CKS(upload(ctx, d_rl, rl.data(), rl.size()));
+        launch_xi_row_norms(rows, d_rs, d_rl, nr, d_nrm, ctx->stream);
+        CKLAUNCH();
+        std::vector<double> hn((size_t)std::max(1, nr));
+        CK(cudaMemcpyAsync(hn.data(), d_nrm, (size_t)nr * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        CKS(sync_stream(ctx));
+        for (int g = 0, k = 0; g < n_groups; ++g) norms[g].assign(hn.begin() + k, hn.begin() + k + nrow[g]), k += nrow[g];
+    } else {
+        parallel_groups([&](int g) {
+            const int w = nidx[g] + 1;
+            norms[g].resize(nrow[g]);
+            for (int r = 0; r < nrow[g]; ++r) {
+                double s = 0.0;
+                const double* row = rows + row_off[g] + (long long)r * w;
+                for (int e = 0; e < w; ++e) s += row[e] * row[e];
+                norms[g][r] = std::sqrt(s);
+            }
+        });
+    }
     double s0 = 0.0;
     for (int g = 0; g < n_groups; ++g)
         for (double v : norms[g]) s0 = std::max(s0, v);
@@ -1210,8 +1239,8 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
     ht.lap("xi_norms");
     // pass 2: keep lists, entry order by p, unique p / q, and every output offset
     struct GPlan {
-        std::vector<int> keep, order, pg, qg, qs, qpos;
-        int nP = 0;
+        std::vector<int> keep, order, pg, qg, qs, qpos, inv, qord, qseg;
+        int nP = 0, q0 = 0, qseg0 = 0, p0 = 0;
         long long ent0 = 0, rowel0 = 0, row0 = 0, u0 = 0, w0 = 0, um0 = 0;
     };
     std::vector<GPlan> plan(n_groups);
@@ -1229,14 +1258,30 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         const int32_t* id = idx + idx_off[g];
         P.pg.resize(nidx[g]); P.qg.resize(nidx[g]);
         for (int e = 0; e < nidx[g]; ++e) { P.pg[e] = id[e] / ngc; P.qg[e] = id[e] % ngc; }
-        P.order.resize(nidx[g]);
-        for (int e = 0; e < nidx[g]; ++e) P.order[e] = e;
-        std::stable_sort(P.order.begin(), P.order.end(), [&](int a, int b) { return P.pg[a] < P.pg[b]; });
-        P.qs.assign(P.qg.begin(), P.qg.end());
-        std::sort(P.qs.begin(), P.qs.end());
-        P.qs.erase(std::unique(P.qs.begin(), P.qs.end()), P.qs.end());
+        // entries by kappa cell (stable counting sort) and the sorted unique gamma cells
+        {
+            std::vector<int> cnt(X.n_kmc + 1, 0);
+            for (int e = 0; e < nidx[g]; ++e) ++cnt[P.pg[e] + 1];
+            for (int i = 1; i <= X.n_kmc; ++i) cnt[i] += cnt[i - 1];
+            P.order.resize(nidx[g]);
+            for (int e = 0; e < nidx[g]; ++e) P.order[cnt[P.pg[e]]++] = e;
+        }
         P.qpos.assign(X.n_gmc, -1);
-        for (size_t i = 0; i < P.qs.size(); ++i) P.qpos[P.qs[i]] = (int)i;
+        for (int e = 0; e < nidx[g]; ++e) P.qpos[P.qg[e]] = 0;
+        P.qs.clear();
+        for (int q = 0; q < X.n_gmc; ++q)
+            if (P.qpos[q] == 0) { P.qpos[q] = (int)P.qs.size(); P.qs.push_back(q); }
+        if (coherent) {
+            const int ne = nidx[g];
+            P.inv.resize(ne);
+            for (int i = 0; i < ne; ++i) P.inv[P.order[i]] = i;
+            P.qseg.assign(P.qs.size() + 1, 0);
+            for (int e = 0; e < ne; ++e) ++P.qseg[P.qpos[P.qg[e]] + 1];
+            for (size_t i = 1; i < P.qseg.size(); ++i) P.qseg[i] += P.qseg[i - 1];
+            std::vector<int> fill(P.qseg.begin(), P.qseg.end() - 1);
+            P.qord.resize(ne);
+            for (int e = 0; e < ne; ++e) P.qord[fill[P.qpos[P.qg[e]]]++] = e;     // stable by q
+        }
     });
     for (int g = 0; g < n_groups; ++g) {
         GPlan& P = plan[g];
@@ -1252,6 +1297,8 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
             ent_qg.push_back(P.qg[e]);
         }
         p_ptr.push_back((int)(ent_total + nidx[g]));
+        P.q0 = (int)idx_q.size();
+        P.p0 = (int)p_prefix.back();
         g_q_off.push_back((long long)idx_q.size());
         g_u_off.push_back(u_total);
         g_nQ.push_back((int)P.qs.size());
@@ -1275,18 +1322,98 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         kept.push_back(g);
     }
     ht.lap("xi_plan");
-    // pass 3: data, in parallel over groups
+    // pass 3: data, in parallel over groups (host) or on the GPU from the caller's rows (coherent)
     std::vector<double> res((size_t)row_total), sum_rows((size_t)row_total);
+    const long long ubase[3] = {0, um_total[0], um_total[0] + um_total[1]};
+    bool dev_filled = false;                   // rows_t, sums, U, U0, W0 already on the device
+    double* d_Uall_p = nullptr;
+    std::vector<double> sig_v;                 // (rows . kc + res) per m = 0 row
+    std::vector<double> U0, W0, res0, sum0;
+    std::vector<double> U[3], resm[3], summ[3];
+    double* rows_t_p = nullptr;
+    float* rows_tf_p = nullptr;
+    if (coherent && !kept.empty()) {
+        std::vector<XiPrepRow> kr;
+        std::vector<int> inv_all((size_t)ent_total), qord_all((size_t)ent_total), pord_all((size_t)ent_total), qseg_all;
+        int ne_max = 0;
+        for (int g : kept) {
+            GPlan& P = plan[g];
+            const int R = (int)P.keep.size(), ne = nidx[g], w = nidx[g] + 1;
+            std::copy(P.inv.begin(), P.inv.end(), inv_all.begin() + P.ent0);
+            std::copy(P.qord.begin(), P.qord.end(), qord_all.begin() + P.ent0);
+            std::copy(P.order.begin(), P.order.end(), pord_all.begin() + P.ent0);
+            P.qseg0 = (int)qseg_all.size();
+            qseg_all.insert(qseg_all.end(), P.qseg.begin(), P.qseg.end());
+            ne_max = std::max(ne_max, ne);
+            for (int rr = 0; rr < R; ++rr) {
+                XiPrepRow k{};
+                k.src = row_off[g] + (long long)P.keep[rr] * w;
+                k.dst = P.rowel0 + rr;
+                k.ent0 = P.ent0;
+                k.u_off = ubase[m[g]] + P.um0 + (long long)rr * X.n_gmc;
+                k.u0_off = P.u0 + (long long)rr * P.qs.size();
+                k.w0_off = P.w0 + (long long)rr * X.n_kmc;
+                k.ne = ne; k.R = R; k.row = (int)(P.row0 + rr); k.m = m[g];
+                k.nQ = (int)P.qs.size(); k.q0 = P.q0; k.qseg0 = P.qseg0;
+                k.nP = P.nP; k.p0 = P.p0;
+                kr.push_back(k);
+            }
+        }
+        if (((size_t)ne_max + 1) * 8 <= 200 * 1024) {
+            DBUF(d_kr, XiPrepRow, "xi_prep_rows", kr.size());
+            DBUF(d_inv, int, "xi_prep_inv", std::max<long long>(1, ent_total));
+            DBUF(d_qord, int, "xi_prep_qord", std::max<long long>(1, ent_total));
+            DBUF(d_pord, int, "xi_prep_pord", std::max<long long>(1, ent_total));
+            DBUF(d_qseg, int, "xi_prep_qseg", std::max<size_t>(1, qseg_all.size()));
+            DBUF(d_pptr0, int, "xi_pptr", p_ptr.size());
+            DBUF(d_idxp0, int, "xi_idxp", idx_p.size());
+            DBUF(d_idxq0, int, "xi_idxq", idx_q.size());
+            DBUF(d_kmc0, double, "xi_kmc", X.n_kmc);
+            DBUF(d_rows0, double, "xi_rows", rowel_total);
+            DBUF(d_rowsf0, float, "xi_rows_f", rowel_total);
+            DBUF(d_res0, double, "xi_res", row_total);
+            DBUF(d_sum0, double, "xi_sum", row_total);
+            DBUF(d_sig0, double, "xi_prep_sig", std::max<long long>(1, row_total));
+            DBUF(d_U0x, double, "xi_Usum", std::max<long long>(1, u_total));
+            DBUF(d_W0x, double, "xi_W0", std::max<long long>(1, w0_total));
+            DBUF(d_Uall, double, "xi_Uall", std::max<long long>(1, ubase[2] + um_total[2]));
+            CKS(upload(ctx, d_kr, kr.data(), kr.size()));
+            CKS(upload(ctx, d_inv, inv_all.data(), inv_all.size()));
+            CKS(upload(ctx, d_qord, qord_all.data(), qord_all.size()));
+            CKS(upload(ctx, d_pord, pord_all.data(), pord_all.size()));
+            CKS(upload(ctx, d_qseg, qseg_all.data(), qseg_all.size()));
+            CKS(upload(ctx, d_pptr0, p_ptr.data(), p_ptr.size()));
+            CKS(upload(ctx, d_idxp0, idx_p.data(), idx_p.size()));
+            CKS(upload(ctx, d_idxq0, idx_q.data(), idx_q.size()));
+            CKS(upload(ctx, d_kmc0, X.kmc.data(), X.kmc.size()));
+            CK(cudaMemsetAsync(d_U0x, 0, (size_t)std::max<long long>(1, u_total) * 8, ctx->stream));
+            CK(cudaMemsetAsync(d_W0x, 0, (size_t)std::max<long long>(1, w0_total) * 8, ctx->stream));
+            CK(cudaMemsetAsync(d_Uall, 0, (size_t)std::max<long long>(1, ubase[2] + um_total[2]) * 8, ctx->stream));
+            XiPrepIdx ix{d_inv, d_qord, d_qseg, d_pord, d_pptr0, d_idxp0, d_idxq0};
+            XiPrepOut xo{d_rows0, d_rowsf0, d_res0, d_sum0, d_sig0, d_Uall, d_U0x, d_W0x};
+            launch_xi_rowprep(rows, d_kr, (int)kr.size(), ne_max, ix, d_kmc0, xo, ctx->stream);
+            CKLAUNCH();
+            sig_v.assign((size_t)row_total, 0.0);
+            CK(cudaMemcpyAsync(res.data(), d_res0, (size_t)row_total * 8, cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaMemcpyAsync(sum_rows.data(), d_sum0, (size_t)row_total * 8, cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaMemcpyAsync(sig_v.data(), d_sig0, (size_t)row_total * 8, cudaMemcpyDeviceToHost, ctx->stream));
+            CKS(sync_stream(ctx));
+            ht.lap("xi_data_gpu");
+            dev_filled = true;
+            d_Uall_p = d_Uall;
+        }
+    }
+    if (!dev_filled) {
     // the transposed rows (FP64 and FP32 copies) are written straight into pinned memory
     CKS(sync_stream(ctx));
     char* bp = big_pinned(ctx, (size_t)rowel_total * 12 + 256);
     if (!bp) return fail(ctx, SGL_ERR_CUDA, "pinned host allocation failed (xi rows)");
-    double* rows_t_p = (double*)bp;
-    float* rows_tf_p = (float*)(bp + ((size_t)rowel_total * 8 + 255) / 256 * 256);
-    std::vector<double> U0((size_t)u_total, 0.0), W0((size_t)w0_total, 0.0), res0, sum0;
-    std::vector<double> U[3], resm[3], summ[3];
+    rows_t_p = (double*)bp;
+    rows_tf_p = (float*)(bp + ((size_t)rowel_total * 8 + 255) / 256 * 256);
+    U0.assign((size_t)u_total, 0.0);
+    W0.assign((size_t)w0_total, 0.0);
     for (int k = 0; k < 3; ++k) U[k].assign((size_t)um_total[k], 0.0);
-    std::vector<double> sig_v((size_t)row_total, 0.0);     // (rows . kc + res) per m = 0 row
+    sig_v.assign((size_t)row_total, 0.0);
     parallel_groups([&](int g) {
         const GPlan& P = plan[g];
         if (P.keep.empty()) return;
@@ -1337,6 +1464,7 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         }
     });
     ht.lap("xi_data");
+    }
     double sigma_var = 0.0;
     for (int g : kept) {
         const GPlan& P = plan[g];
@@ -1391,27 +1519,29 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         CKS(upload(ctx, d_idxp, idx_p.data(), idx_p.size()));
         CKS(upload(ctx, d_pptr, p_ptr.data(), p_ptr.size()));
         CKS(upload(ctx, d_qg, ent_qg.data(), ent_qg.size()));
-        if (rowel_total > 0)
-            CK(cudaMemcpyAsync(d_rows, rows_t_p, (size_t)rowel_total * 8, cudaMemcpyHostToDevice, ctx->stream));
-        CKS(upload(ctx, d_res, res.data(), res.size()));
-        CKS(upload(ctx, d_sum, sum_rows.data(), sum_rows.size()));
+        if (!dev_filled) {
+            if (rowel_total > 0)
+                CK(cudaMemcpyAsync(d_rows, rows_t_p, (size_t)rowel_total * 8, cudaMemcpyHostToDevice, ctx->stream));
+            CKS(upload(ctx, d_res, res.data(), res.size()));
+            CKS(upload(ctx, d_sum, sum_rows.data(), sum_rows.size()));
+        }
         D.g_m = d_gm; D.g_r = d_gr; D.g_nP = d_gnP;
         D.g_p_off = d_goff; D.g_ent_off = d_goff + X.n_groups; D.g_row_off = d_goff + 2 * X.n_groups;
         D.idx_p = d_idxp; D.p_ptr = d_pptr; D.ent_qg = d_qg; D.rows = d_rows; D.res = d_res; D.sum_rows = d_sum;
         {
             DBUF(d_rowsf, float, "xi_rows_f", rowel_total);
-            if (rowel_total > 0)
+            if (rowel_total > 0 && !dev_filled)
                 CK(cudaMemcpyAsync(d_rowsf, rows_tf_p, (size_t)rowel_total * 4, cudaMemcpyHostToDevice, ctx->stream));
             DBUF(d_gnQ, int, "xi_gnQ", g_nQ.size());
             DBUF(d_qoff, long long, "xi_qoff", g_q_off.size());
             DBUF(d_uoff, long long, "xi_uoff", g_u_off.size());
             DBUF(d_idxq, int, "xi_idxq", idx_q.size());
-            DBUF(d_U0, double, "xi_Usum", U0.size());
+            DBUF(d_U0, double, "xi_Usum", std::max<long long>(1, u_total));
             CKS(upload(ctx, d_gnQ, g_nQ.data(), g_nQ.size()));
             CKS(upload(ctx, d_qoff, g_q_off.data(), g_q_off.size()));
             CKS(upload(ctx, d_uoff, g_u_off.data(), g_u_off.size()));
             CKS(upload(ctx, d_idxq, idx_q.data(), idx_q.size()));
-            CKS(upload(ctx, d_U0, U0.data(), U0.size()));
+            if (!dev_filled) CKS(upload(ctx, d_U0, U0.data(), U0.size()));
             CK(cudaStreamSynchronize(ctx->stream));   // host vectors are local
             ht.lap("xi_upload");
             D.rows_f = d_rowsf; D.g_nQ = d_gnQ; D.g_q_off = d_qoff; D.g_u_off = d_uoff; D.idx_q = d_idxq; D.U0 = d_U0;
@@ -1419,10 +1549,10 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         }
         D.R0 = X.R0;
         if (X.R0 > 0) {
-            DBUF(d_W0, double, "xi_W0", W0.size());
+            DBUF(d_W0, double, "xi_W0", std::max<long long>(1, w0_total));
             DBUF(d_r0, double, "xi_res0", res0.size());
             DBUF(d_s0, double, "xi_sum0", sum0.size());
-            CKS(upload(ctx, d_W0, W0.data(), W0.size()));
+            if (!dev_filled) CKS(upload(ctx, d_W0, W0.data(), W0.size()));
             CKS(upload(ctx, d_r0, res0.data(), res0.size()));
             CKS(upload(ctx, d_s0, sum0.data(), sum0.size()));
             D.W0 = d_W0; D.res0 = d_r0; D.sum0 = d_s0;
@@ -1431,10 +1561,11 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
             D.Rm[mm] = X.Rm[mm];
             if (X.Rm[mm] == 0) continue;
             const std::string sfx = std::to_string(mm);
-            DBUF(d_U, double, "xi_U" + sfx, U[mm].size());
+            double* d_U = d_Uall_p ? d_Uall_p + ubase[mm] : dbuf<double>(ctx, "xi_U" + sfx, U[mm].size());
+            if (!d_U) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (xi U)");
             DBUF(d_rm, double, "xi_resm" + sfx, resm[mm].size());
             DBUF(d_sm, double, "xi_summ" + sfx, summ[mm].size());
-            CKS(upload(ctx, d_U, U[mm].data(), U[mm].size()));
+            if (!dev_filled) CKS(upload(ctx, d_U, U[mm].data(), U[mm].size()));
             CKS(upload(ctx, d_rm, resm[mm].data(), resm[mm].size()));
             CKS(upload(ctx, d_sm, summ[mm].data(), summ[mm].size()));
             D.U[mm] = d_U; D.resm[mm] = d_rm; D.summ[mm] = d_sm;

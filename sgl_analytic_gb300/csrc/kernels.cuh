@@ -154,6 +154,34 @@ void launch_mse(long long n, const float* pred, const float* tgt, float* dpred, 
 void launch_adamw(long long n, float* w, const float* g, float* m, float* v, float lr, float b1, float b2, float eps,
                   float wd, float c1, float c2, cudaStream_t st);
 
+// ---- device-side xi group preparation (coherent host-memory access)
+struct XiPrepRow {                 // one kept row
+    long long src;                 // first element of the raw row in the caller's rows
+    long long dst;                 // rows_t offset of entry 0 of its group, + rr
+    long long ent0;                // group's first entry (inverse / q / p orders)
+    long long u_off, u0_off, w0_off;   // row starts in U[m], U0, W0
+    int ne, R, row, m;             // entries, kept rows of the group, global kept-row index, harmonic
+    int nQ, q0, qseg0;             // gamma cells: count, offset into idx_q, offset into qseg
+    int nP, p0;                    // kappa cells: count, global p offset (p_ptr / idx_p)
+};
+struct XiPrepIdx {
+    const int* inv;                // [entries] position of entry e in the group's p-order
+    const int* qord;               // [entries] entries sorted by gamma cell (stable)
+    const int* qseg;               // per group: nQ + 1 segment starts into qord
+    const int* pord;               // [entries] entries in p-order
+    const int* p_ptr;              // global CSR over p-ordered entries
+    const int* idx_p;              // global kappa-cell index of each p
+    const int* idx_q;              // global gamma-cell index of each q
+};
+struct XiPrepOut {
+    double* rt; float* rtf; double* res; double* sums; double* sig;
+    double* U; double* U0; double* W0;
+};
+void launch_xi_row_norms(const double* rows, const long long* row_start, const int* row_len, int nrows,
+                         double* norms, cudaStream_t st);
+void launch_xi_rowprep(const double* rows, const XiPrepRow* kr, int nkept, int ne_max, const XiPrepIdx& ix,
+                       const double* kmc, const XiPrepOut& o, cudaStream_t st);
+
 // ---- positive (vp) Cox closure
 // Cells sorted per shell into runs (one kind and interval bound; runs ordered linear first, then by
 // the first state they change: lo for left runs, hi + 1 for right runs), per-cell weights (w a, w b).

@@ -1,0 +1,86 @@
+// Device-side preparation of the xi_lin groups when the GPU reads host memory coherently
+// (pageable-memory access through the host page tables: Grace + NVLink-C2C).  The caller's rows
+// are read in place, once and coalesced; nothing is staged through the host.
+//   k_xi_row_norms  Euclidean norm of every raw row (the prune threshold)
+//   k_xi_rowprep    one CTA per kept row, the row held in shared memory:
+//                   rows_t[i][rr] = row[order[i]] (through the inverse order; FP64 and FP32 copies),
+//                   the row sum and residual, the per-gamma-cell sums U[row][q] and, for m = 0 rows,
+//                   the per-kappa-cell sums W0[row][p], the compacted U0 and the sigma term
+//                   (row . kc + res).  Every sum runs over a fixed entry order (deterministic).
+#include "kernels.cuh"
+
+namespace sgl {
+
+__global__ void __launch_bounds__(256)
+k_xi_row_norms(const double* __restrict__ rows, const long long* __restrict__ row_start,
+               const int* __restrict__ row_len, int nrows, double* __restrict__ norms) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= nrows) return;
+    const double* r = rows + row_start[warp];
+    const int n = row_len[warp];
+    double a = 0.0;
+    for (int e = lane; e < n; e += 32) a = fma(r[e], r[e], a);
+    a = warp_sum(a);
+    if (lane == 0) norms[warp] = sqrt(a);
+}
+
+__global__ void __launch_bounds__(256)
+k_xi_rowprep(const double* __restrict__ rows, const XiPrepRow* __restrict__ kr, const XiPrepIdx ix,
+             const double* __restrict__ kmc, XiPrepOut o) {
+    extern __shared__ __align__(16) double xr[];
+    __shared__ double sh[32];
+    const XiPrepRow d = kr[blockIdx.x];
+    const double* r = rows + d.src;
+    for (int e = threadIdx.x; e <= d.ne; e += blockDim.x) xr[e] = r[e];
+    __syncthreads();
+    // transposed copies and the row sum
+    const int* iv = ix.inv + d.ent0;
+    double a = 0.0;
+    for (int e = threadIdx.x; e < d.ne; e += blockDim.x) {
+        const double v = xr[e];
+        const long long od = d.dst + (long long)iv[e] * d.R;
+        o.rt[od] = v;
+        o.rtf[od] = (float)v;
+        a += v;
+    }
+    a = block_sum(a, sh);
+    if (threadIdx.x == 0) { o.sums[d.row] = a; o.res[d.row] = xr[d.ne]; }
+    // U[row][q]: one thread per gamma cell of the group, entries in q-order
+    const int* qord = ix.qord + d.ent0;
+    const int* qseg = ix.qseg + d.qseg0;
+    for (int j = threadIdx.x; j < d.nQ; j += blockDim.x) {
+        double s = 0.0;
+        for (int i = qseg[j]; i < qseg[j + 1]; ++i) s += xr[qord[i]];
+        o.U[d.u_off + ix.idx_q[d.q0 + j]] = s;
+        if (d.m == 0) o.U0[d.u0_off + j] = s;
+    }
+    if (d.m != 0) return;
+    // W0[row][p] (entries in p-order, segments from the group's CSR) and the sigma term
+    const int* pord = ix.pord + d.ent0;
+    double dot = 0.0;
+    for (int j = threadIdx.x; j < d.nP; j += blockDim.x) {
+        double s = 0.0;
+        for (int i = ix.p_ptr[d.p0 + j] - (int)d.ent0; i < ix.p_ptr[d.p0 + j + 1] - (int)d.ent0; ++i) s += xr[pord[i]];
+        const int pcell = ix.idx_p[d.p0 + j];
+        o.W0[d.w0_off + pcell] = s;
+        dot = fma(s, kmc[pcell], dot);
+    }
+    dot = block_sum(dot, sh);
+    if (threadIdx.x == 0) o.sig[d.row] = dot + xr[d.ne];
+}
+
+void launch_xi_row_norms(const double* rows, const long long* row_start, const int* row_len, int nrows,
+                         double* norms, cudaStream_t st) {
+    if (nrows > 0) { k_xi_row_norms<<<ceil_div((long long)nrows * 32, 256), 256, 0, st>>>(rows, row_start, row_len, nrows, norms); SGL_COUNT(1); }
+}
+
+void launch_xi_rowprep(const double* rows, const XiPrepRow* kr, int nkept, int ne_max, const XiPrepIdx& ix,
+                       const double* kmc, const XiPrepOut& o, cudaStream_t st) {
+    if (nkept <= 0) return;
+    const size_t sm = ((size_t)ne_max + 1) * sizeof(double);
+    cudaFuncSetAttribute(k_xi_rowprep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_xi_rowprep<<<nkept, 256, sm, st>>>(rows, kr, ix, kmc, o);
+    SGL_COUNT(1);
+}
+
+}  // namespace sgl

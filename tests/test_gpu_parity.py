@@ -206,3 +206,21 @@ def test_cli_end_to_end(tmp_path, ref_sub):
     P = np.array(d["P_s"] + d["P_s_tail"])
     dpeak, _, _ = _pdf_errors(P, ref_sub["pdfx_P"], ref_sub["xi_out"])
     assert dpeak <= TOL_PEAK
+
+
+def test_xi_preparation_paths_agree(pop_sub, monkeypatch):
+    """The xi groups prepared on the GPU from the caller's rows (coherent host access) and on the
+    host give the same ln Phi and PDF (summation orders differ: ~1e-15 relative)."""
+    from sgl_analytic_gb300 import Lam, invert
+    kk, kg = KK16, KG_FULL
+    a = Lam(pop_sub, xi=True)
+    La = a(kk, kg)
+    monkeypatch.setenv("SGL_XI_HOST_PREP", "1")
+    b = Lam(pop_sub, xi=True)
+    Lb = b(kk, kg)
+    assert a.sigma() == pytest.approx(b.sigma(), rel=1e-14)
+    assert np.max(np.abs(La - Lb)) <= 1e-12 * max(1.0, np.max(np.abs(La)))
+    x = np.linspace(-0.35, 0.55, 200)
+    Pa = invert(a, a.sigma(), xi_out=x, phi_tol=1e-8)[1]
+    Pb = invert(b, b.sigma(), xi_out=x, phi_tol=1e-8)[1]
+    assert np.max(np.abs(Pa - Pb)) <= 1e-12 * np.max(Pa)
