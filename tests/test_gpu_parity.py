@@ -224,3 +224,28 @@ def test_xi_preparation_paths_agree(pop_sub, monkeypatch):
     Pa = invert(a, a.sigma(), xi_out=x, phi_tol=1e-8)[1]
     Pb = invert(b, b.sigma(), xi_out=x, phi_tol=1e-8)[1]
     assert np.max(np.abs(Pa - Pb)) <= 1e-12 * np.max(Pa)
+
+
+@pytest.mark.parametrize("zs", ["3", "10", "0.5"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_other_redshifts_match_stored_golden(zs, precision):
+    """The reference's own z_s population (tests/golden/make_fixtures.py, all xi groups) through the
+    whole GPU chain against the reference's stored PDF for that z_s (pdf_zs<z>.json)."""
+    from sgl_analytic_gb300 import Lam, Population, invert
+    from tests.conftest import FULL_DIR
+    path = FULL_DIR / f"cells_zs{zs}_gauss_full.npz"
+    if not path.exists():
+        pytest.skip(f"full z_s={zs} population not present")
+    lam = Lam(Population.load(path), xi=True)
+    ref = json.load(open(GOLDEN / f"pdf_zs{zs}.json"))
+    assert lam.sigma() == pytest.approx(ref["sigma_kappa"], rel=1e-9)
+    x = np.concatenate([ref["xi"], ref["xi_tail"]])
+    _, P, meta = invert(lam, lam.sigma(), xi_out=x, phi_tol=1e-8, precision=precision)
+    P0 = np.concatenate([ref["P_s"], ref["P_s_tail"]])
+    g, rg = meta["grid"], ref["grid"]
+    assert [g[k] for k in ("nk_k", "nk_g", "n_kap", "n_gam")] == [rg[k] for k in ("nk_k", "nk_g", "n_kap", "n_gam")]
+    dpeak, l1, rel_tail = _pdf_errors(P, P0, x)
+    if precision == "fp64":
+        assert dpeak <= TOL_PEAK, dpeak
+    else:
+        assert l1 <= 1e-4 and rel_tail <= 1e-3, (dpeak, l1, rel_tail)
