@@ -194,6 +194,21 @@ struct HostTimer {
     }
 };
 
+// fn(lo, hi) over [0, n) in contiguous blocks on up to 16 host threads (results do not depend on
+// the thread count: every index is written by exactly one block)
+void parallel_for(long long n, const std::function<void(long long, long long)>& fn) {
+    const int nthr = (int)std::max(1LL, std::min<long long>({16LL, (long long)std::thread::hardware_concurrency(),
+                                                            (n + 4095) / 4096}));
+    if (nthr == 1) { fn(0, n); return; }
+    std::vector<std::thread> th;
+    const long long blk = (n + nthr - 1) / nthr;
+    for (int t = 0; t < nthr; ++t) {
+        const long long lo = t * blk, hi = std::min(n, lo + blk);
+        if (lo < hi) th.emplace_back([&fn, lo, hi]() { fn(lo, hi); });
+    }
+    for (auto& x : th) x.join();
+}
+
 // pinned host buffer of at least `bytes` (grow-only; the stream is synchronised before it grows)
 char* big_pinned(sgl_ctx* ctx, size_t bytes) {
     if (bytes <= ctx->big_cap) return ctx->big_pinned;
@@ -428,18 +443,20 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
     std::vector<long long> keyv((size_t)N);
     std::vector<double> sl((size_t)N), sh((size_t)N);
     std::vector<char> direct((size_t)N, 0);
-    for (long long c = 0; c < N; ++c) {
-        const int b = ctx->ig[(size_t)c];
-        const double lo = fe[b], hi = fe[b + 1], wd = hi - lo;
-        double nsd = std::ceil(key * wd / (2.0 * kSepTheta));
-        long long ns = std::max(1LL, (long long)nsd);
-        if (ns > kSepSmax) { direct[(size_t)c] = 1; keyv[(size_t)c] = -1; continue; }
-        long long j = (long long)((ctx->g0[(size_t)c] - lo) / wd * (double)ns);
-        j = std::min(j, ns - 1);
-        sl[(size_t)c] = lo + (double)j * wd / (double)ns;
-        sh[(size_t)c] = lo + (double)(j + 1) * wd / (double)ns;
-        keyv[(size_t)c] = (long long)b * (kSepSmax + 1) + j;
-    }
+    parallel_for(N, [&](long long c0, long long c1) {
+        for (long long c = c0; c < c1; ++c) {
+            const int b = ctx->ig[(size_t)c];
+            const double lo = fe[b], hi = fe[b + 1], wd = hi - lo;
+            double nsd = std::ceil(key * wd / (2.0 * kSepTheta));
+            long long ns = std::max(1LL, (long long)nsd);
+            if (ns > kSepSmax) { direct[(size_t)c] = 1; keyv[(size_t)c] = -1; continue; }
+            long long j = (long long)((ctx->g0[(size_t)c] - lo) / wd * (double)ns);
+            j = std::min(j, ns - 1);
+            sl[(size_t)c] = lo + (double)j * wd / (double)ns;
+            sh[(size_t)c] = lo + (double)(j + 1) * wd / (double)ns;
+            keyv[(size_t)c] = (long long)b * (kSepSmax + 1) + j;
+        }
+    });
     // order: sep cells by (bin, sub-bin) (stable counting sort over the small key range), then
     // direct cells in original order
     long long kmax = -1;
@@ -474,25 +491,20 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
         }
         grp[(size_t)i] = ng;
     }
-    {   // Lagrange weights of each separable cell at its sub-bin's Chebyshev nodes (threads over cells)
-        const int nthr = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), 16));
-        std::vector<std::thread> th;
-        for (int tix = 0; tix < nthr; ++tix)
-            th.emplace_back([&, tix]() {
-                for (long long i = tix; i < n_sep; i += nthr) {
-                    const long long c = order[(size_t)i];
-                    const double lo_s = sl[(size_t)c], hi_s = sh[(size_t)c];
-                    const double u = ((2.0 * ctx->g0[(size_t)c] - lo_s) - hi_s) / (hi_s - lo_s);
-                    for (int a = 0; a < kSepMg; ++a) {
-                        double L = 1.0;
-                        for (int b2 = 0; b2 < kSepMg; ++b2)
-                            if (b2 != a) L = L * ((u - t[b2]) / (t[a] - t[b2]));
-                        wl[(size_t)i * 8 + a] = ctx->w0[(size_t)c] * L;
-                    }
-                }
-            });
-        for (auto& x : th) x.join();
-    }
+    // Lagrange weights of each separable cell at its sub-bin's Chebyshev nodes
+    parallel_for(n_sep, [&](long long i0, long long i1) {
+        for (long long i = i0; i < i1; ++i) {
+            const long long c = order[(size_t)i];
+            const double lo_s = sl[(size_t)c], hi_s = sh[(size_t)c];
+            const double u = ((2.0 * ctx->g0[(size_t)c] - lo_s) - hi_s) / (hi_s - lo_s);
+            for (int a = 0; a < kSepMg; ++a) {
+                double L = 1.0;
+                for (int b2 = 0; b2 < kSepMg; ++b2)
+                    if (b2 != a) L = L * ((u - t[b2]) / (t[a] - t[b2]));
+                wl[(size_t)i * 8 + a] = ctx->w0[(size_t)c] * L;
+            }
+        }
+    });
     const int n_sep_groups = ng + 1;
     const int n_cols_sep = n_sep_groups * kSepMg;
     for (long long i = n_sep; i < N; ++i) {
@@ -505,15 +517,17 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
         nodes.push_back(ctx->g0[(size_t)c]);
     }
     const int n_groups = ng + 1;
-    for (long long i = 0; i < N; ++i) {
-        const long long c = order[(size_t)i];
-        kap[(size_t)i] = ctx->k0[(size_t)c];
-        w[(size_t)i] = ctx->w0[(size_t)c];
-        const ff f = ff_from_double(kap[(size_t)i]);
-        kh[(size_t)i] = f.hi; kl[(size_t)i] = f.lo;
-        wf[(size_t)i] = (float)w[(size_t)i];
-        for (int a = 0; a < 8; ++a) wlf[(size_t)i * 8 + a] = (float)wl[(size_t)i * 8 + a];
-    }
+    parallel_for(N, [&](long long i0, long long i1) {
+        for (long long i = i0; i < i1; ++i) {
+            const long long c = order[(size_t)i];
+            kap[(size_t)i] = ctx->k0[(size_t)c];
+            w[(size_t)i] = ctx->w0[(size_t)c];
+            const ff f = ff_from_double(kap[(size_t)i]);
+            kh[(size_t)i] = f.hi; kl[(size_t)i] = f.lo;
+            wf[(size_t)i] = (float)w[(size_t)i];
+            for (int a = 0; a < 8; ++a) wlf[(size_t)i * 8 + a] = (float)wl[(size_t)i * 8 + a];
+        }
+    });
     // chunks of whole groups: ~4 CTAs per SM over (row tiles x chunks)
     const int row_tiles = std::max(1, ceil_div(nk, 128));
     int nchunks = std::max(1, std::min(n_groups, ceil_div(4 * kNumSMs, row_tiles)));
@@ -883,40 +897,8 @@ sgl_status lambda_eval(sgl_ctx* ctx, int precision, const double* h_kk, int nk, 
     const bool exact_xi = xi_active && !use_interp;
     if (exact_xi && write_phi) return fail(ctx, SGL_ERR_UNSUPPORTED, "exact xi term on an inversion grid");
 
-    const void* G = nullptr;
-    const double2* A1 = nullptr;
-    int fin_precision = precision;
-    if (use_sep) {
-        CKS(build_sep(ctx, h_kg[nkg - 1], nk));
-        const size_t es = elem_size(precision);
-        const long long ld = 2LL * nk;
-        void* Tt = ctx->arena.get("sep_T", (size_t)ctx->sep.n_cols * ld * es);
-        DBUF(d_Ap, double2, "sep_Apart", (long long)ctx->sepd.nchunks * nk);
-        DBUF(d_A1, double2, "sep_A1", nk);
-        void* Gout = ctx->arena.get("lam_G", (size_t)ld * nkg * es);
-        if (!Tt || !Gout) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (lambda)");
-        {
-            Timed t(ctx, precision == SGL_FP64 ? "sep_sweep_f64" : "sep_sweep_mixed", (double)nk * ctx->sep.n_cells,
-                    (double)ctx->sep.n_cols * ld * es);
-            launch_sep_sweep(precision, d_kk, nk, ctx->sepd, Tt, d_Ap, d_A1, st);
-        }
-        CKLAUNCH();
-        if (precision == SGL_FP64) CKS(sep_gemms<double>(ctx, precision, h_kg, d_kg, nk, nkg, Tt, Gout));
-        else CKS(sep_gemms<float>(ctx, precision, h_kg, d_kg, nk, nkg, Tt, Gout));
-        G = Gout; A1 = d_A1;
-    } else {
-        DBUF(d_dir, double, "lam_direct", 2 * npt);
-        DBUF(d_zero, double2, "lam_zero", nk);
-        const double* d_k0 = (const double*)ctx->arena.find("cells_k0");
-        const double* d_g0 = (const double*)ctx->arena.find("cells_g0");
-        const double* d_w0 = (const double*)ctx->arena.find("cells_w0");
-        DBUF(d_dpart, double2, "direct_part", (long long)std::max(1, psi1_direct_chunks((int64_t)ctx->w0.size())) * npt);
-        launch_psi1_direct(d_kk, nk, d_kg, nkg, d_k0, d_g0, d_w0, (int64_t)ctx->w0.size(), d_dir, d_dir + npt, d_dpart, st);
-        CKLAUNCH();
-        CK(cudaMemsetAsync(d_zero, 0, (size_t)nk * sizeof(double2), st));
-        G = d_dir; A1 = d_zero; fin_precision = SGL_FP64;
-    }
-
+    // the xi term first: its kernels run while the host builds the separable plan (first call
+    // for a new kg_max), which has no data dependence on them
     const double* Cre = nullptr; const double* Cim = nullptr;
     SplineAxis sk, sg;
     int ncg = 0;
@@ -962,6 +944,40 @@ sgl_status lambda_eval(sgl_ctx* ctx, int precision, const double* h_kk, int nk, 
         sk.l = d_lk; sk.b = d_bk; sg.l = d_lg; sg.b = d_bg;
         Cre = d_C; Cim = d_C + nq; ncg = n;
     }
+    const void* G = nullptr;
+    const double2* A1 = nullptr;
+    int fin_precision = precision;
+    if (use_sep) {
+        CKS(build_sep(ctx, h_kg[nkg - 1], nk));
+        const size_t es = elem_size(precision);
+        const long long ld = 2LL * nk;
+        void* Tt = ctx->arena.get("sep_T", (size_t)ctx->sep.n_cols * ld * es);
+        DBUF(d_Ap, double2, "sep_Apart", (long long)ctx->sepd.nchunks * nk);
+        DBUF(d_A1, double2, "sep_A1", nk);
+        void* Gout = ctx->arena.get("lam_G", (size_t)ld * nkg * es);
+        if (!Tt || !Gout) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (lambda)");
+        {
+            Timed t(ctx, precision == SGL_FP64 ? "sep_sweep_f64" : "sep_sweep_mixed", (double)nk * ctx->sep.n_cells,
+                    (double)ctx->sep.n_cols * ld * es);
+            launch_sep_sweep(precision, d_kk, nk, ctx->sepd, Tt, d_Ap, d_A1, st);
+        }
+        CKLAUNCH();
+        if (precision == SGL_FP64) CKS(sep_gemms<double>(ctx, precision, h_kg, d_kg, nk, nkg, Tt, Gout));
+        else CKS(sep_gemms<float>(ctx, precision, h_kg, d_kg, nk, nkg, Tt, Gout));
+        G = Gout; A1 = d_A1;
+    } else {
+        DBUF(d_dir, double, "lam_direct", 2 * npt);
+        DBUF(d_zero, double2, "lam_zero", nk);
+        const double* d_k0 = (const double*)ctx->arena.find("cells_k0");
+        const double* d_g0 = (const double*)ctx->arena.find("cells_g0");
+        const double* d_w0 = (const double*)ctx->arena.find("cells_w0");
+        DBUF(d_dpart, double2, "direct_part", (long long)std::max(1, psi1_direct_chunks((int64_t)ctx->w0.size())) * npt);
+        launch_psi1_direct(d_kk, nk, d_kg, nkg, d_k0, d_g0, d_w0, (int64_t)ctx->w0.size(), d_dir, d_dir + npt, d_dpart, st);
+        CKLAUNCH();
+        CK(cudaMemsetAsync(d_zero, 0, (size_t)nk * sizeof(double2), st));
+        G = d_dir; A1 = d_zero; fin_precision = SGL_FP64;
+    }
+
     if (write_phi && fin_precision != precision) return fail(ctx, SGL_ERR_UNSUPPORTED, "inversion grid below 2e5 points");
     {
         Timed t(ctx, "finalize", 0.0, (double)npt * 2 * (elem_size(fin_precision) + (write_phi ? elem_size(precision) : 8)));
@@ -1197,6 +1213,8 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
     // coherent access: the GPU reads the caller's rows in place (norms here, the data in pass 3)
     const bool coherent = ctx->coherent_host && !std::getenv("SGL_XI_HOST_PREP");
     std::vector<std::vector<double>> norms(n_groups);
+    std::vector<double> hn;
+    double* d_raw = nullptr;
     if (coherent) {
         std::vector<long long> rs;
         std::vector<int> rl;
@@ -1205,15 +1223,19 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         const int nr = (int)rs.size();
         DBUF(d_rs, long long, "xi_prep_rs", std::max(1, nr));
         DBUF(d_rl, int, "xi_prep_rl", std::max(1, nr));
-        DBUF(d_nrm, double, "xi_prep_norm", std::max(1, nr));
         CKS(upload(ctx, d_rs, rs.data(), rs.size()));
         CKS(upload(ctx, d_rl, rl.data(), rl.size()));
-        launch_xi_row_norms(rows, d_rs, d_rl, nr, d_nrm, ctx->stream);
+        // one read of the caller's rows over the link into device memory; everything after
+        // reads the device copy
+        d_raw = dbuf<double>(ctx, "xi_raw", (size_t)std::max<long long>(1, row_off[n_groups]));
+        if (!d_raw) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (xi raw rows)");
+        launch_xi_stage_rows(rows, row_off[n_groups], d_raw, ctx->stream);
         CKLAUNCH();
-        std::vector<double> hn((size_t)std::max(1, nr));
-        CK(cudaMemcpyAsync(hn.data(), d_nrm, (size_t)nr * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-        CKS(sync_stream(ctx));
-        for (int g = 0, k = 0; g < n_groups; ++g) norms[g].assign(hn.begin() + k, hn.begin() + k + nrow[g]), k += nrow[g];
+        // the norms are written straight into host memory (coherent); the host reads them after
+        // the per-group index work below, which overlaps these kernels
+        hn.assign((size_t)std::max(1, nr), 0.0);
+        launch_xi_row_norms(d_raw, d_rs, d_rl, nr, hn.data(), ctx->stream);
+        CKLAUNCH();
     } else {
         parallel_groups([&](int g) {
             const int w = nidx[g] + 1;
@@ -1226,18 +1248,10 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
             }
         });
     }
-    double s0 = 0.0;
     for (int g = 0; g < n_groups; ++g)
-        for (double v : norms[g]) s0 = std::max(s0, v);
-    if (s0_override > 0) s0 = s0_override;
-    for (int g = 0; g < n_groups; ++g) {
         if (m[g] < 0 || m[g] > 2) return fail(ctx, SGL_ERR_UNSUPPORTED, "xi harmonic m must be 0, 1 or 2");
-        const int32_t* id = idx + idx_off[g];
-        for (int e = 0; e < nidx[g]; ++e)
-            if (id[e] < 0 || id[e] >= X.n_kmc * ngc) return fail(ctx, SGL_ERR_VALUE, "coarse index out of range");
-    }
-    ht.lap("xi_norms");
-    // pass 2: keep lists, entry order by p, unique p / q, and every output offset
+    // pass 2: entry order by p, unique p / q (index-only, before the norms are known), then the
+    // keep lists and every output offset
     struct GPlan {
         std::vector<int> keep, order, pg, qg, qs, qpos, inv, qord, qseg;
         int nP = 0, q0 = 0, qseg0 = 0, p0 = 0;
@@ -1248,20 +1262,22 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
     std::vector<long long> g_p_off, g_ent_off, g_row_off, p_prefix{0}, rowel_off, g_q_off, g_u_off;
     std::vector<int> kept;                      // groups with rows left after pruning
     long long ent_total = 0, row_total = 0, rowel_total = 0, u_total = 0, w0_total = 0, um_total[3] = {0, 0, 0};
-    // per-group index work in parallel (keep list, entry order by p, unique q), then the serial
-    // concatenation in group order
+    // per-group index work in parallel (entry order by p, unique q), then the keep lists from the
+    // norms, then the serial offsets and the parallel concatenation in group order
+    std::atomic<int> bad_index{0};
     parallel_groups([&](int g) {
         GPlan& P = plan[g];
-        for (int r = 0; r < nrow[g]; ++r)
-            if (!(prune > 0) || norms[g][(size_t)r] > prune * s0) P.keep.push_back(r);
-        if (P.keep.empty()) return;
         const int32_t* id = idx + idx_off[g];
+        for (int e = 0; e < nidx[g]; ++e)
+            if (id[e] < 0 || id[e] >= X.n_kmc * ngc) { bad_index = 1; return; }
         P.pg.resize(nidx[g]); P.qg.resize(nidx[g]);
         for (int e = 0; e < nidx[g]; ++e) { P.pg[e] = id[e] / ngc; P.qg[e] = id[e] % ngc; }
-        // entries by kappa cell (stable counting sort) and the sorted unique gamma cells
+        // entries by kappa cell (stable counting sort), the number of distinct kappa cells and
+        // the sorted unique gamma cells
         {
             std::vector<int> cnt(X.n_kmc + 1, 0);
             for (int e = 0; e < nidx[g]; ++e) ++cnt[P.pg[e] + 1];
+            for (int i = 1; i <= X.n_kmc; ++i) P.nP += cnt[i] > 0;
             for (int i = 1; i <= X.n_kmc; ++i) cnt[i] += cnt[i - 1];
             P.order.resize(nidx[g]);
             for (int e = 0; e < nidx[g]; ++e) P.order[cnt[P.pg[e]]++] = e;
@@ -1283,26 +1299,33 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
             for (int e = 0; e < ne; ++e) P.qord[fill[P.qpos[P.qg[e]]]++] = e;     // stable by q
         }
     });
+    if (coherent) {
+        CKS(sync_stream(ctx));
+        for (int g = 0, k = 0; g < n_groups; ++g) norms[g].assign(hn.begin() + k, hn.begin() + k + nrow[g]), k += nrow[g];
+    }
+    if (bad_index) return fail(ctx, SGL_ERR_VALUE, "coarse index out of range");
+    double s0 = 0.0;
+    for (int g = 0; g < n_groups; ++g)
+        for (double v : norms[g]) s0 = std::max(s0, v);
+    if (s0_override > 0) s0 = s0_override;
+    for (int g = 0; g < n_groups; ++g)
+        for (int r = 0; r < nrow[g]; ++r)
+            if (!(prune > 0) || norms[g][(size_t)r] > prune * s0) plan[g].keep.push_back(r);
+    ht.lap("xi_index");
+    // every offset, serially in group order (O(groups))
+    long long q_total = 0, qseg_total = 0;
     for (int g = 0; g < n_groups; ++g) {
         GPlan& P = plan[g];
         if (P.keep.empty()) continue;
         const int R = (int)P.keep.size(), mg = m[g];
-        for (int i = 0; i < nidx[g]; ++i) {
-            const int e = P.order[i];
-            if (i == 0 || P.pg[e] != P.pg[P.order[i - 1]]) {
-                if (i > 0) p_ptr.push_back((int)(ent_total + i));
-                idx_p.push_back(P.pg[e]);
-                ++P.nP;
-            }
-            ent_qg.push_back(P.qg[e]);
-        }
-        p_ptr.push_back((int)(ent_total + nidx[g]));
-        P.q0 = (int)idx_q.size();
+        P.q0 = (int)q_total;
+        P.qseg0 = (int)qseg_total;
         P.p0 = (int)p_prefix.back();
-        g_q_off.push_back((long long)idx_q.size());
+        g_q_off.push_back(q_total);
         g_u_off.push_back(u_total);
         g_nQ.push_back((int)P.qs.size());
-        idx_q.insert(idx_q.end(), P.qs.begin(), P.qs.end());
+        q_total += (long long)P.qs.size();
+        if (coherent) qseg_total += (long long)P.qs.size() + 1;
         P.ent0 = ent_total; P.rowel0 = rowel_total; P.row0 = row_total; P.u0 = u_total;
         P.w0 = w0_total; P.um0 = um_total[mg];
         if (mg == 0) { w0_total += (long long)R * X.n_kmc; X.R0 += R; }
@@ -1321,6 +1344,39 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         X.m.push_back(mg); X.r.push_back(R); X.nP.push_back(P.nP);
         kept.push_back(g);
     }
+    // the concatenated index arrays, each group filling its own slices in parallel
+    const long long total_p = p_prefix.back();
+    idx_p.resize((size_t)total_p);
+    p_ptr.assign((size_t)total_p + 1, 0);
+    p_ptr[(size_t)total_p] = (int)ent_total;
+    ent_qg.resize((size_t)ent_total);
+    idx_q.resize((size_t)q_total);
+    std::vector<int> inv_all, qord_all, pord_all, qseg_all;
+    if (coherent) {
+        inv_all.resize((size_t)ent_total); qord_all.resize((size_t)ent_total); pord_all.resize((size_t)ent_total);
+        qseg_all.resize((size_t)qseg_total);
+    }
+    parallel_groups([&](int g) {
+        const GPlan& P = plan[g];
+        if (P.keep.empty()) return;
+        const int ne = nidx[g];
+        for (int i = 0, j = 0; i < ne; ++i) {
+            const int e = P.order[i];
+            if (i == 0 || P.pg[e] != P.pg[P.order[i - 1]]) {
+                p_ptr[(size_t)P.p0 + j] = (int)(P.ent0 + i);
+                idx_p[(size_t)P.p0 + j] = P.pg[e];
+                ++j;
+            }
+            ent_qg[(size_t)(P.ent0 + i)] = P.qg[e];
+        }
+        std::copy(P.qs.begin(), P.qs.end(), idx_q.begin() + P.q0);
+        if (coherent) {
+            std::copy(P.inv.begin(), P.inv.end(), inv_all.begin() + P.ent0);
+            std::copy(P.qord.begin(), P.qord.end(), qord_all.begin() + P.ent0);
+            std::copy(P.order.begin(), P.order.end(), pord_all.begin() + P.ent0);
+            std::copy(P.qseg.begin(), P.qseg.end(), qseg_all.begin() + P.qseg0);
+        }
+    });
     ht.lap("xi_plan");
     // pass 3: data, in parallel over groups (host) or on the GPU from the caller's rows (coherent)
     std::vector<double> res((size_t)row_total), sum_rows((size_t)row_total);
@@ -1334,16 +1390,10 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
     float* rows_tf_p = nullptr;
     if (coherent && !kept.empty()) {
         std::vector<XiPrepRow> kr;
-        std::vector<int> inv_all((size_t)ent_total), qord_all((size_t)ent_total), pord_all((size_t)ent_total), qseg_all;
         int ne_max = 0;
         for (int g : kept) {
             GPlan& P = plan[g];
             const int R = (int)P.keep.size(), ne = nidx[g], w = nidx[g] + 1;
-            std::copy(P.inv.begin(), P.inv.end(), inv_all.begin() + P.ent0);
-            std::copy(P.qord.begin(), P.qord.end(), qord_all.begin() + P.ent0);
-            std::copy(P.order.begin(), P.order.end(), pord_all.begin() + P.ent0);
-            P.qseg0 = (int)qseg_all.size();
-            qseg_all.insert(qseg_all.end(), P.qseg.begin(), P.qseg.end());
             ne_max = std::max(ne_max, ne);
             for (int rr = 0; rr < R; ++rr) {
                 XiPrepRow k{};
@@ -1391,7 +1441,7 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
             CK(cudaMemsetAsync(d_Uall, 0, (size_t)std::max<long long>(1, ubase[2] + um_total[2]) * 8, ctx->stream));
             XiPrepIdx ix{d_inv, d_qord, d_qseg, d_pord, d_pptr0, d_idxp0, d_idxq0};
             XiPrepOut xo{d_rows0, d_rowsf0, d_res0, d_sum0, d_sig0, d_Uall, d_U0x, d_W0x};
-            launch_xi_rowprep(rows, d_kr, (int)kr.size(), ne_max, ix, d_kmc0, xo, ctx->stream);
+            launch_xi_rowprep(d_raw, d_kr, (int)kr.size(), ne_max, ix, d_kmc0, xo, ctx->stream);
             CKLAUNCH();
             sig_v.assign((size_t)row_total, 0.0);
             CK(cudaMemcpyAsync(res.data(), d_res0, (size_t)row_total * 8, cudaMemcpyDeviceToHost, ctx->stream));

@@ -23,6 +23,40 @@ __host__ __device__ inline ff ff_from_double(double v) {
     ff r; r.hi = (float)v; r.lo = (float)(v - (double)r.hi); return r;
 }
 
+// Mixed path: ph = k * kap in float-float, half-angle reduced mod pi/2 (three float parts of
+// pi/2 with FMA-exact products), FP32 sincos on the reduced argument, quadrant fix-up.  Returns sin(ph/2), cos(ph/2) and ph (float-float head + tail).
+__device__ inline void halfangle_sincos_ff(ff k, ff kap, float& s, float& c, float& ph_hi, float& ph_lo) {
+    const float p = k.hi * kap.hi;
+    const float e = fmaf(k.hi, kap.hi, -p);
+    const float t = fmaf(k.hi, kap.lo, fmaf(k.lo, kap.hi, e));
+    ph_hi = p; ph_lo = t;
+    const float xh = 0.5f * p, xl = 0.5f * t;
+    const float q = rintf(xh * 0.636619772367581343f);   // 2/pi; exact integer for |q| < 2^24
+    // x - q pi/2 with pi/2 = C1 + C2 + C3 (float parts); the roundings of q*C1 and q*C2 are
+    // recovered exactly with FMA and xh - q*C1 is exact (Sterbenz), so the reduction holds for
+    // every |q| < 2^24 (phases up to ~2.6e7)
+    constexpr float C1 = 1.57079637050628662109375f;
+    constexpr float C2 = -4.371138828673792886547744274139404296875e-08f;
+    constexpr float C3 = -1.7151245100058819e-15f;
+    const float p1 = q * C1, e1 = fmaf(q, C1, -p1);
+    const float p2 = q * C2, e2 = fmaf(q, C2, -p2);
+    float r = xh - p1;
+    r -= e1;
+    r -= p2;
+    r -= e2;
+    r = fmaf(-q, C3, r);
+    r += xl;
+    float sr, cr;
+    sincosf(r, &sr, &cr);
+    const int qi = ((int)q) & 3;
+    switch (qi) {
+        case 0: s = sr;  c = cr;  break;
+        case 1: s = cr;  c = -sr; break;
+        case 2: s = -sr; c = -cr; break;
+        default: s = -cr; c = sr; break;
+    }
+}
+
 // ------------------------------------------------------------------ J0(x) - 1
 // Small-argument series below 1e-3 exactly as the reference forms it (-x^2/4 (1 - x^2/16));
 // above, CUDA's double-precision j0 minus 1.

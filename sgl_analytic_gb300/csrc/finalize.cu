@@ -23,22 +23,46 @@ void launch_grouped_gemm(const GemmDesc<T>* d_descs, int nprob, int tiles, cudaS
 template void launch_grouped_gemm<double>(const GemmDesc<double>*, int, int, cudaStream_t);
 template void launch_grouped_gemm<float>(const GemmDesc<float>*, int, int, cudaStream_t);
 
-// out(i, j) = sum_s ws[s, i, j] (+ beta out(i, j)); ws slices are dense rows x cols, out has row stride ldo
+// out(i, j) = sum_s ws[s, i, j] (+ beta out(i, j)); ws slices are dense rows x cols, out has row
+// stride ldo.  Grid (column blocks, rows).  FP64 slices are summed in FP64.  FP32 slices are summed
+// in float-float (Knuth's TwoSum, errors accumulated in a second float): about 48 significant
+// bits, as accurate as an FP64 sum for a float result, with no FP64 arithmetic.
 template <typename T>
 __global__ void k_sum_slices(const T* __restrict__ ws, int ns, int rows, int cols, T* __restrict__ out, long long ldo,
                              T beta) {
-    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= cols) return;
     const long long n = (long long)rows * cols;
-    if (e >= n) return;
-    double acc = 0.0;                         // slices summed in FP64 in both precisions
-    for (int s = 0; s < ns; ++s) acc += (double)ws[(long long)s * n + e];
-    T* o = out + (e / cols) * ldo + (e % cols);
-    *o = (beta != T(0)) ? (T)(acc + (double)beta * (double)*o) : (T)acc;
+    for (int i = blockIdx.y; i < rows; i += gridDim.y) {
+        const long long e = (long long)i * cols + j;
+        T* o = out + (long long)i * ldo + j;
+        if constexpr (sizeof(T) == 8) {
+            double acc = 0.0;
+            for (int s = 0; s < ns; ++s) acc += ws[(long long)s * n + e];
+            *o = (beta != T(0)) ? acc + beta * *o : acc;
+        } else {
+            float hi = 0.f, lo = 0.f;
+            auto add = [&](float v) {
+                const float t = hi + v, bp = t - hi;
+                lo += (hi - (t - bp)) + (v - bp);
+                hi = t;
+            };
+            for (int s = 0; s < ns; ++s) add(ws[(long long)s * n + e]);
+            if (beta != 0.f) {
+                const float ov = *o, p = beta * ov;
+                lo += fmaf(beta, ov, -p);
+                add(p);
+            }
+            *o = hi + lo;
+        }
+    }
 }
 
 template <typename T>
 void launch_sum_slices(const T* ws, int ns, int rows, int cols, T* out, long long ldo, T beta, cudaStream_t st) {
-    { k_sum_slices<T><<<ceil_div((long long)rows * cols, 256), 256, 0, st>>>(ws, ns, rows, cols, out, ldo, beta); SGL_COUNT(1); }
+    if (rows <= 0 || cols <= 0) return;
+    dim3 grid(ceil_div(cols, 128), std::min(rows, 65535));
+    { k_sum_slices<T><<<grid, 128, 0, st>>>(ws, ns, rows, cols, out, ldo, beta); SGL_COUNT(1); }
 }
 template void launch_sum_slices<double>(const double*, int, int, int, double*, long long, double, cudaStream_t);
 template void launch_sum_slices<float>(const float*, int, int, int, float*, long long, float, cudaStream_t);

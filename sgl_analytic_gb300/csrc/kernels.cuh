@@ -177,6 +177,7 @@ struct XiPrepOut {
     double* rt; float* rtf; double* res; double* sums; double* sig;
     double* U; double* U0; double* W0;
 };
+void launch_xi_stage_rows(const double* rows, long long n, double* dst, cudaStream_t st);
 void launch_xi_row_norms(const double* rows, const long long* row_start, const int* row_len, int nrows,
                          double* norms, cudaStream_t st);
 void launch_xi_rowprep(const double* rows, const XiPrepRow* kr, int nkept, int ne_max, const XiPrepIdx& ix,

@@ -26,40 +26,6 @@ __device__ inline void compensated_fp64(double ph, double& cm1, double& smp, dou
     }
 }
 
-// Mixed path: ph = k * kap in float-float, half-angle reduced mod pi/2 (three float parts of
-// pi/2 with FMA-exact products), FP32 sincos on the reduced argument, quadrant fix-up.  Returns sin(ph/2), cos(ph/2) and ph (float-float head + tail).
-__device__ inline void halfangle_sincos_ff(ff k, ff kap, float& s, float& c, float& ph_hi, float& ph_lo) {
-    const float p = k.hi * kap.hi;
-    const float e = fmaf(k.hi, kap.hi, -p);
-    const float t = fmaf(k.hi, kap.lo, fmaf(k.lo, kap.hi, e));
-    ph_hi = p; ph_lo = t;
-    const float xh = 0.5f * p, xl = 0.5f * t;
-    const float q = rintf(xh * 0.636619772367581343f);   // 2/pi; exact integer for |q| < 2^24
-    // x - q pi/2 with pi/2 = C1 + C2 + C3 (float parts); the roundings of q*C1 and q*C2 are
-    // recovered exactly with FMA and xh - q*C1 is exact (Sterbenz), so the reduction holds for
-    // every |q| < 2^24 (phases up to ~2.6e7)
-    constexpr float C1 = 1.57079637050628662109375f;
-    constexpr float C2 = -4.371138828673792886547744274139404296875e-08f;
-    constexpr float C3 = -1.7151245100058819e-15f;
-    const float p1 = q * C1, e1 = fmaf(q, C1, -p1);
-    const float p2 = q * C2, e2 = fmaf(q, C2, -p2);
-    float r = xh - p1;
-    r -= e1;
-    r -= p2;
-    r -= e2;
-    r = fmaf(-q, C3, r);
-    r += xl;
-    float sr, cr;
-    sincosf(r, &sr, &cr);
-    const int qi = ((int)q) & 3;
-    switch (qi) {
-        case 0: s = sr;  c = cr;  break;
-        case 1: s = cr;  c = -sr; break;
-        case 2: s = -sr; c = -cr; break;
-        default: s = -cr; c = sr; break;
-    }
-}
-
 // ------------------------------------------------------------------ direct sum
 // CTA (output point, cell chunk); threads stride over the chunk's cells; deterministic block sum
 // into part[chunk, point]; a second kernel sums the chunks in a fixed order.
@@ -76,19 +42,39 @@ k_psi1_direct(const double* __restrict__ kk, int nk, const double* __restrict__ 
     const int64_t c0 = (int64_t)blockIdx.y * kDirectChunkCells;
     const int64_t c1 = c0 + kDirectChunkCells < nc ? c0 + kDirectChunkCells : nc;
     double re = 0.0, im = 0.0;
-    for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
-        const double w = w0[c];
-        const double ph = k * k0[c];
-        const double x = g * g0[c];
-        double cm1, smp, sn;
-        compensated_fp64(ph, cm1, smp, sn);
-        const double J = j0(x);
-        double B;
-        if (x < 1e-3) { const double x2 = x * x; B = -x2 * 0.25 * (1.0 - x2 * (1.0 / 16.0)); }
-        else B = J - 1.0;
-        // (cos-1) J + (J-1) and (sin-ph) J + ph (J-1): every term O(A) or O(B)
-        re += w * fma(cm1, J, B);
-        im += w * fma(smp, J, ph * B);
+    if (g == 0.0) {
+        // k_gamma = 0 (the kappa-axis probes): J0 = 1, J0 - 1 = 0
+        for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+            const double w = w0[c];
+            double cm1, smp, sn;
+            compensated_fp64(k * k0[c], cm1, smp, sn);
+            re += w * cm1;
+            im += w * smp;
+        }
+    } else if (k == 0.0) {
+        // k_kappa = 0 (the gamma-axis probes): the phase terms vanish
+        for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+            const double x = g * g0[c];
+            double B;
+            if (x < 1e-3) { const double x2 = x * x; B = -x2 * 0.25 * (1.0 - x2 * (1.0 / 16.0)); }
+            else B = j0(x) - 1.0;
+            re += w0[c] * B;
+        }
+    } else {
+        for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+            const double w = w0[c];
+            const double ph = k * k0[c];
+            const double x = g * g0[c];
+            double cm1, smp, sn;
+            compensated_fp64(ph, cm1, smp, sn);
+            const double J = j0(x);
+            double B;
+            if (x < 1e-3) { const double x2 = x * x; B = -x2 * 0.25 * (1.0 - x2 * (1.0 / 16.0)); }
+            else B = J - 1.0;
+            // (cos-1) J + (J-1) and (sin-ph) J + ph (J-1): every term O(A) or O(B)
+            re += w * fma(cm1, J, B);
+            im += w * fma(smp, J, ph * B);
+        }
     }
     re = block_sum(re, sh);
     im = block_sum(im, sh);

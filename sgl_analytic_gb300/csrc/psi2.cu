@@ -314,10 +314,30 @@ __global__ void k_xi_E(XiDevice x, const double* __restrict__ kk, int nk, const 
     }
 }
 
+// Mixed path: the same table in FP32 with no FP64 transcendental.  The phase k kap is formed in
+// float-float and reduced exactly (halfangle_sincos_ff), then, with s = sin(ph/2), c = cos(ph/2):
+// cos ph = (c - s)(c + s), sin ph = 2 s c, and for m = 0 groups cos ph - 1 = -2 s^2.
+__global__ void k_xi_E_ff(XiDevice x, const double* __restrict__ kk, int nk, const long long* __restrict__ E_off,
+                          const long long* __restrict__ p_prefix, float* __restrict__ E) {
+    const long long P = blockIdx.x;
+    const int g = find_group(p_prefix, x.n_groups, P);
+    const int p = (int)(P - p_prefix[g]);
+    const int nP = x.g_nP[g];
+    const bool cm1 = x.g_m[g] == 0;
+    const ff kap = ff_from_double(x.kmc[x.idx_p[P]]);
+    float* Eg = E + E_off[g];
+    for (int i = threadIdx.x; i < nk; i += blockDim.x) {
+        float s, c, ph_hi, ph_lo;
+        halfangle_sincos_ff(ff_from_double(kk[i]), kap, s, c, ph_hi, ph_lo);
+        Eg[(long long)i * nP + p] = cm1 ? -2.f * s * s : (c - s) * (c + s);
+        Eg[(long long)(nk + i) * nP + p] = 2.f * s * c;
+    }
+}
+
 void launch_xi_E(int precision, const XiDevice& x, const double* kk, int nk, const long long* E_off,
                  const long long* d_p_prefix, int total_p, void* E, cudaStream_t st) {
     if (precision == SGL_FP64) { k_xi_E<double><<<total_p, 128, 0, st>>>(x, kk, nk, E_off, d_p_prefix, (double*)E, 0); SGL_COUNT(1); }
-    else { k_xi_E<float><<<total_p, 128, 0, st>>>(x, kk, nk, E_off, d_p_prefix, (float*)E, 1); SGL_COUNT(1); }
+    else { k_xi_E_ff<<<total_p, 128, 0, st>>>(x, kk, nk, E_off, d_p_prefix, (float*)E); SGL_COUNT(1); }
 }
 
 // V[g, r, j] = sum_q U_g[r, q] (J0 - 1)(gam_q kg_j) for the m = 0 groups (compensated form),

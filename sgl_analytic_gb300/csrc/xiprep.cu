@@ -1,6 +1,7 @@
 // Device-side preparation of the xi_lin groups when the GPU reads host memory coherently
 // (pageable-memory access through the host page tables: Grace + NVLink-C2C).  The caller's rows
-// are read in place, once and coalesced; nothing is staged through the host.
+// are read once, coalesced, straight into device memory; nothing is staged through the host.
+//   k_xi_stage_rows flat copy of the caller's rows into device memory
 //   k_xi_row_norms  Euclidean norm of every raw row (the prune threshold)
 //   k_xi_rowprep    one CTA per kept row, the row held in shared memory:
 //                   rows_t[i][rr] = row[order[i]] (through the inverse order; FP64 and FP32 copies),
@@ -10,6 +11,29 @@
 #include "kernels.cuh"
 
 namespace sgl {
+
+// flat copy of the caller's rows into device memory: 16-byte loads, four independent ones in flight
+// per thread so that enough bytes are outstanding to cover the link's latency.  `lead` doubles
+// (0 or 1) are copied singly so that the vector part starts on a 16-byte boundary of src.
+__global__ void __launch_bounds__(256)
+k_xi_stage_rows(const double* __restrict__ src, long long n, double* __restrict__ dst, int lead) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < lead && t < n) dst[t] = src[t];
+    const long long nv = (n - lead) / 2;
+    const double2* s2 = (const double2*)(src + lead);
+    double* d = dst + lead;
+    long long i = t;
+    for (; i + 3 * stride < nv; i += 4 * stride) {
+        const double2 a = s2[i], b = s2[i + stride], c = s2[i + 2 * stride], e = s2[i + 3 * stride];
+        d[2 * i] = a.x; d[2 * i + 1] = a.y;
+        d[2 * (i + stride)] = b.x; d[2 * (i + stride) + 1] = b.y;
+        d[2 * (i + 2 * stride)] = c.x; d[2 * (i + 2 * stride) + 1] = c.y;
+        d[2 * (i + 3 * stride)] = e.x; d[2 * (i + 3 * stride) + 1] = e.y;
+    }
+    for (; i < nv; i += stride) { const double2 a = s2[i]; d[2 * i] = a.x; d[2 * i + 1] = a.y; }
+    if (t == 0 && lead + 2 * nv < n) dst[n - 1] = src[n - 1];
+}
 
 __global__ void __launch_bounds__(256)
 k_xi_row_norms(const double* __restrict__ rows, const long long* __restrict__ row_start,
@@ -67,6 +91,13 @@ k_xi_rowprep(const double* __restrict__ rows, const XiPrepRow* __restrict__ kr, 
     }
     dot = block_sum(dot, sh);
     if (threadIdx.x == 0) o.sig[d.row] = dot + xr[d.ne];
+}
+
+void launch_xi_stage_rows(const double* rows, long long n, double* dst, cudaStream_t st) {
+    if (n <= 0) return;
+    const int lead = ((uintptr_t)rows & 15) ? 1 : 0;      // rows is 8-byte aligned (doubles)
+    k_xi_stage_rows<<<152 * 8, 256, 0, st>>>(rows, n, dst, lead);
+    SGL_COUNT(1);
 }
 
 void launch_xi_row_norms(const double* rows, const long long* row_start, const int* row_len, int nrows,
