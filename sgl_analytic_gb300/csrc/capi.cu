@@ -279,7 +279,10 @@ sgl_status run_gemms(sgl_ctx* ctx, std::vector<GemmDesc<T>>& d, const std::strin
     for (auto& g : d) fl += 2.0 * g.M * (double)g.N * g.K;
     {
         Timed t(ctx, std::string(sizeof(T) == 8 ? "gemm_f64_" : "gemm_f32_") + tag, fl, 0.0);
-        launch_grouped_gemm<T>(dd, (int)d.size(), tiles, ctx->stream);
+        int layout = (d[0].a_cs == 1 ? 1 : 0) | (d[0].b_cs == 1 ? 2 : 0);
+        for (auto& g : d)
+            if (((g.a_cs == 1 ? 1 : 0) | (g.b_cs == 1 ? 2 : 0)) != layout) layout = -1;
+        launch_grouped_gemm<T>(dd, (int)d.size(), tiles, layout, ctx->stream);
     }
     CKLAUNCH();
     return SGL_OK;

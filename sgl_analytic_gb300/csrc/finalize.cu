@@ -15,13 +15,23 @@ std::atomic<long long>& launch_counter() {
 }
 
 // ------------------------------------------------------------------ GEMM launchers
+// layout (FP32 only): bit 0 = every A is k-contiguous, bit 1 = every B is j-contiguous, -1 = mixed
 template <typename T>
-void launch_grouped_gemm(const GemmDesc<T>* d_descs, int nprob, int tiles, cudaStream_t st) {
+void launch_grouped_gemm(const GemmDesc<T>* d_descs, int nprob, int tiles, int layout, cudaStream_t st) {
     if (tiles <= 0) return;
+    if constexpr (sizeof(T) == 4) {
+        switch (layout) {
+            case 0: gemm_f32_layout_kernel<false, false><<<tiles, 256, 0, st>>>(d_descs, nprob); SGL_COUNT(1); return;
+            case 1: gemm_f32_layout_kernel<true, false><<<tiles, 256, 0, st>>>(d_descs, nprob); SGL_COUNT(1); return;
+            case 2: gemm_f32_layout_kernel<false, true><<<tiles, 256, 0, st>>>(d_descs, nprob); SGL_COUNT(1); return;
+            case 3: gemm_f32_layout_kernel<true, true><<<tiles, 256, 0, st>>>(d_descs, nprob); SGL_COUNT(1); return;
+            default: break;
+        }
+    }
     { grouped_gemm_kernel<T><<<tiles, 256, 0, st>>>(d_descs, nprob); SGL_COUNT(1); }
 }
-template void launch_grouped_gemm<double>(const GemmDesc<double>*, int, int, cudaStream_t);
-template void launch_grouped_gemm<float>(const GemmDesc<float>*, int, int, cudaStream_t);
+template void launch_grouped_gemm<double>(const GemmDesc<double>*, int, int, int, cudaStream_t);
+template void launch_grouped_gemm<float>(const GemmDesc<float>*, int, int, int, cudaStream_t);
 
 // out(i, j) = sum_s ws[s, i, j] (+ beta out(i, j)); ws slices are dense rows x cols, out has row
 // stride ldo.  Grid (column blocks, rows).  FP64 slices are summed in FP64.  FP32 slices are summed

@@ -197,6 +197,107 @@ grouped_gemm_kernel<float>(const GemmDesc<float>* __restrict__ descs, int nprob)
     }
 }
 
+// FP32 with the operand layouts fixed at compile time (AK: A is k-contiguous, BJ: B is
+// j-contiguous).  Same tiling and summation order as the generic FP32 kernel above, but the
+// per-thread load addresses are one base pointer plus constant strides and the edge predicates
+// are hoisted out of the K loop, which keeps the kernel within 128 registers: two CTAs (16 warps)
+// per SM instead of one.
+template <bool AK, bool BJ>
+__global__ void __launch_bounds__(256, 2)
+gemm_f32_layout_kernel(const GemmDesc<float>* __restrict__ descs, int nprob) {
+    constexpr int BM = 128, BN = 128, BK = 16, PAD = 4;
+    __shared__ __align__(16) float As[2][BK][BM + PAD];
+    __shared__ __align__(16) float Bs[2][BK][BN + PAD];
+    const int tile = blockIdx.x;
+    int p = 0, ph = nprob - 1;
+    while (p < ph) {
+        const int mid = (p + ph + 1) >> 1;
+        if (descs[mid].tile_begin <= tile) p = mid; else ph = mid - 1;
+    }
+    const GemmDesc<float> d = descs[p];
+    const int local = tile - d.tile_begin;
+    const int i0 = (local / d.tiles_n) * BM, j0 = (local % d.tiles_n) * BN;
+    if (i0 >= d.M) return;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    // element u of this thread's share of a tile:
+    //   A: AK ? (row ai + 16u, k ak) : (row ai, k ak + 2u)
+    //   B: BJ ? (k bk + 2u, col bj) : (k bk, col bj + 16u)
+    const int ai = AK ? (tid >> 4) : (tid & 127), ak = AK ? (tid & 15) : (tid >> 7);
+    const int bj = BJ ? (tid & 127) : (tid >> 4), bk = BJ ? (tid >> 7) : (tid & 15);
+    const float* pa = d.A + (long long)(i0 + ai) * d.a_rs + (long long)ak * d.a_cs;
+    const float* pb = d.B + (long long)bk * d.b_rs + (long long)(j0 + bj) * d.b_cs;
+    const long long a_u = AK ? 16 * d.a_rs : 2 * d.a_cs, a_t = (long long)BK * d.a_cs;
+    const long long b_u = BJ ? 2 * d.b_rs : 16 * d.b_cs, b_t = (long long)BK * d.b_rs;
+    unsigned a_ok = 0, b_ok = 0;            // bit u: row / column of element u inside the problem
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        if (i0 + ai + (AK ? 16 * u : 0) < d.M) a_ok |= 1u << u;
+        if (j0 + bj + (BJ ? 0 : 16 * u) < d.N) b_ok |= 1u << u;
+    }
+    float ra[8], rb[8];
+    auto load_tiles = [&](int t) {
+        const int k0 = t * BK;
+        const float* qa = pa + t * a_t;
+        const float* qb = pb + t * b_t;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int gka = k0 + ak + (AK ? 0 : 2 * u);
+            ra[u] = ((a_ok >> u) & 1u) && gka < d.K ? qa[u * a_u] : 0.f;
+            const int gkb = k0 + bk + (BJ ? 2 * u : 0);
+            rb[u] = ((b_ok >> u) & 1u) && gkb < d.K ? qb[u * b_u] : 0.f;
+        }
+    };
+    auto store_tiles = [&](int buf) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (AK) As[buf][ak][ai + 16 * u] = ra[u]; else As[buf][ak + 2 * u][ai] = ra[u];
+            if (BJ) Bs[buf][bk + 2 * u][bj] = rb[u]; else Bs[buf][bk][bj + 16 * u] = rb[u];
+        }
+    };
+    float acc[8][8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
+    const int ntiles = (d.K + BK - 1) / BK;
+    load_tiles(0);
+    store_tiles(0);
+    __syncthreads();
+    for (int t = 0; t < ntiles; ++t) {
+        const int cur = t & 1;
+        if (t + 1 < ntiles) load_tiles(t + 1);
+#pragma unroll
+        for (int k = 0; k < BK; ++k) {
+            const float4 a0 = *reinterpret_cast<const float4*>(&As[cur][k][ty * 4]);
+            const float4 a1 = *reinterpret_cast<const float4*>(&As[cur][k][ty * 4 + 64]);
+            const float4 b0 = *reinterpret_cast<const float4*>(&Bs[cur][k][tx * 4]);
+            const float4 b1 = *reinterpret_cast<const float4*>(&Bs[cur][k][tx * 4 + 64]);
+            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+#pragma unroll
+                for (int c = 0; c < 8; ++c) acc[r][c] = fmaf(av[r], bv[c], acc[r][c]);
+        }
+        if (t + 1 < ntiles) store_tiles(cur ^ 1);
+        __syncthreads();
+    }
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const int gi = i0 + ty * 4 + (r & 3) + (r >> 2) * 64;
+        if (gi >= d.M) continue;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const int gj = j0 + tx * 4 + (c & 3) + (c >> 2) * 64;
+            if (gj >= d.N) continue;
+            float* cp = d.C + (long long)gi * d.ldc + gj;
+            float v = d.alpha * acc[r][c];
+            if (d.beta != 0.f) v += d.beta * *cp;
+            *cp = v;
+        }
+    }
+}
+
 // Host helper: fills tile_begin / tiles_n and returns the total tile count.
 template <typename T>
 inline int gemm_plan(GemmDesc<T>* d, int nprob) {

@@ -35,7 +35,7 @@ void launch_cheb_points(double K, int N, double* t, cudaStream_t st);
 
 // ---- GEMM
 template <typename T>
-void launch_grouped_gemm(const GemmDesc<T>* d_descs, int nprob, int tiles, cudaStream_t st);
+void launch_grouped_gemm(const GemmDesc<T>* d_descs, int nprob, int tiles, int layout, cudaStream_t st);
 template <typename T>
 void launch_sum_slices(const T* ws, int nslices, int rows, int cols, T* out, long long ldo, T beta, cudaStream_t st);
 
