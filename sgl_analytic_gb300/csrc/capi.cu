@@ -2136,7 +2136,12 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
     } else {
         CKS(gemm_splitk<float>(ctx, gd<float>(nkap, ldF, 2 * nk, CS, 2 * nk, 1, F, ldF, 1, P3e, ldF, c), "kappa", 8));
     }
-    launch_p3_finish(P, P3e, nkap, ngam, ldF, d_gam, d_P3, st); CKLAUNCH();
+    float* d_P3f = nullptr;
+    if (P == SGL_MIXED) {
+        d_P3f = dbuf<float>(ctx, "inv_P3f", (size_t)nkap * ngam);
+        if (!d_P3f) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (P3f)");
+    }
+    launch_p3_finish(P, P3e, nkap, ngam, ldF, d_gam, d_P3, d_P3f, st); CKLAUNCH();
     cudaEventRecord(ctx->ev[2], st);
     // ---- path integral on the wide grid and the output grid in one launch
     const int nw = o.n_xi_wide;
@@ -2149,8 +2154,8 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
     const double g_def = std::min(g0, gam_max);
     {
         Timed t(ctx, "path_integral", 0.0, (double)xall.size() * o.n_k_int * 2 * 4 * 8);
-        launch_path_integral(d_P3, nkap, ngam, kap.front(), kap.back(), gam.back(), d_x, (int)xall.size(), gam_max,
-                             g_def, o.n_k_int, d_pi, st);
+        launch_path_integral(d_P3, d_P3f, nkap, ngam, kap.front(), kap.back(), gam.back(), d_x, (int)xall.size(),
+                             gam_max, g_def, o.n_k_int, d_pi, st);
     }
     CKLAUNCH();
     cudaEventRecord(ctx->ev[3], st);

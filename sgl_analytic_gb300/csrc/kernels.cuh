@@ -111,9 +111,9 @@ void launch_em_columns(int precision, const void* Phi, int nk, int nkg, double d
                        cudaStream_t st);
 void launch_window(int precision, void* Phi, int nk, int nkg, const double* wk, const double* wg, cudaStream_t st);
 void launch_p3_finish(int precision, const void* P3ext, int nkap, int ngam, int ld, const double* gam, double* P3,
-                      cudaStream_t st);
-void launch_path_integral(const double* P3, int nkap, int ngam, double kap0, double kap1, double gam1,
-                          const double* xi, int nxi, double gmax, double g_def, int n_k_int, double* out,
+                      float* P3f, cudaStream_t st);
+void launch_path_integral(const double* P3, const float* P3f, int nkap, int ngam, double kap0, double kap1,
+                          double gam1, const double* xi, int nxi, double gmax, double g_def, int n_k_int, double* out,
                           cudaStream_t st);
 
 // ---- tcgen05 grouped GEMM (TF32 hi/lo split, FP32 accumulation in TMEM)
