@@ -531,9 +531,10 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
             for (int a = 0; a < 8; ++a) wlf[(size_t)i * 8 + a] = (float)wl[(size_t)i * 8 + a];
         }
     });
-    // chunks of whole groups: ~4 CTAs per SM over (row tiles x chunks)
+    // chunks of whole groups: one wave of ~8 CTAs per SM over (row tiles x chunks); the mixed
+    // sweep's 4-warp CTAs are latency-bound, so residency is what feeds its pipes
     const int row_tiles = std::max(1, ceil_div(nk, 128));
-    int nchunks = std::max(1, std::min(n_groups, ceil_div(4 * kNumSMs, row_tiles)));
+    int nchunks = std::max(1, std::min(n_groups, 8 * kNumSMs / row_tiles));
     const long long target = std::max(1LL, (N + nchunks - 1) / nchunks);
     std::vector<int> cb{0};
     long long acc = 0;

@@ -115,7 +115,7 @@ constexpr int kSweepRows = 128;
 constexpr int kSweepStage = 64;
 
 template <int MODE, typename TT>
-__global__ void __launch_bounds__(kSweepRows)
+__global__ void __launch_bounds__(kSweepRows, MODE == SGL_FP64 ? 4 : 8)
 k_sep_sweep(const double* __restrict__ kk, int nk, SepDevice sd, TT* __restrict__ Tt,
             double2* __restrict__ A_part) {
     // FP64 path stages (kappa, w, wl) as doubles; the mixed path stages float-float kappa and
