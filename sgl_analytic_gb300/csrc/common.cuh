@@ -41,9 +41,10 @@ __device__ __forceinline__ void sincos_reduced(float r, float& s, float& c) {
     c = fmaf(r2, q, 1.f);
 }
 
-// Mixed path: ph = k * kap in float-float, half-angle reduced mod pi/2 (three float parts of
-// pi/2 with FMA-exact products), FP32 sin / cos of the reduced argument, quadrant fix-up.  Returns sin(ph/2), cos(ph/2) and ph (float-float head + tail).
-__device__ inline void halfangle_sincos_ff(ff k, ff kap, float& s, float& c, float& ph_hi, float& ph_lo) {
+// Mixed path: ph = k * kap in float-float, half angle reduced mod pi/2 (three float parts of
+// pi/2 with FMA-exact products).  Returns the reduced argument r, the quadrant q mod 4 and ph
+// (float-float head + tail): ph/2 = r + q pi/2.
+__device__ __forceinline__ void halfangle_reduce_ff(ff k, ff kap, float& r, int& quad, float& ph_hi, float& ph_lo) {
     const float p = k.hi * kap.hi;
     const float e = fmaf(k.hi, kap.hi, -p);
     const float t = fmaf(k.hi, kap.lo, fmaf(k.lo, kap.hi, e));
@@ -58,15 +59,22 @@ __device__ inline void halfangle_sincos_ff(ff k, ff kap, float& s, float& c, flo
     constexpr float C3 = -1.7151245100058819e-15f;
     const float p1 = q * C1, e1 = fmaf(q, C1, -p1);
     const float p2 = q * C2, e2 = fmaf(q, C2, -p2);
-    float r = xh - p1;
-    r -= e1;
-    r -= p2;
-    r -= e2;
-    r = fmaf(-q, C3, r);
-    r += xl;
+    float rr = xh - p1;
+    rr -= e1;
+    rr -= p2;
+    rr -= e2;
+    rr = fmaf(-q, C3, rr);
+    r = rr + xl;
+    quad = ((int)q) & 3;
+}
+
+// sin(ph/2), cos(ph/2) and ph: the reduction above, the reduced sin / cos and the quadrant fix-up.
+__device__ inline void halfangle_sincos_ff(ff k, ff kap, float& s, float& c, float& ph_hi, float& ph_lo) {
+    float r;
+    int qi;
+    halfangle_reduce_ff(k, kap, r, qi, ph_hi, ph_lo);
     float sr, cr;
     sincos_reduced(r, sr, cr);
-    const int qi = ((int)q) & 3;
     switch (qi) {
         case 0: s = sr;  c = cr;  break;
         case 1: s = cr;  c = -sr; break;

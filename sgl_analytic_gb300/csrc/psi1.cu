@@ -114,31 +114,24 @@ void launch_psi1_direct(const double* kk, int nk, const double* kg, int nkg, con
 constexpr int kSweepRows = 128;
 constexpr int kSweepStage = 64;
 
-template <int MODE, typename TT>
-__global__ void __launch_bounds__(kSweepRows, MODE == SGL_FP64 ? 4 : 8)
-k_sep_sweep(const double* __restrict__ kk, int nk, SepDevice sd, TT* __restrict__ Tt,
-            double2* __restrict__ A_part) {
-    // FP64 path stages (kappa, w, wl) as doubles; the mixed path stages float-float kappa and
-    // float weights (prepared once per plan), so its inner loop issues no FP64 instruction.
-    __shared__ TT s_wl[kSweepStage][8];
-    __shared__ TT s_w[kSweepStage];
-    __shared__ TT s_k0[kSweepStage];
-    __shared__ float s_k1[kSweepStage];
+// FP64 sweep (the parity path).
+__global__ void __launch_bounds__(kSweepRows, 4)
+k_sep_sweep_f64(const double* __restrict__ kk, int nk, SepDevice sd, double* __restrict__ Tt,
+                double2* __restrict__ A_part) {
+    __shared__ double s_wl[kSweepStage][8];
+    __shared__ double s_w[kSweepStage];
+    __shared__ double s_k0[kSweepStage];
     __shared__ int s_grp[kSweepStage];
     const int n = blockIdx.x * kSweepRows + threadIdx.x;
     const bool live = n < nk;
     const double k = live ? kk[n] : 0.0;
-    const ff kf = ff_from_double(k);
     const int c_begin = sd.chunk_begin[blockIdx.y], c_end = sd.chunk_begin[blockIdx.y + 1];
     const long long ld = 2LL * nk;
-
-    double ar = 0.0, ai = 0.0;                       // FP64 path
-    float far = 0.f, fai = 0.f, car = 0.f, cai = 0.f;  // mixed path: Kahan-compensated FP32
-    TT tr[8], ti[8];
+    double ar = 0.0, ai = 0.0;
+    double tr[8], ti[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) { tr[j] = TT(0); ti[j] = TT(0); }
+    for (int j = 0; j < 8; ++j) { tr[j] = 0.0; ti[j] = 0.0; }
     int cur = -1;
-
     auto flush = [&](int g) {
         if (g >= 0 && live) {
             const int col0 = sd.gcol0[g], nc = sd.gncol[g];
@@ -151,71 +144,124 @@ k_sep_sweep(const double* __restrict__ kk, int nk, SepDevice sd, TT* __restrict_
             }
         }
 #pragma unroll
-        for (int j = 0; j < 8; ++j) { tr[j] = TT(0); ti[j] = TT(0); }
+        for (int j = 0; j < 8; ++j) { tr[j] = 0.0; ti[j] = 0.0; }
     };
-
     for (int base = c_begin; base < c_end; base += kSweepStage) {
         const int cnt = min(kSweepStage, c_end - base);
         __syncthreads();
         for (int e = threadIdx.x; e < cnt; e += kSweepRows) {
-            if (MODE == SGL_FP64) { s_k0[e] = (TT)sd.kap[base + e]; s_w[e] = (TT)sd.w[base + e]; }
-            else { s_k0[e] = (TT)sd.kap_hi[base + e]; s_k1[e] = sd.kap_lo[base + e]; s_w[e] = (TT)sd.w_f[base + e]; }
+            s_k0[e] = sd.kap[base + e];
+            s_w[e] = sd.w[base + e];
             s_grp[e] = sd.grp[base + e];
         }
-        for (int e = threadIdx.x; e < cnt * 8; e += kSweepRows) {
-            if (MODE == SGL_FP64) s_wl[e >> 3][e & 7] = (TT)sd.wl[(long long)base * 8 + e];
-            else s_wl[e >> 3][e & 7] = (TT)sd.wl_f[(long long)base * 8 + e];
-        }
+        for (int e = threadIdx.x; e < cnt * 8; e += kSweepRows) s_wl[e >> 3][e & 7] = sd.wl[(long long)base * 8 + e];
         __syncthreads();
         for (int e = 0; e < cnt; ++e) {
             const int g = s_grp[e];
             if (g != cur) { flush(cur); cur = g; }
-            if (MODE == SGL_FP64) {
-                const double w = (double)s_w[e];
-                const double ph = k * (double)s_k0[e];
-                double cm1, smp, sn;
-                compensated_fp64(ph, cm1, smp, sn);
-                ar = fma(w, cm1, ar);
-                ai = fma(w, smp, ai);
-                const double cr = cm1 + 1.0;
+            const double w = s_w[e];
+            const double ph = k * s_k0[e];
+            double cm1, smp, sn;
+            compensated_fp64(ph, cm1, smp, sn);
+            ar = fma(w, cm1, ar);
+            ai = fma(w, smp, ai);
+            const double cr = cm1 + 1.0;
 #pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    const double wj = (double)s_wl[e][j];
-                    tr[j] = (TT)fma(wj, cr, (double)tr[j]);
-                    ti[j] = (TT)fma(wj, sn, (double)ti[j]);
-                }
-            } else {
-                ff kapf; kapf.hi = (float)s_k0[e]; kapf.lo = s_k1[e];
-                float s, c, ph_hi, ph_lo;
-                halfangle_sincos_ff(kf, kapf, s, c, ph_hi, ph_lo);
-                const float cm1 = -2.f * s * s;
-                const float sn = 2.f * s * c;
-                const float ph = ph_hi + ph_lo;
-                float smp;
-                if (fabsf(ph) < 1e-2f) {
-                    const float p2 = ph * ph;
-                    smp = -ph * p2 * (1.f / 6.f) * (1.f - p2 * (1.f / 20.f) * (1.f - p2 * (1.f / 42.f)));
-                } else {
-                    smp = (sn - ph_hi) - ph_lo;
-                }
-                const float wf = (float)s_w[e];
-                float y = fmaf(wf, cm1, -car); float t = far + y; car = (t - far) - y; far = t;
-                y = fmaf(wf, smp, -cai); t = fai + y; cai = (t - fai) - y; fai = t;
-                const float cr = cm1 + 1.f;
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    const float wj = (float)s_wl[e][j];
-                    tr[j] = (TT)fmaf(wj, cr, (float)tr[j]);
-                    ti[j] = (TT)fmaf(wj, sn, (float)ti[j]);
-                }
+            for (int j = 0; j < 8; ++j) {
+                tr[j] = fma(s_wl[e][j], cr, tr[j]);
+                ti[j] = fma(s_wl[e][j], sn, ti[j]);
             }
         }
     }
     flush(cur);
-    if (live) {
-        if (MODE == SGL_FP64) A_part[(long long)blockIdx.y * nk + n] = make_double2(ar, ai);
-        else A_part[(long long)blockIdx.y * nk + n] = make_double2((double)far - (double)car, (double)fai - (double)cai);
+    if (live) A_part[(long long)blockIdx.y * nk + n] = make_double2(ar, ai);
+}
+
+// Mixed sweep: float-float phase, FP32 sin / cos of the reduced half angle, Kahan-compensated
+// FP32 sums for A.  The inner loop is issue-bound, so it is kept short:
+//  * each staged cell is packed as three float4 (kappa head, kappa tail, w, group | 8 weights),
+//    read with three broadcast 16-byte shared loads;
+//  * only sin^2(ph/2) and sin(ph/2) cos(ph/2) are needed, so the quadrant fix-up reduces to
+//    choosing sin or cos for the square and the sign of the product (odd quadrants);
+//  * warps whose rows are all past nk skip the arithmetic (they still stage and synchronise).
+__global__ void __launch_bounds__(kSweepRows, 8)
+k_sep_sweep_mixed(const double* __restrict__ kk, int nk, SepDevice sd, float* __restrict__ Tt,
+                  double2* __restrict__ A_part) {
+    __shared__ float4 s_c[kSweepStage][3];
+    const int n = blockIdx.x * kSweepRows + threadIdx.x;
+    const bool live = n < nk;
+    const bool warp_live = blockIdx.x * kSweepRows + (threadIdx.x & ~31) < nk;
+    const ff kf = ff_from_double(live ? kk[n] : 0.0);
+    const int c_begin = sd.chunk_begin[blockIdx.y], c_end = sd.chunk_begin[blockIdx.y + 1];
+    const long long ld = 2LL * nk;
+    float far = 0.f, fai = 0.f, car = 0.f, cai = 0.f;  // Kahan-compensated FP32
+    float tr[8], ti[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) { tr[j] = 0.f; ti[j] = 0.f; }
+    int cur = -1;
+    auto flush = [&](int g) {
+        if (g >= 0 && live) {
+            const int col0 = sd.gcol0[g], nc = sd.gncol[g];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                if (j < nc) {
+                    Tt[(long long)(col0 + j) * ld + n] = tr[j];
+                    Tt[(long long)(col0 + j) * ld + nk + n] = ti[j];
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) { tr[j] = 0.f; ti[j] = 0.f; }
+    };
+    for (int base = c_begin; base < c_end; base += kSweepStage) {
+        const int cnt = min(kSweepStage, c_end - base);
+        __syncthreads();
+        for (int e = threadIdx.x; e < cnt; e += kSweepRows)
+            s_c[e][0] = make_float4(sd.kap_hi[base + e], sd.kap_lo[base + e], sd.w_f[base + e],
+                                    __int_as_float(sd.grp[base + e]));
+        for (int e = threadIdx.x; e < cnt * 2; e += kSweepRows) {
+            const float* w8 = sd.wl_f + (long long)(base + (e >> 1)) * 8 + (e & 1) * 4;
+            s_c[e >> 1][1 + (e & 1)] = make_float4(w8[0], w8[1], w8[2], w8[3]);
+        }
+        __syncthreads();
+        if (!warp_live) continue;
+        for (int e = 0; e < cnt; ++e) {
+            const float4 h = s_c[e][0];
+            const int g = __float_as_int(h.w);
+            if (g != cur) { flush(cur); cur = g; }
+            ff kapf; kapf.hi = h.x; kapf.lo = h.y;
+            float r, ph_hi, ph_lo;
+            int qi;
+            halfangle_reduce_ff(kf, kapf, r, qi, ph_hi, ph_lo);
+            float sr, cr;
+            sincos_reduced(r, sr, cr);
+            const bool odd = qi & 1;
+            const float a = odd ? cr : sr;                    // |sin(ph/2)|
+            const float cm1 = -2.f * a * a;
+            const float sn = (odd ? -2.f : 2.f) * sr * cr;
+            const float ph = ph_hi + ph_lo;
+            float smp;
+            if (fabsf(ph) < 1e-2f) {
+                const float p2 = ph * ph;
+                smp = -ph * p2 * (1.f / 6.f) * (1.f - p2 * (1.f / 20.f) * (1.f - p2 * (1.f / 42.f)));
+            } else {
+                smp = (sn - ph_hi) - ph_lo;
+            }
+            const float wf = h.z;
+            float y = fmaf(wf, cm1, -car); float t = far + y; car = (t - far) - y; far = t;
+            y = fmaf(wf, smp, -cai); t = fai + y; cai = (t - fai) - y; fai = t;
+            const float crr = cm1 + 1.f;
+            const float4 w0 = s_c[e][1], w1 = s_c[e][2];
+            const float wv[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                tr[j] = fmaf(wv[j], crr, tr[j]);
+                ti[j] = fmaf(wv[j], sn, ti[j]);
+            }
+        }
     }
+    flush(cur);
+    if (live) A_part[(long long)blockIdx.y * nk + n] = make_double2((double)far - (double)car, (double)fai - (double)cai);
 }
 
 // A1[n] = sum over chunks (fixed order) of A_part[chunk, n]
@@ -231,9 +277,9 @@ void launch_sep_sweep(int precision, const double* kk, int nk, const SepDevice& 
                       double2* A_part, double2* A1, cudaStream_t st) {
     dim3 grid(ceil_div(nk, kSweepRows), s.nchunks);
     if (precision == SGL_FP64)
-        { k_sep_sweep<SGL_FP64, double><<<grid, kSweepRows, 0, st>>>(kk, nk, s, (double*)Tt, A_part); SGL_COUNT(1); }
+        { k_sep_sweep_f64<<<grid, kSweepRows, 0, st>>>(kk, nk, s, (double*)Tt, A_part); SGL_COUNT(1); }
     else
-        { k_sep_sweep<SGL_MIXED, float><<<grid, kSweepRows, 0, st>>>(kk, nk, s, (float*)Tt, A_part); SGL_COUNT(1); }
+        { k_sep_sweep_mixed<<<grid, kSweepRows, 0, st>>>(kk, nk, s, (float*)Tt, A_part); SGL_COUNT(1); }
     { k_reduce_chunks<<<ceil_div(nk, 256), 256, 0, st>>>(A_part, s.nchunks, nk, A1); SGL_COUNT(1); }
 }
 
