@@ -279,12 +279,137 @@ k_xi_stageA_pack(XiDevice x, const long long* __restrict__ p_prefix, const long 
     }
 }
 
+// Register-tiled form for groups with at most 256 (4 rr x 4 j) tiles: each thread owns one tile
+// for all 4 p of the CTA (64 FP32 accumulators), so the packed (hi, lo) float4 rows are written
+// straight from registers.  All entries of the 4 p stream through shared memory together, copied
+// with cp.async (warp per entry, no index division) so that a batch costs one memory round trip
+// after its gamma-cell indices are known; the usual <= 96 entries are one batch.  Per-p summation
+// order is that of the form above: the results are identical.
+constexpr int kSA2Ent = 96;
+
+// 4-byte asynchronous global -> shared copy (no register staging, many in flight per thread)
+__device__ __forceinline__ void cp_async4(float* sdst, const float* gsrc) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" :: "r"(sa), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all4() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+__global__ void __launch_bounds__(kSAThreads, 2)
+k_xi_stageA_pack_reg(XiDevice x, const long long* __restrict__ p_prefix, const long long* __restrict__ rowel_off,
+                     const float* __restrict__ J, int nkg, const long long* __restrict__ chunk_prefix,
+                     const TcGemmDesc* __restrict__ descs, float* __restrict__ packed) {
+    extern __shared__ __align__(16) float sa2_sm[];
+    __shared__ int s_q[kSA2Ent];
+    const int rpm = (x.r_max + 3) & ~3, nkp = (nkg + 3) & ~3;
+    float* s_rows = sa2_sm;                                 // [kSA2Ent][rpm]
+    float* s_J = sa2_sm + kSA2Ent * rpm;                    // [kSA2Ent][nkp]
+    const long long cidx = blockIdx.x;
+    const int g = find_group(chunk_prefix, x.n_groups, cidx);
+    const int c4 = (int)(cidx - chunk_prefix[g]);
+    const TcGemmDesc d = descs[g];
+    const int r = x.g_r[g], m = x.g_m[g], nP = x.g_nP[g];
+    const int rp = (r + 3) & ~3;
+    const int M = r * nkg;
+    const int njb = nkp / 4, ntask = (rp / 4) * njb;
+    const long long gp0 = p_prefix[g], ent0 = x.g_ent_off[g];
+    const float* rowsg = x.rows_f + rowel_off[g];
+    const float* Jm = J + (long long)m * x.n_gmc * nkg;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool has_task = tid < ntask;
+    const int rb = has_task ? tid / njb : 0, jb = has_task ? tid % njb : 0;
+    int pb[5];                                              // entry bounds of the 4 p (p >= nP: empty)
+#pragma unroll
+    for (int pp = 0; pp < 5; ++pp) pb[pp] = x.p_ptr[gp0 + min(4 * c4 + pp, nP)];
+    float acc[4][16];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 16; ++b) acc[a][b] = 0.f;
+    for (int eb = pb[0]; eb < pb[4]; eb += kSA2Ent) {
+        const int cnt = min(kSA2Ent, pb[4] - eb);
+        __syncthreads();
+        for (int e = tid; e < cnt; e += kSAThreads) s_q[e] = x.ent_qg[eb + e];
+        __syncthreads();
+        // one round trip for the whole batch: every copy is issued before any is waited on
+        for (int e = warp; e < cnt; e += kSAThreads / 32) {
+            const float* src = rowsg + ((long long)(eb + e) - ent0) * r;
+            for (int rr = lane; rr < rp; rr += 32) {
+                if (rr < r) cp_async4(s_rows + e * rpm + rr, src + rr);
+                else s_rows[e * rpm + rr] = 0.f;
+            }
+            const float* js = Jm + (long long)s_q[e] * nkg;
+            for (int j = lane; j < nkp; j += 32) {
+                if (j < nkg) cp_async4(s_J + e * nkp + j, js + j);
+                else s_J[e * nkp + j] = 0.f;
+            }
+        }
+        cp_async_wait_all4();
+        __syncthreads();
+        if (has_task) {
+#pragma unroll
+            for (int pp = 0; pp < 4; ++pp) {
+                const int e_lo = max(pb[pp], eb) - eb, e_hi = min(pb[pp + 1], eb + cnt) - eb;
+                for (int e = e_lo; e < e_hi; ++e) {
+                    const float4 ra = *(const float4*)(s_rows + e * rpm + 4 * rb);
+                    const float4 jv = *(const float4*)(s_J + e * nkp + 4 * jb);
+                    const float av[4] = {ra.x, ra.y, ra.z, ra.w}, bv[4] = {jv.x, jv.y, jv.z, jv.w};
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+#pragma unroll
+                        for (int w = 0; w < 4; ++w) acc[pp][u * 4 + w] = fmaf(av[u], bv[w], acc[pp][u * 4 + w]);
+                }
+            }
+        }
+    }
+    // packed rows: chunk c of K block kb holds p = 16 kb + 4 c .. + 3
+    const int kb = c4 / 4, c = c4 % 4;
+    float* Ap = packed + d.a_off;
+    const long long pstride = (long long)d.Mpad * 16;
+    float* A_hi = Ap + (2LL * kb) * pstride;
+    float* A_lo = Ap + (2LL * kb + 1) * pstride;
+    if (has_task) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int w = 0; w < 4; ++w) {
+                const int rr = 4 * rb + u, j = 4 * jb + w;
+                if (rr < r && j < nkg) {
+                    const int i = rr * nkg + j;
+                    float hv[4], lv[4];
+#pragma unroll
+                    for (int pp = 0; pp < 4; ++pp) {
+                        const float v = acc[pp][u * 4 + w];
+                        hv[pp] = tf32_rna_sa(v);
+                        lv[pp] = tf32_rna_sa(v - hv[pp]);
+                    }
+                    const long long o = (long long)(i >> 3) * 128 + c * 32 + (i & 7) * 4;
+                    *(float4*)(A_hi + o) = make_float4(hv[0], hv[1], hv[2], hv[3]);
+                    *(float4*)(A_lo + o) = make_float4(lv[0], lv[1], lv[2], lv[3]);
+                }
+            }
+    }
+    for (int i = M + tid; i < d.Mpad; i += kSAThreads) {
+        const long long o = (long long)(i >> 3) * 128 + c * 32 + (i & 7) * 4;
+        *(float4*)(A_hi + o) = make_float4(0.f, 0.f, 0.f, 0.f);
+        *(float4*)(A_lo + o) = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
 void launch_xi_stageA_pack(const XiDevice& x, const long long* d_p_prefix, const float* J, int nkg,
                            const long long* d_chunk_prefix, long long nchunks, const TcGemmDesc* d_descs,
                            float* packed, cudaStream_t st) {
     const long long* rowel_off = d_p_prefix + (x.n_groups + 1);
     const int rmax = x.r_max;
-    const size_t sm = (4ULL * rmax * nkg + (size_t)kSAEnt * (((rmax + 3) & ~3) + ((nkg + 3) & ~3))) * 4;
+    const int rpm = (rmax + 3) & ~3, nkp = (nkg + 3) & ~3;
+    if ((rpm / 4) * (nkp / 4) <= kSAThreads) {
+        const size_t sm = (size_t)kSA2Ent * (rpm + nkp) * 4;
+        cudaFuncSetAttribute(k_xi_stageA_pack_reg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_xi_stageA_pack_reg<<<(unsigned)nchunks, kSAThreads, sm, st>>>(x, d_p_prefix, rowel_off, J, nkg,
+                                                                        d_chunk_prefix, d_descs, packed);
+        SGL_COUNT(1);
+        return;
+    }
+    const size_t sm = (4ULL * rmax * nkg + (size_t)kSAEnt * (rpm + nkp)) * 4;
     cudaFuncSetAttribute(k_xi_stageA_pack, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_xi_stageA_pack<<<(unsigned)nchunks, kSAThreads, sm, st>>>(x, d_p_prefix, rowel_off, J, nkg, d_chunk_prefix,
                                                                 d_descs, packed);
