@@ -856,7 +856,7 @@ sgl_status sep_gemms(sgl_ctx* ctx, int precision, const double* h_kg, const doub
             void* U = ctx->arena.get("cheb_U", (size_t)ld * Nch * sizeof(TT));
             if (!Bc || !L || !U) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (cheb)");
             launch_j0m1_table(precision, d_nodes, S.n_cols_sep, d_t, Nch, Bc, st); CKLAUNCH();
-            launch_cheb_matrix(precision, Kg, Nch, d_kg, nkg, L, st); CKLAUNCH();
+            launch_cheb_matrix(precision, Kg, Nch, d_t, d_kg, nkg, L, st); CKLAUNCH();
             CKS(gemm_splitk<TT>(ctx, gd<TT>((int)ld, Nch, S.n_cols_sep, Tt, 1, ld, Bc, Nch, 1, U, Nch), "sep1", msplit));
             CKS(gemm_splitk<TT>(ctx, gd<TT>((int)ld, nkg, Nch, U, Nch, 1, L, 1, Nch, Gout, nkg), "sep2", msplit));
         } else {

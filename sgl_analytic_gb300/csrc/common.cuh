@@ -43,13 +43,15 @@ __device__ __forceinline__ void sincos_reduced(float r, float& s, float& c) {
 
 // Mixed path: ph = k * kap in float-float, half angle reduced mod pi/2 (three float parts of
 // pi/2 with FMA-exact products).  Returns the reduced argument r, the quadrant q mod 4 and ph
-// (float-float head + tail): ph/2 = r + q pi/2.
-__device__ __forceinline__ void halfangle_reduce_ff(ff k, ff kap, float& r, int& quad, float& ph_hi, float& ph_lo) {
+// (float-float head + tail): scale * ph = r + q pi/2.
+// scale = 0.5 reduces ph/2 (the default), scale = 1 reduces ph itself.
+__device__ __forceinline__ void halfangle_reduce_ff(ff k, ff kap, float& r, int& quad, float& ph_hi, float& ph_lo,
+                                                    float scale = 0.5f) {
     const float p = k.hi * kap.hi;
     const float e = fmaf(k.hi, kap.hi, -p);
     const float t = fmaf(k.hi, kap.lo, fmaf(k.lo, kap.hi, e));
     ph_hi = p; ph_lo = t;
-    const float xh = 0.5f * p, xl = 0.5f * t;
+    const float xh = scale * p, xl = scale * t;
     const float q = rintf(xh * 0.636619772367581343f);   // 2/pi; exact integer for |q| < 2^24
     // x - q pi/2 with pi/2 = C1 + C2 + C3 (float parts); the roundings of q*C1 and q*C2 are
     // recovered exactly with FMA and xh - q*C1 is exact (Sterbenz), so the reduction holds for
@@ -73,6 +75,21 @@ __device__ inline void halfangle_sincos_ff(ff k, ff kap, float& s, float& c, flo
     float r;
     int qi;
     halfangle_reduce_ff(k, kap, r, qi, ph_hi, ph_lo);
+    float sr, cr;
+    sincos_reduced(r, sr, cr);
+    switch (qi) {
+        case 0: s = sr;  c = cr;  break;
+        case 1: s = cr;  c = -sr; break;
+        case 2: s = -sr; c = -cr; break;
+        default: s = -cr; c = sr; break;
+    }
+}
+
+// sin(k kap) and cos(k kap) in FP32 from the float-float phase, reduced exactly (full angle).
+__device__ inline void sincos_ff(ff k, ff kap, float& s, float& c) {
+    float r, ph_hi, ph_lo;
+    int qi;
+    halfangle_reduce_ff(k, kap, r, qi, ph_hi, ph_lo, 1.f);
     float sr, cr;
     sincos_reduced(r, sr, cr);
     switch (qi) {

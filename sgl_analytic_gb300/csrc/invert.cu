@@ -48,11 +48,28 @@ __global__ void k_kappa_matrix(const double* __restrict__ kk, int nk, double dkk
     CS[(long long)i * 2 * nk + nk + n] = (TT)(s * w);
 }
 
+// Mixed path: the same matrix with no FP64 transcendental (float-float phase, exact reduction,
+// FP32 sin / cos of the reduced argument).  One CTA per kappa row.
+__global__ void k_kappa_matrix_ff(const double* __restrict__ kk, int nk, double dkk, const double* __restrict__ kap,
+                                  float* __restrict__ CS) {
+    const int i = blockIdx.x;
+    const ff kf = ff_from_double(kap[i]);
+    const float wf = (float)dkk, wh = (float)(0.5 * dkk);
+    float* row = CS + (long long)i * 2 * nk;
+    for (int n = threadIdx.x; n < nk; n += blockDim.x) {
+        float s, c;
+        sincos_ff(ff_from_double(kk[n]), kf, s, c);
+        const float w = (n == 0 || n == nk - 1) ? wh : wf;
+        row[n] = c * w;
+        row[nk + n] = s * w;
+    }
+}
+
 void launch_kappa_matrix(int precision, const double* kk, int nk, double dkk, const double* kap, int nkap, void* CS,
                          cudaStream_t st) {
     const long long tot = (long long)nkap * nk;
     if (precision == SGL_FP64) { k_kappa_matrix<double><<<ceil_div(tot, 256), 256, 0, st>>>(kk, nk, dkk, kap, nkap, (double*)CS); SGL_COUNT(1); }
-    else { k_kappa_matrix<float><<<ceil_div(tot, 256), 256, 0, st>>>(kk, nk, dkk, kap, nkap, (float*)CS); SGL_COUNT(1); }
+    else if (nkap > 0) { k_kappa_matrix_ff<<<nkap, 256, 0, st>>>(kk, nk, dkk, kap, (float*)CS); SGL_COUNT(1); }
 }
 
 // Euler-Maclaurin endpoint columns (sgl_full.py:277-298): from Phi0 = Phi[:, 0], Phi1 = Phi[:, 1],

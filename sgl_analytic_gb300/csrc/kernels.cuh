@@ -30,7 +30,8 @@ void launch_sep_sweep(int precision, const double* kk, int nk, const SepDevice& 
                       double2* A_part, double2* A1, cudaStream_t st);
 void launch_j0m1_table(int precision, const double* nodes, int nn, const double* x, int nx, void* B,
                        cudaStream_t st);
-void launch_cheb_matrix(int precision, double K, int N, const double* x, int nx, void* L, cudaStream_t st);
+void launch_cheb_matrix(int precision, double K, int N, const double* tpts, const double* x, int nx, void* L,
+                        cudaStream_t st);
 void launch_cheb_points(double K, int N, double* t, cudaStream_t st);
 
 // ---- GEMM

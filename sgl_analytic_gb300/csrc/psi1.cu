@@ -294,20 +294,84 @@ __global__ void k_j0m1_table(const double* __restrict__ nodes, int nn, const dou
     B[e] = (TT)j0m1_d(nodes[r] * x[j]);
 }
 
+// J0(a b) - 1 for the mixed path's FP32 tables, from the float-float product x = a b:
+//  * x < 2: the power series sum_k (-y)^k / (k!)^2, y = x^2 / 4, as -y + (y^2/4) T(y) with y kept
+//    as float-float, so the leading term carries no rounding of its own (<= 1.34 ulp);
+//  * 2 <= x < 12: CUDA's FP64 j0, as in the FP64 tables (the series cancels there and the
+//    asymptotic form has not converged);
+//  * x >= 12: Hankel's asymptotic expansion J0 = sqrt(2/(pi x)) (P cos chi - Q sin chi),
+//    chi = x - pi/4, with the first three terms of P and Q (Abramowitz & Stegun 9.2.5, 9.2.9,
+//    9.2.10 at nu = 0) and x reduced mod pi/2 exactly from the float-float product (<= 1.06 ulp).
+// The bounds were checked against FP64 J0 - 1 over the whole range; the errors are unbiased.
+__device__ float j0m1_mixed(double a, double b) {
+    const ff A = ff_from_double(a), B = ff_from_double(b);
+    const float xh = A.hi * B.hi;
+    const float xe = fmaf(A.hi, B.hi, -xh);
+    const float xl = fmaf(A.hi, B.lo, fmaf(A.lo, B.hi, xe));
+    if (xh < 2.f) {
+        const float x2 = xh * xh;
+        const float yh = 0.25f * x2;
+        const float ye = fmaf(0.5f * xh, xl, 0.25f * fmaf(xh, xh, -x2));
+        float T = 1.f;
+#pragma unroll
+        for (int k = 12; k > 2; --k) T = fmaf(-yh * (1.f / (float)(k * k)), T, 1.f);
+        const float corr = (0.25f * yh * yh) * T;
+        return (corr - ye) - yh;
+    }
+    if (xh < 12.f) return (float)j0m1_d(a * b);
+    float r, ph_hi, ph_lo;
+    int qi;
+    halfangle_reduce_ff(A, B, r, qi, ph_hi, ph_lo, 1.f);
+    float sr, cr;
+    sincos_reduced(r, sr, cr);
+    constexpr float kRsqrt2 = 0.70710678118654752f;
+    const float c = (cr + sr) * kRsqrt2, s = (sr - cr) * kRsqrt2;    // cos, sin of r - pi/4
+    float C, S;                                                          // cos, sin of chi
+    switch (qi) {
+        case 0: C = c;  S = s;  break;
+        case 1: C = -s; S = c;  break;
+        case 2: C = -c; S = -s; break;
+        default: C = s; S = -c; break;
+    }
+    const float iz = 1.f / (8.f * xh), iz2 = iz * iz;
+    float P = fmaf(iz2, -108056025.f / 720.f, 11025.f / 24.f);
+    P = fmaf(iz2, P, -4.5f);
+    P = fmaf(iz2, P, 1.f);
+    float Q = fmaf(iz2, -893025.f / 120.f, 225.f / 6.f);
+    Q = fmaf(iz2, Q, -1.f) * iz;
+    const float amp = sqrtf(0.636619772367581343f / xh);
+    return amp * fmaf(P, C, -Q * S) - 1.f;
+}
+
+__global__ void k_j0m1_table_mixed(const double* __restrict__ nodes, int nn, const double* __restrict__ x, int nx,
+                                   float* __restrict__ B) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)nn * nx) return;
+    const int r = (int)(e / nx), j = (int)(e % nx);
+    B[e] = j0m1_mixed(nodes[r], x[j]);
+}
+
 void launch_j0m1_table(int precision, const double* nodes, int nn, const double* x, int nx, void* B, cudaStream_t st) {
     const long long tot = (long long)nn * nx;
     if (tot == 0) return;
     if (precision == SGL_FP64) { k_j0m1_table<double><<<ceil_div(tot, 256), 256, 0, st>>>(nodes, nn, x, nx, (double*)B); SGL_COUNT(1); }
-    else { k_j0m1_table<float><<<ceil_div(tot, 256), 256, 0, st>>>(nodes, nn, x, nx, (float*)B); SGL_COUNT(1); }
+    else { k_j0m1_table_mixed<<<ceil_div(tot, 256), 256, 0, st>>>(nodes, nn, x, nx, (float*)B); SGL_COUNT(1); }
 }
 
 // Barycentric Chebyshev-Lobatto interpolation matrix L (nx x N): points t_j = K/2 (1 - cos(j pi/(N-1))),
 // weights (-1)^j halved at both ends; a point within 1e-14 K of a node gets the exact unit row.
 // One CTA per row.
+// The points t_j come precomputed (k_cheb_points, the same expression); each row keeps its terms
+// wb / (x - t_j) in shared memory between the sum and the normalisation (the first kChebSmem of
+// them; any beyond are recomputed).
+constexpr int kChebSmem = 4096;
+
 template <typename TT>
 __global__ void __launch_bounds__(256)
-k_cheb_matrix(double K, int N, const double* __restrict__ x, int nx, TT* __restrict__ L) {
+k_cheb_matrix(double K, int N, const double* __restrict__ tpts, const double* __restrict__ x, int nx,
+              TT* __restrict__ L) {
     __shared__ double sh[32];
+    __shared__ double s_q[kChebSmem];
     __shared__ int s_hit;
     const int m = blockIdx.x;
     const double xm = x[m];
@@ -315,31 +379,34 @@ k_cheb_matrix(double K, int N, const double* __restrict__ x, int nx, TT* __restr
     __syncthreads();
     double part = 0.0;
     for (int j = threadIdx.x; j < N; j += blockDim.x) {
-        const double t = 0.5 * K * (1.0 - cos(j * M_PI / (N - 1)));
-        const double d = xm - t;
-        if (fabs(d) <= 1e-14 * K) atomicMax(&s_hit, j);
+        const double d = xm - tpts[j];
+        const bool at = fabs(d) <= 1e-14 * K;
+        if (at) atomicMax(&s_hit, j);
         double wb = (j & 1) ? -1.0 : 1.0;
         if (j == 0 || j == N - 1) wb *= 0.5;
-        part += wb / (fabs(d) <= 1e-14 * K ? 1.0 : d);
+        const double q = wb / (at ? 1.0 : d);
+        if (j < kChebSmem) s_q[j] = q;
+        part += q;
     }
     const double tot = block_sum(part, sh);
     const int hit = s_hit;
     for (int j = threadIdx.x; j < N; j += blockDim.x) {
         double v;
         if (hit >= 0) v = (j == hit) ? 1.0 : 0.0;
+        else if (j < kChebSmem) v = s_q[j] / tot;
         else {
-            const double t = 0.5 * K * (1.0 - cos(j * M_PI / (N - 1)));
             double wb = (j & 1) ? -1.0 : 1.0;
             if (j == 0 || j == N - 1) wb *= 0.5;
-            v = (wb / (xm - t)) / tot;
+            v = (wb / (xm - tpts[j])) / tot;
         }
         L[(long long)m * N + j] = (TT)v;
     }
 }
 
-void launch_cheb_matrix(int precision, double K, int N, const double* x, int nx, void* L, cudaStream_t st) {
-    if (precision == SGL_FP64) { k_cheb_matrix<double><<<nx, 256, 0, st>>>(K, N, x, nx, (double*)L); SGL_COUNT(1); }
-    else { k_cheb_matrix<float><<<nx, 256, 0, st>>>(K, N, x, nx, (float*)L); SGL_COUNT(1); }
+void launch_cheb_matrix(int precision, double K, int N, const double* tpts, const double* x, int nx, void* L,
+                        cudaStream_t st) {
+    if (precision == SGL_FP64) { k_cheb_matrix<double><<<nx, 256, 0, st>>>(K, N, tpts, x, nx, (double*)L); SGL_COUNT(1); }
+    else { k_cheb_matrix<float><<<nx, 256, 0, st>>>(K, N, tpts, x, nx, (float*)L); SGL_COUNT(1); }
 }
 
 __global__ void k_cheb_points(double K, int N, double* __restrict__ t) {
