@@ -272,7 +272,10 @@ void resolve_stats(sgl_ctx* c) {
 template <typename T>
 sgl_status run_gemms(sgl_ctx* ctx, std::vector<GemmDesc<T>>& d, const std::string& tag) {
     if (d.empty()) return SGL_OK;
-    const int tiles = gemm_plan(d.data(), (int)d.size());
+    int tiles = gemm_plan(d.data(), (int)d.size());
+    // FP64 problems too small for one wave of 64 x 64 tiles run on 16 x 16 tiles
+    const bool small = sizeof(T) == 8 && tiles < kNumSMs;
+    if (small) tiles = gemm_plan(d.data(), (int)d.size(), 16, 16);
     DBUF(dd, GemmDesc<T>, "gemm_desc_" + tag, d.size());
     CKS(upload(ctx, dd, d.data(), d.size()));
     double fl = 0.0;
@@ -282,6 +285,7 @@ sgl_status run_gemms(sgl_ctx* ctx, std::vector<GemmDesc<T>>& d, const std::strin
         int layout = (d[0].a_cs == 1 ? 1 : 0) | (d[0].b_cs == 1 ? 2 : 0);
         for (auto& g : d)
             if (((g.a_cs == 1 ? 1 : 0) | (g.b_cs == 1 ? 2 : 0)) != layout) layout = -1;
+        if (small) layout = kSmallTiles;
         launch_grouped_gemm<T>(dd, (int)d.size(), tiles, layout, ctx->stream);
     }
     CKLAUNCH();
@@ -904,6 +908,8 @@ sgl_status lambda_eval(sgl_ctx* ctx, int precision, const double* h_kk, int nk, 
     // the xi term first: its kernels run while the host builds the separable plan (first call
     // for a new kg_max), which has no data dependence on them
     const double* Cre = nullptr; const double* Cim = nullptr;
+    const float* Cf = nullptr;
+    long long nq_f = 0;
     SplineAxis sk, sg;
     int ncg = 0;
     if (use_interp) {
@@ -947,6 +953,16 @@ sgl_status lambda_eval(sgl_ctx* ctx, int precision, const double* h_kk, int nk, 
         launch_spline_basis(d_kg, nkg, kgm, d_kng, n, d_lg, d_bg, st); CKLAUNCH();
         sk.l = d_lk; sk.b = d_bk; sg.l = d_lg; sg.b = d_bg;
         Cre = d_C; Cim = d_C + nq; ncg = n;
+        if (precision == SGL_MIXED && write_phi) {
+            // FP32 copies for the mixed finalize's FP32 spline evaluation
+            DBUF(d_Cf, float, "spl_Cf", 2 * nq);
+            DBUF(d_bkf, float, "spl_bkf", 4 * nk);
+            DBUF(d_bgf, float, "spl_bgf", 4 * nkg);
+            launch_to_float(d_C, d_Cf, 2 * nq, st); CKLAUNCH();
+            launch_to_float(d_bk, d_bkf, 4LL * nk, st); CKLAUNCH();
+            launch_to_float(d_bg, d_bgf, 4LL * nkg, st); CKLAUNCH();
+            sk.bf = d_bkf; sg.bf = d_bgf; Cf = d_Cf; nq_f = nq;
+        }
     }
     const void* G = nullptr;
     const double2* A1 = nullptr;
@@ -986,7 +1002,7 @@ sgl_status lambda_eval(sgl_ctx* ctx, int precision, const double* h_kk, int nk, 
     {
         Timed t(ctx, "finalize", 0.0, (double)npt * 2 * (elem_size(fin_precision) + (write_phi ? elem_size(precision) : 8)));
         launch_finalize(fin_precision, write_phi, G, nk, nkg, A1, d_kk, ctx->V, Cre, Cim, ncg, sk, sg, out_re, out_im,
-                        nkg, st);
+                        nkg, st, Cf, nq_f);
     }
     CKLAUNCH();
     if (exact_xi) {

@@ -15,10 +15,18 @@ std::atomic<long long>& launch_counter() {
 }
 
 // ------------------------------------------------------------------ GEMM launchers
-// layout (FP32 only): bit 0 = every A is k-contiguous, bit 1 = every B is j-contiguous, -1 = mixed
+// layout (FP32): bit 0 = every A is k-contiguous, bit 1 = every B is j-contiguous, -1 = mixed.
+// layout kSmallTiles (FP64): the descriptors were planned with 16 x 16 tiles.
 template <typename T>
 void launch_grouped_gemm(const GemmDesc<T>* d_descs, int nprob, int tiles, int layout, cudaStream_t st) {
     if (tiles <= 0) return;
+    if constexpr (sizeof(T) == 8) {
+        if (layout == kSmallTiles) {
+            gemm_f64_small_kernel<16><<<tiles, 256, 0, st>>>(d_descs, nprob);
+            SGL_COUNT(1);
+            return;
+        }
+    }
     if constexpr (sizeof(T) == 4) {
         switch (layout) {
             case 0: gemm_f32_layout_kernel<false, false><<<tiles, 256, 0, st>>>(d_descs, nprob); SGL_COUNT(1); return;
@@ -163,6 +171,62 @@ __global__ void k_finalize(const TT* __restrict__ G, int nk, int nkg, const doub
     }
 }
 
+__global__ void k_to_float(const double* __restrict__ src, float* __restrict__ dst, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = (float)src[i];
+}
+
+void launch_to_float(const double* src, float* dst, long long n, cudaStream_t st) {
+    if (n > 0) { k_to_float<<<ceil_div(n, 256), 256, 0, st>>>(src, dst, n); SGL_COUNT(1); }
+}
+
+// Mixed path with FP32 spline: the xi term's bicubic spline is a convex combination of its
+// coefficients (B-spline weights >= 0, summing to 1), so FP32 evaluation adds ~1e-7 of |Q| to
+// ln Phi (at most ~4e-8 of Phi, as Phi <= e^{-|Q|}); the sum of the large terms of ln Phi and
+// the reduction of its phase stay FP64.
+__global__ void k_finalize_mixed(const float* __restrict__ G, int nk, int nkg, const double2* __restrict__ A1,
+                                 const double* __restrict__ kk, double V, const float* __restrict__ Cre,
+                                 const float* __restrict__ Cim, int ncg, SplineAxis sk, SplineAxis sg,
+                                 float* __restrict__ out_re, float* __restrict__ out_im, long long ld_out) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = blockIdx.y;
+    if (m >= nkg) return;
+    const long long e = (long long)n * nkg + m;
+    const double k = kk[n];
+    double re = (double)G[e] + A1[n].x - 0.5 * (k * k * V);
+    double im = (double)G[(long long)nk * nkg + e] + A1[n].y;
+    if (Cre != nullptr) {
+        const int lk = sk.l[n], lg = sg.l[m];
+        const float4 bk = *reinterpret_cast<const float4*>(sk.bf + 4 * n);
+        const float4 bg = *reinterpret_cast<const float4*>(sg.bf + 4 * m);
+        const float bka[4] = {bk.x, bk.y, bk.z, bk.w}, bgb[4] = {bg.x, bg.y, bg.z, bg.w};
+        float qr = 0.f, qi = 0.f;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            float rr = 0.f, ri = 0.f;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const long long ci = (long long)(lk + a) * ncg + (lg + b);
+                rr = fmaf(bgb[b], Cre[ci], rr);
+                ri = fmaf(bgb[b], Cim[ci], ri);
+            }
+            qr = fmaf(bka[a], rr, qr);
+            qi = fmaf(bka[a], ri, qi);
+        }
+        re += (double)qr;
+        im += (double)qi;
+    }
+    const double two_pi = 6.283185307179586;
+    const double qn = rint(im * (1.0 / two_pi));
+    const float r = (float)fma(-qn, two_pi, im);
+    float s, c;
+    sincosf(r, &s, &c);
+    const float mag = expf((float)re);
+    const long long eo = (long long)n * ld_out + m;
+    out_re[eo] = mag * c;
+    out_im[eo] = mag * s;
+}
+
 // Mixed path exp: the phase is reduced mod 2 pi in FP64, the rest is FP32.
 template <>
 __global__ void k_finalize<float, 1>(const float* __restrict__ G, int nk, int nkg, const double2* __restrict__ A1,
@@ -209,8 +273,15 @@ __global__ void k_finalize<float, 1>(const float* __restrict__ G, int nk, int nk
 
 void launch_finalize(int precision, int write_phi, const void* G, int nk, int nkg, const double2* A1, const double* kk,
                      double V, const double* C_re, const double* C_im, int ncg, SplineAxis sk, SplineAxis sg,
-                     void* out_re, void* out_im, long long ld_out, cudaStream_t st) {
+                     void* out_re, void* out_im, long long ld_out, cudaStream_t st, const float* Cf, long long nq) {
     dim3 grid(ceil_div(nkg, 128), nk);
+    if (precision == SGL_MIXED && write_phi && (C_re == nullptr || (Cf && sk.bf && sg.bf))) {
+        k_finalize_mixed<<<grid, 128, 0, st>>>((const float*)G, nk, nkg, A1, kk, V, C_re ? Cf : nullptr,
+                                               C_re ? Cf + nq : nullptr, ncg, sk, sg, (float*)out_re,
+                                               (float*)out_im, ld_out);
+        SGL_COUNT(1);
+        return;
+    }
     if (precision == SGL_FP64) {
         if (write_phi) { k_finalize<double, 1><<<grid, 128, 0, st>>>((const double*)G, nk, nkg, A1, kk, V, C_re, C_im, ncg, sk, sg, out_re, out_im, ld_out); SGL_COUNT(1); }
         else { k_finalize<double, 0><<<grid, 128, 0, st>>>((const double*)G, nk, nkg, A1, kk, V, C_re, C_im, ncg, sk, sg, out_re, out_im, ld_out); SGL_COUNT(1); }

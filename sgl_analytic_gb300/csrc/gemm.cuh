@@ -298,14 +298,55 @@ gemm_f32_layout_kernel(const GemmDesc<float>* __restrict__ descs, int nprob) {
     }
 }
 
+// FP64, 16 x 16 output tiles, one output per thread: for problems too small to fill the GPU with
+// 64 x 64 tiles (the 101 x 101 spline-coefficient products).  Each output accumulates over k in
+// the same order as the tiled kernel, so the results are identical.
+template <int B>
+__global__ void __launch_bounds__(B * B)
+gemm_f64_small_kernel(const GemmDesc<double>* __restrict__ descs, int nprob) {
+    __shared__ double As[B][B + 1];
+    __shared__ double Bs[B][B + 1];
+    const int tile = blockIdx.x;
+    int p = 0, ph = nprob - 1;
+    while (p < ph) {
+        const int mid = (p + ph + 1) >> 1;
+        if (descs[mid].tile_begin <= tile) p = mid; else ph = mid - 1;
+    }
+    const GemmDesc<double> d = descs[p];
+    const int local = tile - d.tile_begin;
+    const int i0 = (local / d.tiles_n) * B, j0 = (local % d.tiles_n) * B;
+    if (i0 >= d.M) return;
+    const int tx = threadIdx.x % B, ty = threadIdx.x / B;
+    double acc = 0.0;
+    for (int k0 = 0; k0 < d.K; k0 += B) {
+        {
+            const int gi = i0 + ty, gk = k0 + tx;        // A(i0 + ty, k0 + tx) -> As[tx][ty]
+            As[tx][ty] = (gi < d.M && gk < d.K) ? d.A[(long long)gi * d.a_rs + (long long)gk * d.a_cs] : 0.0;
+            const int gk2 = k0 + ty, gj = j0 + tx;       // B(k0 + ty, j0 + tx) -> Bs[ty][tx]
+            Bs[ty][tx] = (gk2 < d.K && gj < d.N) ? d.B[(long long)gk2 * d.b_rs + (long long)gj * d.b_cs] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < B; ++k) acc = fma(As[k][ty], Bs[k][tx], acc);
+        __syncthreads();
+    }
+    const int gi = i0 + ty, gj = j0 + tx;
+    if (gi < d.M && gj < d.N) {
+        double* cp = d.C + (long long)gi * d.ldc + gj;
+        double v = d.alpha * acc;
+        if (d.beta != 0.0) v += d.beta * *cp;
+        *cp = v;
+    }
+}
+
 // Host helper: fills tile_begin / tiles_n and returns the total tile count.
 template <typename T>
-inline int gemm_plan(GemmDesc<T>* d, int nprob) {
+inline int gemm_plan(GemmDesc<T>* d, int nprob, int bm = GemmCfg<T>::BM, int bn = GemmCfg<T>::BN) {
     int t = 0;
     for (int p = 0; p < nprob; ++p) {
-        d[p].tiles_n = ceil_div(d[p].N, GemmCfg<T>::BN);
+        d[p].tiles_n = ceil_div(d[p].N, bn);
         d[p].tile_begin = t;
-        t += ceil_div(d[p].M, GemmCfg<T>::BM) * d[p].tiles_n;
+        t += ceil_div(d[p].M, bm) * d[p].tiles_n;
     }
     return t;
 }

@@ -35,6 +35,7 @@ void launch_cheb_matrix(int precision, double K, int N, const double* tpts, cons
 void launch_cheb_points(double K, int N, double* t, cudaStream_t st);
 
 // ---- GEMM
+constexpr int kSmallTiles = 100;   // launch_grouped_gemm layout code for 16 x 16 FP64 tiles
 template <typename T>
 void launch_grouped_gemm(const GemmDesc<T>* d_descs, int nprob, int tiles, int layout, cudaStream_t st);
 template <typename T>
@@ -95,13 +96,18 @@ void launch_xi_V(const XiDevice& x, const double* J0m1, int nkg, double* V, int 
 struct SplineAxis {              // per evaluation point: interval l (first coefficient) + 4 weights
     const int* l = nullptr;
     const double* b = nullptr;   // [n * 4]
+    const float* bf = nullptr;   // FP32 copy of b (mixed path), or null
 };
+void launch_to_float(const double* src, float* dst, long long n, cudaStream_t st);
 void launch_spline_basis(const double* x, int n, double xmax, const double* knots, int ncoef, int* l, double* b,
                          cudaStream_t st);
 // out = G + A1[n] - 1/2 kk^2 V + spline(C) ; mode 0: write lnPhi (double planes), mode 1: write Phi (TT planes)
+// Cf (mixed path, optional): FP32 copies of C_re then C_im (2 ncoef_k ncg floats) for an FP32 spline
+// evaluation; sk.bf and sg.bf must then be set too.
 void launch_finalize(int precision, int write_phi, const void* G, int nk, int nkg, const double2* A1, const double* kk,
                      double V, const double* C_re, const double* C_im, int ncg, SplineAxis sk, SplineAxis sg,
-                     void* out_re, void* out_im, long long ld_out, cudaStream_t st);
+                     void* out_re, void* out_im, long long ld_out, cudaStream_t st, const float* Cf = nullptr,
+                     long long nq = 0);
 
 // ---- inversion
 void launch_hankel_matrix(int precision, const double* kg, int nkg, double dkg, const double* gam, int ngam, int ld,
