@@ -110,6 +110,13 @@ struct sgl_ctx {
     // reset whenever the stream has been synchronised
     char* pinned = nullptr;
     size_t pinned_cap = 0, pinned_off = 0;
+    // second stream for the xi term, which runs concurrently with the separable part of ln Phi
+    // (fork / join by events); it has its own pinned staging ring.  swap_side() exchanges the two
+    // so that every helper keeps using ctx->stream / ctx->pinned.
+    cudaStream_t side = nullptr;
+    char* side_pinned = nullptr;
+    size_t side_pinned_cap = 0, side_pinned_off = 0;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // pinned host buffer for the large per-population arrays built on the host (grow-only)
     char* big_pinned = nullptr;
     size_t big_cap = 0;
@@ -161,6 +168,9 @@ T* dbuf(sgl_ctx* ctx, const std::string& name, size_t count) {
 sgl_status sync_stream(sgl_ctx* ctx) {
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->pinned_off = 0;
+    // the other stream's staging ring is reused only once that stream is idle too
+    if (ctx->side && cudaStreamQuery(ctx->side) == cudaSuccess) ctx->side_pinned_off = 0;
+    cudaGetLastError();        // a not-ready query is not an error
     return SGL_OK;
 }
 
@@ -193,6 +203,14 @@ struct HostTimer {
         t0 = t1;
     }
 };
+
+// exchanges the context's stream (and its pinned staging ring) with the side stream
+void swap_side(sgl_ctx* c) {
+    std::swap(c->stream, c->side);
+    std::swap(c->pinned, c->side_pinned);
+    std::swap(c->pinned_cap, c->side_pinned_cap);
+    std::swap(c->pinned_off, c->side_pinned_off);
+}
 
 // fn(lo, hi) over [0, n) in contiguous blocks on up to 16 host threads (results do not depend on
 // the thread count: every index is written by exactly one block)
@@ -258,6 +276,7 @@ struct Timed {
 void resolve_stats(sgl_ctx* c) {
     if (c->pending.empty()) return;
     cudaStreamSynchronize(c->stream);
+    if (c->side) cudaStreamSynchronize(c->side);
     for (auto& p : c->pending) {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, p.a, p.b);
@@ -450,6 +469,7 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
     std::vector<long long> keyv((size_t)N);
     std::vector<double> sl((size_t)N), sh((size_t)N);
     std::vector<char> direct((size_t)N, 0);
+    std::atomic<int> below{0};                 // some cell lies below its gamma bin
     parallel_for(N, [&](long long c0, long long c1) {
         for (long long c = c0; c < c1; ++c) {
             const int b = ctx->ig[(size_t)c];
@@ -462,19 +482,46 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
             sl[(size_t)c] = lo + (double)j * wd / (double)ns;
             sh[(size_t)c] = lo + (double)(j + 1) * wd / (double)ns;
             keyv[(size_t)c] = (long long)b * (kSepSmax + 1) + j;
+            if (j < 0) below = 1;
         }
     });
-    // order: sep cells by (bin, sub-bin) (stable counting sort over the small key range), then
-    // direct cells in original order
-    long long kmax = -1;
-    for (long long c = 0; c < N; ++c) kmax = std::max(kmax, keyv[(size_t)c]);
-    std::vector<long long> cnt((size_t)(kmax + 2), 0), order((size_t)N);
+    // order: sep cells by sub-bin (the reference's np.unique over the sub-bins' lower edges
+    // rounded to 14 decimals, ascending), then direct cells in original order.  A cell whose
+    // gamma lies below its bin (possible in the reference's populations) gets a negative sub-bin
+    // index, as in the reference (truncation toward zero, no lower clamp): its sub-bin lies below
+    // the bin.  Without such cells, (bin, sub-bin) order is the lower-edge order and a stable
+    // counting sort over the small key range gives it; with them, the sub-bins are ranked by
+    // their rounded lower edges.
+    std::vector<long long> order((size_t)N);
     long long n_sep = 0;
-    for (long long c = 0; c < N; ++c) if (!direct[(size_t)c]) { ++cnt[(size_t)keyv[(size_t)c] + 1]; ++n_sep; }
-    for (size_t i = 1; i < cnt.size(); ++i) cnt[i] += cnt[i - 1];
-    for (long long c = 0, d = n_sep; c < N; ++c) {
-        if (direct[(size_t)c]) order[(size_t)d++] = c;
-        else order[(size_t)cnt[(size_t)keyv[(size_t)c]]++] = c;
+    for (long long c = 0; c < N; ++c) n_sep += !direct[(size_t)c];
+    if (!below) {
+        long long kmax = -1;
+        for (long long c = 0; c < N; ++c) kmax = std::max(kmax, keyv[(size_t)c]);
+        std::vector<long long> cnt((size_t)(kmax + 2), 0);
+        for (long long c = 0; c < N; ++c) if (!direct[(size_t)c]) ++cnt[(size_t)keyv[(size_t)c] + 1];
+        for (size_t i = 1; i < cnt.size(); ++i) cnt[i] += cnt[i - 1];
+        for (long long c = 0, d = n_sep; c < N; ++c) {
+            if (direct[(size_t)c]) order[(size_t)d++] = c;
+            else order[(size_t)cnt[(size_t)keyv[(size_t)c]]++] = c;
+        }
+    } else {
+        std::vector<long long> edge((size_t)N, 0);
+        long long d = 0, e = n_sep;
+        for (long long c = 0; c < N; ++c) {
+            if (direct[(size_t)c]) { order[(size_t)e++] = c; continue; }
+            edge[(size_t)c] = std::llrint(sl[(size_t)c] * 1e14);
+            order[(size_t)d++] = c;
+        }
+        std::stable_sort(order.begin(), order.begin() + n_sep,
+                         [&](long long a, long long b) { return edge[(size_t)a] < edge[(size_t)b]; });
+        // dense group keys in that order
+        long long key = -1, prev_edge = 0;
+        for (long long i = 0; i < n_sep; ++i) {
+            const long long c = order[(size_t)i];
+            if (i == 0 || edge[(size_t)c] != prev_edge) { ++key; prev_edge = edge[(size_t)c]; }
+            keyv[(size_t)c] = key;
+        }
     }
     const long long n_dir = N - n_sep;
 
@@ -713,7 +760,7 @@ sgl_status xi_eval(sgl_ctx* ctx, int precision, const double* d_kk, const double
         DBUF(dd, TcGemmDesc, "tc_desc_xi", v.size());
         DBUF(dpk, TcPackDesc, "tc_pack_xi", pk.size());
         DBUF(dcp, long long, "xi_chunk_prefix", chunk_prefix.size());
-        DBUF(packed, float, "tc_packed", std::max<long long>(pfl, 1));
+        DBUF(packed, float, "tc_packed_xi", std::max<long long>(pfl, 1));
         CKS(upload(ctx, dd, v.data(), v.size()));
         CKS(upload(ctx, dpk, pk.data(), pk.size()));
         CKS(upload(ctx, dcp, chunk_prefix.data(), chunk_prefix.size()));
@@ -890,7 +937,7 @@ sgl_status sep_gemms(sgl_ctx* ctx, int precision, const double* h_kg, const doub
 // write_phi = 1 writes Phi = exp(ln Phi) in the precision's element type (inversion path).
 sgl_status lambda_eval(sgl_ctx* ctx, int precision, const double* h_kk, int nk, const double* h_kg, int nkg,
                        int write_phi, void* out_re, void* out_im) {
-    const cudaStream_t st = ctx->stream;
+    cudaStream_t st = ctx->stream;
     const long long npt = (long long)nk * nkg;
     DBUF(d_kk, double, "grid_kk", nk);
     DBUF(d_kg, double, "grid_kg", nkg);
@@ -905,13 +952,23 @@ sgl_status lambda_eval(sgl_ctx* ctx, int precision, const double* h_kk, int nk, 
     const bool exact_xi = xi_active && !use_interp;
     if (exact_xi && write_phi) return fail(ctx, SGL_ERR_UNSUPPORTED, "exact xi term on an inversion grid");
 
-    // the xi term first: its kernels run while the host builds the separable plan (first call
-    // for a new kg_max), which has no data dependence on them
+    // the xi term first, on the side stream when the separable part follows: its kernels run
+    // while the host builds the separable plan (first call for a new kg_max) and concurrently
+    // with the separable kernels, which have no data dependence on them.  Profiling keeps one
+    // stream so that every kernel is timed alone.
     const double* Cre = nullptr; const double* Cim = nullptr;
     const float* Cf = nullptr;
     long long nq_f = 0;
     SplineAxis sk, sg;
     int ncg = 0;
+    const bool fork = use_interp && use_sep && ctx->side && !ctx->profiling && !ctx->vp_on;
+    if (fork) {
+        CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
+        CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+        swap_side(ctx);
+        st = ctx->stream;
+    }
+    const sgl_status xi_status = [&]() -> sgl_status {
     if (use_interp) {
         SplineHost& Sg = ctx->splines[n];
         SplineHost& Sk = ctx->splines[nkc];
@@ -964,6 +1021,16 @@ sgl_status lambda_eval(sgl_ctx* ctx, int precision, const double* h_kk, int nk, 
             sk.bf = d_bkf; sg.bf = d_bgf; Cf = d_Cf; nq_f = nq;
         }
     }
+    return SGL_OK;
+    }();
+    if (fork) {
+        // join point recorded even when the xi part failed, so the main stream never waits on
+        // an event from an earlier call
+        cudaEventRecord(ctx->ev_join, ctx->stream);
+        swap_side(ctx);
+        st = ctx->stream;
+    }
+    CKS(xi_status);
     const void* G = nullptr;
     const double2* A1 = nullptr;
     int fin_precision = precision;
@@ -998,6 +1065,7 @@ sgl_status lambda_eval(sgl_ctx* ctx, int precision, const double* h_kk, int nk, 
         G = d_dir; A1 = d_zero; fin_precision = SGL_FP64;
     }
 
+    if (fork) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
     if (write_phi && fin_precision != precision) return fail(ctx, SGL_ERR_UNSUPPORTED, "inversion grid below 2e5 points");
     {
         Timed t(ctx, "finalize", 0.0, (double)npt * 2 * (elem_size(fin_precision) + (write_phi ? elem_size(precision) : 8)));
@@ -1082,6 +1150,12 @@ sgl_status sgl_ctx_create(int device, sgl_ctx** out) {
         g_create_error = "stream creation failed"; delete ctx; return SGL_ERR_CUDA;
     }
     for (auto& ev : ctx->ev) cudaEventCreate(&ev);
+    if (cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        ctx->side = nullptr;          // no second stream: the xi term runs in order on the first
+        cudaGetLastError();
+    }
     {
         int pa = 0, pt = 0;
         cudaDeviceGetAttribute(&pa, cudaDevAttrPageableMemoryAccess, device);
@@ -1094,6 +1168,13 @@ sgl_status sgl_ctx_create(int device, sgl_ctx** out) {
         ctx->pinned = nullptr; ctx->pinned_cap = 0;
         cudaGetLastError();
     }
+    if (ctx->side) {
+        ctx->side_pinned_cap = 4u << 20;
+        if (cudaHostAlloc((void**)&ctx->side_pinned, ctx->side_pinned_cap, cudaHostAllocDefault) != cudaSuccess) {
+            ctx->side_pinned = nullptr; ctx->side_pinned_cap = 0;
+            cudaGetLastError();
+        }
+    }
     *out = ctx;
     return SGL_OK;
 }
@@ -1102,12 +1183,17 @@ void sgl_ctx_destroy(sgl_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    if (ctx->side) cudaStreamSynchronize(ctx->side);
     ctx->arena.release();
     for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
     resolve_stats(ctx);
     for (auto& ev : ctx->ev_pool) cudaEventDestroy(ev);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->big_pinned) cudaFreeHost(ctx->big_pinned);
+    if (ctx->side_pinned) cudaFreeHost(ctx->side_pinned);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -1170,6 +1256,9 @@ sgl_status sgl_lam_set_cells(sgl_ctx* ctx, int64_t n_cells, const double* w0, co
     if (n_cells < 0 || (n_cells > 0 && (!w0 || !k0 || !g0 || !ig)) || !fe_g || n_fe_g < 2)
         return fail(ctx, SGL_ERR_VALUE, "invalid cell arrays");
     if (!std::isfinite(V)) return fail(ctx, SGL_ERR_VALUE, "V must be finite");
+    for (int i = 0; i + 1 < n_fe_g; ++i)
+        if (!(fe_g[i + 1] > fe_g[i]) || !std::isfinite(fe_g[i + 1]))
+            return fail(ctx, SGL_ERR_VALUE, "gamma bin edges must be finite and increasing");
     for (int64_t c = 0; c < n_cells; ++c) {
         if (!std::isfinite(w0[c]) || !std::isfinite(k0[c]) || !std::isfinite(g0[c]))
             return fail(ctx, SGL_ERR_VALUE, "non-finite cell value");

@@ -60,6 +60,29 @@ def test_psi1_separable_full_width(lam1, ref_sub):
     assert np.max(np.abs(L[::2, ::32] - ref_sub["psi1_grid"])) <= TOL_LN
 
 
+def test_cells_below_their_gamma_bin(pop_sub):
+    """Cells whose gamma lies below their bin's lower edge (the reference's z_s = 10 population
+    has two: gamma = 0 in a bin starting at 2.9e-3, and 7e-10 in [1e-9, 1.08e-9)).  The separable
+    plan keeps the reference's negative sub-bin index (truncation toward zero, no lower clamp) and
+    orders the sub-bins by their lower edges; the GPU matches the oracle's separable form."""
+    import dataclasses
+
+    from oracle import lam_oracle as LO
+    from sgl_analytic_gb300 import Lam
+    g0 = pop_sub.g0.copy()
+    lo = pop_sub.fe_g[pop_sub.ig]
+    c0 = int(np.argmax(lo))                    # highest bin: gamma = 0 lies many sub-bins below
+    c1 = int(np.argmax(np.where(pop_sub.ig == np.median(pop_sub.ig).astype(int), lo, -1.0)))
+    g0[c0] = 0.0
+    g0[c1] = 0.7 * lo[c1]
+    assert np.sum(g0 < lo) == 2
+    pop = dataclasses.replace(pop_sub, g0=g0)
+    L = Lam(pop, xi=False)(KK16, KG_FULL)
+    O = LO.OracleLam(pop.w0, pop.k0, g0, pop.ig, pop.fe_g, pop.V, None, method="sep")
+    Lo = O(KK16, KG_FULL)
+    assert _ln_close(L[::3, ::17], Lo[::3, ::17])
+
+
 def test_psi1_separable_mixed_precision(lam1, ref_sub):
     from sgl_analytic_gb300._lib import SGL_MIXED
     Lm = lam1.engine.lnphi(KK16, KG_FULL, SGL_MIXED)[::2, ::32]
