@@ -405,7 +405,7 @@ sgl_status gemm_splitk_simt(sgl_ctx* ctx, GemmDesc<T> g, const std::string& tag,
 
 // FP32 on the tensor cores.  K split into >= min_split slices (FP32 accumulation in TMEM within a
 // slice), slices combined in FP64 by the fixed-order sum.
-sgl_status gemm_splitk_tc(sgl_ctx* ctx, GemmDesc<float> g, const std::string& tag, int min_split) {
+sgl_status gemm_splitk_tc(sgl_ctx* ctx, GemmDesc<float> g, const std::string& tag, int min_split, int parts = 3) {
     int split = std::max(1, std::min(min_split, std::max(1, g.K / 32)));
     const long long slice = (long long)g.M * g.N;
     const bool direct = split == 1 && g.beta == 0.f;
@@ -428,7 +428,7 @@ sgl_status gemm_splitk_tc(sgl_ctx* ctx, GemmDesc<float> g, const std::string& ta
         t.alpha = g.alpha;
         v.push_back(t);
     }
-    CKS(run_tc_gemms(ctx, v, tag, 3));
+    CKS(run_tc_gemms(ctx, v, tag, parts));
     if (!direct) {
         launch_sum_slices<float>(ws, (int)v.size(), g.M, g.N, g.C, g.ldc, g.beta, ctx->stream);
         CKLAUNCH();
@@ -1083,8 +1083,10 @@ sgl_status lambda_eval(sgl_ctx* ctx, int precision, const double* h_kk, int nk, 
 }
 
 // Direct evaluation on a small grid into HOST planes (Lam._direct_call for < 200000 points).
+// precision SGL_MIXED: the Psi_1 sums from FP32 terms (k-reach probes of the mixed path); the xi
+// term stays FP64.
 sgl_status lambda_direct(sgl_ctx* ctx, const double* h_kk, int nk, const double* h_kg, int nkg, double* re,
-                         double* im) {
+                         double* im, int precision = SGL_FP64) {
     const cudaStream_t st = ctx->stream;
     const long long npt = (long long)nk * nkg;
     DBUF(d_kk, double, "dir_kk", nk);
@@ -1096,7 +1098,8 @@ sgl_status lambda_direct(sgl_ctx* ctx, const double* h_kk, int nk, const double*
     const double* d_g0 = (const double*)ctx->arena.find("cells_g0");
     const double* d_w0 = (const double*)ctx->arena.find("cells_w0");
     DBUF(d_dpart, double2, "direct_part", (long long)std::max(1, psi1_direct_chunks((int64_t)ctx->w0.size())) * npt);
-    launch_psi1_direct(d_kk, nk, d_kg, nkg, d_k0, d_g0, d_w0, (int64_t)ctx->w0.size(), d_out, d_out + npt, d_dpart, st);
+    launch_psi1_direct(d_kk, nk, d_kg, nkg, d_k0, d_g0, d_w0, (int64_t)ctx->w0.size(), d_out, d_out + npt, d_dpart, st,
+                       precision);
     CKLAUNCH();
     bool xi = false;
     if (ctx->xi.on || ctx->vp_on) {
@@ -2146,8 +2149,8 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
         std::vector<double> ks(nprobe), re(nprobe), im(nprobe);
         for (int j = 0; j < nprobe; ++j) ks[j] = k0v * std::pow(1.25, (double)j);
         const double zero = 0.0;
-        if (ax == 0) CKS(lambda_direct(ctx, ks.data(), nprobe, &zero, 1, re.data(), im.data()));
-        else CKS(lambda_direct(ctx, &zero, 1, ks.data(), nprobe, re.data(), im.data()));
+        if (ax == 0) CKS(lambda_direct(ctx, ks.data(), nprobe, &zero, 1, re.data(), im.data(), o.precision));
+        else CKS(lambda_direct(ctx, &zero, 1, ks.data(), nprobe, re.data(), im.data(), o.precision));
         int pick = -1, amin = 0;
         double best = 1e300;
         for (int j = 0; j < nprobe; ++j) {
@@ -2233,8 +2236,10 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
     } else {
         // F = Phi M_hi + Phi M_lo (split Hankel matrix)
         CKS(gemm_splitk<float>(ctx, gd<float>(2 * nk, ngam, nkg, Phi, nkg, 1, M, ldF, 1, F, ldF), "hankel", 8));
-        CKS(gemm_splitk<float>(ctx, gd<float>(2 * nk, ngam, nkg, Phi, nkg, 1, (const float*)M + (size_t)nkg * ldF, ldF,
-                                              1, F, ldF, 1.0, 1.0), "hankel_lo", 8));
+        // the M_lo term is a correction of relative size 2^-24: BF16 operands on the tensor cores
+        // carry it to ~0.4%, i.e. ~2e-10 of F
+        CKS(gemm_splitk_tc(ctx, gd<float>(2 * nk, ngam, nkg, Phi, nkg, 1, (const float*)M + (size_t)nkg * ldF, ldF,
+                                          1, F, ldF, 1.0, 1.0), "hankel_lo", 1, 1));
     }
     launch_em_columns(P, Phi, nk, nkg, dkg, F, ldF, ngam, st); CKLAUNCH();
     if (P == SGL_FP64) {

@@ -25,7 +25,7 @@ struct SepDevice {
 int psi1_direct_chunks(int64_t nc);
 void launch_psi1_direct(const double* kk, int nk, const double* kg, int nkg, const double* k0,
                         const double* g0, const double* w0, int64_t nc, double* re, double* im,
-                        double2* part, cudaStream_t st);
+                        double2* part, cudaStream_t st, int precision = SGL_FP64);
 void launch_sep_sweep(int precision, const double* kk, int nk, const SepDevice& s, void* Tt,
                       double2* A_part, double2* A1, cudaStream_t st);
 void launch_j0m1_table(int precision, const double* nodes, int nn, const double* x, int nx, void* B,

@@ -26,6 +26,55 @@ __device__ inline void compensated_fp64(double ph, double& cm1, double& smp, dou
     }
 }
 
+// J0(a b) - 1 for the mixed path's FP32 tables, from the float-float product x = a b:
+//  * x < 2: the power series sum_k (-y)^k / (k!)^2, y = x^2 / 4, as -y + (y^2/4) T(y) with y kept
+//    as float-float, so the leading term carries no rounding of its own (<= 1.34 ulp);
+//  * 2 <= x < 12: CUDA's FP64 j0, as in the FP64 tables (the series cancels there and the
+//    asymptotic form has not converged);
+//  * x >= 12: Hankel's asymptotic expansion J0 = sqrt(2/(pi x)) (P cos chi - Q sin chi),
+//    chi = x - pi/4, with the first three terms of P and Q (Abramowitz & Stegun 9.2.5, 9.2.9,
+//    9.2.10 at nu = 0) and x reduced mod pi/2 exactly from the float-float product (<= 1.06 ulp).
+// The bounds were checked against FP64 J0 - 1 over the whole range; the errors are unbiased.
+__device__ float j0m1_mixed(double a, double b) {
+    const ff A = ff_from_double(a), B = ff_from_double(b);
+    const float xh = A.hi * B.hi;
+    const float xe = fmaf(A.hi, B.hi, -xh);
+    const float xl = fmaf(A.hi, B.lo, fmaf(A.lo, B.hi, xe));
+    if (xh < 2.f) {
+        const float x2 = xh * xh;
+        const float yh = 0.25f * x2;
+        const float ye = fmaf(0.5f * xh, xl, 0.25f * fmaf(xh, xh, -x2));
+        float T = 1.f;
+#pragma unroll
+        for (int k = 12; k > 2; --k) T = fmaf(-yh * (1.f / (float)(k * k)), T, 1.f);
+        const float corr = (0.25f * yh * yh) * T;
+        return (corr - ye) - yh;
+    }
+    if (xh < 12.f) return (float)j0m1_d(a * b);
+    float r, ph_hi, ph_lo;
+    int qi;
+    halfangle_reduce_ff(A, B, r, qi, ph_hi, ph_lo, 1.f);
+    float sr, cr;
+    sincos_reduced(r, sr, cr);
+    constexpr float kRsqrt2 = 0.70710678118654752f;
+    const float c = (cr + sr) * kRsqrt2, s = (sr - cr) * kRsqrt2;    // cos, sin of r - pi/4
+    float C, S;                                                          // cos, sin of chi
+    switch (qi) {
+        case 0: C = c;  S = s;  break;
+        case 1: C = -s; S = c;  break;
+        case 2: C = -c; S = -s; break;
+        default: C = s; S = -c; break;
+    }
+    const float iz = 1.f / (8.f * xh), iz2 = iz * iz;
+    float P = fmaf(iz2, -108056025.f / 720.f, 11025.f / 24.f);
+    P = fmaf(iz2, P, -4.5f);
+    P = fmaf(iz2, P, 1.f);
+    float Q = fmaf(iz2, -893025.f / 120.f, 225.f / 6.f);
+    Q = fmaf(iz2, Q, -1.f) * iz;
+    const float amp = sqrtf(0.636619772367581343f / xh);
+    return amp * fmaf(P, C, -Q * S) - 1.f;
+}
+
 // ------------------------------------------------------------------ direct sum
 // CTA (output point, cell chunk); threads stride over the chunk's cells; deterministic block sum
 // into part[chunk, point]; a second kernel sums the chunks in a fixed order.
@@ -81,6 +130,58 @@ k_psi1_direct(const double* __restrict__ kk, int nk, const double* __restrict__ 
     if (threadIdx.x == 0) part[(long long)blockIdx.y * gridDim.x + pt] = make_double2(re, im);
 }
 
+// Mixed direct sum for the k-reach probes (and other small grids): the terms in FP32 from the
+// float-float phase (exact reduction) and the FP32 J0 - 1 of the tables, accumulated in FP64.  On
+// the two probe lines one of the factors is exactly 1 (k_gamma = 0: J0 = 1; k_kappa = 0: no
+// phase), and only that factor's work is done.
+__global__ void __launch_bounds__(256)
+k_psi1_direct_mixed(const double* __restrict__ kk, int nk, const double* __restrict__ kg, int nkg,
+                    const double* __restrict__ k0, const double* __restrict__ g0,
+                    const double* __restrict__ w0, int64_t nc, double2* __restrict__ part) {
+    __shared__ double sh[32];
+    const int pt = blockIdx.x;
+    const int n = pt / nkg, m = pt % nkg;
+    const double k = kk[n], g = kg[m];
+    const ff kf = ff_from_double(k);
+    const int64_t c0 = (int64_t)blockIdx.y * kDirectChunkCells;
+    const int64_t c1 = c0 + kDirectChunkCells < nc ? c0 + kDirectChunkCells : nc;
+    double re = 0.0, im = 0.0;
+    for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+        const double w = w0[c];
+        float cm1 = 0.f, smp = 0.f, ph = 0.f;
+        if (k != 0.0) {
+            float r, ph_hi, ph_lo;
+            int qi;
+            halfangle_reduce_ff(kf, ff_from_double(k0[c]), r, qi, ph_hi, ph_lo);
+            float sr, cr;
+            sincos_reduced(r, sr, cr);
+            const bool odd = qi & 1;
+            const float a = odd ? cr : sr;
+            cm1 = -2.f * a * a;
+            const float sn = (odd ? -2.f : 2.f) * sr * cr;
+            ph = ph_hi + ph_lo;
+            if (fabsf(ph) < 1e-2f) {
+                const float p2 = ph * ph;
+                smp = -ph * p2 * (1.f / 6.f) * (1.f - p2 * (1.f / 20.f) * (1.f - p2 * (1.f / 42.f)));
+            } else {
+                smp = (sn - ph_hi) - ph_lo;
+            }
+        }
+        if (g == 0.0) {
+            re = fma(w, (double)cm1, re);
+            im = fma(w, (double)smp, im);
+        } else {
+            const float B = j0m1_mixed(g, g0[c]);
+            // (cos-1) J + (J-1) and (sin-ph) J + ph (J-1), J = 1 + B
+            re = fma(w, (double)fmaf(cm1, 1.f + B, B), re);
+            im = fma(w, (double)fmaf(smp, 1.f + B, ph * B), im);
+        }
+    }
+    re = block_sum(re, sh);
+    im = block_sum(im, sh);
+    if (threadIdx.x == 0) part[(long long)blockIdx.y * gridDim.x + pt] = make_double2(re, im);
+}
+
 __global__ void k_direct_reduce(const double2* __restrict__ part, int nchunks, int npt, double* __restrict__ re,
                                 double* __restrict__ im) {
     const int pt = blockIdx.x * blockDim.x + threadIdx.x;
@@ -95,12 +196,13 @@ int psi1_direct_chunks(int64_t nc) { return (int)((nc + kDirectChunkCells - 1) /
 
 void launch_psi1_direct(const double* kk, int nk, const double* kg, int nkg, const double* k0,
                         const double* g0, const double* w0, int64_t nc, double* re, double* im,
-                        double2* part, cudaStream_t st) {
+                        double2* part, cudaStream_t st, int precision) {
     const int npt = nk * nkg;
     if (npt == 0) return;
     const int nch = psi1_direct_chunks(nc) > 0 ? psi1_direct_chunks(nc) : 1;
     dim3 grid(npt, nch);
-    { k_psi1_direct<<<grid, 256, 0, st>>>(kk, nk, kg, nkg, k0, g0, w0, nc, part); SGL_COUNT(1); }
+    if (precision == SGL_MIXED) { k_psi1_direct_mixed<<<grid, 256, 0, st>>>(kk, nk, kg, nkg, k0, g0, w0, nc, part); SGL_COUNT(1); }
+    else { k_psi1_direct<<<grid, 256, 0, st>>>(kk, nk, kg, nkg, k0, g0, w0, nc, part); SGL_COUNT(1); }
     { k_direct_reduce<<<ceil_div(npt, 256), 256, 0, st>>>(part, nch, npt, re, im); SGL_COUNT(1); }
 }
 
@@ -292,55 +394,6 @@ __global__ void k_j0m1_table(const double* __restrict__ nodes, int nn, const dou
     if (e >= (long long)nn * nx) return;
     const int r = (int)(e / nx), j = (int)(e % nx);
     B[e] = (TT)j0m1_d(nodes[r] * x[j]);
-}
-
-// J0(a b) - 1 for the mixed path's FP32 tables, from the float-float product x = a b:
-//  * x < 2: the power series sum_k (-y)^k / (k!)^2, y = x^2 / 4, as -y + (y^2/4) T(y) with y kept
-//    as float-float, so the leading term carries no rounding of its own (<= 1.34 ulp);
-//  * 2 <= x < 12: CUDA's FP64 j0, as in the FP64 tables (the series cancels there and the
-//    asymptotic form has not converged);
-//  * x >= 12: Hankel's asymptotic expansion J0 = sqrt(2/(pi x)) (P cos chi - Q sin chi),
-//    chi = x - pi/4, with the first three terms of P and Q (Abramowitz & Stegun 9.2.5, 9.2.9,
-//    9.2.10 at nu = 0) and x reduced mod pi/2 exactly from the float-float product (<= 1.06 ulp).
-// The bounds were checked against FP64 J0 - 1 over the whole range; the errors are unbiased.
-__device__ float j0m1_mixed(double a, double b) {
-    const ff A = ff_from_double(a), B = ff_from_double(b);
-    const float xh = A.hi * B.hi;
-    const float xe = fmaf(A.hi, B.hi, -xh);
-    const float xl = fmaf(A.hi, B.lo, fmaf(A.lo, B.hi, xe));
-    if (xh < 2.f) {
-        const float x2 = xh * xh;
-        const float yh = 0.25f * x2;
-        const float ye = fmaf(0.5f * xh, xl, 0.25f * fmaf(xh, xh, -x2));
-        float T = 1.f;
-#pragma unroll
-        for (int k = 12; k > 2; --k) T = fmaf(-yh * (1.f / (float)(k * k)), T, 1.f);
-        const float corr = (0.25f * yh * yh) * T;
-        return (corr - ye) - yh;
-    }
-    if (xh < 12.f) return (float)j0m1_d(a * b);
-    float r, ph_hi, ph_lo;
-    int qi;
-    halfangle_reduce_ff(A, B, r, qi, ph_hi, ph_lo, 1.f);
-    float sr, cr;
-    sincos_reduced(r, sr, cr);
-    constexpr float kRsqrt2 = 0.70710678118654752f;
-    const float c = (cr + sr) * kRsqrt2, s = (sr - cr) * kRsqrt2;    // cos, sin of r - pi/4
-    float C, S;                                                          // cos, sin of chi
-    switch (qi) {
-        case 0: C = c;  S = s;  break;
-        case 1: C = -s; S = c;  break;
-        case 2: C = -c; S = -s; break;
-        default: C = s; S = -c; break;
-    }
-    const float iz = 1.f / (8.f * xh), iz2 = iz * iz;
-    float P = fmaf(iz2, -108056025.f / 720.f, 11025.f / 24.f);
-    P = fmaf(iz2, P, -4.5f);
-    P = fmaf(iz2, P, 1.f);
-    float Q = fmaf(iz2, -893025.f / 120.f, 225.f / 6.f);
-    Q = fmaf(iz2, Q, -1.f) * iz;
-    const float amp = sqrtf(0.636619772367581343f / xh);
-    return amp * fmaf(P, C, -Q * S) - 1.f;
 }
 
 __global__ void k_j0m1_table_mixed(const double* __restrict__ nodes, int nn, const double* __restrict__ x, int nx,
