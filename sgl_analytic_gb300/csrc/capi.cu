@@ -5,7 +5,9 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <functional>
+#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -13,6 +15,8 @@
 #include <thread>
 #include <unordered_map>
 #include <vector>
+
+#include <unistd.h>
 
 #include "kernels.cuh"
 
@@ -81,6 +85,15 @@ struct Pending { std::string tag; cudaEvent_t a, b; double flops, bytes; };
 
 }  // namespace
 
+// host scratch of the separable plan, reused between plans (sizes follow the cell count)
+struct SepScratch {
+    std::vector<long long> keyv, order;
+    std::vector<double> sl, sh, kap, w, wl;
+    std::vector<char> direct;
+    std::vector<float> kh, kl, wf, wlf;
+    std::vector<int> grp;
+};
+
 struct sgl_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -93,6 +106,7 @@ struct sgl_ctx {
     bool has_cells = false;
     SepHost sep;
     SepDevice sepd;
+    SepScratch sep_scratch;
     int sep_precision_ready = -1;
     XiHost xi;
     XiDevice xid;
@@ -212,19 +226,96 @@ void swap_side(sgl_ctx* c) {
     std::swap(c->pinned_off, c->side_pinned_off);
 }
 
-// fn(lo, hi) over [0, n) in contiguous blocks on up to 16 host threads (results do not depend on
-// the thread count: every index is written by exactly one block)
-void parallel_for(long long n, const std::function<void(long long, long long)>& fn) {
-    const int nthr = (int)std::max(1LL, std::min<long long>({16LL, (long long)std::thread::hardware_concurrency(),
-                                                            (n + 4095) / 4096}));
-    if (nthr == 1) { fn(0, n); return; }
-    std::vector<std::thread> th;
-    const long long blk = (n + nthr - 1) / nthr;
-    for (int t = 0; t < nthr; ++t) {
-        const long long lo = t * blk, hi = std::min(n, lo + blk);
-        if (lo < hi) th.emplace_back([&fn, lo, hi]() { fn(lo, hi); });
+// Persistent host worker pool for the population preparation: spawning threads costs ~0.3 ms per
+// batch of 16 on the Grace host, more than most of the parallel passes themselves.  run() hands
+// out task indices [0, ntasks) through an atomic counter; the calling thread works too.  One job
+// at a time: a caller that finds the pool busy (another context on another host thread), or a
+// process forked after the pool started, runs its tasks inline.  Every task writes disjoint
+// outputs, so results never depend on the scheduling.
+class HostPool {
+  public:
+    static HostPool& get() {
+        static HostPool pool;
+        return pool;
     }
-    for (auto& x : th) x.join();
+    void run(int ntasks, const std::function<void(int)>& fn) {
+        std::unique_lock<std::mutex> busy(run_mu_, std::try_to_lock);
+        if (!busy.owns_lock() || workers_.empty() || getpid() != pid_ || ntasks <= 1) {
+            for (int t = 0; t < ntasks; ++t) fn(t);
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            job_ = &fn;
+            ntasks_ = ntasks;
+            next_ = 0;
+            pending_ = (int)workers_.size();
+            ++gen_;
+        }
+        cv_.notify_all();
+        for (int t; (t = next_.fetch_add(1)) < ntasks;) fn(t);
+        std::unique_lock<std::mutex> lk(mu_);
+        done_cv_.wait(lk, [&] { return pending_ == 0; });
+        job_ = nullptr;
+    }
+    int size() const { return (int)workers_.size() + 1; }
+
+  private:
+    HostPool() : pid_(getpid()) {
+        const int n = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), 16)) - 1;
+        for (int i = 0; i < n; ++i) workers_.emplace_back([this] { loop(); });
+    }
+    ~HostPool() {
+        if (getpid() != pid_) {                  // forked child: the workers are the parent's
+            for (auto& w : workers_) w.detach();
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+            ++gen_;
+        }
+        cv_.notify_all();
+        for (auto& w : workers_) if (w.joinable()) w.join();
+    }
+    void loop() {
+        long long seen = 0;
+        for (;;) {
+            const std::function<void(int)>* job;
+            int nt;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return gen_ != seen; });
+                seen = gen_;
+                if (stop_) return;
+                job = job_;
+                nt = ntasks_;
+            }
+            for (int t; (t = next_.fetch_add(1)) < nt;) (*job)(t);
+            std::lock_guard<std::mutex> lk(mu_);
+            if (--pending_ == 0) done_cv_.notify_one();
+        }
+    }
+    std::vector<std::thread> workers_;
+    std::mutex run_mu_, mu_;
+    std::condition_variable cv_, done_cv_;
+    const std::function<void(int)>* job_ = nullptr;
+    int ntasks_ = 0, pending_ = 0;
+    std::atomic<int> next_{0};
+    long long gen_ = 0;
+    bool stop_ = false;
+    pid_t pid_;
+};
+
+// fn(lo, hi) over [0, n) in contiguous blocks on the pool (every index written by one block)
+void parallel_for(long long n, const std::function<void(long long, long long)>& fn) {
+    const int nblk = (int)std::max(1LL, std::min<long long>(4LL * HostPool::get().size(), (n + 2047) / 2048));
+    if (nblk == 1) { fn(0, n); return; }
+    const long long blk = (n + nblk - 1) / nblk;
+    HostPool::get().run(nblk, [&](int b) {
+        const long long lo = (long long)b * blk, hi = std::min(n, lo + blk);
+        if (lo < hi) fn(lo, hi);
+    });
 }
 
 // pinned host buffer of at least `bytes` (grow-only; the stream is synchronised before it grows)
@@ -466,9 +557,14 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
         const int b = kSepMg - 1 - a;
         t[a] = std::cos((double)(2 * b + 1) * M_PI / (double)(2 * kSepMg));
     }
-    std::vector<long long> keyv((size_t)N);
-    std::vector<double> sl((size_t)N), sh((size_t)N);
-    std::vector<char> direct((size_t)N, 0);
+    // per-cell scratch kept in the context between calls (no fresh pages to fault in)
+    SepScratch& S0 = ctx->sep_scratch;
+    std::vector<long long>& keyv = S0.keyv;
+    std::vector<double>& sl = S0.sl;
+    std::vector<double>& sh = S0.sh;
+    std::vector<char>& direct = S0.direct;
+    keyv.resize((size_t)N); sl.resize((size_t)N); sh.resize((size_t)N);
+    direct.assign((size_t)N, 0);
     std::atomic<int> below{0};                 // some cell lies below its gamma bin
     parallel_for(N, [&](long long c0, long long c1) {
         for (long long c = c0; c < c1; ++c) {
@@ -485,6 +581,7 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
             if (j < 0) below = 1;
         }
     });
+    ht.lap("sep_keys");
     // order: sep cells by sub-bin (the reference's np.unique over the sub-bins' lower edges
     // rounded to 14 decimals, ascending), then direct cells in original order.  A cell whose
     // gamma lies below its bin (possible in the reference's populations) gets a negative sub-bin
@@ -492,7 +589,8 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
     // the bin.  Without such cells, (bin, sub-bin) order is the lower-edge order and a stable
     // counting sort over the small key range gives it; with them, the sub-bins are ranked by
     // their rounded lower edges.
-    std::vector<long long> order((size_t)N);
+    std::vector<long long>& order = S0.order;
+    order.resize((size_t)N);
     long long n_sep = 0;
     for (long long c = 0; c < N; ++c) n_sep += !direct[(size_t)c];
     if (!below) {
@@ -525,9 +623,21 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
     }
     const long long n_dir = N - n_sep;
 
-    std::vector<double> kap((size_t)N), w((size_t)N), wl((size_t)N * 8, 0.0), nodes;
-    std::vector<float> kh((size_t)N), kl((size_t)N), wf((size_t)N), wlf((size_t)N * 8, 0.f);
-    std::vector<int> grp((size_t)N), gcol0, gncol;
+    ht.lap("sep_sort");
+    std::vector<double>& kap = S0.kap;
+    std::vector<double>& w = S0.w;
+    std::vector<double>& wl = S0.wl;
+    std::vector<float>& kh = S0.kh;
+    std::vector<float>& kl = S0.kl;
+    std::vector<float>& wf = S0.wf;
+    std::vector<float>& wlf = S0.wlf;
+    std::vector<int>& grp = S0.grp;
+    kap.resize((size_t)N); w.resize((size_t)N); kh.resize((size_t)N); kl.resize((size_t)N); wf.resize((size_t)N);
+    grp.resize((size_t)N);
+    wl.assign((size_t)N * 8, 0.0);
+    wlf.assign((size_t)N * 8, 0.f);
+    std::vector<double> nodes;
+    std::vector<int> gcol0, gncol;
     int ng = -1;
     long long prev = -2;
     double maxnode = 0.0;
@@ -545,6 +655,7 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
         }
         grp[(size_t)i] = ng;
     }
+    ht.lap("sep_groups");
     // Lagrange weights of each separable cell at its sub-bin's Chebyshev nodes
     parallel_for(n_sep, [&](long long i0, long long i1) {
         for (long long i = i0; i < i1; ++i) {
@@ -582,6 +693,7 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
             for (int a = 0; a < 8; ++a) wlf[(size_t)i * 8 + a] = (float)wl[(size_t)i * 8 + a];
         }
     });
+    ht.lap("sep_weights");
     // chunks of whole groups: one wave of ~8 CTAs per SM over (row tiles x chunks); the mixed
     // sweep's 4-warp CTAs are latency-bound, so residency is what feeds its pipes
     const int row_tiles = std::max(1, ceil_div(nk, 128));
@@ -599,6 +711,7 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
     S.key = key; S.n_cells = (int)N; S.n_groups = n_groups; S.n_cols_sep = n_cols_sep;
     S.n_cols = n_cols_sep + (int)n_dir; S.n_direct = (int)n_dir; S.chunk_begin = cb; S.max_sep_node = maxnode;
 
+    ht.lap("sep_chunks");
     DBUF(d_kap, double, "sep_kap", N);
     DBUF(d_w, double, "sep_w", N);
     DBUF(d_wl, double, "sep_wl", N * 8);
@@ -631,7 +744,7 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
     D.kap = d_kap; D.w = d_w; D.wl = d_wl; D.kap_hi = d_kh; D.kap_lo = d_kl; D.w_f = d_wf; D.wl_f = d_wlf;
     D.grp = d_grp; D.gcol0 = d_gc0; D.gncol = d_gnc; D.chunk_begin = d_cb;
     ctx->sep_precision_ready = 1;
-    ht.lap("sep_plan");
+    ht.lap("sep_upload");
     return SGL_OK;
 }
 
@@ -1313,14 +1426,7 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
     // group writes disjoint, precomputed slices; the results do not depend on the thread count):
     //   1. row norms (prune threshold)        2. per-group index structure (serial, index-only)
     //   3. transposed kept rows, sums, 1-D reach stacks, U sums
-    const int nthr = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), 32));
-    auto parallel_groups = [&](const std::function<void(int)>& fn) {
-        std::vector<std::thread> th;
-        std::atomic<int> next{0};
-        for (int t = 0; t < nthr; ++t)
-            th.emplace_back([&]() { for (int g; (g = next.fetch_add(1)) < n_groups;) fn(g); });
-        for (auto& t : th) t.join();
-    };
+    auto parallel_groups = [&](const std::function<void(int)>& fn) { HostPool::get().run(n_groups, fn); };
     HostTimer ht(ctx);
     // coherent access: the GPU reads the caller's rows in place (norms here, the data in pass 3)
     const bool coherent = ctx->coherent_host && !std::getenv("SGL_XI_HOST_PREP");
@@ -1341,7 +1447,10 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         // reads the device copy
         d_raw = dbuf<double>(ctx, "xi_raw", (size_t)std::max<long long>(1, row_off[n_groups]));
         if (!d_raw) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (xi raw rows)");
-        launch_xi_stage_rows(rows, row_off[n_groups], d_raw, ctx->stream);
+        {
+            Timed t(ctx, "xi_stage_rows", 0.0, 16.0 * (double)row_off[n_groups]);
+            launch_xi_stage_rows(rows, row_off[n_groups], d_raw, ctx->stream);
+        }
         CKLAUNCH();
         // the norms are written straight into host memory (coherent); the host reads them after
         // the per-group index work below, which overlaps these kernels
@@ -1365,7 +1474,7 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
     // pass 2: entry order by p, unique p / q (index-only, before the norms are known), then the
     // keep lists and every output offset
     struct GPlan {
-        std::vector<int> keep, order, pg, qg, qs, qpos, inv, qord, qseg;
+        std::vector<int> keep, order, pg, qg, qs, qpos, qord, qseg;
         int nP = 0, q0 = 0, qseg0 = 0, p0 = 0;
         long long ent0 = 0, rowel0 = 0, row0 = 0, u0 = 0, w0 = 0, um0 = 0;
     };
@@ -1401,8 +1510,6 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
             if (P.qpos[q] == 0) { P.qpos[q] = (int)P.qs.size(); P.qs.push_back(q); }
         if (coherent) {
             const int ne = nidx[g];
-            P.inv.resize(ne);
-            for (int i = 0; i < ne; ++i) P.inv[P.order[i]] = i;
             P.qseg.assign(P.qs.size() + 1, 0);
             for (int e = 0; e < ne; ++e) ++P.qseg[P.qpos[P.qg[e]] + 1];
             for (size_t i = 1; i < P.qseg.size(); ++i) P.qseg[i] += P.qseg[i - 1];
@@ -1463,9 +1570,9 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
     p_ptr[(size_t)total_p] = (int)ent_total;
     ent_qg.resize((size_t)ent_total);
     idx_q.resize((size_t)q_total);
-    std::vector<int> inv_all, qord_all, pord_all, qseg_all;
+    std::vector<int> qord_all, pord_all, qseg_all;
     if (coherent) {
-        inv_all.resize((size_t)ent_total); qord_all.resize((size_t)ent_total); pord_all.resize((size_t)ent_total);
+        qord_all.resize((size_t)ent_total); pord_all.resize((size_t)ent_total);
         qseg_all.resize((size_t)qseg_total);
     }
     parallel_groups([&](int g) {
@@ -1483,7 +1590,6 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         }
         std::copy(P.qs.begin(), P.qs.end(), idx_q.begin() + P.q0);
         if (coherent) {
-            std::copy(P.inv.begin(), P.inv.end(), inv_all.begin() + P.ent0);
             std::copy(P.qord.begin(), P.qord.end(), qord_all.begin() + P.ent0);
             std::copy(P.order.begin(), P.order.end(), pord_all.begin() + P.ent0);
             std::copy(P.qseg.begin(), P.qseg.end(), qseg_all.begin() + P.qseg0);
@@ -1502,11 +1608,14 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
     float* rows_tf_p = nullptr;
     if (coherent && !kept.empty()) {
         std::vector<XiPrepRow> kr;
-        int ne_max = 0;
+        std::vector<int2> tiles;                 // transpose tiles: (group's first row in kr, i0)
+        int ne_max = 0, r_max = 0;
         for (int g : kept) {
             GPlan& P = plan[g];
             const int R = (int)P.keep.size(), ne = nidx[g], w = nidx[g] + 1;
             ne_max = std::max(ne_max, ne);
+            r_max = std::max(r_max, R);
+            for (int i0 = 0; i0 < ne; i0 += 64) tiles.push_back(make_int2((int)kr.size(), i0));
             for (int rr = 0; rr < R; ++rr) {
                 XiPrepRow k{};
                 k.src = row_off[g] + (long long)P.keep[rr] * w;
@@ -1521,9 +1630,9 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
                 kr.push_back(k);
             }
         }
-        if (((size_t)ne_max + 1) * 8 <= 200 * 1024) {
+        if (((size_t)ne_max + 1) * 8 <= 200 * 1024 && r_max <= 256) {
             DBUF(d_kr, XiPrepRow, "xi_prep_rows", kr.size());
-            DBUF(d_inv, int, "xi_prep_inv", std::max<long long>(1, ent_total));
+            DBUF(d_tiles, int2, "xi_prep_tiles", std::max<size_t>(1, tiles.size()));
             DBUF(d_qord, int, "xi_prep_qord", std::max<long long>(1, ent_total));
             DBUF(d_pord, int, "xi_prep_pord", std::max<long long>(1, ent_total));
             DBUF(d_qseg, int, "xi_prep_qseg", std::max<size_t>(1, qseg_all.size()));
@@ -1539,11 +1648,14 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
             DBUF(d_U0x, double, "xi_Usum", std::max<long long>(1, u_total));
             DBUF(d_W0x, double, "xi_W0", std::max<long long>(1, w0_total));
             DBUF(d_Uall, double, "xi_Uall", std::max<long long>(1, ubase[2] + um_total[2]));
-            CKS(upload(ctx, d_kr, kr.data(), kr.size()));
-            CKS(upload(ctx, d_inv, inv_all.data(), inv_all.size()));
-            CKS(upload(ctx, d_qord, qord_all.data(), qord_all.size()));
-            CKS(upload(ctx, d_pord, pord_all.data(), pord_all.size()));
-            CKS(upload(ctx, d_qseg, qseg_all.data(), qseg_all.size()));
+            // the device reads these host arrays directly (no staging memcpy on the host)
+            static_assert(sizeof(XiPrepRow) % 4 == 0, "word copy");
+            launch_copy_from_host(kr.data(), kr.size() * sizeof(XiPrepRow), d_kr, ctx->stream);
+            launch_copy_from_host(tiles.data(), tiles.size() * sizeof(int2), d_tiles, ctx->stream);
+            launch_copy_from_host(qord_all.data(), qord_all.size() * 4, d_qord, ctx->stream);
+            launch_copy_from_host(pord_all.data(), pord_all.size() * 4, d_pord, ctx->stream);
+            launch_copy_from_host(qseg_all.data(), qseg_all.size() * 4, d_qseg, ctx->stream);
+            CKLAUNCH();
             CKS(upload(ctx, d_pptr0, p_ptr.data(), p_ptr.size()));
             CKS(upload(ctx, d_idxp0, idx_p.data(), idx_p.size()));
             CKS(upload(ctx, d_idxq0, idx_q.data(), idx_q.size()));
@@ -1551,9 +1663,16 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
             CK(cudaMemsetAsync(d_U0x, 0, (size_t)std::max<long long>(1, u_total) * 8, ctx->stream));
             CK(cudaMemsetAsync(d_W0x, 0, (size_t)std::max<long long>(1, w0_total) * 8, ctx->stream));
             CK(cudaMemsetAsync(d_Uall, 0, (size_t)std::max<long long>(1, ubase[2] + um_total[2]) * 8, ctx->stream));
-            XiPrepIdx ix{d_inv, d_qord, d_qseg, d_pord, d_pptr0, d_idxp0, d_idxq0};
+            XiPrepIdx ix{d_qord, d_qseg, d_pord, d_pptr0, d_idxp0, d_idxq0};
             XiPrepOut xo{d_rows0, d_rowsf0, d_res0, d_sum0, d_sig0, d_Uall, d_U0x, d_W0x};
-            launch_xi_rowprep(d_raw, d_kr, (int)kr.size(), ne_max, ix, d_kmc0, xo, ctx->stream);
+            {
+                Timed t(ctx, "xi_transpose", 0.0, 20.0 * (double)rowel_total);
+                launch_xi_transpose(d_raw, d_kr, d_tiles, (int)tiles.size(), d_pord, d_rows0, d_rowsf0, ctx->stream);
+            }
+            {
+                Timed t(ctx, "xi_rowprep", 0.0, 8.0 * (double)rowel_total);
+                launch_xi_rowprep(d_raw, d_kr, (int)kr.size(), ne_max, ix, d_kmc0, xo, ctx->stream);
+            }
             CKLAUNCH();
             sig_v.assign((size_t)row_total, 0.0);
             CK(cudaMemcpyAsync(res.data(), d_res0, (size_t)row_total * 8, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1680,7 +1799,9 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         CKS(upload(ctx, d_pp, pp.data(), pp.size()));
         CKS(upload(ctx, d_idxp, idx_p.data(), idx_p.size()));
         CKS(upload(ctx, d_pptr, p_ptr.data(), p_ptr.size()));
-        CKS(upload(ctx, d_qg, ent_qg.data(), ent_qg.size()));
+        if (coherent) launch_copy_from_host(ent_qg.data(), ent_qg.size() * 4, d_qg, ctx->stream);
+        else CKS(upload(ctx, d_qg, ent_qg.data(), ent_qg.size()));
+        CKLAUNCH();
         if (!dev_filled) {
             if (rowel_total > 0)
                 CK(cudaMemcpyAsync(d_rows, rows_t_p, (size_t)rowel_total * 8, cudaMemcpyHostToDevice, ctx->stream));

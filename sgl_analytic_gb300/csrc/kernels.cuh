@@ -172,7 +172,6 @@ struct XiPrepRow {                 // one kept row
     int nP, p0;                    // kappa cells: count, global p offset (p_ptr / idx_p)
 };
 struct XiPrepIdx {
-    const int* inv;                // [entries] position of entry e in the group's p-order
     const int* qord;               // [entries] entries sorted by gamma cell (stable)
     const int* qseg;               // per group: nQ + 1 segment starts into qord
     const int* pord;               // [entries] entries in p-order
@@ -185,8 +184,14 @@ struct XiPrepOut {
     double* U; double* U0; double* W0;
 };
 void launch_xi_stage_rows(const double* rows, long long n, double* dst, cudaStream_t st);
+// bytes must be a multiple of 4, both pointers 4-byte aligned; src is host memory the device
+// reads coherently
+void launch_copy_from_host(const void* src, size_t bytes, void* dst, cudaStream_t st);
 void launch_xi_row_norms(const double* rows, const long long* row_start, const int* row_len, int nrows,
                          double* norms, cudaStream_t st);
+// tiles: (first kept row of the group in kr, first entry i0); at most 256 kept rows per group
+void launch_xi_transpose(const double* rows, const XiPrepRow* kr, const int2* tiles, int ntiles, const int* pord,
+                         double* rt, float* rtf, cudaStream_t st);
 void launch_xi_rowprep(const double* rows, const XiPrepRow* kr, int nkept, int ne_max, const XiPrepIdx& ix,
                        const double* kmc, const XiPrepOut& o, cudaStream_t st);
 

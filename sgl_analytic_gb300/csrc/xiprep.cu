@@ -3,8 +3,8 @@
 // are read once, coalesced, straight into device memory; nothing is staged through the host.
 //   k_xi_stage_rows flat copy of the caller's rows into device memory
 //   k_xi_row_norms  Euclidean norm of every raw row (the prune threshold)
+//   k_xi_transpose  rows_t[i][rr] = row_rr[order[i]] (FP64 and FP32 copies), coalesced tiles
 //   k_xi_rowprep    one CTA per kept row, the row held in shared memory:
-//                   rows_t[i][rr] = row[order[i]] (through the inverse order; FP64 and FP32 copies),
 //                   the row sum and residual, the per-gamma-cell sums U[row][q] and, for m = 0 rows,
 //                   the per-kappa-cell sums W0[row][p], the compacted U0 and the sigma term
 //                   (row . kc + res).  Every sum runs over a fixed entry order (deterministic).
@@ -57,16 +57,9 @@ k_xi_rowprep(const double* __restrict__ rows, const XiPrepRow* __restrict__ kr, 
     const double* r = rows + d.src;
     for (int e = threadIdx.x; e <= d.ne; e += blockDim.x) xr[e] = r[e];
     __syncthreads();
-    // transposed copies and the row sum
-    const int* iv = ix.inv + d.ent0;
+    // the row sum (the transposed copies come from k_xi_transpose)
     double a = 0.0;
-    for (int e = threadIdx.x; e < d.ne; e += blockDim.x) {
-        const double v = xr[e];
-        const long long od = d.dst + (long long)iv[e] * d.R;
-        o.rt[od] = v;
-        o.rtf[od] = (float)v;
-        a += v;
-    }
+    for (int e = threadIdx.x; e < d.ne; e += blockDim.x) a += xr[e];
     a = block_sum(a, sh);
     if (threadIdx.x == 0) { o.sums[d.row] = a; o.res[d.row] = xr[d.ne]; }
     // U[row][q]: one thread per gamma cell of the group, entries in q-order
@@ -93,11 +86,56 @@ k_xi_rowprep(const double* __restrict__ rows, const XiPrepRow* __restrict__ kr, 
     if (threadIdx.x == 0) o.sig[d.row] = dot + xr[d.ne];
 }
 
+// word copy of a host array the device reads coherently (the source must stay alive until the
+// stream reaches this copy)
+__global__ void k_copy_words(const uint32_t* __restrict__ src, long long n, uint32_t* __restrict__ dst) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) dst[i] = src[i];
+}
+
+void launch_copy_from_host(const void* src, size_t bytes, void* dst, cudaStream_t st) {
+    const long long n = (long long)(bytes / 4);
+    if (n <= 0) return;
+    k_copy_words<<<(unsigned)std::min<long long>(152 * 8, (n + 255) / 256), 256, 0, st>>>((const uint32_t*)src, n,
+                                                                                          (uint32_t*)dst);
+    SGL_COUNT(1);
+}
+
 void launch_xi_stage_rows(const double* rows, long long n, double* dst, cudaStream_t st) {
     if (n <= 0) return;
     const int lead = ((uintptr_t)rows & 15) ? 1 : 0;      // rows is 8-byte aligned (doubles)
     k_xi_stage_rows<<<152 * 8, 256, 0, st>>>(rows, n, dst, lead);
     SGL_COUNT(1);
+}
+
+// rows_t[i][rr] = row_rr[order[i]] (FP64 and FP32), one CTA per tile of kXiTransTile entries of a
+// group: the tile's rows_t region is contiguous, so the writes are coalesced; the gathers from the
+// group's rows hit L2.
+constexpr int kXiTransTile = 64;
+
+__global__ void __launch_bounds__(256)
+k_xi_transpose(const double* __restrict__ rows, const XiPrepRow* __restrict__ kr, const int2* __restrict__ tiles,
+               const int* __restrict__ pord, double* __restrict__ rt, float* __restrict__ rtf) {
+    __shared__ long long s_src[256];
+    __shared__ int s_po[kXiTransTile];
+    const int2 tl = tiles[blockIdx.x];
+    const XiPrepRow d0 = kr[tl.x];
+    const int R = d0.R, i0 = tl.y, ni = min(kXiTransTile, d0.ne - i0);
+    for (int rr = threadIdx.x; rr < R; rr += blockDim.x) s_src[rr] = kr[tl.x + rr].src;
+    for (int il = threadIdx.x; il < ni; il += blockDim.x) s_po[il] = pord[d0.ent0 + i0 + il];
+    __syncthreads();
+    const long long base = d0.dst + (long long)i0 * R;
+    for (int t = threadIdx.x; t < ni * R; t += blockDim.x) {
+        const int il = t / R, rr = t - il * R;
+        const double v = rows[s_src[rr] + s_po[il]];
+        rt[base + t] = v;
+        rtf[base + t] = (float)v;
+    }
+}
+
+void launch_xi_transpose(const double* rows, const XiPrepRow* kr, const int2* tiles, int ntiles, const int* pord,
+                         double* rt, float* rtf, cudaStream_t st) {
+    if (ntiles > 0) { k_xi_transpose<<<ntiles, 256, 0, st>>>(rows, kr, tiles, pord, rt, rtf); SGL_COUNT(1); }
 }
 
 void launch_xi_row_norms(const double* rows, const long long* row_start, const int* row_len, int nrows,
