@@ -44,8 +44,7 @@ XI_OUT = np.concatenate([np.linspace(-1.0, 1.0, 1601), np.linspace(1.005, 9.0, 1
 # DRAM bytes (read + write) per launch of the dominant kernels, from one ncu capture of this
 # workload (profiles/ holds the summaries and the commands)
 TRAFFIC = {"gemm_f32_xi": 1.2079e9,         # profiles/gemm_f32_xi_zs1.md
-           "xi_stageA": 1.4768e9,          # profiles/xi_stageA_pack_zs1.md
-           "gemm_tc_sep3": 2.140e8}        # profiles/tc_gemm_sep3_zs1.md
+           "xi_stageA": 1.4778e9}          # profiles/xi_stageA_pack_zs1.md
 
 
 def dist_env():
