@@ -2353,12 +2353,16 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
     const double dkg = kg[1] - kg[0], dkk = kk[1] - kk[0];
     launch_hankel_matrix(P, d_kg, nkg, dkg, d_gam, ngam, ldF, M, st); CKLAUNCH();
     launch_kappa_matrix(P, d_kk, nk, dkk, d_kap, nkap, CS, st); CKLAUNCH();
+    // mixed path: the transform sums run in >= 16 FP32 K-slices combined in float-float.  The PDF
+    // tail is most sensitive to their FP32 chain length: on the reference's z_s = 1 population
+    // 16 slices give a tail error of 5.9e-4 against 8.5e-4 with 8.
+    constexpr int kTransformSplit = 16;
     const double c = 1.0 / (2.0 * M_PI * M_PI);
     if (P == SGL_FP64) {
         CKS(gemm_splitk<double>(ctx, gd<double>(2 * nk, ngam, nkg, Phi, nkg, 1, M, ldF, 1, F, ldF), "hankel"));
     } else {
         // F = Phi M_hi + Phi M_lo (split Hankel matrix)
-        CKS(gemm_splitk<float>(ctx, gd<float>(2 * nk, ngam, nkg, Phi, nkg, 1, M, ldF, 1, F, ldF), "hankel", 8));
+        CKS(gemm_splitk<float>(ctx, gd<float>(2 * nk, ngam, nkg, Phi, nkg, 1, M, ldF, 1, F, ldF), "hankel", kTransformSplit));
         // the M_lo term is a correction of relative size 2^-24: BF16 operands on the tensor cores
         // carry it to ~0.4%, i.e. ~2e-10 of F
         CKS(gemm_splitk_tc(ctx, gd<float>(2 * nk, ngam, nkg, Phi, nkg, 1, (const float*)M + (size_t)nkg * ldF, ldF,
@@ -2368,7 +2372,7 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
     if (P == SGL_FP64) {
         CKS(gemm_splitk<double>(ctx, gd<double>(nkap, ldF, 2 * nk, CS, 2 * nk, 1, F, ldF, 1, P3e, ldF, c), "kappa"));
     } else {
-        CKS(gemm_splitk<float>(ctx, gd<float>(nkap, ldF, 2 * nk, CS, 2 * nk, 1, F, ldF, 1, P3e, ldF, c), "kappa", 8));
+        CKS(gemm_splitk<float>(ctx, gd<float>(nkap, ldF, 2 * nk, CS, 2 * nk, 1, F, ldF, 1, P3e, ldF, c), "kappa", kTransformSplit));
     }
     float* d_P3f = nullptr;
     if (P == SGL_MIXED) {
