@@ -34,7 +34,7 @@ constexpr int kXiCoarse = 101;             // Lam(xi_coarse=101)
 constexpr double kSigReach = 12.0, kPppK = 18.0, kPppG = 96.0, kBoxReach = 6.0;
 constexpr double kPtsPerSigKap = 72.0, kPtsPerSigGam = 36.0;
 constexpr double kTailKapMax = 0.99, kTailGamMax = 0.8, kTailPppG = 12.0;
-constexpr double kInvertBlockPts = 20000000.0, kOutGridMax = 3.4e7;
+constexpr double kOutGridMax = 3.4e7;
 
 thread_local std::string g_create_error;
 
@@ -2298,8 +2298,12 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
     }
     if ((double)n_kap * (double)n_gam > kOutGridMax)
         return fail(ctx, SGL_ERR_UNSUPPORTED, "geometric output grid (n_kap * n_gam > OUT_GRID_MAX) not implemented");
-    if ((double)nk_k * (double)nk_g > kInvertBlockPts)
-        return fail(ctx, SGL_ERR_UNSUPPORTED, "blocked inversion (nk_k * nk_g > 2e7) not implemented");
+    // Above 2e7 k-points the reference accumulates Phi, the Hankel product and the kappa transform
+    // over k_kappa row blocks to bound host memory (_invert_blocked, sgl_full.py:97-157; "same sums,
+    // partial-sum order -> roundoff").  The whole grid fits in HBM here, so the same sums run
+    // unblocked; allocation failure is reported as such.  The Phi rows are one grid dimension of
+    // the composition kernel, hence the axis limit.
+    if (nk_k > 65535) return fail(ctx, SGL_ERR_UNSUPPORTED, "k_kappa axis longer than 65535 points");
     if (nk_k < 2 || nk_g < 2) return fail(ctx, SGL_ERR_VALUE, "degenerate k grid");
     const std::vector<double> kk = linspace(0.0, k_k_max, nk_k);
     const std::vector<double> kg = linspace(0.0, k_g_max, nk_g);
