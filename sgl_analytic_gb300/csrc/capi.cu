@@ -959,12 +959,13 @@ sgl_status vp_lnR_device(sgl_ctx* ctx, int precision, const double* d_kv, int nk
     const VpDevice& D = ctx->vpd;
     void* tables = ctx->arena.get("vp_tables", vp_table_bytes(precision, D.U, nk, nq));
     const int rows = vp_rows_per_pass(D.nsh, nk, nq, (size_t)8 << 30);
-    void* zb = ctx->arena.get("vp_z", (size_t)D.nsh * 49 * 16 * (size_t)rows * nq);
+    const int pieces = rows == nk ? vp_pieces(D.nsh, rows, nq) : 1;     // split runs only in a single pass
+    void* zb = ctx->arena.get("vp_z", (size_t)D.nsh * 49 * 16 * (size_t)rows * nq * pieces);
     if (!tables || !zb) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (vp)");
     const double pts = (double)nk * nq;
     Timed t(ctx, precision == SGL_FP64 ? "vp_lnR_f64" : "vp_lnR_mixed", pts * (double)D.ncells * 12.0,
             pts * D.nsh * 49 * 16.0 * 2);
-    launch_vp_lnR(precision, D, d_kv, nk, d_qv, nq, tables, (double2*)zb, rows, d_re, d_im, ctx->stream);
+    launch_vp_lnR(precision, D, d_kv, nk, d_qv, nq, tables, (double2*)zb, rows, d_re, d_im, ctx->stream, pieces);
     CKLAUNCH();
     return SGL_OK;
 }
@@ -1218,7 +1219,10 @@ sgl_status lambda_direct(sgl_ctx* ctx, const double* h_kk, int nk, const double*
     CKLAUNCH();
     bool xi = false;
     if (ctx->xi.on || ctx->vp_on) {
-        CKS(xi_any(ctx, SGL_FP64, d_kk, h_kk, nk, d_kg, h_kg, nkg, d_out + 2 * npt, d_out + 3 * npt));
+        // the vp closure's term follows the requested precision (its mixed ln R is within ~2e-8 of
+        // FP64); the gauss term's exact line kernels are FP64
+        CKS(xi_any(ctx, ctx->vp_on ? precision : SGL_FP64, d_kk, h_kk, nk, d_kg, h_kg, nkg, d_out + 2 * npt,
+                   d_out + 3 * npt));
         xi = true;
     }
     std::vector<double> h((size_t)(4 * npt));

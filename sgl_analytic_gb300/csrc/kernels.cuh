@@ -217,7 +217,9 @@ struct VpDevice {
 size_t vp_table_bytes(int precision, int U, int nk, int nq);
 int vp_rows_per_pass(int nsh, int nk, int nq, size_t z_cap_bytes);
 void launch_vp_lnR(int precision, const VpDevice& d, const double* kv, int nk, const double* qv, int nq, void* tables,
-                   double2* zbuf, int rows_per_pass, double* out_re, double* out_im, cudaStream_t st);
+                   double2* zbuf, int rows_per_pass, double* out_re, double* out_im, cudaStream_t st, int npieces = 1);
+// pieces per shell for the phase-1 kernel so that a small point grid still fills the GPU
+int vp_pieces(int nsh, int rows, int nq);
 
 // ---- 1-D CF sweep and FMA probes
 int sweep1d_chunks(int nk, long long nc);

@@ -87,14 +87,20 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 template <typename TT>
 __global__ void __launch_bounds__(kZThreads)
 k_vp_z(VpDevice d, const typename V2<TT>::T* __restrict__ e, const typename V2<TT>::T* __restrict__ Jt, int nk,
-       int nq, int kb, int nkc, double2* __restrict__ zp, double2* __restrict__ alin, long long NP) {
+       int nq, int kb, int nkc, double2* __restrict__ zp, double2* __restrict__ alin, long long NP, int npieces) {
     using T2 = typename V2<TT>::T;
     __shared__ __align__(16) T2 s_e[2][kZCh][kZK];
     __shared__ __align__(16) T2 s_J[2][kZCh][kZQ];
     __shared__ __align__(16) T2 s_w[2][kZCh];
     constexpr bool MIX = sizeof(TT) == 4;
     constexpr int EB = (int)sizeof(T2);
-    const int s = blockIdx.z;
+    // blockIdx.z = (shell, piece): a piece is a contiguous part of the shell's run list.  Each run's
+    // contribution to the states is additive, so pieces write partial z and A_lin (their own
+    // slices of zp / alin) that the chain kernel sums in piece order.  More than one piece only
+    // when the point tile grid alone would leave the GPU idle (the k-reach probes).
+    const int s = blockIdx.z / npieces, piece = blockIdx.z % npieces;
+    zp += (long long)piece * d.nsh * kVpNS * NP;
+    alin += (long long)piece * d.nsh * NP;
     const int q0 = blockIdx.x * kZQ, k0 = kb + blockIdx.y * kZK, kend = kb + nkc;
     const int t = threadIdx.x, tq = t % 16, tk = t / 16;
     // my points: (k0 + tk + 8 m, q0 + tq + 16 i), index P = 2 m + i
@@ -140,7 +146,9 @@ k_vp_z(VpDevice d, const typename V2<TT>::T* __restrict__ e, const typename V2<T
         }
         cp_async_commit();
     };
-    const int r0 = d.sh_run[s], r1 = d.sh_run[s + 1];
+    const int rs0 = d.sh_run[s], rs1 = d.sh_run[s + 1];
+    const int r0 = rs0 + (int)((long long)(rs1 - rs0) * piece / npieces);
+    const int r1 = rs0 + (int)((long long)(rs1 - rs0) * (piece + 1) / npieces);
     int buf = 0;
     if (r0 < r1) issue(0, d.run_cell[r0], d.run_cell[r0 + 1]);
     for (int r = r0; r < r1; ++r) {
@@ -231,7 +239,7 @@ k_vp_z(VpDevice d, const typename V2<TT>::T* __restrict__ e, const typename V2<T
 
 __global__ void __launch_bounds__(kChPts)
 k_vp_chain(VpDevice d, const double2* __restrict__ zp, const double2* __restrict__ alin, long long NP, int nq, int kb,
-           double* __restrict__ out_re, double* __restrict__ out_im) {
+           double* __restrict__ out_re, double* __restrict__ out_im, int npieces) {
     extern __shared__ __align__(16) unsigned char vsm[];
     double (*ar)[kChPts] = (double (*)[kChPts])vsm;                       // alpha (normalised)
     double (*ai)[kChPts] = (double (*)[kChPts])(vsm + 1 * kVpNS * kChPts * 8);
@@ -250,10 +258,18 @@ k_vp_chain(VpDevice d, const double2* __restrict__ zp, const double2* __restrict
             __syncthreads();
         }
         if (!live) continue;
-        const double2 al = alin[(long long)s * NP + p];
+        double2 al = alin[(long long)s * NP + p];
+        for (int pc = 1; pc < npieces; ++pc) {
+            const double2 a2 = alin[((long long)pc * d.nsh + s) * NP + p];
+            al.x += a2.x; al.y += a2.y;
+        }
         double mr = 0.0, mi = 0.0;
         for (int j = 0; j < kVpNS; ++j) {
-            const double2 zz = zp[((long long)s * kVpNS + j) * NP + p];
+            double2 zz = zp[((long long)s * kVpNS + j) * NP + p];
+            for (int pc = 1; pc < npieces; ++pc) {
+                const double2 z2 = zp[(((long long)pc * d.nsh + s) * kVpNS + j) * NP + p];
+                zz.x += z2.x; zz.y += z2.y;
+            }
             const double uj = d.u[j], wj = d.w[j];
             const double zr = fma(uj, al.x, zz.x), zi = fma(uj, al.y, zz.y);
             br[j][t] = zr; bi[j][t] = zi;
@@ -310,6 +326,101 @@ k_vp_chain(VpDevice d, const double2* __restrict__ zp, const double2* __restrict
     out_im[o] = atan2(si, sr);
 }
 
+// The same chain for few points (the k-reach probe lines): one CTA per point, one thread per state.
+// The per-state work (mat-vec over i in the same order, exp, sincos, normalisation) runs in
+// parallel; the two ordered sums (the projection's weighted mean, the final state sum) stay on
+// one thread in state order, and the maxima are order-free, so the results are those of
+// k_vp_chain.
+constexpr int kChSmallThreads = 64;
+
+__global__ void __launch_bounds__(kChSmallThreads)
+k_vp_chain_small(VpDevice d, const double2* __restrict__ zp, const double2* __restrict__ alin, long long NP, int nq,
+                 int kb, double* __restrict__ out_re, double* __restrict__ out_im, int npieces) {
+    __shared__ double sK[kVpNS * kVpNS];
+    __shared__ double zr_s[kVpNS], zi_s[kVpNS], ar[kVpNS], ai[kVpNS];
+    __shared__ double red[kChSmallThreads];
+    __shared__ double s_mr, s_mi;
+    const int j = threadIdx.x;
+    const long long p = blockIdx.x;
+    const bool st = j < kVpNS;
+    double scale = 0.0;
+    for (int s = 0; s < d.nsh; ++s) {
+        __syncthreads();
+        if (s > 0) {
+            const double* Ks = d.K + (long long)(s - 1) * kVpNS * kVpNS;
+            for (int e = j; e < kVpNS * kVpNS; e += kChSmallThreads) sK[e] = Ks[e];
+        }
+        double2 al = alin[(long long)s * NP + p];
+        for (int pc = 1; pc < npieces; ++pc) {
+            const double2 a2 = alin[((long long)pc * d.nsh + s) * NP + p];
+            al.x += a2.x; al.y += a2.y;
+        }
+        if (st) {
+            double2 zz = zp[((long long)s * kVpNS + j) * NP + p];
+            for (int pc = 1; pc < npieces; ++pc) {
+                const double2 z2 = zp[(((long long)pc * d.nsh + s) * kVpNS + j) * NP + p];
+                zz.x += z2.x; zz.y += z2.y;
+            }
+            const double uj = d.u[j];
+            zr_s[j] = fma(uj, al.x, zz.x);
+            zi_s[j] = fma(uj, al.y, zz.y);
+        }
+        __syncthreads();
+        if (j == 0) {
+            double mr = 0.0, mi = 0.0;
+            for (int i = 0; i < kVpNS; ++i) { mr = fma(d.w[i], zr_s[i], mr); mi = fma(d.w[i], zi_s[i], mi); }
+            s_mr = mr; s_mi = mi;
+        }
+        __syncthreads();
+        double zr = 0.0, zi = 0.0;
+        if (st) { zr = zr_s[j] - s_mr; zi = zi_s[j] - s_mi; }
+        red[j] = st ? zr : -1e300;
+        __syncthreads();
+        for (int o = kChSmallThreads / 2; o > 0; o >>= 1) {
+            if (j < o) red[j] = fmax(red[j], red[j + o]);
+            __syncthreads();
+        }
+        const double mx = red[0];
+        __syncthreads();
+        double nr = 0.0, ni = 0.0;
+        if (st) {
+            double gr, gi;
+            if (s == 0) { gr = d.w[j]; gi = 0.0; }
+            else {
+                gr = 0.0; gi = 0.0;
+                for (int i = 0; i < kVpNS; ++i) {
+                    const double kij = sK[i * kVpNS + j];
+                    gr = fma(kij, ar[i], gr); gi = fma(kij, ai[i], gi);
+                }
+            }
+            const double m = exp(zr - mx);
+            double sn, cs;
+            sincos(zi, &sn, &cs);
+            const double er = m * cs, ei = m * sn;
+            nr = gr * er - gi * ei;
+            ni = gr * ei + gi * er;
+        }
+        red[j] = st ? nr * nr + ni * ni : 0.0;
+        __syncthreads();
+        for (int o = kChSmallThreads / 2; o > 0; o >>= 1) {
+            if (j < o) red[j] = fmax(red[j], red[j + o]);
+            __syncthreads();
+        }
+        const double nrm = sqrt(red[0]);
+        const double inv = 1.0 / nrm;
+        if (st) { ar[j] = nr * inv; ai[j] = ni * inv; }
+        scale += mx + log(nrm);
+    }
+    __syncthreads();
+    if (j == 0) {
+        double sr = 0.0, si = 0.0;
+        for (int i = 0; i < kVpNS; ++i) { sr += ar[i]; si += ai[i]; }
+        const long long o = (long long)kb * nq + p;
+        out_re[o] = scale + 0.5 * log(sr * sr + si * si);
+        out_im[o] = atan2(si, sr);
+    }
+}
+
 size_t vp_table_bytes(int precision, int U, int nk, int nq) {
     const size_t es = precision == SGL_FP64 ? 8 : 4;
     return 2 * es * ((size_t)U * nk + (size_t)U * nq) + 256;
@@ -324,8 +435,14 @@ int vp_rows_per_pass(int nsh, int nk, int nq, size_t z_cap_bytes) {
     return (int)((nk + passes - 1) / passes);
 }
 
+int vp_pieces(int nsh, int rows, int nq) {
+    const long long base = (long long)ceil_div(nq, kZQ) * ceil_div(rows, kZK) * nsh;
+    const long long want = 8LL * kNumSMs;                   // CTAs of 128 threads
+    return (int)std::max(1LL, std::min(32LL, (want + base - 1) / base));
+}
+
 void launch_vp_lnR(int precision, const VpDevice& d, const double* kv, int nk, const double* qv, int nq, void* tables,
-                   double2* zbuf, int rows_per_pass, double* out_re, double* out_im, cudaStream_t st) {
+                   double2* zbuf, int rows_per_pass, double* out_re, double* out_im, cudaStream_t st, int npieces) {
     const long long tot = (long long)d.U * (nk + nq);
     const size_t es = precision == SGL_FP64 ? 8 : 4;
     void* e = tables;
@@ -343,16 +460,24 @@ void launch_vp_lnR(int precision, const VpDevice& d, const double* kv, int nk, c
         const int nkc = nk - kb < rows_per_pass ? nk - kb : rows_per_pass;
         const long long NP = (long long)nkc * nq;
         double2* zp = zbuf;
-        double2* al = zbuf + (long long)d.nsh * kVpNS * NP;
-        dim3 g1(ceil_div(nq, kZQ), ceil_div(nkc, kZK), d.nsh);
+        double2* al = zbuf + (long long)npieces * d.nsh * kVpNS * NP;
+        dim3 g1(ceil_div(nq, kZQ), ceil_div(nkc, kZK), d.nsh * npieces);
         if (precision == SGL_FP64) {
-            k_vp_z<double><<<g1, kZThreads, 0, st>>>(d, (const double2*)e, (const double2*)Jt, nk, nq, kb, nkc, zp, al, NP);
+            k_vp_z<double><<<g1, kZThreads, 0, st>>>(d, (const double2*)e, (const double2*)Jt, nk, nq, kb, nkc, zp, al, NP,
+                                                     npieces);
             SGL_COUNT(1);
         } else {
-            k_vp_z<float><<<g1, kZThreads, 0, st>>>(d, (const float2*)e, (const float2*)Jt, nk, nq, kb, nkc, zp, al, NP);
+            k_vp_z<float><<<g1, kZThreads, 0, st>>>(d, (const float2*)e, (const float2*)Jt, nk, nq, kb, nkc, zp, al, NP,
+                                                    npieces);
             SGL_COUNT(1);
         }
-        { k_vp_chain<<<ceil_div(NP, kChPts), kChPts, chain_smem, st>>>(d, zp, al, NP, nq, kb, out_re, out_im); SGL_COUNT(1); }
+        if (NP <= 4LL * kNumSMs) {
+            k_vp_chain_small<<<(unsigned)NP, kChSmallThreads, 0, st>>>(d, zp, al, NP, nq, kb, out_re, out_im, npieces);
+            SGL_COUNT(1);
+        } else {
+            k_vp_chain<<<ceil_div(NP, kChPts), kChPts, chain_smem, st>>>(d, zp, al, NP, nq, kb, out_re, out_im, npieces);
+            SGL_COUNT(1);
+        }
     }
 }
 
