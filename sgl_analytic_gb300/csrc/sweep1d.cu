@@ -5,8 +5,9 @@
 //
 // CTA (k tile of 256 rows, cell chunk): each thread owns one k; the chunk's cells stream through
 // shared memory in tiles of 512 (coalesced loads, broadcast reads).  FP64 path: FP64 sincos of the
-// half angle; mixed path: float-float phase, Cody-Waite reduction, FP32 sincos, Kahan-compensated
-// FP32 accumulation within the chunk, FP64 across chunks (fixed order: deterministic).
+// half angle; mixed path: float-float phase, exact reduction mod pi/2, FP32 sin / cos of the reduced
+// half angle (Taylor polynomials), Kahan-compensated FP32 accumulation within the chunk, FP64 across
+// chunks (fixed order: deterministic).
 //
 // Also: FMA-throughput probes used as the measured FP64 / FP32 peaks of the CF-sweep roofline.
 #include "kernels.cuh"
@@ -16,47 +17,14 @@ namespace sgl {
 constexpr int kSwRows = 256;
 constexpr int kSwTile = 512;
 
-__device__ inline void ff_phase_sincos(ff k, float kh, float kl, float& s, float& c, float& ph_hi, float& ph_lo) {
-    const float p = k.hi * kh;
-    const float e = fmaf(k.hi, kh, -p);
-    const float t = fmaf(k.hi, kl, fmaf(k.lo, kh, e));
-    ph_hi = p; ph_lo = t;
-    const float xh = 0.5f * p, xl = 0.5f * t;
-    const float q = rintf(xh * 0.636619772367581343f);   // 2/pi; exact integer for |q| < 2^24
-    // x - q pi/2 with pi/2 = C1 + C2 + C3 (float parts); the roundings of q*C1 and q*C2 are
-    // recovered exactly with FMA and xh - q*C1 is exact (Sterbenz), so the reduction holds for
-    // every |q| < 2^24 (phases up to ~2.6e7)
-    constexpr float C1 = 1.57079637050628662109375f;
-    constexpr float C2 = -4.371138828673792886547744274139404296875e-08f;
-    constexpr float C3 = -1.7151245100058819e-15f;
-    const float p1 = q * C1, e1 = fmaf(q, C1, -p1);
-    const float p2 = q * C2, e2 = fmaf(q, C2, -p2);
-    float r = xh - p1;
-    r -= e1;
-    r -= p2;
-    r -= e2;
-    r = fmaf(-q, C3, r);
-    r += xl;
-    float sr, cr;
-    sincosf(r, &sr, &cr);
-    switch (((int)q) & 3) {
-        case 0: s = sr;  c = cr;  break;
-        case 1: s = cr;  c = -sr; break;
-        case 2: s = -sr; c = -cr; break;
-        default: s = -cr; c = sr; break;
-    }
-}
-
 template <int MODE>
 __global__ void __launch_bounds__(kSwRows)
 k_sweep1d(const double* __restrict__ kk, int nk, const double* __restrict__ kap, const double* __restrict__ w,
           const float* __restrict__ kh, const float* __restrict__ kl, const float* __restrict__ wf,
           long long nc, long long per_chunk, double2* __restrict__ part) {
-    __shared__ double s_k[kSwTile];
-    __shared__ double s_w[kSwTile];
-    __shared__ float s_kh[kSwTile];
-    __shared__ float s_kl[kSwTile];
-    __shared__ float s_wf[kSwTile];
+    __shared__ double s_k[MODE == SGL_FP64 ? kSwTile : 1];
+    __shared__ double s_w[MODE == SGL_FP64 ? kSwTile : 1];
+    __shared__ float4 s_c[MODE == SGL_FP64 ? 1 : kSwTile];     // (kappa head, kappa tail, w, -)
     const int n = blockIdx.x * kSwRows + threadIdx.x;
     const double k = n < nk ? kk[n] : 0.0;
     const ff kf = ff_from_double(k);
@@ -69,7 +37,7 @@ k_sweep1d(const double* __restrict__ kk, int nk, const double* __restrict__ kap,
         __syncthreads();
         for (int e = threadIdx.x; e < cnt; e += kSwRows) {
             if (MODE == SGL_FP64) { s_k[e] = kap[base + e]; s_w[e] = w[base + e]; }
-            else { s_kh[e] = kh[base + e]; s_kl[e] = kl[base + e]; s_wf[e] = wf[base + e]; }
+            else s_c[e] = make_float4(kh[base + e], kl[base + e], wf[base + e], 0.f);
         }
         __syncthreads();
         if (MODE == SGL_FP64) {
@@ -90,18 +58,28 @@ k_sweep1d(const double* __restrict__ kk, int nk, const double* __restrict__ kap,
             }
         } else {
             for (int e = 0; e < cnt; ++e) {
-                float s, c, ph_hi, ph_lo;
-                ff_phase_sincos(kf, s_kh[e], s_kl[e], s, c, ph_hi, ph_lo);
-                const float cm1 = -2.f * s * s;
+                const float4 cv = s_c[e];
+                ff kapf; kapf.hi = cv.x; kapf.lo = cv.y;
+                float r, ph_hi, ph_lo;
+                int qi;
+                halfangle_reduce_ff(kf, kapf, r, qi, ph_hi, ph_lo);
+                float sr, cr;
+                sincos_reduced(r, sr, cr);
+                // only sin^2(ph/2) and sin(ph/2) cos(ph/2) enter: the quadrant picks sin or cos
+                // for the square and the sign of the product
+                const bool odd = qi & 1;
+                const float a = odd ? cr : sr;
+                const float cm1 = -2.f * a * a;
+                const float sn = (odd ? -2.f : 2.f) * sr * cr;
                 const float ph = ph_hi + ph_lo;
                 float smp;
                 if (fabsf(ph) < 1e-2f) {
                     const float p2 = ph * ph;
                     smp = -ph * p2 * (1.f / 6.f) * (1.f - p2 * (1.f / 20.f) * (1.f - p2 * (1.f / 42.f)));
                 } else {
-                    smp = (2.f * s * c - ph_hi) - ph_lo;
+                    smp = (sn - ph_hi) - ph_lo;
                 }
-                const float wv = s_wf[e];
+                const float wv = cv.z;
                 float y = fmaf(wv, cm1, -car); float t = far + y; car = (t - far) - y; far = t;
                 y = fmaf(wv, smp, -cai); t = fai + y; cai = (t - fai) - y; fai = t;
             }
