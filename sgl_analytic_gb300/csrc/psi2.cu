@@ -294,7 +294,7 @@ __device__ __forceinline__ void cp_async4(float* sdst, const float* gsrc) {
 }
 __device__ __forceinline__ void cp_async_wait_all4() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-__global__ void __launch_bounds__(kSAThreads, 2)
+__global__ void __launch_bounds__(kSAThreads, 3)
 k_xi_stageA_pack_reg(XiDevice x, const long long* __restrict__ p_prefix, const long long* __restrict__ rowel_off,
                      const float* __restrict__ J, int nkg, const long long* __restrict__ chunk_prefix,
                      const TcGemmDesc* __restrict__ descs, float* __restrict__ packed) {
