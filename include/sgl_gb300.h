@@ -39,7 +39,10 @@ typedef enum {
 /* Arithmetic of the Lambda evaluation and of the inversion. */
 typedef enum {
     SGL_FP64 = 0,   /* FP64 throughout: parity path, max|d lnPhi| <= 1e-10 vs the reference */
-    SGL_MIXED = 1   /* float-float phase reduction + FP32 sincos/GEMMs, FP64 cross-tile sums */
+    SGL_MIXED = 1   /* float-float phase with exact reduction, FP32 sin/cos/J0 and SIMT GEMMs,
+                       FP64 split-K and cross-tile combines; the k-reach probes sum FP32 terms in
+                       FP64.  Bars: PDF L1 <= 1e-4, tail relative error <= 1e-3 (met on the
+                       reference's populations; few-cell, heavy-weight populations want FP64) */
 } sgl_precision;
 
 /* Options of the inversion; defaults = pipeline.run's gauss chain (pipeline.py:221-239). */
@@ -193,7 +196,10 @@ void sgl_invert_opts_default(sgl_invert_opts* opts);
  * Replaces sgl_full.invert (sgl_full.py:159-375) with sgl.vector_grid (sgl.py:1229-1258) and
  * sgl.P_vector_joint (sgl.py:1127-1156): measured k-reach, width-relative grid with the tail
  * box, Hankel + Fourier transforms, Euler-Maclaurin endpoint term, constant-mu path integral.
- * P_out: n_xi doubles (host).  meta may be NULL. */
+ * Grids above 2e7 k-points, which the reference inverts in k_kappa row blocks (_invert_blocked,
+ * sgl_full.py:97-157), run the same sums unblocked in device memory (up to 65535 k_kappa rows);
+ * SGL_ERR_CUDA reports an allocation that does not fit.  P_out: n_xi doubles (host).  meta may
+ * be NULL. */
 sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_invert_opts* opts,
                    double* P_out, sgl_invert_meta* meta);
 
