@@ -917,20 +917,25 @@ sgl_status xi_eval(sgl_ctx* ctx, int precision, const double* d_kk, const double
         }
         CKS(run_tc_gemms(ctx, v, "xi", 2));
     }
-    double* d_V = nullptr;
+    const int nsplit = std::max(1, std::min(X.n_groups, 16));
+    DBUF(d_part, double, "xi_sq_part", 2LL * nsplit * nk * nkg);
     if (precision == SGL_MIXED) {
-        // compensated m = 0 form: V = U (J0 - 1) in FP64 from an FP64 J0 - 1 table
-        d_V = dbuf<double>(ctx, "xi_V", (size_t)X.total_rows * nkg);
+        // compensated m = 0 form: V = U (J0 - 1) in FP64 from an FP64 J0 - 1 table (rounded to FP32
+        // where formed), and the float-float correction tables of the square kernel
+        DBUF(d_Vf, float, "xi_Vf", (long long)X.total_rows * nkg);
+        DBUF(d_kres, float2, "xi_kres", (long long)nk * X.total_rows);
+        DBUF(d_hq, float2, "xi_hq", (long long)X.total_rows * nkg);
         DBUF(d_J64, double, "xi_J64", 4LL * X.n_gmc * nkg);
-        if (!d_V) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (xi V)");
         launch_bessel_tables(SGL_FP64, ctx->xid.gmc, X.n_gmc, d_kg, nkg, d_J64, st); CKLAUNCH();
-        launch_xi_V(ctx->xid, d_J64 + 3LL * X.n_gmc * nkg, nkg, d_V, X.total_rows, st); CKLAUNCH();
-    }
-    {
-        const int nsplit = std::max(1, std::min(X.n_groups, 16));
-        DBUF(d_part, double, "xi_sq_part", 2LL * nsplit * nk * nkg);
+        launch_xi_V_mixed(ctx->xid, d_J64 + 3LL * X.n_gmc * nkg, nkg, d_Vf, X.total_rows, d_kk, nk, d_kg, d_kres, d_hq,
+                          st);
+        CKLAUNCH();
         Timed t(ctx, "xi_square", 0.0, (double)tG * es);
-        launch_xi_square(precision, ctx->xid, d_off + 2 * X.n_groups, G, d_kk, nk, d_kg, nkg, d_V, nsplit, d_part,
+        launch_xi_square_mixed(ctx->xid, d_off + 2 * X.n_groups, (const float*)G, nk, nkg, d_Vf, d_kres, d_hq,
+                               X.total_rows, nsplit, d_part, d_re, d_im, st);
+    } else {
+        Timed t(ctx, "xi_square", 0.0, (double)tG * es);
+        launch_xi_square(precision, ctx->xid, d_off + 2 * X.n_groups, G, d_kk, nk, d_kg, nkg, nullptr, nsplit, d_part,
                          d_re, d_im, st);
     }
     CKLAUNCH();

@@ -91,6 +91,11 @@ void launch_xi_square(int precision, const XiDevice& x, const long long* G_off, 
                       const double* kg, int nkg, const double* V, int nsplit, double* part, double* out_re,
                       double* out_im, cudaStream_t st);
 void launch_xi_V(const XiDevice& x, const double* J0m1, int nkg, double* V, int total_rows, cudaStream_t st);
+void launch_xi_V_mixed(const XiDevice& x, const double* J0m1, int nkg, float* Vf, int total_rows, const double* kk,
+                       int nk, const double* kg, float2* kres, float2* hq, cudaStream_t st);
+void launch_xi_square_mixed(const XiDevice& x, const long long* G_off, const float* G, int nk, int nkg, const float* Vf,
+                            const float2* kres, const float2* hq, int rows, int nsplit, double* part, double* out_re,
+                            double* out_im, cudaStream_t st);
 
 // ---- spline + composition
 struct SplineAxis {              // per evaluation point: interval l (first coefficient) + 4 weights

@@ -467,7 +467,8 @@ void launch_xi_E(int precision, const XiDevice& x, const double* kk, int nk, con
 
 // V[g, r, j] = sum_q U_g[r, q] (J0 - 1)(gam_q kg_j) for the m = 0 groups (compensated form),
 // U_g = sum over p of the group's rows; one CTA per (group row), threads over j.  FP64.
-__global__ void k_xi_V(XiDevice x, const double* __restrict__ J0m1, int nkg, double* __restrict__ V) {
+template <typename VT>
+__global__ void k_xi_V(XiDevice x, const double* __restrict__ J0m1, int nkg, VT* __restrict__ V) {
     const int R = blockIdx.x;                     // global row index
     int g = 0;
     {
@@ -483,12 +484,102 @@ __global__ void k_xi_V(XiDevice x, const double* __restrict__ J0m1, int nkg, dou
     for (int j = threadIdx.x; j < nkg; j += blockDim.x) {
         double a = 0.0;
         for (int q = 0; q < nQ; ++q) a = fma(U[q], J0m1[(long long)qs[q] * nkg + j], a);
-        V[(long long)R * nkg + j] = a;
+        V[(long long)R * nkg + j] = (VT)a;
     }
 }
 
 void launch_xi_V(const XiDevice& x, const double* J0m1, int nkg, double* V, int total_rows, cudaStream_t st) {
-    if (total_rows > 0) { k_xi_V<<<total_rows, 128, 0, st>>>(x, J0m1, nkg, V); SGL_COUNT(1); }
+    if (total_rows > 0) { k_xi_V<double><<<total_rows, 128, 0, st>>>(x, J0m1, nkg, V); SGL_COUNT(1); }
+}
+
+// Mixed path: V rounded to FP32 where it is formed (the square kernel adds it in FP32), and the two
+// per-row correction terms of the square kernel as float-float tables, formed once in FP64:
+//   kres[n][R] = k_n res_R (m = 0 rows: imaginary part)   hq[R][j] = q_j res_R / 2 (m = 1 rows)
+__global__ void k_xi_corr_tables(const double* __restrict__ res, int rows, const double* __restrict__ kk, int nk,
+                                 const double* __restrict__ kg, int nkg, float2* __restrict__ kres,
+                                 float2* __restrict__ hq) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long n1 = (long long)nk * rows, n2 = (long long)rows * nkg;
+    if (t < n1) {
+        const double v = kk[t / rows] * res[t % rows];
+        const ff f = ff_from_double(v);
+        kres[t] = make_float2(f.hi, f.lo);
+    } else if (t < n1 + n2) {
+        const long long u = t - n1;
+        const double v = (0.5 * kg[u % nkg]) * res[u / nkg];
+        const ff f = ff_from_double(v);
+        hq[u] = make_float2(f.hi, f.lo);
+    }
+}
+
+void launch_xi_V_mixed(const XiDevice& x, const double* J0m1, int nkg, float* Vf, int total_rows, const double* kk,
+                       int nk, const double* kg, float2* kres, float2* hq, cudaStream_t st) {
+    if (total_rows <= 0) return;
+    k_xi_V<float><<<total_rows, 128, 0, st>>>(x, J0m1, nkg, Vf);
+    SGL_COUNT(1);
+    const long long tot = (long long)nk * total_rows + (long long)total_rows * nkg;
+    k_xi_corr_tables<<<ceil_div(tot, 256), 256, 0, st>>>(x.res, total_rows, kk, nk, kg, nkg, kres, hq);
+    SGL_COUNT(1);
+}
+
+__global__ void k_xi_square_sum(const double* __restrict__ part, int nsplit, long long npt, double* __restrict__ out_re,
+                                double* __restrict__ out_im);
+
+// round(b + (h + l)) in FP32 for a float-float addend (TwoSum of b and h, then the tails)
+__device__ __forceinline__ float add_ff(float b, float2 hl) {
+    const float s = b + hl.x, bp = s - b;
+    const float err = (b - (s - bp)) + (hl.x - bp);
+    return s + (err + hl.y);
+}
+
+// Mixed square: no FP64 arithmetic per element.  The FP64 form's fma(k, res, b) and
+// fma(q/2, res, a) round k res and q res / 2 once in FP64 and add them to the FP32 G value; here
+// the same FP64 products come as float-float tables and the sum is rounded once to FP32.
+__global__ void k_xi_square_mixed(XiDevice x, const long long* __restrict__ G_off, const float* __restrict__ G,
+                                  int nk, int nkg, const float* __restrict__ Vf, const float2* __restrict__ kres,
+                                  const float2* __restrict__ hq, int rows, int nsplit, double* __restrict__ part) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long npt = (long long)nk * nkg;
+    if (e >= npt) return;
+    const int n = (int)(e / nkg), j = (int)(e % nkg);
+    const int per = (x.n_groups + nsplit - 1) / nsplit;
+    const int g0 = blockIdx.y * per, g1 = min(x.n_groups, g0 + per);
+    double re = 0.0, im = 0.0;
+    for (int g = g0; g < g1; ++g) {
+        const int r = x.g_r[g], m = x.g_m[g];
+        const double sign = (m == 0) ? 1.0 : ((m & 1) ? -2.0 : 2.0);
+        const float* Gg = G + G_off[g] + (long long)n * r * nkg + j;
+        const float* Gi = G + G_off[g] + (long long)(nk + n) * r * nkg + j;
+        const long long R0 = x.g_row_off[g];
+        float gre = 0.f, gim = 0.f;
+        for (int rr = 0; rr < r; ++rr) {
+            float a = Gg[(long long)rr * nkg];
+            float b = Gi[(long long)rr * nkg];
+            if (m == 0) {
+                a += Vf[(R0 + rr) * nkg + j];
+                b = add_ff(b, kres[(long long)n * rows + R0 + rr]);
+            } else if (m == 1) {
+                a = add_ff(a, hq[(R0 + rr) * nkg + j]);
+            }
+            gre = fmaf(a, a, fmaf(-b, b, gre));
+            gim = fmaf(a, b, gim);
+        }
+        re = fma(0.5 * sign, (double)gre, re);
+        im = fma(0.5 * sign, 2.0 * (double)gim, im);
+    }
+    part[(long long)blockIdx.y * npt + e] = re;
+    part[(long long)(nsplit + blockIdx.y) * npt + e] = im;
+}
+
+void launch_xi_square_mixed(const XiDevice& x, const long long* G_off, const float* G, int nk, int nkg, const float* Vf,
+                            const float2* kres, const float2* hq, int rows, int nsplit, double* part, double* out_re,
+                            double* out_im, cudaStream_t st) {
+    const long long tot = (long long)nk * nkg;
+    dim3 grid(ceil_div(tot, 128), nsplit);
+    k_xi_square_mixed<<<grid, 128, 0, st>>>(x, G_off, G, nk, nkg, Vf, kres, hq, rows, nsplit, part);
+    SGL_COUNT(1);
+    k_xi_square_sum<<<ceil_div(tot, 256), 256, 0, st>>>(part, nsplit, tot, out_re, out_im);
+    SGL_COUNT(1);
 }
 
 // stage C: thread per output (n, j) and group chunk (blockIdx.y); groups and rows in a fixed
