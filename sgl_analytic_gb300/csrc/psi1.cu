@@ -26,11 +26,35 @@ __device__ inline void compensated_fp64(double ph, double& cm1, double& smp, dou
     }
 }
 
+// float-float arithmetic (Dekker / Knuth error-free transforms with FMA)
+__device__ __forceinline__ ff ff_fast_sum(float a, float b) {      // |a| >= |b|
+    ff r; r.hi = a + b; r.lo = b - (r.hi - a); return r;
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+    const float s = a.hi + b.hi, bb = s - a.hi;
+    const float e = (a.hi - (s - bb)) + (b.hi - bb);
+    return ff_fast_sum(s, e + (a.lo + b.lo));
+}
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return ff_fast_sum(p, e);
+}
+__device__ __forceinline__ ff ff_div_f(ff a, float b) {
+    const float q1 = a.hi / b;
+    const float p = q1 * b, e = fmaf(q1, b, -p);
+    const float r = ((a.hi - p) - e) + a.lo;
+    return ff_fast_sum(q1, r / b);
+}
+
 // J0(a b) - 1 for the mixed path's FP32 tables, from the float-float product x = a b:
 //  * x < 2: the power series sum_k (-y)^k / (k!)^2, y = x^2 / 4, as -y + (y^2/4) T(y) with y kept
 //    as float-float, so the leading term carries no rounding of its own (<= 1.34 ulp);
-//  * 2 <= x < 12: CUDA's FP64 j0, as in the FP64 tables (the series cancels there and the
-//    asymptotic form has not converged);
+//  * 2 <= x < 12: the same power series term by term in float-float arithmetic (32 terms; the
+//    largest term is ~4e3 at x = 12, and float-float's ~48 bits leave the sum within 1e-10
+//    relative, so the FP32 result is correctly rounded to within 0.5001 ulp);
 //  * x >= 12: Hankel's asymptotic expansion J0 = sqrt(2/(pi x)) (P cos chi - Q sin chi),
 //    chi = x - pi/4, with the first three terms of P and Q (Abramowitz & Stegun 9.2.5, 9.2.9,
 //    9.2.10 at nu = 0) and x reduced mod pi/2 exactly from the float-float product (<= 1.06 ulp).
@@ -50,7 +74,19 @@ __device__ float j0m1_mixed(double a, double b) {
         const float corr = (0.25f * yh * yh) * T;
         return (corr - ye) - yh;
     }
-    if (xh < 12.f) return (float)j0m1_d(a * b);
+    if (xh < 12.f) {
+        // y = x^2 / 4 in float-float; t_k = t_{k-1} (-y) / k^2, S = sum t_k
+        const float p = xh * xh;
+        const ff y = ff_fast_sum(p, fmaf(2.f * xh, xl, fmaf(xh, xh, -p)));
+        const ff ny = {-0.25f * y.hi, -0.25f * y.lo};
+        ff t = {1.f, 0.f}, S = {0.f, 0.f};
+#pragma unroll 4
+        for (int k = 1; k <= 32; ++k) {
+            t = ff_div_f(ff_mul(t, ny), (float)(k * k));
+            S = ff_add(S, t);
+        }
+        return S.hi + S.lo;
+    }
     float r, ph_hi, ph_lo;
     int qi;
     halfangle_reduce_ff(A, B, r, qi, ph_hi, ph_lo, 1.f);
