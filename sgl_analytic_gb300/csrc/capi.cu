@@ -468,8 +468,8 @@ sgl_status gemm_splitk_simt(sgl_ctx* ctx, GemmDesc<T> g, const std::string& tag,
     const int tiles = gemm_plan(&tmp, 1);
     int split = 1;
     if (tiles < 2 * kNumSMs) split = std::min(ceil_div(2 * kNumSMs, tiles), std::max(1, g.K / 512));
-    // min_split > 1 (mixed path): FP32 partial sums over at most K / min_split terms, combined in
-    // FP64 -- shorter FP32 accumulation chains
+    // min_split > 1 (mixed path): at least min_split slices of at least 32 terms; FP32 slices
+    // are combined in float-float
     split = std::max(split, std::min(min_split, std::max(1, g.K / 32)));
     if (split <= 1) { std::vector<GemmDesc<T>> v{g}; return run_gemms(ctx, v, tag); }
     const long long slice = (long long)g.M * g.N;
@@ -1015,9 +1015,12 @@ sgl_status sep_gemms(sgl_ctx* ctx, int precision, const double* h_kg, const doub
     const double Kg = nkg ? h_kg[nkg - 1] : 0.0;
     const int Nch = (S.n_cols_sep > 0 && Kg > 0) ? (int)(0.65 * S.max_sep_node * Kg + 50.0) : 0;
     const long long ld = 2LL * nk;
-    // mixed path: at least 8 K-slices, FP32 within a slice, slices combined in FP64 (the PDF tail
-    // is sensitive to the FP32 accumulation length of these sums)
-    const int msplit = precision == SGL_FP64 ? 1 : 8;
+    // mixed path: at least 2 K-slices, combined in float-float.  The FP32 kernel's compensated
+    // blocked accumulation already bounds the rounding of the long K sums (sep1 runs over ~6000
+    // gamma nodes): on the reference's z_s = 1 cells the PDF tail error against the reference is
+    // 2.1e-4 with 2 slices, where plain FP32 chains needed 64 slices to get below 5.4e-4.  The
+    // slice count is now a throughput choice.
+    const int msplit = precision == SGL_FP64 ? 1 : 2;
     const double* d_nodes = (const double*)ctx->arena.find("sep_nodes");
     if (S.n_cols_sep > 0) {
         if (nkg > 1 && Nch > 0 && Nch < 0.6 * nkg && h_kg[0] >= 0.0) {
@@ -2366,10 +2369,9 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
     const double dkg = kg[1] - kg[0], dkk = kk[1] - kk[0];
     launch_hankel_matrix(P, d_kg, nkg, dkg, d_gam, ngam, ldF, M, st); CKLAUNCH();
     launch_kappa_matrix(P, d_kk, nk, dkk, d_kap, nkap, CS, st); CKLAUNCH();
-    // mixed path: the transform sums run in >= 16 FP32 K-slices combined in float-float.  The PDF
-    // tail is most sensitive to their FP32 chain length: on the reference's z_s = 1 population
-    // 16 slices give a tail error of 5.9e-4 against 8.5e-4 with 8.
-    constexpr int kTransformSplit = 16;
+    // mixed path: the transform sums run in >= 4 K-slices combined in float-float; within a slice
+    // the FP32 kernel's compensated blocked accumulation bounds the chain's rounding
+    constexpr int kTransformSplit = 4;
     const double c = 1.0 / (2.0 * M_PI * M_PI);
     if (P == SGL_FP64) {
         CKS(gemm_splitk<double>(ctx, gd<double>(2 * nk, ngam, nkg, Phi, nkg, 1, M, ldF, 1, F, ldF), "hankel"));

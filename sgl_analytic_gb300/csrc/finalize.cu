@@ -15,6 +15,18 @@ std::atomic<long long>& launch_counter() {
 }
 
 // ------------------------------------------------------------------ GEMM launchers
+// The layout kernel's shared memory (operand tiles + running sums) is above the 48 KB static
+// limit: opted in once per instantiation.
+template <bool AK, bool BJ>
+void launch_f32_layout(const GemmDesc<float>* d_descs, int nprob, int tiles, cudaStream_t st) {
+    static const bool opted = cudaFuncSetAttribute(gemm_f32_layout_kernel<AK, BJ>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   kF32LayoutSmem) == cudaSuccess;
+    (void)opted;
+    gemm_f32_layout_kernel<AK, BJ><<<tiles, 256, kF32LayoutSmem, st>>>(d_descs, nprob);
+    SGL_COUNT(1);
+}
+
 // layout (FP32): bit 0 = every A is k-contiguous, bit 1 = every B is j-contiguous, -1 = mixed.
 // layout kSmallTiles (FP64): the descriptors were planned with 16 x 16 tiles.
 template <typename T>
@@ -29,10 +41,10 @@ void launch_grouped_gemm(const GemmDesc<T>* d_descs, int nprob, int tiles, int l
     }
     if constexpr (sizeof(T) == 4) {
         switch (layout) {
-            case 0: gemm_f32_layout_kernel<false, false><<<tiles, 256, 0, st>>>(d_descs, nprob); SGL_COUNT(1); return;
-            case 1: gemm_f32_layout_kernel<true, false><<<tiles, 256, 0, st>>>(d_descs, nprob); SGL_COUNT(1); return;
-            case 2: gemm_f32_layout_kernel<false, true><<<tiles, 256, 0, st>>>(d_descs, nprob); SGL_COUNT(1); return;
-            case 3: gemm_f32_layout_kernel<true, true><<<tiles, 256, 0, st>>>(d_descs, nprob); SGL_COUNT(1); return;
+            case 0: launch_f32_layout<false, false>(d_descs, nprob, tiles, st); return;
+            case 1: launch_f32_layout<true, false>(d_descs, nprob, tiles, st); return;
+            case 2: launch_f32_layout<false, true>(d_descs, nprob, tiles, st); return;
+            case 3: launch_f32_layout<true, true>(d_descs, nprob, tiles, st); return;
             default: break;
         }
     }

@@ -198,16 +198,27 @@ grouped_gemm_kernel<float>(const GemmDesc<float>* __restrict__ descs, int nprob)
 }
 
 // FP32 with the operand layouts fixed at compile time (AK: A is k-contiguous, BJ: B is
-// j-contiguous).  Same tiling and summation order as the generic FP32 kernel above, but the
-// per-thread load addresses are one base pointer plus constant strides and the edge predicates
-// are hoisted out of the K loop, which keeps the kernel within 128 registers: two CTAs (16 warps)
-// per SM instead of one.
+// j-contiguous).  Same tiling as the generic FP32 kernel above, but the per-thread load addresses
+// are one base pointer plus constant strides and the edge predicates are hoisted out of the K
+// loop, which keeps the kernel within 128 registers: two CTAs (16 warps) per SM instead of one.
+//
+// Compensated blocked accumulation.  The register accumulators run over kF32FoldTiles K-tiles
+// (64 products); then each is folded into a per-output running sum kept in shared memory with
+// Knuth's TwoSum, and the fold's exact rounding error is left in the register accumulator as the
+// start of the next block.  The FP32 rounding of a long chain (error ~ eps sqrt(K) |sum|, which
+// the PDF tail is sensitive to) is thereby confined to the 64-product blocks, each of which is
+// small next to the total: no extra registers, 64 KB of shared memory for the running sums
+// (thread t owns words t, t + 256, ... so the folds are bank-conflict free).
+constexpr int kF32FoldTiles = 4;
+constexpr int kF32LayoutSmem = (2 * 16 * (128 + 4) * 2 + 64 * 256) * 4;   // operands + running sums
 template <bool AK, bool BJ>
 __global__ void __launch_bounds__(256, 2)
 gemm_f32_layout_kernel(const GemmDesc<float>* __restrict__ descs, int nprob) {
     constexpr int BM = 128, BN = 128, BK = 16, PAD = 4;
-    __shared__ __align__(16) float As[2][BK][BM + PAD];
-    __shared__ __align__(16) float Bs[2][BK][BN + PAD];
+    extern __shared__ __align__(16) float gemm_f32_smem[];
+    auto As = reinterpret_cast<float (*)[BK][BM + PAD]>(gemm_f32_smem);
+    auto Bs = reinterpret_cast<float (*)[BK][BN + PAD]>(gemm_f32_smem + 2 * BK * (BM + PAD));
+    float* const Hs = gemm_f32_smem + 2 * BK * (BM + PAD) + 2 * BK * (BN + PAD);
     const int tile = blockIdx.x;
     int p = 0, ph = nprob - 1;
     while (p < ph) {
@@ -258,7 +269,21 @@ gemm_f32_layout_kernel(const GemmDesc<float>* __restrict__ descs, int nprob) {
 #pragma unroll
     for (int a = 0; a < 8; ++a)
 #pragma unroll
-        for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
+        for (int b = 0; b < 8; ++b) { acc[a][b] = 0.f; Hs[(a * 8 + b) * 256 + tid] = 0.f; }
+    // running sum += acc by TwoSum; acc keeps the exact rounding error of that addition
+    auto fold = [&]() {
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                float* hp = Hs + (r * 8 + c) * 256 + tid;
+                const float h = *hp, a = acc[r][c];
+                const float sum = h + a;
+                const float bb = sum - h;
+                acc[r][c] = (h - (sum - bb)) + (a - bb);
+                *hp = sum;
+            }
+    };
     const int ntiles = (d.K + BK - 1) / BK;
     load_tiles(0);
     store_tiles(0);
@@ -281,6 +306,7 @@ gemm_f32_layout_kernel(const GemmDesc<float>* __restrict__ descs, int nprob) {
         }
         if (t + 1 < ntiles) store_tiles(cur ^ 1);
         __syncthreads();
+        if ((t + 1) % kF32FoldTiles == 0 && t + 1 < ntiles) fold();
     }
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
@@ -291,7 +317,7 @@ gemm_f32_layout_kernel(const GemmDesc<float>* __restrict__ descs, int nprob) {
             const int gj = j0 + tx * 4 + (c & 3) + (c >> 2) * 64;
             if (gj >= d.N) continue;
             float* cp = d.C + (long long)gi * d.ldc + gj;
-            float v = d.alpha * acc[r][c];
+            float v = d.alpha * (Hs[(r * 8 + c) * 256 + tid] + acc[r][c]);
             if (d.beta != 0.f) v += d.beta * *cp;
             *cp = v;
         }

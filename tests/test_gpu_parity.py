@@ -267,10 +267,11 @@ def test_grid_above_block_threshold_matches_reference(precision):
     if precision == "fp64":
         assert dpeak <= TOL_PEAK, dpeak
     else:
-        # 300 cells carrying the weight of 80k: ln Phi is a sum of few large terms, and the mixed
-        # path's FP32 Lambda evaluation leaves a tail error of 1.6e-3 here (FP64 Lambda with the
-        # FP32 inversion: 7.9e-4).  The L1 bar holds; the tail bar is met on the reference's own
-        # populations (z_s = 0.5, 1, 3, 10), not on this one.
+        # 300 cells carrying the weight of 80k: ln Phi is a sum of few large terms.  The worst
+        # tail point sits at 1.0e-6 of the peak, where the mixed path's FP32 noise (about equal
+        # parts Lambda and inversion; no single stage dominates when run in FP64) leaves a
+        # relative error of 1.2e-3 to 1.7e-3.  The L1 bar holds; the tail bar is met on the
+        # reference's own populations (z_s = 0.5, 1, 3, 10), not on this one.
         assert l1 <= 1e-4, (dpeak, l1, rel_tail)
         assert rel_tail <= 3e-3, (dpeak, l1, rel_tail)
 
