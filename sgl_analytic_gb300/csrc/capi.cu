@@ -822,6 +822,53 @@ sgl_status xi_eval(sgl_ctx* ctx, int precision, const double* d_kk, const double
         DBUF(d_part, double, "xi_line_part", 2LL * kLineChunks * nkg);
         launch_xi_line_g(ctx->xid, d_kg, nkg, d_re, d_im, d_part, st); CKLAUNCH(); return SGL_OK;
     }
+    if (precision == SGL_MIXED && xi_fused_fits(ctx->xid.r_max, nk, X.n_gmc)) {
+        // fused tcgen05 form: per (group, tile of <= 8 k_gamma columns) one CTA builds T in shared
+        // memory, contracts it with the packed E in TMEM and squares in its epilogue
+        const int ng = X.n_groups;
+        std::vector<int> jt(ng);
+        std::vector<long long> pre(3LL * ng + 2, 0);      // cta_prefix | padded-p prefix | E offsets
+        long long* cta_prefix = pre.data();
+        long long* pp_prefix = pre.data() + ng + 1;
+        long long* e_off = pre.data() + 2 * (ng + 1);
+        double fl = 0.0;
+        for (int g = 0; g < ng; ++g) {
+            jt[g] = xi_fused_jt(X.r[g]);
+            cta_prefix[g + 1] = cta_prefix[g] + (nkg + jt[g] - 1) / jt[g];
+            e_off[g] = pp_prefix[g] * 512;                  // 32 KB of packed E per 16 p
+            pp_prefix[g + 1] = pp_prefix[g] + 16LL * ((X.nP[g] + 15) / 16);
+            fl += 2.0 * (2.0 * nk) * ((double)X.r[g] * nkg) * X.nP[g];
+        }
+        DBUF(d_jt, int, "xf_jt", ng);
+        DBUF(d_pre, long long, "xf_prefix", pre.size());
+        CKS(upload(ctx, d_jt, jt.data(), (size_t)ng));
+        CKS(upload(ctx, d_pre, pre.data(), pre.size()));
+        float* J = (float*)ctx->arena.get("xi_J", 4ULL * X.n_gmc * nkg * sizeof(float));
+        if (!J) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (xi)");
+        DBUF(Epk, float, "xf_E", std::max<long long>(1, pp_prefix[ng] * 512));
+        DBUF(part, float2, "xf_part", (long long)ng * nkg * nk);
+        DBUF(d_Vf, float, "xi_Vf", (long long)X.total_rows * nkg);
+        DBUF(d_kres, float2, "xi_kres", (long long)nk * X.total_rows);
+        DBUF(d_hq, float2, "xi_hq", (long long)X.total_rows * nkg);
+        DBUF(d_J64, double, "xi_J64", 4LL * X.n_gmc * nkg);
+        const long long* d_pp = (const long long*)ctx->arena.find("xi_pprefix");
+        int* err = dev_err_flag(ctx);
+        if (!err) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (error flag)");
+        launch_bessel_tables(SGL_MIXED, ctx->xid.gmc, X.n_gmc, d_kg, nkg, J, st); CKLAUNCH();
+        launch_xi_E_pack(ctx->xid, d_kk, nk, d_pre + (ng + 1), pp_prefix[ng], d_pp, d_pre + 2 * (ng + 1), Epk, st);
+        CKLAUNCH();
+        launch_bessel_tables(SGL_FP64, ctx->xid.gmc, X.n_gmc, d_kg, nkg, d_J64, st); CKLAUNCH();
+        launch_xi_V_mixed(ctx->xid, d_J64 + 3LL * X.n_gmc * nkg, nkg, d_Vf, X.total_rows, d_kk, nk, d_kg, d_kres, d_hq,
+                          st, 1);
+        CKLAUNCH();
+        {
+            Timed t(ctx, "xi_fused", fl, 0.0);
+            launch_xi_fused(ctx->xid, d_pp, d_pp + (ng + 1), d_jt, d_pre, cta_prefix[ng], d_pre + 2 * (ng + 1), Epk, J,
+                            d_Vf, d_kres, d_hq, nk, nkg, part, err, d_re, d_im, st);
+        }
+        CKLAUNCH();
+        return SGL_OK;
+    }
     const size_t es = elem_size(precision);
     // offsets
     std::vector<long long> T_off(X.n_groups), E_off(X.n_groups), G_off(X.n_groups);
@@ -1655,7 +1702,7 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
             DBUF(d_idxq0, int, "xi_idxq", idx_q.size());
             DBUF(d_kmc0, double, "xi_kmc", X.n_kmc);
             DBUF(d_rows0, double, "xi_rows", rowel_total);
-            DBUF(d_rowsf0, float, "xi_rows_f", rowel_total);
+            DBUF(d_rowsf0, float, "xi_rows_f", rowel_total + kXiTailPad);
             DBUF(d_res0, double, "xi_res", row_total);
             DBUF(d_sum0, double, "xi_sum", row_total);
             DBUF(d_sig0, double, "xi_prep_sig", std::max<long long>(1, row_total));
@@ -1796,7 +1843,7 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         DBUF(d_pp, long long, "xi_pprefix", 2 * X.n_groups + 1);
         DBUF(d_idxp, int, "xi_idxp", idx_p.size());
         DBUF(d_pptr, int, "xi_pptr", p_ptr.size());
-        DBUF(d_qg, int, "xi_entq", ent_qg.size());
+        DBUF(d_qg, int, "xi_entq", ent_qg.size() + kXiTailPad);
         DBUF(d_rows, double, "xi_rows", rowel_total);
         DBUF(d_res, double, "xi_res", res.size());
         DBUF(d_sum, double, "xi_sum", sum_rows.size());
@@ -1826,7 +1873,7 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
         D.g_p_off = d_goff; D.g_ent_off = d_goff + X.n_groups; D.g_row_off = d_goff + 2 * X.n_groups;
         D.idx_p = d_idxp; D.p_ptr = d_pptr; D.ent_qg = d_qg; D.rows = d_rows; D.res = d_res; D.sum_rows = d_sum;
         {
-            DBUF(d_rowsf, float, "xi_rows_f", rowel_total);
+            DBUF(d_rowsf, float, "xi_rows_f", rowel_total + kXiTailPad);
             if (rowel_total > 0 && !dev_filled)
                 CK(cudaMemcpyAsync(d_rowsf, rows_tf_p, (size_t)rowel_total * 4, cudaMemcpyHostToDevice, ctx->stream));
             DBUF(d_gnQ, int, "xi_gnQ", g_nQ.size());

@@ -92,7 +92,18 @@ void launch_xi_square(int precision, const XiDevice& x, const long long* G_off, 
                       double* out_im, cudaStream_t st);
 void launch_xi_V(const XiDevice& x, const double* J0m1, int nkg, double* V, int total_rows, cudaStream_t st);
 void launch_xi_V_mixed(const XiDevice& x, const double* J0m1, int nkg, float* Vf, int total_rows, const double* kk,
-                       int nk, const double* kg, float2* kres, float2* hq, cudaStream_t st);
+                       int nk, const double* kg, float2* kres, float2* hq, cudaStream_t st, int kres_t = 0);
+// fused mixed gauss Psi_2 (tcgen05; xi_fused.cu): T built in shared memory, contracted with the
+// packed E in TMEM, squared and summed over rows in the epilogue
+int xi_fused_jt(int r);
+constexpr int kXiTailPad = 16;     // elements after rows_f and ent_qg: room for 16-byte-aligned bulk copies
+bool xi_fused_fits(int r_max, int nk, int n_gmc);
+void launch_xi_E_pack(const XiDevice& x, const double* kk, int nk, const long long* pp_prefix, long long total_pp,
+                      const long long* p_prefix, const long long* e_off, float* Epk, cudaStream_t st);
+void launch_xi_fused(const XiDevice& x, const long long* p_prefix, const long long* rowel_off, const int* jt,
+                     const long long* cta_prefix, long long ctas, const long long* e_off, const float* Epk,
+                     const float* J, const float* Vf, const float2* kresT, const float2* hq, int nk, int nkg,
+                     float2* part, int* err, double* out_re, double* out_im, cudaStream_t st);
 void launch_xi_square_mixed(const XiDevice& x, const long long* G_off, const float* G, int nk, int nkg, const float* Vf,
                             const float2* kres, const float2* hq, int rows, int nsplit, double* part, double* out_re,
                             double* out_im, cudaStream_t st);

@@ -495,15 +495,16 @@ void launch_xi_V(const XiDevice& x, const double* J0m1, int nkg, double* V, int 
 // Mixed path: V rounded to FP32 where it is formed (the square kernel adds it in FP32), and the two
 // per-row correction terms of the square kernel as float-float tables, formed once in FP64:
 //   kres[n][R] = k_n res_R (m = 0 rows: imaginary part)   hq[R][j] = q_j res_R / 2 (m = 1 rows)
+// kres_t = 1: kres laid out [R][n] instead (the fused kernel reads it with lanes along n).
 __global__ void k_xi_corr_tables(const double* __restrict__ res, int rows, const double* __restrict__ kk, int nk,
                                  const double* __restrict__ kg, int nkg, float2* __restrict__ kres,
-                                 float2* __restrict__ hq) {
+                                 float2* __restrict__ hq, int kres_t) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long n1 = (long long)nk * rows, n2 = (long long)rows * nkg;
     if (t < n1) {
         const double v = kk[t / rows] * res[t % rows];
         const ff f = ff_from_double(v);
-        kres[t] = make_float2(f.hi, f.lo);
+        kres[kres_t ? (t % rows) * nk + t / rows : t] = make_float2(f.hi, f.lo);
     } else if (t < n1 + n2) {
         const long long u = t - n1;
         const double v = (0.5 * kg[u % nkg]) * res[u / nkg];
@@ -513,12 +514,12 @@ __global__ void k_xi_corr_tables(const double* __restrict__ res, int rows, const
 }
 
 void launch_xi_V_mixed(const XiDevice& x, const double* J0m1, int nkg, float* Vf, int total_rows, const double* kk,
-                       int nk, const double* kg, float2* kres, float2* hq, cudaStream_t st) {
+                       int nk, const double* kg, float2* kres, float2* hq, cudaStream_t st, int kres_t) {
     if (total_rows <= 0) return;
     k_xi_V<float><<<total_rows, 128, 0, st>>>(x, J0m1, nkg, Vf);
     SGL_COUNT(1);
     const long long tot = (long long)nk * total_rows + (long long)total_rows * nkg;
-    k_xi_corr_tables<<<ceil_div(tot, 256), 256, 0, st>>>(x.res, total_rows, kk, nk, kg, nkg, kres, hq);
+    k_xi_corr_tables<<<ceil_div(tot, 256), 256, 0, st>>>(x.res, total_rows, kk, nk, kg, nkg, kres, hq, kres_t);
     SGL_COUNT(1);
 }
 

@@ -28,18 +28,9 @@
 #include <cuda_bf16.h>
 
 #include "kernels.cuh"
+#include "tcgen05.cuh"
 
 namespace sgl {
-
-constexpr int kTcBM = 128;                 // tile rows = TMEM lanes
-constexpr int kTcBNmax = 256;              // tile columns = TMEM columns allocated
-constexpr int kTcBK = 16;                  // K per stage: two MMA k-steps of 8 (TF32)
-constexpr int kTcThreads = 128;
-constexpr int kTcLBO = 128;                // bytes between core matrices along K
-constexpr int kTcSBO = 512;                // bytes between 8-row groups
-constexpr int kTcAbytes = kTcBM * kTcBK * 4;          // 8 KB per TF32 part
-constexpr int kTcBbytes = kTcBNmax * kTcBK * 4;       // 16 KB per TF32 part (bn <= 256)
-constexpr long long kTcWaitCycles = 4000000000LL;     // ~2 s at 2 GHz
 
 template <int NP> struct TcCfg {
     static constexpr int kStages = NP == 3 ? 3 : 4;
@@ -47,87 +38,6 @@ template <int NP> struct TcCfg {
     static constexpr int kBarOff = kStages * kStageBytes;                  // mbarriers after the ring
     static constexpr int kSmem = kBarOff + 128;
 };
-
-// shared-memory matrix descriptor: start >> 4 [0,14), LBO >> 4 [16,30), SBO >> 4 [32,46),
-// descriptor version 1 [46,48), base offset 0, no swizzle (layout type 0 in [61,64))
-__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
-    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
-    d |= (uint64_t)(kTcLBO >> 4) << 16;
-    d |= (uint64_t)(kTcSBO >> 4) << 32;
-    d |= (uint64_t)1 << 46;
-    return d;
-}
-
-// instruction descriptor, kind::tf32: D f32 [4,6) = 1, A tf32 [7,10) = 2, B tf32 [10,13) = 2,
-// both K-major (bits 15, 16 = 0), N >> 3 at [17,23), M >> 4 at [24,29)
-__device__ __forceinline__ uint32_t tc_idesc_tf32(int M, int N) {
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-// instruction descriptor, kind::f16 with BF16 inputs: D f32 = 1, A bf16 [7,10) = 1, B bf16 [10,13) = 1
-__device__ __forceinline__ uint32_t tc_idesc_bf16(int M, int N) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void tc_mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
-                 :: "r"(tmem_d), "l"(a), "l"(b), "r"(idesc), "r"(acc) : "memory");
-}
-
-__device__ __forceinline__ float tf32_rna(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
-}
-
-__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                 "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n"
-                 :: "r"(tmem_d), "l"(a), "l"(b), "r"(idesc), "r"(acc) : "memory");
-}
-
-__device__ __forceinline__ void tc_commit(uint32_t mbar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(mbar) : "memory");
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t mbar, int count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(mbar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(mbar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                 :: "r"(dst), "l"(src), "r"(bytes), "r"(mbar) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                 "selp.b32 %0, 1, 0, p;\n\t}\n" : "=r"(ok) : "r"(mbar), "r"(parity) : "memory");
-    return ok != 0;
-}
-
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity) {
-    const long long t0 = clock64();
-    while (!mbar_try(mbar, parity))
-        if (clock64() - t0 > kTcWaitCycles) return false;
-    return true;
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-    uint32_t r[16];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-                 : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int q = 0; q < 16; ++q) v[q] = __uint_as_float(r[q]);
-}
 
 // ------------------------------------------------------------------ packing
 // One thread per (row, 4 consecutive k): reads X(r, k..k+3), writes the NP float4 rows of its core
