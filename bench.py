@@ -42,10 +42,12 @@ WORKLOAD = ("z_s=1 default flat LCDM PDF: reference z_s=1 population (79,574 fin
             "groups with the reference's z_s=1 shapes (shell-30 groups scaled to each shell's row norm), "
             "gauss closure, CLI ln mu grids (1601 + 1600 points), FP64 oracle-pinned")
 XI_OUT = np.concatenate([np.linspace(-1.0, 1.0, 1601), np.linspace(1.005, 9.0, 1600)])
+XI_COARSE = 101        # the gauss term's coarse k grid per axis (Lam xi_coarse default)
 # DRAM bytes (read + write) per launch of the dominant kernels, from one ncu capture of this
 # workload (profiles/ holds the summaries and the commands)
 TRAFFIC = {"gemm_f32_xi": 1.2079e9,         # profiles/gemm_f32_xi_zs1.md
-           "xi_stageA": 1.4778e9}          # profiles/xi_stageA_pack_zs1.md
+           "xi_stageA": 1.4778e9,          # profiles/xi_stageA_pack_zs1.md
+           "xi_fused": 2.7385e8}           # profiles/xi_fused_zs1.md
 
 
 def dist_env():
@@ -473,6 +475,15 @@ def main():
                 # the kernel runs on the FP32 FMA pipe (SIMT): its own ceiling is the FMA probe
                 f32 = eng.measure_peak(False)
                 roof["simt_fp32"] = {"peak": f32, "frac": ach / f32, "peak_source": "FP32 FMA probe, this run"}
+            if top == "xi_fused":
+                # the fused Psi_2 kernel's tensor-core contraction (above) is fed by its CUDA-core
+                # producer, which forms T = rows x J_m entry by entry in FP32: its FMA work per launch
+                # is sum over groups of entries x rows x coarse k_gamma columns
+                t_fl = 2.0 * float(np.sum(pop.xg_nidx.astype(np.float64) * pop.xg_nrow)) * XI_COARSE
+                f32 = eng.measure_peak(False)
+                a32 = t_fl / (per_ms / 1e3) / 1e12
+                roof["producer_fp32"] = {"flops_per_launch": t_fl, "achieved": a32, "peak": f32, "frac": a32 / f32,
+                                         "peak_source": "FP32 FMA probe, this run"}
         else:
             ach = r["bytes"] / r["launches"] / (per_ms / 1e3) / 1e9
             roof = {"kernel": top, "bound": "hbm", "achieved": ach, "peak": float(pk["hbm_gbs"]), "unit": "GB/s",

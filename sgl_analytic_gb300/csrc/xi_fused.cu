@@ -452,14 +452,23 @@ __global__ void k_xi_fused_sum(const float2* __restrict__ part, const int* __res
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (long long)nk * nkg) return;
     const int j = (int)(e / nk), n = (int)(e % nk);
+    const long long stride = (long long)nkg * nk;
+    const float2* pp = part + (long long)j * nk + n;
     double re = 0.0, im = 0.0;
-    for (int g = 0; g < n_groups; ++g) {
-        const int m = g_m[g];
+    auto add = [&](int m, float2 v) {
         const double sign = (m == 0) ? 1.0 : ((m & 1) ? -2.0 : 2.0);
-        const float2 v = part[((long long)g * nkg + j) * nk + n];
         re = fma(0.5 * sign, (double)v.x, re);
         im = fma(0.5 * sign, 2.0 * (double)v.y, im);
+    };
+    int g = 0;
+    for (; g + 8 <= n_groups; g += 8) {            // eight loads in flight, summed in group order
+        float2 v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = pp[(long long)(g + k) * stride];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) add(g_m[g + k], v[k]);
     }
+    for (; g < n_groups; ++g) add(g_m[g], pp[(long long)g * stride]);
     out_re[(long long)n * nkg + j] = re;
     out_im[(long long)n * nkg + j] = im;
 }
