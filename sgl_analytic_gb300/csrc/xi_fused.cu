@@ -12,15 +12,17 @@
 // G never reach global memory: the unfused form writes and re-reads about 2 GB of them per PDF.
 //
 // Pipeline (kXfStages shared-memory stages of 64 KB: E 4 x 8 KB [part][cos | sin], T 2 x 16 KB [part]):
-//   8 producer warps  build the T tile of a 16-p K block from the CSR entries (rows and gamma-cell
-//                     indices bulk-copied to shared memory in chunks, J_m of the CTA's columns staged
-//                     once), one warp per (4-p block, column half) with lanes over rows, split it into
-//                     TF32 hi + lo and store it in the canonical K-major layout; fence.proxy.async, arrive;
+//   12 producer warps build the T tile of a 16-p K block from the CSR entries: 3 warps per 4-p block,
+//                     lanes over (column half, row) tasks; each block's entries (rows and gamma-cell
+//                     indices) stream through its own two shared-memory chunk buffers by bulk copy,
+//                     J_m of the CTA's columns is staged once; T is split into TF32 hi + lo and
+//                     stored in the canonical K-major layout; fence.proxy.async, one arrival per warp;
 //   1 copy thread     brings the packed E block (both parts, both halves) with one bulk copy;
 //   1 MMA thread      issues A0 B0 + A0 B1 + A1 B0 (TF32 hi/lo, ~2^-21 per product) into the cos and
 //                     sin accumulators (TMEM columns 0 and 256) and commits each stage to its "empty"
 //                     barrier.
 // The summation order of T over entries and of the squares over rr is that of the unfused kernels.
+// The epilogue's correction terms are staged by the producers in the freed chunk buffers.
 // Every wait is bounded; a wait that runs out sets *err and the CTA skips to its TMEM release.
 #include "kernels.cuh"
 #include "tcgen05.cuh"
@@ -37,12 +39,12 @@ constexpr int kXfProdWarps = 4 * kXfGroupWarps;
 constexpr int kXfProd = kXfProdWarps * 32;
 constexpr int kXfThreads = kXfProd + 64;             // + copy warp + MMA warp
 constexpr int kXfJt = 8;                             // k_gamma columns per CTA at most
-constexpr int kXfChunk = 64;                         // entries per chunk of one warp pair
+constexpr int kXfChunk = 64;                         // entries per chunk of one warp group
 constexpr int kXfSmemStages = kXfStages * kXfStageBytes;
 constexpr int kXfRowsBuf = kXfChunk * kXfRMax * 4 + 64;      // + room for the aligned superset
 constexpr int kXfQBuf = kXfChunk * 4 + 64;
-constexpr int kXfPairs = 4;                          // producer warp groups, one per 4-p block
-constexpr int kXfChunkBytes = kXfPairs * 2 * (kXfRowsBuf + kXfQBuf);
+constexpr int kXfBlocks = 4;                          // producer warp groups, one per 4-p block of a K block
+constexpr int kXfChunkBytes = kXfBlocks * 2 * (kXfRowsBuf + kXfQBuf);
 constexpr int kXfSmemFixed = kXfSmemStages + kXfChunkBytes;
 static_assert(2 * kXfRMax <= 32 * kXfGroupWarps, "one (row, column half) task per producer lane");
 static_assert(kXfRMax * 128 * 8 + kXfRMax * kXfJt * 8 <= kXfChunkBytes, "epilogue tables fit the chunk buffers");
@@ -66,7 +68,7 @@ __device__ __forceinline__ float xf_add_ff(float b, float2 hl) {   // round(b + 
 int xi_fused_jt(int r) { return r <= 0 ? 0 : std::min(kXfJt, 256 / r); }
 
 // stages, entry chunks, J_m columns, then the mbarriers, the TMEM address and the failure flag
-size_t xi_fused_smem(int n_gmc) { return (size_t)kXfSmemFixed + (size_t)n_gmc * kXfJt * 4 + 8 * (2 * kXfStages + 1 + 2 * kXfPairs) + 32; }
+size_t xi_fused_smem(int n_gmc) { return (size_t)kXfSmemFixed + (size_t)n_gmc * kXfJt * 4 + 8 * (2 * kXfStages + 1 + 2 * kXfBlocks) + 32; }
 
 bool xi_fused_fits(int r_max, int nk, int n_gmc) {
     return nk >= 1 && nk <= 128 && r_max >= 1 && r_max <= kXfRMax && xi_fused_smem(n_gmc) <= 227 * 1024;
@@ -118,7 +120,7 @@ struct XiFusedArgs {
     int* err;
 };
 
-// one entry chunk of a warp pair: entries [ea, eb) of its 4-p block in K block kb, at most kXfChunk
+// one entry chunk of a warp group: entries [ea, eb) of its 4-p block in K block kb, at most kXfChunk
 struct XfChunk { int kb, ea, eb; };
 
 __global__ void __launch_bounds__(kXfThreads, 1)
@@ -137,8 +139,8 @@ k_xi_fused(XiFusedArgs a) {
     float* s_J = (float*)(xsm + kXfSmemFixed);                           // [n_gmc][8]
     const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(xsm);
     const uint32_t boff = kXfSmemFixed + n_gmc * kXfJt * 4;
-    const uint32_t bar = sbase + boff;                   // full[S], empty[S], done, chunk[pairs][2]
-    constexpr int kNBar = 2 * kXfStages + 1 + 2 * kXfPairs;
+    const uint32_t bar = sbase + boff;                   // full[S], empty[S], done, chunk[groups][2]
+    constexpr int kNBar = 2 * kXfStages + 1 + 2 * kXfBlocks;
     const uint32_t tslot = bar + 8 * kNBar;
     volatile int* s_fail = (volatile int*)(xsm + boff + 8 * kNBar + 8);
     auto full = [&](int s) { return bar + 8 * s; };
@@ -156,7 +158,7 @@ k_xi_fused(XiFusedArgs a) {
             mbar_init(empty(s), 1);
         }
         mbar_init(done, 1);
-        for (int b = 0; b < 2 * kXfPairs; ++b) mbar_init(cbar(b >> 1, b & 1), 1);
+        for (int b = 0; b < 2 * kXfBlocks; ++b) mbar_init(cbar(b >> 1, b & 1), 1);
         *s_fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -188,7 +190,7 @@ k_xi_fused(XiFusedArgs a) {
         const int jh = active ? t / r : 0, rr = active ? t - jh * r : 0;
         const bool issuer = sub == 0 && lane == 0;
         float* const rbuf0 = (float*)(xsm + kXfSmemStages + (pb * 2) * kXfRowsBuf);
-        int* const qbuf0 = (int*)(xsm + kXfSmemStages + 2 * kXfPairs * kXfRowsBuf + (pb * 2) * kXfQBuf);
+        int* const qbuf0 = (int*)(xsm + kXfSmemStages + 2 * kXfBlocks * kXfRowsBuf + (pb * 2) * kXfQBuf);
         auto lo_of = [&](int kb) { return pptr[min(16 * kb + 4 * pb, nP)]; };
         auto hi_of = [&](int kb) { return pptr[min(16 * kb + 4 * pb + 4, nP)]; };
         auto rows_at = [&](int e) { return rowsg + (long long)(e - ent0) * r; };
