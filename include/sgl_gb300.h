@@ -39,10 +39,11 @@ typedef enum {
 /* Arithmetic of the Lambda evaluation and of the inversion. */
 typedef enum {
     SGL_FP64 = 0,   /* FP64 throughout: parity path, max|d lnPhi| <= 1e-10 vs the reference */
-    SGL_MIXED = 1   /* float-float phase with exact reduction, FP32 sin/cos/J0 and SIMT GEMMs,
-                       FP64 split-K and cross-tile combines; the k-reach probes sum FP32 terms in
-                       FP64.  Bars: PDF L1 <= 1e-4, tail relative error <= 1e-3 (met on the
-                       reference's populations; few-cell, heavy-weight populations want FP64) */
+    SGL_MIXED = 1   /* float-float phase with exact reduction, FP32 sin/cos/J0, SIMT GEMMs with
+                       compensated blocked accumulation and float-float split-K combines, the gauss
+                       xi term on tcgen05 (TF32 hi/lo); the k-reach probes sum FP32 terms in FP64.
+                       Bars: PDF L1 <= 1e-4, tail relative error <= 1e-3 (met on the reference's
+                       populations; few-cell, heavy-weight populations want FP64) */
 } sgl_precision;
 
 /* Options of the inversion; defaults = pipeline.run's gauss chain (pipeline.py:221-239). */

@@ -283,7 +283,7 @@ k_xi_fused(XiFusedArgs a) {
                 }
             }
             if (nxt.kb != cur.kb) {
-                // the pair's share of K block kb is complete: its stage must have been consumed by the
+                // the group's share of K block kb is complete: its stage must have been consumed by the
                 // MMAs of kb - S
                 const int kb = cur.kb, s = kb % kXfStages;
                 if (kb >= kXfStages && !mbar_wait_sleep(empty(s), (uint32_t)(((kb / kXfStages) - 1) & 1)))
