@@ -110,6 +110,25 @@ def test_xi_term_mixed_vs_fp64(lamx, ref_sub):
     assert np.max(np.abs(Q - Qr)) <= 1e-5 * max(1.0, np.max(np.abs(Qr)))
 
 
+@pytest.mark.parametrize("rows", [5, 17])
+def test_xi_term_mixed_few_rows(pop_sub, ref_sub, rows):
+    """Groups with fewer rows than one warp of row tasks (the committed groups have 33-36): the
+    mixed xi term (fused tcgen05 kernel) against the FP64 term on the coarse grid."""
+    from dataclasses import replace
+
+    from sgl_analytic_gb300 import Lam
+    from sgl_analytic_gb300._lib import SGL_FP64, SGL_MIXED
+    # each group's rows are nrow x (nidx + 1), row-major (the last column is the residual)
+    nr, nc = pop_sub.xg_nrow.astype(np.int64), pop_sub.xg_nidx.astype(np.int64) + 1
+    off = np.concatenate([[0], np.cumsum(nr * nc)])
+    blocks = [pop_sub.xg_rows[off[g]:off[g] + rows * nc[g]] for g in range(nr.size)]
+    pop = replace(pop_sub, xg_nrow=np.full(nr.size, rows, np.int32), xg_rows=np.concatenate(blocks))
+    lam = Lam(pop, xi=True)
+    Q64 = lam.engine.xi_term(ref_sub["kkc"], ref_sub["kgc"], SGL_FP64)
+    Qmx = lam.engine.xi_term(ref_sub["kkc"], ref_sub["kgc"], SGL_MIXED)
+    assert np.max(np.abs(Qmx - Q64)) <= 1e-5 * max(1.0, np.max(np.abs(Q64)))
+
+
 def test_lambda_full_grid_mixed_vs_fp64(lamx):
     from sgl_analytic_gb300._lib import SGL_FP64, SGL_MIXED
     L64 = lamx.engine.lnphi(KK16, KG_FULL, SGL_FP64)
