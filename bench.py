@@ -505,7 +505,7 @@ def main():
                 "config": {"workload": WORKLOAD, "precision": args.precision,
                            "k_grid": f"{g['nk_k']}x{g['nk_g']}", "out_grid": f"{g['n_kap']}x{g['n_gam']}",
                            "parallelism": f"replicas x{world}", "pdfs_in_flight": max(1, args.slots),
-                           "l2": "per-PDF working set > L2 (Psi_2 intermediates ~2.5 GB, T 190 MB)"},
+                           "l2": "inputs > L2 every step (xi group rows 151 MB FP32, separable T 86 MB, Phi 29 MB)"},
                 "accuracy": {"pdf_l1_vs_fp64": l1, "bar": 1e-4, "tail_rel_vs_fp64": tail_rel, "tail_bar": 1e-3},
                 "single_stream": {"value": single_value, "unit": "PDF/s", "ms_per_pdf": single_ms},
                 "batched": batched,
