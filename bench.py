@@ -313,7 +313,7 @@ def main():
                     help="PDFs in flight at once (contexts on their own streams) for the headline value")
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--workload", default="zs1_pdf", choices=("zs1_pdf", "cf_sweep", "surrogate"))
     ap.add_argument("--sur-epochs", type=int, default=20)
     ap.add_argument("--sweep-instances", type=int, default=8)
