@@ -186,7 +186,7 @@ sgl_status sgl_mlp_mse(sgl_ctx* ctx, int64_t n, const float* pred, const float* 
 sgl_status sgl_mlp_adamw(sgl_ctx* ctx, int64_t n, float* w, const float* g, float* m, float* v, float lr,
                          float b1, float b2, float eps, float wd, int step);
 
-/* Measured FMA throughput of this GPU/* Measured FMA throughput of this GPU (fp64 = 1: FP64, 0: FP32), TFLOP/s (2 flops per FMA):
+/* Measured FMA throughput of this GPU (fp64 = 1: FP64, 0: FP32), TFLOP/s (2 flops per FMA):
  * the denominator of the CF-sweep roofline.  No counterpart in the reference. */
 sgl_status sgl_measure_peak(sgl_ctx* ctx, int fp64, double* tflops);
 
