@@ -1,24 +1,28 @@
 #!/usr/bin/env python
 """Benchmark: z_s=1 magnification PDFs per second on one GB300 (plain GPU solver).
 
-One step = one full PDF of the z_s=1 default-cosmology workload (sgl_analytic_gb300.workloads):
-measured k-reach probes, ln Phi on the 1688 x 2150 k-grid (separable Psi_1 over 79,574 cells +
-201 xi_lin groups on the 101^2 coarse grid + bicubic spline), exp, Hankel and kappa transforms,
+One step = one full PDF of generate_pdf_lnmu(1.0) with the default flat LCDM cosmology, on the
+reference's own z_s=1 population (tests/golden/full/cells_zs1_gauss_full.npz, made by the
+reference's code: 79,574 fine cells and 201 xi_lin groups): measured k-reach probes, ln Phi on the
+1683 x 2687 k-grid (separable Psi_1 + the gauss xi term on the 101^2 coarse grid + bicubic
+spline), exp, Hankel and kappa transforms onto the 2400 x 796 (kappa, gamma) grid,
 Euler-Maclaurin term, constant-mu path integrals on 500 + 3201 ln mu points, normalisation.
+Without that file a labelled stand-in (xi groups synthesised from one shell) is used.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64] [--impl ours|reference]
 
 * value    PDFs/s with the population resident in HBM, device-timed with CUDA events on the
-           engine's stream (max over ranks; N ranks run N independent replicas: weak scaling).
+           engine's streams (max over ranks; N ranks run N independent replicas: weak scaling).
 * e2e      the same metric through the drop-in call Lam(population) + invert(...) with HOST
            buffers: population upload (H2D), every PDF stage, P_s read back (D2H) per step.
 * roofline the kernel with the largest device time in the timed region: its algorithmic FLOPs
            (or bytes) per launch / its event-timed duration, against the measured peak.
-* accuracy every PDF of the timed arm is checked against the FP64 oracle-pinned GPU path:
-           PDF L1 over ln mu in [-1, 9] (bar 1e-4) and the tail relative error (bar 1e-3).
-* fp64_path the parity path (max |d ln Phi| <= 1e-10 vs the reference) timed the same way.
+* accuracy every PDF of the timed regions and of the e2e loop, against the reference's stored
+           z_s=1 PDF (pdf_zs1.json) and against the FP64 path: max |dP| / peak, PDF L1 over
+           ln mu in [-1, 9] (bar 1e-4) and the tail relative error for ln mu > 1 (bar 1e-3).
+* fp64_path the parity path (max |dP| / peak <= 1e-9 vs the reference) timed the same way.
 * --impl reference  the reference algorithm on the host CPU cores (the FP64 NumPy oracle that
-           restates sgl_full.Lam / invert; the reference itself is Python and cannot be shipped).
+           restates sgl_full.Lam / invert; the reference itself needs Numba, absent on the host).
 """
 from __future__ import annotations
 
@@ -37,17 +41,49 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-METRIC = "z_s=1 PDFs/sec on 1 GB300: plain GPU solver at PDF L1<=1e-4 (surrogate+judge not built)"
-WORKLOAD = ("z_s=1 default flat LCDM PDF: reference z_s=1 population (79,574 fine cells) + 201 xi_lin "
-            "groups with the reference's z_s=1 shapes (shell-30 groups scaled to each shell's row norm), "
-            "gauss closure, CLI ln mu grids (1601 + 1600 points), FP64 oracle-pinned")
+METRIC = "z_s=1 PDFs/sec on 1 GB300: plain GPU solver at PDF L1<=1e-4"
+FULL_POP = ROOT / "tests" / "golden" / "full" / "cells_zs1_gauss_full.npz"
+REF_PDF = ROOT / "tests" / "golden" / "pdf_zs1.json"
+WORKLOAD_REAL = ("z_s=1 default flat LCDM PDF (generate_pdf_lnmu(1.0) defaults): the reference's own z_s=1 "
+                 "population (79,574 fine cells, all 201 xi_lin groups), gauss closure, CLI ln mu grids "
+                 "(1601 + 1600 points); accuracy against the reference's stored pdf_zs1.json")
+WORKLOAD_STANDIN = ("STAND-IN (the reference's full z_s=1 population file is absent): the reference's z_s=1 "
+                    "cells + 201 xi_lin groups synthesised from shell 30, gauss closure, CLI ln mu grids")
 XI_OUT = np.concatenate([np.linspace(-1.0, 1.0, 1601), np.linspace(1.005, 9.0, 1600)])
 XI_COARSE = 101        # the gauss term's coarse k grid per axis (Lam xi_coarse default)
-# DRAM bytes (read + write) per launch of the dominant kernels, from one ncu capture of this
-# workload (profiles/ holds the summaries and the commands)
-TRAFFIC = {"gemm_f32_xi": 1.2079e9,         # profiles/gemm_f32_xi_zs1.md
-           "xi_stageA": 1.4778e9,          # profiles/xi_stageA_pack_zs1.md
-           "xi_fused": 2.7385e8}           # profiles/xi_fused_zs1.md
+# DRAM bytes (read + write) per launch of the dominant kernels on this workload, from one ncu
+# capture each (dram__bytes_read.sum + dram__bytes_write.sum)
+TRAFFIC = {"xi_fused": 2.7385e8}
+
+
+def load_workload():
+    """(population, workload description, reference PDF or None): the reference's own z_s=1
+    population when its file is present, else the labelled stand-in."""
+    from sgl_analytic_gb300 import Population
+    from sgl_analytic_gb300.workloads import zs1_population
+    if FULL_POP.exists():
+        ref = json.loads(REF_PDF.read_text())
+        P0 = np.concatenate([ref["P_s"], ref["P_s_tail"]])
+        x0 = np.concatenate([ref["xi"], ref["xi_tail"]])
+        assert np.array_equal(x0, XI_OUT)
+        return Population.load(FULL_POP), WORKLOAD_REAL, P0
+    return zs1_population(), WORKLOAD_STANDIN, None
+
+
+def pdf_errors(P, Pref):
+    """(max|dP| / peak, L1 over ln mu, tail relative error for ln mu > 1 where Pref > 1e-6 peak)."""
+    peak = float(np.max(Pref))
+    l1 = float(np.trapezoid(np.abs(P - Pref), XI_OUT))
+    tail = (XI_OUT > 1.0) & (np.abs(Pref) > 1e-6 * peak)
+    rel = float(np.max(np.abs(P[tail] - Pref[tail]) / np.abs(Pref[tail]))) if tail.any() else 0.0
+    return float(np.max(np.abs(P - Pref))) / peak, l1, rel
+
+
+def worst(Ps, Pref):
+    """Worst (dpeak, L1, tail) over a list of PDFs."""
+    e = np.array([pdf_errors(P, Pref) for P in Ps])
+    return {"pdfs_checked": len(Ps), "max_dP_over_peak": float(e[:, 0].max()), "pdf_l1": float(e[:, 1].max()),
+            "tail_rel": float(e[:, 2].max())}
 
 
 def dist_env():
@@ -127,8 +163,7 @@ def run_reference(args, rank, world):
     """--impl reference: the reference algorithm on the CPU (rank 0 only)."""
     if rank != 0:
         return
-    from sgl_analytic_gb300.workloads import zs1_population
-    pop = zs1_population()
+    pop, workload, _ = load_workload()
     for _ in range(args.warmup):
         cpu_baseline_sample(pop)
     ts = [cpu_baseline_sample(pop) for _ in range(args.steps)]
@@ -137,9 +172,10 @@ def run_reference(args, rank, world):
     cores = os.cpu_count()
     line = {"metric": METRIC, "value": v, "unit": "PDF/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded shapes of the "
-            "reference z_s=1 build; real cells)", "impl": "reference",
-            "config": {"workload": WORKLOAD, "precision": "fp64", "device": "host CPU"},
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "reference z_s=1 population" if workload == WORKLOAD_REAL else "synthetic stand-in",
+            "impl": "reference",
+            "config": {"workload": workload, "precision": "fp64", "device": "host CPU"},
             "cpu_baseline": {"value": v, "unit": "PDF/s", "cores": cores, "kind": "port",
                              "sample": "one full z_s=1 PDF per step (NumPy oracle restating sgl_full.Lam, "
                                        "separable Psi_1, _Qxi_gauss, _Q_interpolated and invert; BLAS threads "
@@ -338,10 +374,9 @@ def main():
     import torch
     from sgl_analytic_gb300 import Lam, invert
     from sgl_analytic_gb300._lib import Engine
-    from sgl_analytic_gb300.workloads import zs1_population
 
     torch.cuda.set_device(local)
-    pop = zs1_population()
+    pop, workload, Pref = load_workload()
     eng = Engine(local)
     lam = Lam(pop, xi=True, engine=eng, precision=args.precision)
     sig = lam.sigma()
@@ -367,8 +402,10 @@ def main():
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     P = None
+    timed_P = []
     for _ in range(args.steps):
         _, P, meta = step()
+        timed_P.append(P)
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
@@ -406,7 +443,7 @@ def main():
         b0.record(master)
         for ss in sstreams:
             ss.wait_event(b0)
-        outs = bs.solve(XI_OUT, repeats=args.steps, phi_tol=1e-8)
+        outs = bs.solve(XI_OUT, repeats=args.steps, keep_all=True, phi_tol=1e-8)
         for ss in sstreams:
             ev = torch.cuda.Event()
             ev.record(ss)
@@ -419,10 +456,9 @@ def main():
             t = torch.tensor([bms], device="cuda")
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             bms = float(t.item())
-        Pb = outs[0][1]
+        batched_P = [P_ for slot in outs for P_ in slot]
         batched = {"slots": args.slots, "pdfs": args.slots * args.steps * world,
-                   "value": world * args.slots * args.steps / (bms / 1e3), "ms": bms,
-                   "pdf_l1_vs_fp64": float(np.trapezoid(np.abs(Pb - P64), XI_OUT))}
+                   "value": world * args.slots * args.steps / (bms / 1e3), "ms": bms}
         bs.close()
         value = batched["value"]
     # clocks sampled over both timed regions (one PDF at a time, then the batched headline)
@@ -439,19 +475,24 @@ def main():
         ms64 = e0.elapsed_time(e1)
         fp64_line = {"value": args.fp64_steps / (ms64 / 1e3), "unit": "PDF/s", "ms_per_pdf": ms64 / args.fp64_steps,
                      "steps": args.fp64_steps}
-    l1 = float(np.trapezoid(np.abs(P - P64), XI_OUT))
-    tail = (XI_OUT > 1.0) & (np.abs(P64) > 1e-6 * np.max(P64))
-    tail_rel = float(np.max(np.abs(P[tail] - P64[tail]) / np.abs(P64[tail]))) if tail.any() else 0.0
+    # accuracy of every PDF of both timed regions (checked after the timing)
+    all_P = timed_P + (batched_P if batched else [])
     # ---- e2e: drop-in call with host buffers (population upload + PDF + read-back)
     h2d = sum(a.nbytes for a in (pop.w0, pop.k0, pop.g0, pop.ig, pop.fe_g, pop.xg_m, pop.xg_nrow, pop.xg_nidx,
                                  pop.xg_idx, pop.xg_rows, pop.ce_k, pop.ce_g))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    e2e_P = []
     for _ in range(args.e2e_steps):
         lam_e = Lam(pop, xi=True, engine=eng, precision=args.precision)
         _, Pe, _ = invert(lam_e, lam_e.sigma(), xi_out=XI_OUT, phi_tol=1e-8, precision=args.precision)
+        e2e_P.append(Pe)
     torch.cuda.synchronize()
     e2e = args.e2e_steps / (time.perf_counter() - t0)
+    accuracy = {"bar_l1": 1e-4, "bar_tail": 1e-3, "vs_fp64_path": worst(all_P + e2e_P, P64)}
+    if Pref is not None:
+        accuracy["vs_reference_pdf"] = worst(all_P + e2e_P, Pref)
+        accuracy["fp64_path_vs_reference_pdf"] = worst([P64], Pref)
     # ---- roofline of the dominant kernel
     pk, pk_src = peaks()
     tags = {k: v for k, v in stats.items() if not k.startswith("_")}
@@ -501,12 +542,13 @@ def main():
                 "warmup": max(3, args.warmup), "ms_per_step": 1e3 * world / value, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64" if args.precision == "fp64" else "f32+f64",
-                "data": "synthetic (reference z_s=1 cells; xi groups from real shell statistics)",
-                "config": {"workload": WORKLOAD, "precision": args.precision,
+                "data": ("the reference's own z_s=1 population (built by its code, tests/golden/make_fixtures.py)"
+                         if Pref is not None else "synthetic stand-in (reference z_s=1 cells; xi groups from shell 30)"),
+                "config": {"workload": workload, "precision": args.precision,
                            "k_grid": f"{g['nk_k']}x{g['nk_g']}", "out_grid": f"{g['n_kap']}x{g['n_gam']}",
                            "parallelism": f"replicas x{world}", "pdfs_in_flight": max(1, args.slots),
                            "l2": "inputs > L2 every step (xi group rows 151 MB FP32, separable T 86 MB, Phi 29 MB)"},
-                "accuracy": {"pdf_l1_vs_fp64": l1, "bar": 1e-4, "tail_rel_vs_fp64": tail_rel, "tail_bar": 1e-3},
+                "accuracy": accuracy,
                 "single_stream": {"value": single_value, "unit": "PDF/s", "ms_per_pdf": single_ms},
                 "batched": batched,
                 "fp64_path": fp64_line,

@@ -9,7 +9,7 @@
  * A context is re-entrant but must not be shared by two host threads at once.
  *
  * Each function names the reference (sgl_analytic v0.2.0, src/sgl_analytic/) interface it
- * replaces.  The reference-side binding (a ctypes stub) is shown in INTEGRATION.md.
+ * replaces.  The package's own host layer (sgl_analytic_gb300/_lib.py) binds it with ctypes.
  */
 #ifndef SGL_GB300_H
 #define SGL_GB300_H
@@ -214,8 +214,9 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
  * device array (16 x 32768 double2) that every GPU loading the library holds until exit; nk is
  * limited to 32768 and larger nk is rejected (SGL_ERR_VALUE).  kk, k0, w0, out_re, out_im are
  * device-accessible pointers; stream is a cudaStream_t (NULL = legacy default stream); the call
- * is asynchronous on that stream.  The first call on each device resolves the array's device
- * address (cudaGetSymbolAddress) with that device current: make it before any stream capture.
+ * is asynchronous on that stream.  Every call looks up the array's device address
+ * (cudaGetSymbolAddress) with the caller's device current; the first call on a device may load
+ * the library's device code there, so make it before any stream capture.
  * All calls share the array, so calls that overlap on the GPU (other streams, other threads)
  * race; every partial the call reads is written by the same call, so nothing needs clearing.
  * Errors: sgl_last_error(NULL, ...). */

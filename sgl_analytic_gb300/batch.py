@@ -45,9 +45,9 @@ class BatchSolver:
     def streams(self):
         return [e.stream for e in self.engines]
 
-    def solve(self, xi_out, repeats=1, **invert_kw):
+    def solve(self, xi_out, repeats=1, keep_all=False, **invert_kw):
         """Runs `repeats` PDFs on every loaded slot concurrently; returns the last (xi, P, meta) of
-        each slot."""
+        each slot, or with keep_all every slot's list of all its PDFs' P."""
         xi_out = np.asarray(xi_out, float)
         live = [i for i in range(self.slots) if self.lams[i] is not None]
         if not live:
@@ -56,10 +56,12 @@ class BatchSolver:
         def run(i):
             lam = self.lams[i]
             s = lam.sigma()
-            out = None
+            out, every = None, []
             for _ in range(repeats):
                 out = invert(lam, s, xi_out=xi_out, **invert_kw)
-            return out
+                if keep_all:
+                    every.append(out[1])
+            return every if keep_all else out
 
         futs = [self._pool.submit(run, i) for i in live]
         return [f.result() for f in futs]

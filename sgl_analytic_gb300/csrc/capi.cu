@@ -30,6 +30,7 @@ constexpr int kSepMg = 8;
 constexpr int kSepSmax = 64;
 constexpr long long kSepMinPoints = 200000;  // sgl_full.py:3038
 constexpr int kXiCoarse = 101;             // Lam(xi_coarse=101)
+constexpr int kXiGroupRows = 48;           // longest xi group the fused mixed Psi_2 kernel takes
 // sgl.py:1176-1193 and sgl_full.py:33-60
 constexpr double kSigReach = 12.0, kPppK = 18.0, kPppG = 96.0, kBoxReach = 6.0;
 constexpr double kPtsPerSigKap = 72.0, kPtsPerSigGam = 36.0;
@@ -1467,6 +1468,31 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
     if (!ctx) return SGL_ERR_VALUE;
     if (n_groups < 0 || n_ce_k < 2 || n_ce_g < 2 || !ce_k || !ce_g) return fail(ctx, SGL_ERR_VALUE, "invalid xi arrays");
     CK(cudaSetDevice(ctx->device));
+    // Psi_2 sums the squares of the rows independently (sign_m / 2 sum_r G_r^2), so a group of
+    // more than kXiGroupRows rows is the same as its consecutive row ranges taken as groups of
+    // their own over the same coarse cells.  Such groups are split here into near-equal ranges;
+    // their rows stay where they are (a group's rows are row-major and contiguous), only the index
+    // lists are repeated.  The fused mixed kernel then covers every group.
+    std::vector<int32_t> sp_m, sp_nrow, sp_nidx, sp_idx;
+    {
+        bool any = false;
+        for (int g = 0; g < n_groups; ++g) any |= nrow[g] > kXiGroupRows;
+        if (any) {
+            long long io = 0;
+            for (int g = 0; g < n_groups; ++g) {
+                if (nidx[g] < 1 || nrow[g] < 0) return fail(ctx, SGL_ERR_VALUE, "xi group with no rows or no coarse cells");
+                const int parts = std::max(1, (nrow[g] + kXiGroupRows - 1) / kXiGroupRows);
+                for (int p = 0; p < parts; ++p) {
+                    const int r0 = (int)((long long)nrow[g] * p / parts), r1 = (int)((long long)nrow[g] * (p + 1) / parts);
+                    sp_m.push_back(m[g]); sp_nrow.push_back(r1 - r0); sp_nidx.push_back(nidx[g]);
+                    sp_idx.insert(sp_idx.end(), idx + io, idx + io + nidx[g]);
+                }
+                io += nidx[g];
+            }
+            n_groups = (int)sp_m.size();
+            m = sp_m.data(); nrow = sp_nrow.data(); nidx = sp_nidx.data(); idx = sp_idx.data();
+        }
+    }
     XiHost X;
     X.n_kmc = n_ce_k - 1; X.n_gmc = n_ce_g - 1;
     const int ngc = X.n_gmc;

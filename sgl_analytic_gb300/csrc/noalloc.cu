@@ -7,7 +7,6 @@
 // a caching allocator or memory pool at start-up (a second allocator would fragment it or fail
 // under the cap), or a runtime whose policy forbids allocations from third-party libraries on its
 // streams.  The caller passes device-accessible inputs and outputs and the stream to run on.
-#include <mutex>
 #include <string>
 
 #include "kernels.cuh"
@@ -75,12 +74,6 @@ __global__ void k_cf_kappa_reduce(const double2* __restrict__ part, int nk, doub
 
 std::string& sgl_noctx_error();   // message slot read by sgl_last_error(NULL, ...)
 
-namespace {
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[kMaxDevices] = {nullptr};
-}  // namespace
-
 extern "C" sgl_status sgl_cf_kappa_noalloc(const double* kk, int nk, const double* k0, const double* w0,
                                            int64_t n_cells, double* out_re, double* out_im, void* stream) {
     using namespace sgl;
@@ -93,26 +86,20 @@ extern "C" sgl_status sgl_cf_kappa_noalloc(const double* kk, int nk, const doubl
         sgl_noctx_error() = "sgl_cf_kappa_noalloc: null pointer or negative n_cells";
         return SGL_ERR_VALUE;
     }
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-        sgl_noctx_error() = std::string("sgl_cf_kappa_noalloc: no current CUDA device: ") + cudaGetErrorString(e);
-        return SGL_ERR_CUDA;
-    }
+    // The device address of the scratch array, looked up on every call with the caller's device
+    // current.  The lookup is a host-side query, not stream work; it is repeated rather than cached
+    // so that a context torn down and recreated (cudaDeviceReset), which may reload the module at
+    // another address, is followed.  The first call on a device may load the module: make it
+    // before any stream capture.
     void* scratch = nullptr;
-    {
-        // once per device, with that device current: the device address of the scratch array
-        std::lock_guard<std::mutex> lock(g_noalloc_mu);
-        if (!g_noalloc_ptr[dev]) {
-            void* p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_noalloc_partials);
-            if (e != cudaSuccess || !p) {
-                sgl_noctx_error() = std::string("sgl_cf_kappa_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e);
-                return SGL_ERR_CUDA;
-            }
-            g_noalloc_ptr[dev] = p;
-        }
-        scratch = g_noalloc_ptr[dev];
+    cudaError_t e = cudaGetSymbolAddress(&scratch, g_noalloc_partials);
+    if (e != cudaSuccess || !scratch) {
+        int dev = -1;
+        const cudaError_t ed = cudaGetDevice(&dev);
+        sgl_noctx_error() = std::string("sgl_cf_kappa_noalloc: cudaGetSymbolAddress of the scratch array failed on device ") +
+                            (ed == cudaSuccess ? std::to_string(dev) : std::string("(none current)")) + ": " +
+                            cudaGetErrorString(e);
+        return SGL_ERR_CUDA;
     }
     cudaStream_t st = (cudaStream_t)stream;
     dim3 grid(ceil_div(nk, kNoAllocRows), kNoAllocChunks);

@@ -33,21 +33,27 @@ constexpr int kXfStages = 2;
 constexpr int kXfABytes = 4 * 8192;                  // E: [part][cos | sin] x 128 lanes x 16 p
 constexpr int kXfBPart = 16384;                      // T: 256 columns x 16 p, per part
 constexpr int kXfStageBytes = kXfABytes + 2 * kXfBPart;
-constexpr int kXfRMax = 36;                          // rows per group (8 r tasks <= producer threads)
+constexpr int kXfRMax = 48;                          // rows per group (2 r tasks <= producer threads)
 constexpr int kXfGroupWarps = 3;                     // producer warps per 4-p block
 constexpr int kXfProdWarps = 4 * kXfGroupWarps;
 constexpr int kXfProd = kXfProdWarps * 32;
 constexpr int kXfThreads = kXfProd + 64;             // + copy warp + MMA warp
 constexpr int kXfJt = 8;                             // k_gamma columns per CTA at most
-constexpr int kXfChunk = 64;                         // entries per chunk of one warp group
+constexpr int kXfChunk = 64;                         // entries per chunk of one warp group, at most
+constexpr int kXfRowsCap = 64 * 36;                  // row values per chunk buffer: 64 entries of <= 36 rows,
+                                                     // fewer entries per chunk for longer groups
 constexpr int kXfSmemStages = kXfStages * kXfStageBytes;
-constexpr int kXfRowsBuf = kXfChunk * kXfRMax * 4 + 64;      // + room for the aligned superset
+constexpr int kXfRowsBuf = kXfRowsCap * 4 + 64;      // + room for the aligned superset
 constexpr int kXfQBuf = kXfChunk * 4 + 64;
 constexpr int kXfBlocks = 4;                          // producer warp groups, one per 4-p block of a K block
 constexpr int kXfChunkBytes = kXfBlocks * 2 * (kXfRowsBuf + kXfQBuf);
 constexpr int kXfSmemFixed = kXfSmemStages + kXfChunkBytes;
 static_assert(2 * kXfRMax <= 32 * kXfGroupWarps, "one (row, column half) task per producer lane");
 static_assert(kXfRMax * 128 * 8 + kXfRMax * kXfJt * 8 <= kXfChunkBytes, "epilogue tables fit the chunk buffers");
+static_assert(kXfRowsCap / kXfRMax >= 4, "a chunk holds a few entries of the longest group");
+
+// entries per chunk for a group of r rows: the chunk's rows fill at most kXfRowsCap values
+__host__ __device__ constexpr int xf_chunk_entries(int r) { return r * kXfChunk <= kXfRowsCap ? kXfChunk : kXfRowsCap / r; }
 
 
 __device__ __forceinline__ int xf_find(const long long* prefix, int ng, long long v) {
@@ -120,7 +126,8 @@ struct XiFusedArgs {
     int* err;
 };
 
-// one entry chunk of a warp group: entries [ea, eb) of its 4-p block in K block kb, at most kXfChunk
+// one entry chunk of a warp group: entries [ea, eb) of its 4-p block in K block kb, at most
+// xf_chunk_entries(r)
 struct XfChunk { int kb, ea, eb; };
 
 __global__ void __launch_bounds__(kXfThreads, 1)
@@ -206,9 +213,10 @@ k_xi_fused(XiFusedArgs a) {
             bulk_g2s((uint32_t)__cvta_generic_to_shared(rbuf0) + buf * kXfRowsBuf, (const void*)r0a, rb, cb);
             bulk_g2s((uint32_t)__cvta_generic_to_shared(qbuf0) + buf * kXfQBuf, (const void*)q0a, qb, cb);
         };
+        const int chunk = xf_chunk_entries(r);
         XfChunk cur{0, lo_of(0), 0};
         int cur_hi = hi_of(0);
-        cur.eb = min(cur.ea + kXfChunk, cur_hi);
+        cur.eb = min(cur.ea + chunk, cur_hi);
         if (issuer) issue(cur, 0);
         int ci = 0, issued = 0;                         // chunk counters: buffer ci & 1, parity (ci >> 1) & 1
         float acc[4][4];                                // [p of the block][column of the half]
@@ -238,7 +246,7 @@ k_xi_fused(XiFusedArgs a) {
                 nxt.ea = nxt.kb < nkb ? lo_of(nxt.kb) : 0;
                 nxt_hi = nxt.kb < nkb ? hi_of(nxt.kb) : 0;
             }
-            nxt.eb = nxt.kb < nkb ? min(nxt.ea + kXfChunk, nxt_hi) : nxt.ea;
+            nxt.eb = nxt.kb < nkb ? min(nxt.ea + chunk, nxt_hi) : nxt.ea;
             if (nxt.kb < nkb) {
                 if (issuer) issue(nxt, (ci + 1) & 1);
                 issued = ci + 1;

@@ -166,9 +166,15 @@ def run(zs, cfg="full", nord=4, grid_scale=1.0, xi_out=None, split=10.0, exact_s
             xi_tail = np.linspace(1.005, 9.0, 1600)
     nx = len(xi_out)
     xall = np.asarray(xi_out, float) if xi_tail is None else np.concatenate([xi_out, xi_tail])
+    # window=None: "auto" for a positive closure, False for gauss; n_xi_wide=None: 500 for gauss,
+    # 4000 otherwise (reference pipeline.py:216-231)
+    if window is None:
+        window = "auto" if xi_closure != "gauss" else False
+    if window not in (False, True, "auto"):
+        raise ValueError(f"window must be True, False, 'auto' or None, got {window!r}")
     if n_xi_wide is None:
-        n_xi_wide = 500
-    xa, Pa, meta = invert(lam, sig, xi_out=xall, tail_box=tail_box, phi_tol=phi_tol, nproc=1, window=False,
+        n_xi_wide = 500 if xi_closure == "gauss" else 4000
+    xa, Pa, meta = invert(lam, sig, xi_out=xall, tail_box=tail_box, phi_tol=phi_tol, nproc=1, window=window,
                           n_xi_wide=n_xi_wide)
     t_inv = time.time()
     out = dict(t_stages=dict(build=t_build - t0, lam=t_lam - t_build, invert=t_inv - t_lam), zs=zs,
@@ -181,7 +187,7 @@ def run(zs, cfg="full", nord=4, grid_scale=1.0, xi_out=None, split=10.0, exact_s
                N_fil=info.get("N_fil"), V_weak=info.get("V_weak"), mean=meta["mean"], var=meta["var"],
                skew=meta["skew"], sigmaDL=meta["sigmaDL"],
                grid={k: v for k, v in meta["grid"].items() if isinstance(v, (int, float))},
-               tail_box=bool(tail_box), xi_closure=xi_closure, window=False, n_xi_wide=n_xi_wide,
+               tail_box=bool(tail_box), xi_closure=xi_closure, window=window, n_xi_wide=n_xi_wide,
                pos_closure=None, engine=dict(precision=precision, device_ms=meta["device_ms"]),
                seconds=time.time() - t0, xi=np.asarray(xa[:nx]).tolist(), P_s=np.asarray(Pa[:nx]).tolist())
     if xi_tail is not None:

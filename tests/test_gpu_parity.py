@@ -110,23 +110,39 @@ def test_xi_term_mixed_vs_fp64(lamx, ref_sub):
     assert np.max(np.abs(Q - Qr)) <= 1e-5 * max(1.0, np.max(np.abs(Qr)))
 
 
-@pytest.mark.parametrize("rows", [5, 17])
-def test_xi_term_mixed_few_rows(pop_sub, ref_sub, rows):
-    """Groups with fewer rows than one warp of row tasks (the committed groups have 33-36): the
-    mixed xi term (fused tcgen05 kernel) against the FP64 term on the coarse grid."""
+def _groups_with_rows(pop_sub, rows):
+    """pop_sub with every xi group given `rows` rows: the first rows of each group, and beyond its
+    own rows, copies of them scaled by 0.9^(pass) (each group's rows are nrow x (nidx + 1),
+    row-major; the last column is the residual)."""
     from dataclasses import replace
-
-    from sgl_analytic_gb300 import Lam
-    from sgl_analytic_gb300._lib import SGL_FP64, SGL_MIXED
-    # each group's rows are nrow x (nidx + 1), row-major (the last column is the residual)
     nr, nc = pop_sub.xg_nrow.astype(np.int64), pop_sub.xg_nidx.astype(np.int64) + 1
     off = np.concatenate([[0], np.cumsum(nr * nc)])
-    blocks = [pop_sub.xg_rows[off[g]:off[g] + rows * nc[g]] for g in range(nr.size)]
-    pop = replace(pop_sub, xg_nrow=np.full(nr.size, rows, np.int32), xg_rows=np.concatenate(blocks))
-    lam = Lam(pop, xi=True)
+    blocks = []
+    for g in range(nr.size):
+        R = pop_sub.xg_rows[off[g]:off[g + 1]].reshape(nr[g], nc[g])
+        blocks.append(np.concatenate([R[r % nr[g]] * 0.9 ** (r // nr[g]) for r in range(rows)]))
+    return replace(pop_sub, xg_nrow=np.full(nr.size, rows, np.int32), xg_rows=np.concatenate(blocks))
+
+
+@pytest.mark.parametrize("rows", [5, 17, 37, 48, 60])
+def test_xi_term_mixed_few_rows(pop_sub, ref_sub, rows):
+    """Groups of 5 and 17 rows (fewer than one warp of row tasks), 37 (the reference's longest
+    groups at z_s = 1), 48 (the fused kernel's longest: fewer entries per chunk) and 60 (split into
+    two groups of 30 rows by the engine): the mixed xi term (fused tcgen05 kernel) against the FP64
+    term on the coarse grid, and for the longer groups the FP64 term against the oracle."""
+    from oracle import lam_oracle as LO
+    from sgl_analytic_gb300 import Lam
+    from sgl_analytic_gb300._lib import SGL_FP64, SGL_MIXED
+    pop = _groups_with_rows(pop_sub, rows)
+    lam = Lam(pop, xi=True, xi_prune=0.0)          # no pruning: the oracle below sees every row
     Q64 = lam.engine.xi_term(ref_sub["kkc"], ref_sub["kgc"], SGL_FP64)
     Qmx = lam.engine.xi_term(ref_sub["kkc"], ref_sub["kgc"], SGL_MIXED)
     assert np.max(np.abs(Qmx - Q64)) <= 1e-5 * max(1.0, np.max(np.abs(Q64)))
+    if rows > 36:
+        X = LO.XiGroups(pop.groups(), pop.ce_k, pop.ce_g, prune=0.0)
+        ol = LO.OracleLam(pop.w0, pop.k0, pop.g0, pop.ig, pop.fe_g, pop.V, X)
+        Qo = ol.qxi(ref_sub["kkc"][::10], ref_sub["kgc"][::10])
+        assert np.max(np.abs(Q64[::10, ::10] - Qo)) <= TOL_LN * max(1.0, np.max(np.abs(Qo)))
 
 
 def test_lambda_full_grid_mixed_vs_fp64(lamx):
