@@ -71,6 +71,16 @@ typedef struct {
     double xi_coarse, xi_coarse_k;             /* vp closure's coarse grid (gamma, kappa); 0 otherwise */
 } sgl_invert_meta;
 
+/* The inversion grid of one population (the reference's meta["grid"], sgl_full.py:187-262):
+ * k_kappa = linspace(0, k_k_max, nk_k), k_gamma = linspace(0, k_g_max, nk_g); the output box
+ * kappa = linspace(kap_min, kap_max, n_kap), gamma = linspace(0, gam_max, n_gam); sigma_kappa; and
+ * |Phi| at the two reach cuts (they decide the "auto" window). */
+typedef struct {
+    int64_t nk_k, nk_g, n_kap, n_gam;
+    double k_k_max, k_g_max, kap_min, kap_max, gam_max, sigma;
+    double phi_at_k_cut, phi_at_g_cut;
+} sgl_grid;
+
 /* Library / context ------------------------------------------------------------------- */
 int sgl_abi_version(void);
 
@@ -203,6 +213,41 @@ void sgl_invert_opts_default(sgl_invert_opts* opts);
  * be NULL. */
 sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_invert_opts* opts,
                    double* P_out, sgl_invert_meta* meta);
+
+/* The grid half of sgl_pdf: vector_grid (sgl.py:1229-1258), the tail box and the measured k-reach
+ * (_reach, sgl_full.py:38-47; the grid logic of invert, sgl_full.py:187-262) for the context's
+ * population, without evaluating Phi on the grid.  With the vp closure installed its coarse grid
+ * grows with the box, as in sgl_pdf. */
+sgl_status sgl_plan_grid(sgl_ctx* ctx, const sgl_invert_opts* opts, sgl_grid* grid);
+
+/* The inversion half of sgl_pdf for a caller-owned Phi: Phi = exp(ln Phi) on the grid's tensor k
+ * grid as two FP64 planes (re, im; nk_k x nk_g row-major), host pointers (phi_on_device = 0) or
+ * device pointers on the context's device (1).  Applies the window (opts->window), the Hankel and
+ * kappa transforms with the Euler-Maclaurin term, the constant-mu path integrals, normalisation and
+ * moments: the part of sgl_full.invert after `Phi = np.exp(lam(k_k, k_g))` (sgl_full.py:272-375,
+ * sgl.P_vector_joint sgl.py:1127-1156).  For SGL_MIXED Phi is rounded to FP32 first.  Given the grid
+ * sgl_plan_grid returns and exp(sgl_lnphi) on it, the result is sgl_pdf's.  Needs no population. */
+sgl_status sgl_invert(sgl_ctx* ctx, const double* phi_re, const double* phi_im, int phi_on_device,
+                      const sgl_grid* grid, const double* xi_out, int n_xi, const sgl_invert_opts* opts,
+                      double* P_out, sgl_invert_meta* meta);
+
+/* Batched plain solver -----------------------------------------------------------------------
+ * No counterpart in the reference, which solves one pipeline.run per PDF (pipeline.py:114-274).
+ * A batch owns `slots` contexts on one device; load each slot's population through the context
+ * sgl_batch_slot returns (sgl_lam_set_cells / sgl_lam_set_xi / sgl_vp_set), then sgl_batch_pdf runs
+ * n_jobs PDFs, job j on slot job_slot[j] (a slot may take many jobs; they run in order), all with
+ * the same options and ln mu grid: P_out is n_jobs x n_xi, meta (optional) n_jobs entries,
+ * job_status (optional) each job's status (SGL_ERR_STATE: not run because an earlier job of its
+ * slot failed).  The slots run concurrently, each on its own host thread of the batch and its own
+ * streams.  Returns the first failure (message: sgl_last_error(NULL, ...)).  The slot contexts
+ * belong to the batch: do not destroy them. */
+typedef struct sgl_batch sgl_batch;
+sgl_status sgl_batch_create(int device, int slots, sgl_batch** out);
+void sgl_batch_destroy(sgl_batch* batch);
+int sgl_batch_slots(const sgl_batch* batch);
+sgl_ctx* sgl_batch_slot(sgl_batch* batch, int slot);
+sgl_status sgl_batch_pdf(sgl_batch* batch, int n_jobs, const int32_t* job_slot, const double* xi_out, int n_xi,
+                         const sgl_invert_opts* opts, double* P_out, sgl_invert_meta* meta, int32_t* job_status);
 
 /* Allocation-free entry point ------------------------------------------------------------
  * No counterpart in the reference.  For callers that may not allocate device memory (a host that

@@ -23,12 +23,29 @@ EXPORTS = ("sgl_abi_version", "sgl_ctx_create", "sgl_ctx_destroy", "sgl_last_err
            "sgl_lam_set_xi", "sgl_lam_sigma", "sgl_lnphi", "sgl_xi_term", "sgl_sweep_set_cells", "sgl_sweep_eval", "sgl_measure_peak",
            "sgl_vp_set", "sgl_vp_lnR", "sgl_invert_opts_default", "sgl_pdf",
            "sgl_gemm_bf16", "sgl_mlp_bias_act", "sgl_mlp_act_grad", "sgl_mlp_col_sum", "sgl_mlp_mse", "sgl_mlp_adamw",
-           "sgl_cf_kappa_noalloc")
+           "sgl_plan_grid", "sgl_invert", "sgl_batch_create", "sgl_batch_destroy", "sgl_batch_slots",
+           "sgl_batch_slot", "sgl_batch_pdf", "sgl_cf_kappa_noalloc")
 
 
 class InvertOpts(C.Structure):
     _fields_ = [("precision", C.c_int), ("tail_box", C.c_int), ("phi_tol", C.c_double),
                 ("n_xi_wide", C.c_int), ("n_k_int", C.c_int), ("xi_reach", C.c_double), ("window", C.c_int)]
+
+
+class Grid(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("nk_k", "nk_g", "n_kap", "n_gam")] + \
+               [(n, C.c_double) for n in ("k_k_max", "k_g_max", "kap_min", "kap_max", "gam_max", "sigma",
+                                          "phi_at_k_cut", "phi_at_g_cut")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+    @classmethod
+    def from_dict(cls, d):
+        g = cls()
+        for n, t in cls._fields_:
+            setattr(g, n, int(d[n]) if t is C.c_int64 else float(d[n]))
+        return g
 
 
 class InvertMeta(C.Structure):
@@ -95,8 +112,19 @@ def lib():
         L.sgl_invert_opts_default.argtypes = [C.POINTER(InvertOpts)]
         L.sgl_invert_opts_default.restype = None
         L.sgl_pdf.argtypes = [vp, dp, C.c_int, C.POINTER(InvertOpts), dp, C.POINTER(InvertMeta)]
-        for name in ("sgl_ctx_create", "sgl_ctx_stream", "sgl_ctx_profile", "sgl_lam_set_cells", "sgl_lam_set_xi", "sgl_lam_sigma", "sgl_lnphi",
-                     "sgl_xi_term", "sgl_pdf", "sgl_vp_set", "sgl_vp_lnR"):
+        L.sgl_plan_grid.argtypes = [vp, C.POINTER(InvertOpts), C.POINTER(Grid)]
+        L.sgl_invert.argtypes = [vp, vp, vp, C.c_int, C.POINTER(Grid), dp, C.c_int, C.POINTER(InvertOpts), dp,
+                                 C.POINTER(InvertMeta)]
+        L.sgl_batch_create.argtypes = [C.c_int, C.c_int, C.POINTER(vp)]
+        L.sgl_batch_destroy.argtypes = [vp]
+        L.sgl_batch_destroy.restype = None
+        L.sgl_batch_slots.argtypes = [vp]
+        L.sgl_batch_slots.restype = C.c_int
+        L.sgl_batch_slot.argtypes = [vp, C.c_int]
+        L.sgl_batch_slot.restype = vp
+        L.sgl_batch_pdf.argtypes = [vp, C.c_int, ip, dp, C.c_int, C.POINTER(InvertOpts), dp, C.POINTER(InvertMeta), ip]
+        for name in ("sgl_batch_create", "sgl_batch_pdf", "sgl_ctx_create", "sgl_ctx_stream", "sgl_ctx_profile", "sgl_lam_set_cells", "sgl_lam_set_xi", "sgl_lam_sigma", "sgl_lnphi",
+                     "sgl_xi_term", "sgl_pdf", "sgl_vp_set", "sgl_vp_lnR", "sgl_plan_grid", "sgl_invert"):
             getattr(L, name).restype = C.c_int
         if L.sgl_abi_version() != 2:
             raise RuntimeError("libsgl_gb300.so ABI version mismatch; rebuild it")
@@ -117,10 +145,15 @@ def _raise(status, msg):
 
 
 class Engine:
-    """One engine context on one CUDA device (own stream and device arena)."""
+    """One engine context on one CUDA device (own stream and device arena).  With `handle`, a view
+    of a context that something else owns (a batch slot): close() then leaves it alone."""
 
-    def __init__(self, device=0):
+    def __init__(self, device=0, handle=None, owner=None):
         L = lib()
+        if handle is not None:
+            self._h, self._L, self.device, self._owner = C.c_void_p(handle), L, int(device), owner
+            return
+        self._owner = None
         h = C.c_void_p()
         st = L.sgl_ctx_create(int(device), C.byref(h))
         if st != SGL_OK:
@@ -133,7 +166,8 @@ class Engine:
 
     def close(self):
         if getattr(self, "_h", None):
-            self._L.sgl_ctx_destroy(self._h)
+            if getattr(self, "_owner", None) is None:
+                self._L.sgl_ctx_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -261,10 +295,7 @@ class Engine:
         self._check(self._L.sgl_measure_peak(self._h, int(bool(fp64)), C.byref(t)), "sgl_measure_peak")
         return t.value
 
-    def pdf(self, xi_out, precision=SGL_FP64, tail_box=True, phi_tol=1e-8, n_xi_wide=500, n_k_int=2400,
-            xi_reach=24.0, window=False):
-        x = np.ascontiguousarray(xi_out, np.float64)
-        out = np.empty(x.size)
+    def _opts(self, precision, tail_box, phi_tol, n_xi_wide, n_k_int, xi_reach, window):
         o = InvertOpts()
         self._L.sgl_invert_opts_default(C.byref(o))
         o.precision, o.tail_box, o.phi_tol = int(precision), int(bool(tail_box)), float(phi_tol)
@@ -272,6 +303,94 @@ class Engine:
         if window not in (True, False, "auto", None):
             raise ValueError(f"window must be True, False or 'auto', got {window!r}")
         o.window = 2 if window == "auto" else (1 if window is True else 0)
+        return o
+
+    def pdf(self, xi_out, precision=SGL_FP64, tail_box=True, phi_tol=1e-8, n_xi_wide=500, n_k_int=2400,
+            xi_reach=24.0, window=False):
+        x = np.ascontiguousarray(xi_out, np.float64)
+        out = np.empty(x.size)
+        o = self._opts(precision, tail_box, phi_tol, n_xi_wide, n_k_int, xi_reach, window)
         meta = InvertMeta()
         self._check(self._L.sgl_pdf(self._h, _ptr(x), x.size, C.byref(o), _ptr(out), C.byref(meta)), "sgl_pdf")
         return out, meta.as_dict()
+
+    def plan_grid(self, precision=SGL_FP64, tail_box=True, phi_tol=1e-8, xi_reach=24.0):
+        """The inversion grid of the loaded population (sgl_plan_grid): a dict of sgl_grid's fields."""
+        o = self._opts(precision, tail_box, phi_tol, 500, 2400, xi_reach, False)
+        g = Grid()
+        self._check(self._L.sgl_plan_grid(self._h, C.byref(o), C.byref(g)), "sgl_plan_grid")
+        return g.as_dict()
+
+    def invert_phi(self, phi, grid, xi_out, precision=SGL_FP64, tail_box=True, phi_tol=1e-8, n_xi_wide=500,
+                   n_k_int=2400, xi_reach=24.0, window=False):
+        """P_s on xi_out from a caller-owned Phi on `grid` (sgl_invert).  phi: a complex (nk_k, nk_g)
+        NumPy array (host), or a pair (re, im) of device pointers (ints) to FP64 planes on this
+        engine's device."""
+        x = np.ascontiguousarray(xi_out, np.float64)
+        out = np.empty(x.size)
+        o = self._opts(precision, tail_box, phi_tol, n_xi_wide, n_k_int, xi_reach, window)
+        g = Grid.from_dict(grid)
+        meta = InvertMeta()
+        if isinstance(phi, tuple):
+            re_p, im_p, on_dev = C.c_void_p(int(phi[0])), C.c_void_p(int(phi[1])), 1
+            keep = None
+        else:
+            phi = np.asarray(phi)
+            if phi.shape != (g.nk_k, g.nk_g):
+                raise ValueError(f"Phi has shape {phi.shape}, the grid is {(g.nk_k, g.nk_g)}")
+            keep = (np.ascontiguousarray(phi.real, np.float64), np.ascontiguousarray(phi.imag, np.float64))
+            re_p, im_p, on_dev = C.c_void_p(keep[0].ctypes.data), C.c_void_p(keep[1].ctypes.data), 0
+        self._check(self._L.sgl_invert(self._h, re_p, im_p, on_dev, C.byref(g), _ptr(x), x.size, C.byref(o), _ptr(out),
+                                       C.byref(meta)), "sgl_invert")
+        del keep
+        return out, meta.as_dict()
+
+
+class Batch:
+    """The native batched solver (sgl_batch_*): `slots` contexts on one device and a host thread
+    per slot.  slot(i) is an Engine view of slot i's context (load its population through it)."""
+
+    def __init__(self, slots=4, device=0):
+        self._L = lib()
+        h = C.c_void_p()
+        st = self._L.sgl_batch_create(int(device), int(slots), C.byref(h))
+        if st != SGL_OK:
+            buf = C.create_string_buffer(512)
+            self._L.sgl_last_error(None, buf, 512)
+            _raise(st, "sgl_batch_create: " + buf.value.decode())
+        self._h = h
+        self.device = int(device)
+        self.engines = [Engine(device, handle=self._L.sgl_batch_slot(h, i), owner=self) for i in range(int(slots))]
+
+    def slot(self, i):
+        return self.engines[i]
+
+    def pdf(self, job_slot, xi_out, precision=SGL_FP64, tail_box=True, phi_tol=1e-8, n_xi_wide=500, n_k_int=2400,
+            xi_reach=24.0, window=False):
+        """Runs one PDF per entry of job_slot (the slot it runs on); returns (P [jobs, n_xi], metas)."""
+        js = np.ascontiguousarray(job_slot, np.int32)
+        x = np.ascontiguousarray(xi_out, np.float64)
+        out = np.empty((js.size, x.size))
+        o = self.engines[0]._opts(precision, tail_box, phi_tol, n_xi_wide, n_k_int, xi_reach, window)
+        metas = (InvertMeta * max(1, js.size))()
+        status = np.zeros(max(1, js.size), np.int32)
+        st = self._L.sgl_batch_pdf(self._h, js.size, _ptr(js, C.c_int32), _ptr(x), x.size, C.byref(o), _ptr(out),
+                                   metas, _ptr(status, C.c_int32))
+        if st != SGL_OK:
+            buf = C.create_string_buffer(1024)
+            self._L.sgl_last_error(None, buf, 1024)
+            _raise(st, buf.value.decode())
+        return out, [metas[i].as_dict() for i in range(js.size)]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            for e in self.engines:
+                e._h = None
+            self._L.sgl_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -210,6 +210,21 @@ grouped_gemm_kernel<float>(const GemmDesc<float>* __restrict__ descs, int nprob)
 // small next to the total: no extra registers, 64 KB of shared memory for the running sums
 // (thread t owns words t, t + 256, ... so the folds are bank-conflict free).
 constexpr int kF32FoldTiles = 4;
+
+// two FP32 lanes in one 64-bit register for the packed FMA (fma.rn.f32x2 rounds each lane like fmaf)
+__device__ __forceinline__ unsigned long long f32x2_pack(float a, float b) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float2 f32x2_unpack(unsigned long long v) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+__device__ __forceinline__ void f32x2_fma(unsigned long long& acc, unsigned long long a, unsigned long long b) {
+    asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(acc) : "l"(a), "l"(b));
+}
 constexpr int kF32LayoutSmem = (2 * 16 * (128 + 4) * 2 + 64 * 256) * 4;   // operands + running sums
 template <bool AK, bool BJ>
 __global__ void __launch_bounds__(256, 2)
@@ -265,23 +280,33 @@ gemm_f32_layout_kernel(const GemmDesc<float>* __restrict__ descs, int nprob) {
             if (BJ) Bs[buf][bk + 2 * u][bj] = rb[u]; else Bs[buf][bk][bj + 16 * u] = rb[u];
         }
     };
-    float acc[8][8];
+    // accumulators in column pairs: acc2[r][q] holds (acc[r][2q], acc[r][2q + 1]) for the packed FMA
+    unsigned long long acc2[8][4];
 #pragma unroll
-    for (int a = 0; a < 8; ++a)
+    for (int a = 0; a < 8; ++a) {
 #pragma unroll
-        for (int b = 0; b < 8; ++b) { acc[a][b] = 0.f; Hs[(a * 8 + b) * 256 + tid] = 0.f; }
+        for (int q = 0; q < 4; ++q) acc2[a][q] = 0ull;
+#pragma unroll
+        for (int b = 0; b < 8; ++b) Hs[(a * 8 + b) * 256 + tid] = 0.f;
+    }
     // running sum += acc by TwoSum; acc keeps the exact rounding error of that addition
     auto fold = [&]() {
 #pragma unroll
         for (int r = 0; r < 8; ++r)
 #pragma unroll
-            for (int c = 0; c < 8; ++c) {
-                float* hp = Hs + (r * 8 + c) * 256 + tid;
-                const float h = *hp, a = acc[r][c];
-                const float sum = h + a;
-                const float bb = sum - h;
-                acc[r][c] = (h - (sum - bb)) + (a - bb);
-                *hp = sum;
+            for (int q = 0; q < 4; ++q) {
+                const float2 a2 = f32x2_unpack(acc2[r][q]);
+                float av2[2] = {a2.x, a2.y};
+#pragma unroll
+                for (int h2 = 0; h2 < 2; ++h2) {
+                    float* hp = Hs + (r * 8 + 2 * q + h2) * 256 + tid;
+                    const float h = *hp, a = av2[h2];
+                    const float sum = h + a;
+                    const float bb = sum - h;
+                    av2[h2] = (h - (sum - bb)) + (a - bb);
+                    *hp = sum;
+                }
+                acc2[r][q] = f32x2_pack(av2[0], av2[1]);
             }
     };
     const int ntiles = (d.K + BK - 1) / BK;
@@ -298,11 +323,14 @@ gemm_f32_layout_kernel(const GemmDesc<float>* __restrict__ descs, int nprob) {
             const float4 b0 = *reinterpret_cast<const float4*>(&Bs[cur][k][tx * 4]);
             const float4 b1 = *reinterpret_cast<const float4*>(&Bs[cur][k][tx * 4 + 64]);
             const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-            const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+            const unsigned long long bp[4] = {f32x2_pack(b0.x, b0.y), f32x2_pack(b0.z, b0.w), f32x2_pack(b1.x, b1.y),
+                                              f32x2_pack(b1.z, b1.w)};
 #pragma unroll
-            for (int r = 0; r < 8; ++r)
+            for (int r = 0; r < 8; ++r) {
+                const unsigned long long ap = f32x2_pack(av[r], av[r]);
 #pragma unroll
-                for (int c = 0; c < 8; ++c) acc[r][c] = fmaf(av[r], bv[c], acc[r][c]);
+                for (int q = 0; q < 4; ++q) f32x2_fma(acc2[r][q], ap, bp[q]);
+            }
         }
         if (t + 1 < ntiles) store_tiles(cur ^ 1);
         __syncthreads();
@@ -317,7 +345,8 @@ gemm_f32_layout_kernel(const GemmDesc<float>* __restrict__ descs, int nprob) {
             const int gj = j0 + tx * 4 + (c & 3) + (c >> 2) * 64;
             if (gj >= d.N) continue;
             float* cp = d.C + (long long)gi * d.ldc + gj;
-            float v = d.alpha * (Hs[(r * 8 + c) * 256 + tid] + acc[r][c]);
+            const float2 a2 = f32x2_unpack(acc2[r][c >> 1]);
+            float v = d.alpha * (Hs[(r * 8 + c) * 256 + tid] + ((c & 1) ? a2.y : a2.x));
             if (d.beta != 0.f) v += d.beta * *cp;
             *cp = v;
         }

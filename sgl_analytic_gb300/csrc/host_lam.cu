@@ -1,552 +1,9 @@
-// Host runtime and C ABI: context, device arena, per-population plans, and the per-PDF pipeline
-// (grid plan -> reach probes -> ln Phi -> exp -> transforms -> path integral -> moments).
-// Mirrors the control flow of the reference's Lam (sgl_full.py:2711-3452) and invert
-// (sgl_full.py:159-375) for the default gauss chain.
-#include <algorithm>
-#include <atomic>
-#include <chrono>
-#include <condition_variable>
-#include <functional>
-#include <mutex>
-#include <cmath>
-#include <cstdio>
-#include <cstring>
-#include <string>
-#include <thread>
-#include <unordered_map>
-#include <vector>
+// Population plans and ln Phi: the cell compaction and separable plan (Lam.__init__,
+// _sep_gamma_nodes), the xi_lin group plans, and ln Phi on a tensor grid (Lam.__call__ /
+// _direct_call: separable Psi_1, the gauss Psi_2 term with its coarse-grid spline).
+#include "host.cuh"
 
-#include <unistd.h>
-
-#include "kernels.cuh"
-
-using namespace sgl;
-
-namespace {
-
-// ------------------------------------------------------------------ constants (reference)
-constexpr double kSepTheta = 0.5;          // sgl_full.py:3036
-constexpr int kSepMg = 8;
-constexpr int kSepSmax = 64;
-constexpr long long kSepMinPoints = 200000;  // sgl_full.py:3038
-constexpr int kXiCoarse = 101;             // Lam(xi_coarse=101)
-constexpr int kXiGroupRows = 48;           // longest xi group the fused mixed Psi_2 kernel takes
-// sgl.py:1176-1193 and sgl_full.py:33-60
-constexpr double kSigReach = 12.0, kPppK = 18.0, kPppG = 96.0, kBoxReach = 6.0;
-constexpr double kPtsPerSigKap = 72.0, kPtsPerSigGam = 36.0;
-constexpr double kTailKapMax = 0.99, kTailGamMax = 0.8, kTailPppG = 12.0;
-constexpr double kOutGridMax = 3.4e7;
-
-thread_local std::string g_create_error;
-
-struct Arena {                         // grow-only named device buffers
-    std::unordered_map<std::string, std::pair<void*, size_t>> bufs;
-    void* get(const std::string& name, size_t bytes) {
-        auto it = bufs.find(name);
-        if (bytes == 0) bytes = 16;
-        if (it != bufs.end() && it->second.second >= bytes) return it->second.first;
-        if (it != bufs.end()) { cudaFree(it->second.first); bufs.erase(it); }
-        void* p = nullptr;
-        if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
-        bufs[name] = {p, bytes};
-        return p;
-    }
-    void* find(const std::string& name) const {
-        auto it = bufs.find(name);
-        return it == bufs.end() ? nullptr : it->second.first;
-    }
-    void release() { for (auto& kv : bufs) cudaFree(kv.second.first); bufs.clear(); }
-};
-
-struct SepHost {
-    double key = -1.0;
-    int n_cells = 0, n_groups = 0, n_cols = 0, n_cols_sep = 0, n_direct = 0;
-    std::vector<int> chunk_begin;
-    double max_sep_node = 0.0;
-};
-
-struct XiHost {
-    bool on = false;
-    int n_groups = 0, n_kmc = 0, n_gmc = 0, total_p = 0, total_rows = 0;
-    std::vector<int> m, r, nP;
-    std::vector<long long> p_prefix_rowel;   // p_prefix (n_groups+1) then rowel_off (n_groups)
-    std::vector<double> kmc, gmc;
-    // sigma contribution: sum over m=0 rows of (rows . kc + res)^2
-    double sigma_var = 0.0;
-    int R0 = 0, Rm[3] = {0, 0, 0};
-};
-
-struct SplineHost {
-    int n = 0;
-    std::vector<double> knots, minv;
-};
-
-struct StatRow { long long launches = 0; double ms = 0, flops = 0, bytes = 0; };
-struct Pending { std::string tag; cudaEvent_t a, b; double flops, bytes; };
-
-}  // namespace
-
-// host scratch of the separable plan, reused between plans (sizes follow the cell count)
-struct SepScratch {
-    std::vector<long long> keyv, order;
-    std::vector<double> sl, sh, kap, w, wl;
-    std::vector<char> direct;
-    std::vector<float> kh, kl, wf, wlf;
-    std::vector<int> grp;
-};
-
-struct sgl_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::string err;
-    Arena arena;
-    // population (host copies)
-    std::vector<double> w0, k0, g0, fe_g;
-    std::vector<int> ig;
-    double V = 0.0;
-    bool has_cells = false;
-    SepHost sep;
-    SepDevice sepd;
-    SepScratch sep_scratch;
-    int sep_precision_ready = -1;
-    XiHost xi;
-    XiDevice xid;
-    long long sweep_n = -1;          // cells of the 1-D sweep (sgl_sweep_set_cells)
-    std::unordered_map<int, SplineHost> splines;   // not-a-knot collocation inverses by node count
-    // positive (vp) Cox closure replacing the gauss xi term (sgl_vp_set)
-    bool vp_on = false;
-    VpDevice vpd;
-    double vp_shear = 0.0;
-    int vp_xi_coarse = 101, vp_xi_coarse_k = 0;   // coarse grid (gamma, kappa); grown by sgl_pdf's rule
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-    int* dev_err = nullptr;          // raised by kernels whose bounded waits ran out
-    bool coherent_host = false;      // the GPU reads pageable host memory through the host page tables
-    // pinned staging ring for small uploads (pageable copies would serialise host and device);
-    // reset whenever the stream has been synchronised
-    char* pinned = nullptr;
-    size_t pinned_cap = 0, pinned_off = 0;
-    // second stream for the xi term, which runs concurrently with the separable part of ln Phi
-    // (fork / join by events); it has its own pinned staging ring.  swap_side() exchanges the two
-    // so that every helper keeps using ctx->stream / ctx->pinned.
-    cudaStream_t side = nullptr;
-    char* side_pinned = nullptr;
-    size_t side_pinned_cap = 0, side_pinned_off = 0;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    // pinned host buffer for the large per-population arrays built on the host (grow-only)
-    char* big_pinned = nullptr;
-    size_t big_cap = 0;
-    // per-kernel statistics (sgl_ctx_profile)
-    bool profiling = false;
-    long long launches_at_enable = 0;
-    std::vector<cudaEvent_t> ev_pool;
-    std::vector<Pending> pending;
-    std::unordered_map<std::string, StatRow> stats;
-};
-
-namespace {
-
-// ------------------------------------------------------------------ error helpers
-sgl_status fail(sgl_ctx* c, sgl_status s, const std::string& msg) {
-    if (c) c->err = msg;
-    return s;
-}
-
-#define CK(call)                                                                              \
-    do {                                                                                      \
-        cudaError_t e_ = (call);                                                              \
-        if (e_ != cudaSuccess)                                                                \
-            return fail(ctx, SGL_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
-    } while (0)
-
-#define CKLAUNCH()                                                                            \
-    do {                                                                                      \
-        cudaError_t e_ = cudaGetLastError();                                                  \
-        if (e_ != cudaSuccess)                                                                \
-            return fail(ctx, SGL_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e_));   \
-    } while (0)
-
-#define CKS(expr)                                                                             \
-    do {                                                                                      \
-        sgl_status s_ = (expr);                                                               \
-        if (s_ != SGL_OK) return s_;                                                          \
-    } while (0)
-
-template <typename T>
-T* dbuf(sgl_ctx* ctx, const std::string& name, size_t count) {
-    return (T*)ctx->arena.get(name, count * sizeof(T));
-}
-
-#define DBUF(var, T, name, count)                                                             \
-    T* var = dbuf<T>(ctx, name, (size_t)(count));                                             \
-    if (!var) return fail(ctx, SGL_ERR_CUDA, std::string("device allocation failed: ") + name)
-
-sgl_status sync_stream(sgl_ctx* ctx) {
-    CK(cudaStreamSynchronize(ctx->stream));
-    ctx->pinned_off = 0;
-    // the other stream's staging ring is reused only once that stream is idle too
-    if (ctx->side && cudaStreamQuery(ctx->side) == cudaSuccess) ctx->side_pinned_off = 0;
-    cudaGetLastError();        // a not-ready query is not an error
-    return SGL_OK;
-}
-
-template <typename T>
-sgl_status upload(sgl_ctx* ctx, T* dst, const T* src, size_t n) {
-    if (n == 0) return SGL_OK;
-    const size_t bytes = n * sizeof(T);
-    if (ctx->pinned && ctx->pinned_off + bytes <= ctx->pinned_cap) {
-        char* stage = ctx->pinned + ctx->pinned_off;
-        std::memcpy(stage, src, bytes);
-        ctx->pinned_off += (bytes + 255) & ~(size_t)255;
-        CK(cudaMemcpyAsync(dst, stage, bytes, cudaMemcpyHostToDevice, ctx->stream));
-        return SGL_OK;
-    }
-    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    return SGL_OK;
-}
-
-// host-side phase timing, recorded in the context's statistics as "host_<tag>" while profiling
-struct HostTimer {
-    sgl_ctx* c; std::chrono::steady_clock::time_point t0;
-    explicit HostTimer(sgl_ctx* c_) : c(c_), t0(std::chrono::steady_clock::now()) {}
-    void lap(const char* tag) {
-        const auto t1 = std::chrono::steady_clock::now();
-        if (c->profiling) {
-            StatRow& r = c->stats[std::string("host_") + tag];
-            r.launches += 1;
-            r.ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
-        }
-        t0 = t1;
-    }
-};
-
-// exchanges the context's stream (and its pinned staging ring) with the side stream
-void swap_side(sgl_ctx* c) {
-    std::swap(c->stream, c->side);
-    std::swap(c->pinned, c->side_pinned);
-    std::swap(c->pinned_cap, c->side_pinned_cap);
-    std::swap(c->pinned_off, c->side_pinned_off);
-}
-
-// Persistent host worker pool for the population preparation: spawning threads costs ~0.3 ms per
-// batch of 16 on the Grace host, more than most of the parallel passes themselves.  run() hands
-// out task indices [0, ntasks) through an atomic counter; the calling thread works too.  One job
-// at a time: a caller that finds the pool busy (another context on another host thread), or a
-// process forked after the pool started, runs its tasks inline.  Every task writes disjoint
-// outputs, so results never depend on the scheduling.
-class HostPool {
-  public:
-    static HostPool& get() {
-        static HostPool pool;
-        return pool;
-    }
-    void run(int ntasks, const std::function<void(int)>& fn) {
-        std::unique_lock<std::mutex> busy(run_mu_, std::try_to_lock);
-        if (!busy.owns_lock() || workers_.empty() || getpid() != pid_ || ntasks <= 1) {
-            for (int t = 0; t < ntasks; ++t) fn(t);
-            return;
-        }
-        {
-            std::lock_guard<std::mutex> lk(mu_);
-            job_ = &fn;
-            ntasks_ = ntasks;
-            next_ = 0;
-            pending_ = (int)workers_.size();
-            ++gen_;
-        }
-        cv_.notify_all();
-        for (int t; (t = next_.fetch_add(1)) < ntasks;) fn(t);
-        std::unique_lock<std::mutex> lk(mu_);
-        done_cv_.wait(lk, [&] { return pending_ == 0; });
-        job_ = nullptr;
-    }
-    int size() const { return (int)workers_.size() + 1; }
-
-  private:
-    HostPool() : pid_(getpid()) {
-        const int n = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), 16)) - 1;
-        for (int i = 0; i < n; ++i) workers_.emplace_back([this] { loop(); });
-    }
-    ~HostPool() {
-        if (getpid() != pid_) {                  // forked child: the workers are the parent's
-            for (auto& w : workers_) w.detach();
-            return;
-        }
-        {
-            std::lock_guard<std::mutex> lk(mu_);
-            stop_ = true;
-            ++gen_;
-        }
-        cv_.notify_all();
-        for (auto& w : workers_) if (w.joinable()) w.join();
-    }
-    void loop() {
-        long long seen = 0;
-        for (;;) {
-            const std::function<void(int)>* job;
-            int nt;
-            {
-                std::unique_lock<std::mutex> lk(mu_);
-                cv_.wait(lk, [&] { return gen_ != seen; });
-                seen = gen_;
-                if (stop_) return;
-                job = job_;
-                nt = ntasks_;
-            }
-            for (int t; (t = next_.fetch_add(1)) < nt;) (*job)(t);
-            std::lock_guard<std::mutex> lk(mu_);
-            if (--pending_ == 0) done_cv_.notify_one();
-        }
-    }
-    std::vector<std::thread> workers_;
-    std::mutex run_mu_, mu_;
-    std::condition_variable cv_, done_cv_;
-    const std::function<void(int)>* job_ = nullptr;
-    int ntasks_ = 0, pending_ = 0;
-    std::atomic<int> next_{0};
-    long long gen_ = 0;
-    bool stop_ = false;
-    pid_t pid_;
-};
-
-// fn(lo, hi) over [0, n) in contiguous blocks on the pool (every index written by one block)
-void parallel_for(long long n, const std::function<void(long long, long long)>& fn) {
-    const int nblk = (int)std::max(1LL, std::min<long long>(4LL * HostPool::get().size(), (n + 2047) / 2048));
-    if (nblk == 1) { fn(0, n); return; }
-    const long long blk = (n + nblk - 1) / nblk;
-    HostPool::get().run(nblk, [&](int b) {
-        const long long lo = (long long)b * blk, hi = std::min(n, lo + blk);
-        if (lo < hi) fn(lo, hi);
-    });
-}
-
-// pinned host buffer of at least `bytes` (grow-only; the stream is synchronised before it grows)
-char* big_pinned(sgl_ctx* ctx, size_t bytes) {
-    if (bytes <= ctx->big_cap) return ctx->big_pinned;
-    cudaStreamSynchronize(ctx->stream);
-    if (ctx->big_pinned) cudaFreeHost(ctx->big_pinned);
-    ctx->big_pinned = nullptr; ctx->big_cap = 0;
-    const size_t cap = std::max(bytes, (size_t)64 << 20);
-    if (cudaHostAlloc((void**)&ctx->big_pinned, cap, cudaHostAllocDefault) != cudaSuccess) {
-        ctx->big_pinned = nullptr;
-        return nullptr;
-    }
-    ctx->big_cap = cap;
-    return ctx->big_pinned;
-}
-
-// numpy.linspace: a + i * step (separately rounded), last point = b exactly
-std::vector<double> linspace(double a, double b, long long n) {
-    std::vector<double> v((size_t)n);
-    if (n == 1) { v[0] = a; return v; }
-    const double step = (b - a) / (double)(n - 1);
-    for (long long i = 0; i < n; ++i) { volatile double t = (double)i * step; v[(size_t)i] = t + a; }
-    v[(size_t)n - 1] = b;
-    return v;
-}
-
-size_t elem_size(int precision) { return precision == SGL_FP64 ? sizeof(double) : sizeof(float); }
-
-// Scoped device timer of one tagged launch (only when profiling is on).
-struct Timed {
-    sgl_ctx* c; std::string tag; double flops, bytes; cudaEvent_t a = nullptr, b = nullptr;
-    Timed(sgl_ctx* c_, std::string t, double f, double by) : c(c_), tag(std::move(t)), flops(f), bytes(by) {
-        if (!c->profiling) return;
-        a = take(); b = take();
-        cudaEventRecord(a, c->stream);
-    }
-    cudaEvent_t take() {
-        if (c->ev_pool.empty()) { cudaEvent_t e; cudaEventCreate(&e); return e; }
-        cudaEvent_t e = c->ev_pool.back(); c->ev_pool.pop_back(); return e;
-    }
-    ~Timed() {
-        if (!c->profiling) return;
-        cudaEventRecord(b, c->stream);
-        c->pending.push_back(Pending{tag, a, b, flops, bytes});
-    }
-};
-
-void resolve_stats(sgl_ctx* c) {
-    if (c->pending.empty()) return;
-    cudaStreamSynchronize(c->stream);
-    if (c->side) cudaStreamSynchronize(c->side);
-    for (auto& p : c->pending) {
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, p.a, p.b);
-        StatRow& r = c->stats[p.tag];
-        r.launches += 1; r.ms += ms; r.flops += p.flops; r.bytes += p.bytes;
-        c->ev_pool.push_back(p.a); c->ev_pool.push_back(p.b);
-    }
-    c->pending.clear();
-}
-
-// ------------------------------------------------------------------ GEMM dispatch
-template <typename T>
-sgl_status run_gemms(sgl_ctx* ctx, std::vector<GemmDesc<T>>& d, const std::string& tag) {
-    if (d.empty()) return SGL_OK;
-    int tiles = gemm_plan(d.data(), (int)d.size());
-    // FP64 problems too small for one wave of 64 x 64 tiles run on 16 x 16 tiles
-    const bool small = sizeof(T) == 8 && tiles < kNumSMs;
-    if (small) tiles = gemm_plan(d.data(), (int)d.size(), 16, 16);
-    DBUF(dd, GemmDesc<T>, "gemm_desc_" + tag, d.size());
-    CKS(upload(ctx, dd, d.data(), d.size()));
-    double fl = 0.0;
-    for (auto& g : d) fl += 2.0 * g.M * (double)g.N * g.K;
-    {
-        Timed t(ctx, std::string(sizeof(T) == 8 ? "gemm_f64_" : "gemm_f32_") + tag, fl, 0.0);
-        int layout = (d[0].a_cs == 1 ? 1 : 0) | (d[0].b_cs == 1 ? 2 : 0);
-        for (auto& g : d)
-            if (((g.a_cs == 1 ? 1 : 0) | (g.b_cs == 1 ? 2 : 0)) != layout) layout = -1;
-        if (small) layout = kSmallTiles;
-        launch_grouped_gemm<T>(dd, (int)d.size(), tiles, layout, ctx->stream);
-    }
-    CKLAUNCH();
-    return SGL_OK;
-}
-
-// device error flag of this context (zeroed on first use)
-int* dev_err_flag(sgl_ctx* ctx) {
-    if (!ctx->dev_err) {
-        ctx->dev_err = (int*)ctx->arena.get("dev_err", sizeof(int));
-        if (ctx->dev_err) cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), ctx->stream);
-    }
-    return ctx->dev_err;
-}
-
-// reads (and clears) the flag; call after the stream has work queued that may raise it
-sgl_status check_dev_err(sgl_ctx* ctx) {
-    if (!ctx->dev_err) return SGL_OK;
-    int h = 0;
-    CK(cudaMemcpyAsync(&h, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    CKS(sync_stream(ctx));
-    if (h) {
-        CK(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), ctx->stream));
-        return fail(ctx, SGL_ERR_CUDA, "tensor-core GEMM: a bounded mbarrier wait ran out");
-    }
-    return SGL_OK;
-}
-
-// parts = 2: operands to ~22 bits (3 MMAs per K-step); parts = 3: FP32 operands exactly (6 MMAs)
-sgl_status run_tc_gemms(sgl_ctx* ctx, std::vector<TcGemmDesc>& d, const std::string& tag, int parts) {
-    if (d.empty()) return SGL_OK;
-    std::vector<TcPackDesc> pk(2 * d.size());
-    int tiles = 0;
-    long long quads = 0;
-    const long long pfl = tc_gemm_plan(d.data(), (int)d.size(), parts, pk.data(), &tiles, &quads);
-    DBUF(dd, TcGemmDesc, "tc_desc_" + tag, d.size());
-    DBUF(dp, TcPackDesc, "tc_pack_" + tag, pk.size());
-    DBUF(packed, float, "tc_packed", std::max<long long>(pfl, 1));
-    CKS(upload(ctx, dd, d.data(), d.size()));
-    CKS(upload(ctx, dp, pk.data(), pk.size()));
-    int* err = dev_err_flag(ctx);
-    if (!err) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (error flag)");
-    double fl = 0.0;
-    for (auto& g : d) fl += 2.0 * g.M * (double)g.N * g.K;
-    {
-        Timed t(ctx, "gemm_tc_" + tag, fl, (double)pfl * 4.0);
-        launch_tc_gemm(parts, dd, (int)d.size(), tiles, dp, quads, packed, err, ctx->stream);
-    }
-    CKLAUNCH();
-    return SGL_OK;
-}
-
-template <typename T>
-GemmDesc<T> gd(int M, int N, int K, const void* A, long long ars, long long acs, const void* B, long long brs,
-               long long bcs, void* C, long long ldc, double alpha = 1.0, double beta = 0.0) {
-    GemmDesc<T> g{};
-    g.M = M; g.N = N; g.K = K;
-    g.A = (const T*)A; g.a_rs = ars; g.a_cs = acs;
-    g.B = (const T*)B; g.b_rs = brs; g.b_cs = bcs;
-    g.C = (T*)C; g.ldc = ldc;
-    g.alpha = (T)alpha; g.beta = (T)beta;
-    return g;
-}
-
-// One GEMM with split-K when it would under-fill the GPU: K slices write workspace slices,
-// then a fixed-order sum (deterministic).  SIMT kernels (FP64, and FP32 where chosen below).
-template <typename T>
-sgl_status gemm_splitk_simt(sgl_ctx* ctx, GemmDesc<T> g, const std::string& tag, int min_split = 1) {
-    GemmDesc<T> tmp = g;
-    const int tiles = gemm_plan(&tmp, 1);
-    int split = 1;
-    if (tiles < 2 * kNumSMs) split = std::min(ceil_div(2 * kNumSMs, tiles), std::max(1, g.K / 512));
-    // min_split > 1 (mixed path): at least min_split slices of at least 32 terms; FP32 slices
-    // are combined in float-float
-    split = std::max(split, std::min(min_split, std::max(1, g.K / 32)));
-    if (split <= 1) { std::vector<GemmDesc<T>> v{g}; return run_gemms(ctx, v, tag); }
-    const long long slice = (long long)g.M * g.N;
-    DBUF(ws, T, "splitk_ws_" + tag, slice * split);
-    std::vector<GemmDesc<T>> v;
-    const int kc = ceil_div(g.K, split);
-    for (int s = 0; s < split; ++s) {
-        const int k0 = s * kc, k1 = std::min(g.K, k0 + kc);
-        if (k1 <= k0) continue;
-        GemmDesc<T> p = g;
-        p.K = k1 - k0;
-        p.A = g.A + (long long)k0 * g.a_cs;
-        p.B = g.B + (long long)k0 * g.b_rs;
-        p.C = ws + (long long)v.size() * slice;
-        p.ldc = g.N;
-        p.beta = T(0);
-        v.push_back(p);
-    }
-    CKS(run_gemms(ctx, v, tag));
-    launch_sum_slices<T>(ws, (int)v.size(), g.M, g.N, g.C, g.ldc, g.beta, ctx->stream);
-    CKLAUNCH();
-    return SGL_OK;
-}
-
-// FP32 on the tensor cores.  K split into >= min_split slices (FP32 accumulation in TMEM within a
-// slice), slices combined in FP64 by the fixed-order sum.
-sgl_status gemm_splitk_tc(sgl_ctx* ctx, GemmDesc<float> g, const std::string& tag, int min_split, int parts = 3) {
-    int split = std::max(1, std::min(min_split, std::max(1, g.K / 32)));
-    const long long slice = (long long)g.M * g.N;
-    const bool direct = split == 1 && g.beta == 0.f;
-    float* ws = nullptr;
-    if (!direct) {
-        ws = dbuf<float>(ctx, "splitk_ws_" + tag, (size_t)(slice * split));
-        if (!ws) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (split-K workspace)");
-    }
-    std::vector<TcGemmDesc> v;
-    const int kc = ceil_div(g.K, split);
-    for (int s = 0; s < split; ++s) {
-        const int k0 = s * kc, k1 = std::min(g.K, k0 + kc);
-        if (k1 <= k0) continue;
-        TcGemmDesc t{};
-        t.M = g.M; t.N = g.N; t.K = k1 - k0;
-        t.A = g.A + (long long)k0 * g.a_cs; t.a_rs = g.a_rs; t.a_cs = g.a_cs;
-        t.B = g.B + (long long)k0 * g.b_rs; t.b_rs = g.b_rs; t.b_cs = g.b_cs;
-        if (direct) { t.C = g.C; t.c_rs = g.ldc; t.c_cs = 1; }
-        else { t.C = ws + (long long)v.size() * slice; t.c_rs = g.N; t.c_cs = 1; }
-        t.alpha = g.alpha;
-        v.push_back(t);
-    }
-    CKS(run_tc_gemms(ctx, v, tag, parts));
-    if (!direct) {
-        launch_sum_slices<float>(ws, (int)v.size(), g.M, g.N, g.C, g.ldc, g.beta, ctx->stream);
-        CKLAUNCH();
-    }
-    return SGL_OK;
-}
-
-// Mixed-path GEMMs that run on the tensor cores with TF32-split operands: none of the separable
-// Psi_1 or transform GEMMs.  The tail relative error of the mixed PDF (bar 1e-3) was measured with
-// each moved to tcgen05.  On the bench workload: all on SIMT 3.6e-4; sep2 + sep3 3.5e-4; kappa
-// 6.4e-4; the Hankel pair 5.0e-4; sep1 2.0e-3; more K-slices do not help (3x: 1.2e-3, 6x: 1.8e-3
-// with all six moved).  On the reference's own z_s = 1 population against its stored PDF:
-// sep2 + sep3 on tcgen05 1.30e-3, on SIMT 8.5e-4.  The tensor core's FP32 accumulation has a
-// per-instruction bias that the Fourier sums do not cancel, where SIMT FMAs round to nearest.
-// (The Hankel correction term, of relative size 2^-24, does run on BF16 tensor cores.)
-bool tc_for(const std::string& /*tag*/) {
-    return false;
-}
-
-template <typename T>
-sgl_status gemm_splitk(sgl_ctx* ctx, GemmDesc<T> g, const std::string& tag, int min_split = 1) {
-    if constexpr (sizeof(T) == 4) {
-        if (tc_for(tag)) return gemm_splitk_tc(ctx, g, tag, min_split);
-    }
-    return gemm_splitk_simt<T>(ctx, g, tag, min_split);
-}
+namespace sglh {
 
 // ------------------------------------------------------------------ separable plan
 // Restates _sep_gamma_nodes (sgl_full.py:2631-2661) for kg_max = key.
@@ -991,62 +448,6 @@ sgl_status xi_eval(sgl_ctx* ctx, int precision, const double* d_kk, const double
 }
 
 // numpy.unwrap along a strided line (period 2 pi, discontinuity pi)
-void unwrap_line(double* p, int n, long long stride) {
-    double corr = 0.0;
-    for (int i = 1; i < n; ++i) {
-        const double dd = p[(long long)i * stride] - (p[(long long)(i - 1) * stride] - corr);
-        double ddmod = std::fmod(dd + M_PI, 2.0 * M_PI);
-        if (ddmod < 0) ddmod += 2.0 * M_PI;
-        ddmod -= M_PI;
-        if (ddmod == -M_PI && dd > 0) ddmod = M_PI;
-        double pc = ddmod - dd;
-        if (std::fabs(dd) < M_PI) pc = 0.0;
-        corr += pc;
-        p[(long long)i * stride] += corr;
-    }
-}
-
-// ln R on kv x qv into device planes (tables, z buffer from the arena; rows in passes of <= 8 GiB z)
-sgl_status vp_lnR_device(sgl_ctx* ctx, int precision, const double* d_kv, int nk, const double* d_qv, int nq,
-                         double* d_re, double* d_im) {
-    const VpDevice& D = ctx->vpd;
-    void* tables = ctx->arena.get("vp_tables", vp_table_bytes(precision, D.U, nk, nq));
-    const int rows = vp_rows_per_pass(D.nsh, nk, nq, (size_t)8 << 30);
-    const int pieces = rows == nk ? vp_pieces(D.nsh, rows, nq) : 1;     // split runs only in a single pass
-    void* zb = ctx->arena.get("vp_z", (size_t)D.nsh * 49 * 16 * (size_t)rows * nq * pieces);
-    if (!tables || !zb) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (vp)");
-    const double pts = (double)nk * nq;
-    Timed t(ctx, precision == SGL_FP64 ? "vp_lnR_f64" : "vp_lnR_mixed", pts * (double)D.ncells * 12.0,
-            pts * D.nsh * 49 * 16.0 * 2);
-    launch_vp_lnR(precision, D, d_kv, nk, d_qv, nq, tables, (double2*)zb, rows, d_re, d_im, ctx->stream, pieces);
-    CKLAUNCH();
-    return SGL_OK;
-}
-
-// vp closure term on kk x kg (Closure.qxi, pos_closure.py:690-705): ln R, its imaginary part
-// unwrapped along k_kappa at the first k_gamma column and then along k_gamma, minus
-// shear_var kg^2 / 4.  Device planes out.
-sgl_status vp_qxi(sgl_ctx* ctx, int precision, const double* d_kk, int nk, const double* d_kg, const double* h_kg,
-                  int nkg, double* d_re, double* d_im) {
-    const cudaStream_t st = ctx->stream;
-    CKS(vp_lnR_device(ctx, precision, d_kk, nk, d_kg, nkg, d_re, d_im));
-    const long long npt = (long long)nk * nkg;
-    std::vector<double> im((size_t)npt), re((size_t)npt);
-    CK(cudaMemcpyAsync(im.data(), d_im, npt * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(re.data(), d_re, npt * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CKS(sync_stream(ctx));
-    unwrap_line(im.data(), nk, nkg);                              // first column along k_kappa
-    for (int i = 0; i < nk; ++i) unwrap_line(im.data() + (long long)i * nkg, nkg, 1);
-    for (long long e2 = 0; e2 < npt; ++e2) {
-        const double q = h_kg[e2 % nkg];
-        re[(size_t)e2] -= 0.25 * ctx->vp_shear * q * q;
-    }
-    CKS(upload(ctx, d_re, re.data(), (size_t)npt));
-    CKS(upload(ctx, d_im, im.data(), (size_t)npt));
-    CKS(sync_stream(ctx));
-    return SGL_OK;
-}
-
 sgl_status xi_any(sgl_ctx* ctx, int precision, const double* d_kk, const double* h_kk, int nk, const double* d_kg,
                   const double* h_kg, int nkg, double* d_re, double* d_im) {
     if (ctx->vp_on) return vp_qxi(ctx, precision, d_kk, nk, d_kg, h_kg, nkg, d_re, d_im);
@@ -1258,7 +659,7 @@ sgl_status lambda_eval(sgl_ctx* ctx, int precision, const double* h_kk, int nk, 
 // precision SGL_MIXED: the Psi_1 sums from FP32 terms (k-reach probes of the mixed path); the xi
 // term stays FP64.
 sgl_status lambda_direct(sgl_ctx* ctx, const double* h_kk, int nk, const double* h_kg, int nkg, double* re,
-                         double* im, int precision = SGL_FP64) {
+                         double* im, int precision) {
     const cudaStream_t st = ctx->stream;
     const long long npt = (long long)nk * nkg;
     DBUF(d_kk, double, "dir_kk", nk);
@@ -1299,134 +700,9 @@ double trapz(const double* y, const double* x, int n) {
     for (int i = 0; i + 1 < n; ++i) s += (x[i + 1] - x[i]) * (y[i + 1] + y[i]) / 2.0;
     return s;
 }
+}  // namespace sglh
 
-}  // namespace
-
-// Message of the last failed call that has no context (sgl_ctx_create, sgl_cf_kappa_noalloc).
-std::string& sgl_noctx_error() { return g_create_error; }
-
-// ================================================================== C ABI
 extern "C" {
-
-int sgl_abi_version(void) { return SGL_ABI_VERSION; }
-
-sgl_status sgl_ctx_create(int device, sgl_ctx** out) {
-    if (!out) { g_create_error = "out is NULL"; return SGL_ERR_VALUE; }
-    *out = nullptr;
-    int n = 0;
-    cudaError_t e = cudaGetDeviceCount(&n);
-    if (e != cudaSuccess || n == 0) {
-        g_create_error = std::string("no CUDA device: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "count 0");
-        return SGL_ERR_CUDA;
-    }
-    if (device < 0 || device >= n) { g_create_error = "device index out of range"; return SGL_ERR_VALUE; }
-    e = cudaSetDevice(device);
-    if (e != cudaSuccess) { g_create_error = cudaGetErrorString(e); return SGL_ERR_CUDA; }
-    sgl_ctx* ctx = new sgl_ctx();
-    ctx->device = device;
-    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
-        g_create_error = "stream creation failed"; delete ctx; return SGL_ERR_CUDA;
-    }
-    for (auto& ev : ctx->ev) cudaEventCreate(&ev);
-    if (cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
-        ctx->side = nullptr;          // no second stream: the xi term runs in order on the first
-        cudaGetLastError();
-    }
-    {
-        int pa = 0, pt = 0;
-        cudaDeviceGetAttribute(&pa, cudaDevAttrPageableMemoryAccess, device);
-        cudaDeviceGetAttribute(&pt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
-        ctx->coherent_host = pa == 1 && pt == 1;
-        cudaGetLastError();
-    }
-    ctx->pinned_cap = 16u << 20;
-    if (cudaHostAlloc((void**)&ctx->pinned, ctx->pinned_cap, cudaHostAllocDefault) != cudaSuccess) {
-        ctx->pinned = nullptr; ctx->pinned_cap = 0;
-        cudaGetLastError();
-    }
-    if (ctx->side) {
-        ctx->side_pinned_cap = 4u << 20;
-        if (cudaHostAlloc((void**)&ctx->side_pinned, ctx->side_pinned_cap, cudaHostAllocDefault) != cudaSuccess) {
-            ctx->side_pinned = nullptr; ctx->side_pinned_cap = 0;
-            cudaGetLastError();
-        }
-    }
-    *out = ctx;
-    return SGL_OK;
-}
-
-void sgl_ctx_destroy(sgl_ctx* ctx) {
-    if (!ctx) return;
-    cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
-    if (ctx->side) cudaStreamSynchronize(ctx->side);
-    ctx->arena.release();
-    for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
-    resolve_stats(ctx);
-    for (auto& ev : ctx->ev_pool) cudaEventDestroy(ev);
-    if (ctx->pinned) cudaFreeHost(ctx->pinned);
-    if (ctx->big_pinned) cudaFreeHost(ctx->big_pinned);
-    if (ctx->side_pinned) cudaFreeHost(ctx->side_pinned);
-    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
-    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
-    if (ctx->side) cudaStreamDestroy(ctx->side);
-    cudaStreamDestroy(ctx->stream);
-    delete ctx;
-}
-
-int sgl_last_error(const sgl_ctx* ctx, char* buf, int buflen) {
-    const std::string& m = ctx ? ctx->err : g_create_error;
-    if (buf && buflen > 0) {
-        const int n = std::min((int)m.size(), buflen - 1);
-        std::memcpy(buf, m.data(), (size_t)n);
-        buf[n] = 0;
-    }
-    return (int)m.size();
-}
-
-sgl_status sgl_ctx_stream(sgl_ctx* ctx, void** stream) {
-    if (!ctx || !stream) return SGL_ERR_VALUE;
-    *stream = (void*)ctx->stream;
-    return SGL_OK;
-}
-
-sgl_status sgl_ctx_profile(sgl_ctx* ctx, int enable) {
-    if (!ctx) return SGL_ERR_VALUE;
-    resolve_stats(ctx);
-    if (enable && !ctx->profiling) ctx->launches_at_enable = sgl::launch_counter();
-    if (!enable && ctx->profiling) ctx->stats["_launches"].launches += sgl::launch_counter() - ctx->launches_at_enable;
-    ctx->profiling = enable != 0;
-    return SGL_OK;
-}
-
-int sgl_stats_json(sgl_ctx* ctx, char* buf, int buflen, int reset) {
-    if (!ctx) return -1;
-    resolve_stats(ctx);
-    if (ctx->profiling) {
-        ctx->stats["_launches"].launches += sgl::launch_counter() - ctx->launches_at_enable;
-        ctx->launches_at_enable = sgl::launch_counter();
-    }
-    std::string js = "{";
-    bool first = true;
-    char tmp[512];
-    for (auto& kv : ctx->stats) {
-        std::snprintf(tmp, sizeof(tmp), "%s\"%s\": {\"launches\": %lld, \"ms\": %.6f, \"flops\": %.6e, \"bytes\": %.6e}",
-                      first ? "" : ", ", kv.first.c_str(), kv.second.launches, kv.second.ms, kv.second.flops,
-                      kv.second.bytes);
-        js += tmp;
-        first = false;
-    }
-    js += "}";
-    if (buf && buflen > 0) {
-        const int n = std::min((int)js.size(), buflen - 1);
-        std::memcpy(buf, js.data(), (size_t)n);
-        buf[n] = 0;
-    }
-    if (reset) ctx->stats.clear();
-    return (int)js.size();
-}
 
 sgl_status sgl_lam_set_cells(sgl_ctx* ctx, int64_t n_cells, const double* w0, const double* k0, const double* g0,
                              const int32_t* ig, const double* fe_g, int n_fe_g, double V) {
@@ -1980,165 +1256,6 @@ sgl_status sgl_lnphi(sgl_ctx* ctx, const double* kk, int nkk, const double* kg, 
     return SGL_OK;
 }
 
-sgl_status sgl_vp_set(sgl_ctx* ctx, int nstate, const double* u, const double* w, int n_shells, const double* K,
-                      int n_unique, const double* ku, const double* gu, int64_t n_cells, const int32_t* cu,
-                      const double* cw, int n_groups, const int64_t* gstart, const int32_t* sh_g, const double* ga,
-                      const double* gb, const double* gc, const int32_t* glo, const int32_t* ghi, double shear_var) {
-    if (!ctx) return SGL_ERR_VALUE;
-    if (n_shells == 0) { ctx->vp_on = false; return SGL_OK; }
-    if (nstate != 48) return fail(ctx, SGL_ERR_UNSUPPORTED, "vp closure: only the 48-state chain is built");
-    if (n_shells < 0 || n_unique < 1 || n_cells < 0 || n_groups < 0 || !u || !w || !ku || !gu || !gstart || !sh_g ||
-        (n_shells > 1 && !K) || (n_cells > 0 && (!cu || !cw)) || (n_groups > 0 && (!ga || !gb || !gc || !glo || !ghi)))
-        return fail(ctx, SGL_ERR_VALUE, "vp closure: missing arrays");
-    if (!std::isfinite(shear_var) || shear_var < 0) return fail(ctx, SGL_ERR_VALUE, "vp closure: shear_var must be finite, >= 0");
-    for (int j = 0; j < nstate; ++j)
-        if (!std::isfinite(u[j]) || !std::isfinite(w[j]) || (j > 0 && !(u[j] > u[j - 1])))
-            return fail(ctx, SGL_ERR_VALUE, "vp closure: state nodes must be finite and increasing");
-    for (long long e = 0; e < (long long)(n_shells - 1) * nstate * nstate; ++e)
-        if (!std::isfinite(K[e])) return fail(ctx, SGL_ERR_VALUE, "vp closure: non-finite transition matrix");
-    for (int i = 0; i < n_unique; ++i)
-        if (!std::isfinite(ku[i]) || !std::isfinite(gu[i])) return fail(ctx, SGL_ERR_VALUE, "vp closure: non-finite cell");
-    for (int64_t c = 0; c < n_cells; ++c)
-        if (cu[c] < 0 || cu[c] >= n_unique || !std::isfinite(cw[c]))
-            return fail(ctx, SGL_ERR_VALUE, "vp closure: cell index out of range or non-finite weight");
-    if (sh_g[0] != 0 || sh_g[n_shells] != n_groups) return fail(ctx, SGL_ERR_VALUE, "vp closure: shell offsets must span the groups");
-    for (int s = 0; s < n_shells; ++s)
-        if (sh_g[s + 1] < sh_g[s]) return fail(ctx, SGL_ERR_VALUE, "vp closure: shell offsets must be non-decreasing");
-    if (gstart[0] != 0 || gstart[n_groups] != n_cells) return fail(ctx, SGL_ERR_VALUE, "vp closure: group offsets must span the cells");
-    for (int g = 0; g < n_groups; ++g) {
-        if (gstart[g + 1] < gstart[g]) return fail(ctx, SGL_ERR_VALUE, "vp closure: group offsets must be non-decreasing");
-        if (!std::isfinite(ga[g]) || !std::isfinite(gb[g])) return fail(ctx, SGL_ERR_VALUE, "vp closure: non-finite rate");
-        if (glo[g] < 0 || ghi[g] >= nstate || glo[g] > ghi[g]) return fail(ctx, SGL_ERR_VALUE, "vp closure: bad rate interval");
-        // rate intervals (pos_closure_fused.py:18-48): c = 0 on all states, or c = -1 on an interval
-        // that reaches one end of the state grid
-        if (gc[g] == -1.0) {
-            if (ghi[g] != nstate - 1 && glo[g] != 0)
-                return fail(ctx, SGL_ERR_VALUE, "vp closure: clipped rate support must reach an end of the state grid");
-        } else if (gc[g] != 0.0) {
-            return fail(ctx, SGL_ERR_VALUE, "vp closure: rate offset c must be 0 or -1");
-        }
-    }
-    // zero stationary mean of every rate (pos_closure.py:15): the kernels rely on it
-    for (int g = 0; g < n_groups; ++g) {
-        double m = 0.0, mx = 0.0;
-        for (int j = 0; j < nstate; ++j) {
-            double D;
-            if (gc[g] == 0.0) D = ga[g] * u[j] + gb[g];
-            else if (j < glo[g] || j > ghi[g]) D = -1.0;
-            else D = -1.0 + (u[j] - u[ghi[g] == nstate - 1 ? glo[g] : ghi[g]]) * ga[g] + gb[g];
-            m += w[j] * D;
-            mx = std::max(mx, std::fabs(D));
-        }
-        if (std::fabs(m) > 1e-11 * std::max(mx, 1e-300) && mx > 0)
-            return fail(ctx, SGL_ERR_VALUE, "vp closure: a group's rate does not keep the mean (E_w[lam] != 1)");
-    }
-    // runs: per shell, groups ordered linear first, then by the first state they change
-    // (left: lo, right: hi + 1); cells concatenated with weights (w a, w b)
-    std::vector<int> cu_s, run_kind, run_bound, sh_run{0};
-    std::vector<double2> wab;
-    std::vector<float2> wabf;
-    std::vector<long long> run_cell{0};
-    cu_s.reserve((size_t)n_cells); wab.reserve((size_t)n_cells); wabf.reserve((size_t)n_cells);
-    for (int sh = 0; sh < n_shells; ++sh) {
-        std::vector<std::pair<int, int>> keyed;        // (sort key, group)
-        for (int g = sh_g[sh]; g < sh_g[sh + 1]; ++g) {
-            if (ga[g] == 0.0 && gb[g] == 0.0 && gc[g] == 0.0) continue;
-            if (gstart[g + 1] == gstart[g]) continue;
-            int key;
-            if (gc[g] == 0.0) key = -1;
-            else if (ghi[g] == nstate - 1) key = 2 * glo[g];            // left
-            else key = 2 * (ghi[g] + 1) + 1;                            // right
-            keyed.emplace_back(key, g);
-        }
-        std::stable_sort(keyed.begin(), keyed.end(), [](const std::pair<int, int>& x, const std::pair<int, int>& y) {
-            return x.first < y.first;
-        });
-        int cur_key = INT32_MIN;
-        for (const auto& kg : keyed) {
-            const int g = kg.second;
-            if (kg.first != cur_key) {
-                if (cur_key != INT32_MIN) run_cell.push_back((long long)cu_s.size());
-                cur_key = kg.first;
-                run_kind.push_back(gc[g] == 0.0 ? 0 : (ghi[g] == nstate - 1 ? 1 : 2));
-                run_bound.push_back(gc[g] == 0.0 ? 0 : (ghi[g] == nstate - 1 ? glo[g] : ghi[g]));
-            }
-            for (int64_t c = gstart[g]; c < gstart[g + 1]; ++c) {
-                cu_s.push_back(cu[c]);
-                const double2 v = make_double2(cw[c] * ga[g], cw[c] * gb[g]);
-                wab.push_back(v);
-                wabf.push_back(make_float2((float)v.x, (float)v.y));
-            }
-        }
-        if (cur_key != INT32_MIN) run_cell.push_back((long long)cu_s.size());
-        sh_run.push_back((int)run_kind.size());
-    }
-    const int nruns = (int)run_kind.size();
-    const long long ncs = (long long)cu_s.size();
-    CK(cudaSetDevice(ctx->device));
-    VpDevice D;
-    D.nsh = n_shells; D.U = n_unique; D.nruns = nruns; D.ncells = ncs;
-    DBUF(d_u, double, "vp_u", nstate);
-    DBUF(d_w, double, "vp_w", nstate);
-    DBUF(d_K, double, "vp_K", std::max<long long>(1, (long long)(n_shells - 1) * nstate * nstate));
-    DBUF(d_ku, double, "vp_ku", n_unique);
-    DBUF(d_gu, double, "vp_gu", n_unique);
-    DBUF(d_cu, int, "vp_cu", std::max<long long>(1, ncs));
-    DBUF(d_wab, double2, "vp_wab", std::max<long long>(1, ncs));
-    DBUF(d_wabf, float2, "vp_wabf", std::max<long long>(1, ncs));
-    DBUF(d_rc, long long, "vp_run_cell", nruns + 1);
-    DBUF(d_rk, int, "vp_run_kind", 2 * std::max(1, nruns));
-    DBUF(d_sr, int, "vp_sh_run", n_shells + 1);
-    CKS(upload(ctx, d_u, u, nstate));
-    CKS(upload(ctx, d_w, w, nstate));
-    if (n_shells > 1) CKS(upload(ctx, d_K, K, (size_t)(n_shells - 1) * nstate * nstate));
-    CKS(upload(ctx, d_ku, ku, n_unique));
-    CKS(upload(ctx, d_gu, gu, n_unique));
-    if (ncs > 0) {
-        CKS(upload(ctx, d_cu, cu_s.data(), (size_t)ncs));
-        CKS(upload(ctx, d_wab, wab.data(), (size_t)ncs));
-        CKS(upload(ctx, d_wabf, wabf.data(), (size_t)ncs));
-    }
-    CKS(upload(ctx, d_rc, run_cell.data(), run_cell.size()));
-    if (nruns > 0) {
-        CKS(upload(ctx, d_rk, run_kind.data(), (size_t)nruns));
-        CKS(upload(ctx, d_rk + nruns, run_bound.data(), (size_t)nruns));
-    }
-    CKS(upload(ctx, d_sr, sh_run.data(), sh_run.size()));
-    CKS(sync_stream(ctx));
-    D.u = d_u; D.w = d_w; D.K = d_K; D.ku = d_ku; D.gu = d_gu; D.cu = d_cu; D.wab = d_wab; D.wabf = d_wabf;
-    D.run_cell = d_rc; D.run_kind = d_rk; D.run_bound = d_rk + nruns; D.sh_run = d_sr;
-    ctx->vpd = D;
-    ctx->vp_shear = shear_var;
-    ctx->vp_xi_coarse = kXiCoarse;
-    ctx->vp_xi_coarse_k = 0;
-    ctx->vp_on = true;
-    return SGL_OK;
-}
-
-sgl_status sgl_vp_lnR(sgl_ctx* ctx, const double* kv, int nk, const double* qv, int nq, int precision,
-                      double* out_re, double* out_im) {
-    if (!ctx) return SGL_ERR_VALUE;
-    if (!ctx->vp_on) return fail(ctx, SGL_ERR_STATE, "vp closure not set");
-    if (nk < 1 || nq < 1 || !kv || !qv || !out_re || !out_im) return fail(ctx, SGL_ERR_VALUE, "empty grid");
-    if (precision != SGL_FP64 && precision != SGL_MIXED) return fail(ctx, SGL_ERR_VALUE, "unknown precision");
-    for (int i = 0; i < nk; ++i) if (!std::isfinite(kv[i])) return fail(ctx, SGL_ERR_VALUE, "non-finite k_kappa");
-    for (int i = 0; i < nq; ++i) if (!std::isfinite(qv[i])) return fail(ctx, SGL_ERR_VALUE, "non-finite k_gamma");
-    CK(cudaSetDevice(ctx->device));
-    const long long npt = (long long)nk * nq;
-    DBUF(d_kv, double, "vpr_k", nk);
-    DBUF(d_qv, double, "vpr_q", nq);
-    DBUF(d_o, double, "vpr_out", 2 * npt);
-    CKS(upload(ctx, d_kv, kv, nk));
-    CKS(upload(ctx, d_qv, qv, nq));
-    CKS(vp_lnR_device(ctx, precision, d_kv, nk, d_qv, nq, d_o, d_o + npt));
-    CK(cudaMemcpyAsync(out_re, d_o, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaMemcpyAsync(out_im, d_o + npt, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    CKS(sync_stream(ctx));
-    for (long long p = 0; p < npt; ++p)
-        if (!std::isfinite(out_re[p]) || !std::isfinite(out_im[p])) return fail(ctx, SGL_ERR_NONFINITE, "non-finite ln R");
-    return SGL_OK;
-}
-
 sgl_status sgl_xi_term(sgl_ctx* ctx, const double* kk, int nkk, const double* kg, int nkg, int precision,
                        double* out_re, double* out_im) {
     if (!ctx) return SGL_ERR_VALUE;
@@ -2159,374 +1276,6 @@ sgl_status sgl_xi_term(sgl_ctx* ctx, const double* kk, int nkk, const double* kg
     CK(cudaMemcpyAsync(out_im, d_o + npt, npt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CKS(sync_stream(ctx));
     CKS(check_dev_err(ctx));
-    return SGL_OK;
-}
-
-// ------------------------------------------------------------------ surrogate MLP building blocks
-sgl_status sgl_gemm_bf16(sgl_ctx* ctx, int M, int N, int K, const float* A, int64_t a_rs, int64_t a_cs, const float* B,
-                         int64_t b_rs, int64_t b_cs, float* C, int64_t c_rs, int64_t c_cs, float alpha) {
-    if (!ctx) return SGL_ERR_VALUE;
-    if (M < 0 || N < 0 || K < 0 || (M > 0 && N > 0 && (!A || !B || !C))) return fail(ctx, SGL_ERR_VALUE, "invalid GEMM arguments");
-    if (M == 0 || N == 0) return SGL_OK;
-    CK(cudaSetDevice(ctx->device));
-    std::vector<TcGemmDesc> v(1);
-    TcGemmDesc& t = v[0];
-    t = TcGemmDesc{};
-    t.M = M; t.N = N; t.K = K;
-    t.A = A; t.a_rs = a_rs; t.a_cs = a_cs;
-    t.B = B; t.b_rs = b_rs; t.b_cs = b_cs;
-    t.C = C; t.c_rs = c_rs; t.c_cs = c_cs;
-    t.alpha = alpha;
-    return run_tc_gemms(ctx, v, "bf16", 1);
-}
-
-sgl_status sgl_mlp_bias_act(sgl_ctx* ctx, int M, int N, const float* Z, const float* bias, float* Zb, float* A, int silu) {
-    if (!ctx || M < 0 || N < 0) return SGL_ERR_VALUE;
-    launch_bias_act(M, N, Z, bias, Zb, A, silu, ctx->stream);
-    CKLAUNCH();
-    return SGL_OK;
-}
-
-sgl_status sgl_mlp_act_grad(sgl_ctx* ctx, int M, int N, const float* dA, const float* Zb, float* dZ) {
-    if (!ctx || M < 0 || N < 0) return SGL_ERR_VALUE;
-    launch_act_grad(M, N, dA, Zb, dZ, ctx->stream);
-    CKLAUNCH();
-    return SGL_OK;
-}
-
-sgl_status sgl_mlp_col_sum(sgl_ctx* ctx, int M, int N, const float* X, float* out) {
-    if (!ctx || M < 0 || N < 0) return SGL_ERR_VALUE;
-    launch_col_sum(M, N, X, out, ctx->stream);
-    CKLAUNCH();
-    return SGL_OK;
-}
-
-sgl_status sgl_mlp_mse(sgl_ctx* ctx, int64_t n, const float* pred, const float* target, float* dpred, double* loss) {
-    if (!ctx || n < 1 || !pred || !target || !dpred || !loss) return SGL_ERR_VALUE;
-    const int nb = mse_blocks(n);
-    DBUF(part, double, "mse_part", nb);
-    launch_mse(n, pred, target, dpred, part, ctx->stream);
-    CKLAUNCH();
-    std::vector<double> h((size_t)nb);
-    CK(cudaMemcpyAsync(h.data(), part, nb * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    CKS(sync_stream(ctx));
-    CKS(check_dev_err(ctx));
-    double a = 0.0;
-    for (double v : h) a += v;
-    *loss = a / (double)n;
-    return SGL_OK;
-}
-
-sgl_status sgl_mlp_adamw(sgl_ctx* ctx, int64_t n, float* w, const float* g, float* m, float* v, float lr, float b1,
-                         float b2, float eps, float wd, int step) {
-    if (!ctx || n < 0 || step < 1) return SGL_ERR_VALUE;
-    const float c1 = 1.f - std::pow(b1, (float)step), c2 = 1.f - std::pow(b2, (float)step);
-    launch_adamw(n, w, g, m, v, lr, b1, b2, eps, wd, c1, c2, ctx->stream);
-    CKLAUNCH();
-    return SGL_OK;
-}
-
-sgl_status sgl_sweep_set_cells(sgl_ctx* ctx, int64_t n_cells, const double* kap, const double* w) {
-    if (!ctx) return SGL_ERR_VALUE;
-    if (n_cells < 1 || !kap || !w) return fail(ctx, SGL_ERR_VALUE, "empty cell list");
-    CK(cudaSetDevice(ctx->device));
-    std::vector<float> kh((size_t)n_cells), kl((size_t)n_cells), wf((size_t)n_cells);
-    for (int64_t c = 0; c < n_cells; ++c) {
-        if (!std::isfinite(kap[c]) || !std::isfinite(w[c])) return fail(ctx, SGL_ERR_VALUE, "non-finite cell");
-        const ff f = ff_from_double(kap[c]);
-        kh[(size_t)c] = f.hi; kl[(size_t)c] = f.lo; wf[(size_t)c] = (float)w[c];
-    }
-    DBUF(d_k, double, "sw_kap", n_cells);
-    DBUF(d_w, double, "sw_w", n_cells);
-    DBUF(d_kh, float, "sw_kh", n_cells);
-    DBUF(d_kl, float, "sw_kl", n_cells);
-    DBUF(d_wf, float, "sw_wf", n_cells);
-    CK(cudaMemcpyAsync(d_k, kap, (size_t)n_cells * 8, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(d_w, w, (size_t)n_cells * 8, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(d_kh, kh.data(), (size_t)n_cells * 4, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(d_kl, kl.data(), (size_t)n_cells * 4, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(d_wf, wf.data(), (size_t)n_cells * 4, cudaMemcpyHostToDevice, ctx->stream));
-    CKS(sync_stream(ctx));
-    ctx->sweep_n = n_cells;
-    return SGL_OK;
-}
-
-sgl_status sgl_sweep_eval(sgl_ctx* ctx, const double* kk, int nk, int precision, double* out_re, double* out_im) {
-    if (!ctx) return SGL_ERR_VALUE;
-    if (ctx->sweep_n < 1) return fail(ctx, SGL_ERR_STATE, "sweep cells not set");
-    if (nk < 1 || !kk || !out_re || !out_im) return fail(ctx, SGL_ERR_VALUE, "empty k grid");
-    if (precision != SGL_FP64 && precision != SGL_MIXED) return fail(ctx, SGL_ERR_VALUE, "unknown precision");
-    for (int i = 0; i < nk; ++i) if (!std::isfinite(kk[i])) return fail(ctx, SGL_ERR_VALUE, "non-finite kk");
-    CK(cudaSetDevice(ctx->device));
-    const long long nc = ctx->sweep_n;
-    const int nch = sweep1d_chunks(nk, nc);
-    DBUF(d_kk, double, "sw_kk", nk);
-    DBUF(d_part, double2, "sw_part", (long long)nch * nk);
-    DBUF(d_out, double, "sw_out", 2LL * nk);
-    CKS(upload(ctx, d_kk, kk, nk));
-    {
-        Timed t(ctx, precision == SGL_FP64 ? "sweep1d_f64" : "sweep1d_mixed", (double)nk * nc, (double)nk * 0 + nc * 16.0);
-        launch_sweep1d(precision, d_kk, nk, (const double*)ctx->arena.find("sw_kap"), (const double*)ctx->arena.find("sw_w"),
-                       (const float*)ctx->arena.find("sw_kh"), (const float*)ctx->arena.find("sw_kl"),
-                       (const float*)ctx->arena.find("sw_wf"), nc, nch, d_part, d_out, d_out + nk, ctx->stream);
-    }
-    CKLAUNCH();
-    CK(cudaMemcpyAsync(out_re, d_out, (size_t)nk * 8, cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaMemcpyAsync(out_im, d_out + nk, (size_t)nk * 8, cudaMemcpyDeviceToHost, ctx->stream));
-    CKS(sync_stream(ctx));
-    for (int i = 0; i < nk; ++i)
-        if (!std::isfinite(out_re[i]) || !std::isfinite(out_im[i])) return fail(ctx, SGL_ERR_NONFINITE, "non-finite sweep");
-    return SGL_OK;
-}
-
-sgl_status sgl_measure_peak(sgl_ctx* ctx, int fp64, double* tflops) {
-    if (!ctx || !tflops) return SGL_ERR_VALUE;
-    CK(cudaSetDevice(ctx->device));
-    const int blocks = kNumSMs * 8, iters = fp64 ? 512 : 8192;
-    DBUF(d_o, double, "peak_out", (long long)blocks * 256);
-    launch_fma_probe(fp64, d_o, blocks, iters, ctx->stream);     // warm-up
-    CKLAUNCH();
-    cudaEvent_t a, b;
-    cudaEventCreate(&a); cudaEventCreate(&b);
-    cudaEventRecord(a, ctx->stream);
-    for (int r = 0; r < 5; ++r) launch_fma_probe(fp64, d_o, blocks, iters, ctx->stream);
-    cudaEventRecord(b, ctx->stream);
-    CKS(sync_stream(ctx));
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, a, b);
-    cudaEventDestroy(a); cudaEventDestroy(b);
-    *tflops = 5.0 * (double)blocks * 256 * iters * 8 * 2 / (ms * 1e-3) / 1e12;
-    return SGL_OK;
-}
-
-void sgl_invert_opts_default(sgl_invert_opts* o) {
-    if (!o) return;
-    o->precision = SGL_FP64;
-    o->tail_box = 1;
-    o->phi_tol = 1e-8;
-    o->n_xi_wide = 500;
-    o->n_k_int = 2400;
-    o->xi_reach = 24.0;
-    o->window = 0;
-}
-
-sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_invert_opts* opts, double* P_out,
-                   sgl_invert_meta* meta) {
-    if (!ctx) return SGL_ERR_VALUE;
-    if (!ctx->has_cells) return fail(ctx, SGL_ERR_STATE, "cells not set");
-    if (n_xi < 0 || (n_xi > 0 && (!xi_out || !P_out))) return fail(ctx, SGL_ERR_VALUE, "invalid output grid");
-    sgl_invert_opts o;
-    sgl_invert_opts_default(&o);
-    if (opts) o = *opts;
-    if (o.precision != SGL_FP64 && o.precision != SGL_MIXED) return fail(ctx, SGL_ERR_VALUE, "unknown precision");
-    if (o.n_xi_wide < 2 || o.n_k_int < 2 || !(o.phi_tol > 0) || !(o.xi_reach > 0) || o.window < 0 || o.window > 2)
-        return fail(ctx, SGL_ERR_VALUE, "invalid inversion options");
-    for (int i = 0; i < n_xi; ++i) if (!std::isfinite(xi_out[i])) return fail(ctx, SGL_ERR_VALUE, "non-finite xi_out");
-    CK(cudaSetDevice(ctx->device));
-    CKS(sync_stream(ctx));
-    const cudaStream_t st = ctx->stream;
-    double sigma;
-    CKS(sgl_lam_sigma(ctx, &sigma));
-    if (!(sigma > 0) || !std::isfinite(sigma)) return fail(ctx, SGL_ERR_VALUE, "sigma_kappa must be positive");
-    // ---- vector_grid (sgl.py:1229-1258)
-    const double sig_xi = 2.0 * sigma;
-    const double xi_max = o.xi_reach * sig_xi, xi_min = -kBoxReach * sig_xi;
-    double kap_max = 1.0 - std::exp(-0.5 * xi_max);
-    const double kap_min = -kBoxReach * sigma;
-    double gam_max = kBoxReach * sigma;
-    const double g0 = gam_max;
-    double k_k_max = kSigReach / sigma, k_g_max = kSigReach / sigma;
-    long long n_kap = (long long)std::ceil((kap_max - kap_min) / (sigma / kPtsPerSigKap)) + 1;
-    long long n_gam = (long long)std::ceil(gam_max / (sigma / kPtsPerSigGam)) + 1;
-    // ---- invert grid logic (sgl_full.py:191-262)
-    double kap_max_new = kap_max, gam_max_new = gam_max;
-    if (o.tail_box) { kap_max_new = std::max(kap_max, kTailKapMax); gam_max_new = std::max(g0, kTailGamMax); }
-    double dk_k = 2.0 * M_PI / (kPppK * std::max(std::fabs(kap_min), kap_max));
-    double dk_g = 2.0 * M_PI / (kPppG * gam_max);
-    if (o.tail_box && kTailPppG > 0) dk_g = std::min(dk_g, 2.0 * M_PI / (kTailPppG * gam_max_new));
-    if (kap_max_new != kap_max || gam_max_new != gam_max) {
-        kap_max = kap_max_new; gam_max = gam_max_new;
-        n_kap = (long long)std::ceil((kap_max - kap_min) / (sigma / kPtsPerSigKap)) + 1;
-        n_gam = (long long)std::ceil(gam_max / (sigma / kPtsPerSigGam)) + 1;
-    }
-    // ---- measured reach (_reach, sgl_full.py:38-47): 20 probes k0 * 1.25^j per axis
-    const int nprobe = (int)std::ceil(std::log(64.0) / std::log(1.25)) + 1;
-    double reach[2], phic[2];
-    for (int ax = 0; ax < 2; ++ax) {
-        const double k0v = ax == 0 ? k_k_max : k_g_max;
-        std::vector<double> ks(nprobe), re(nprobe), im(nprobe);
-        for (int j = 0; j < nprobe; ++j) ks[j] = k0v * std::pow(1.25, (double)j);
-        const double zero = 0.0;
-        if (ax == 0) CKS(lambda_direct(ctx, ks.data(), nprobe, &zero, 1, re.data(), im.data(), o.precision));
-        else CKS(lambda_direct(ctx, &zero, 1, ks.data(), nprobe, re.data(), im.data(), o.precision));
-        int pick = -1, amin = 0;
-        double best = 1e300;
-        for (int j = 0; j < nprobe; ++j) {
-            const double phi = std::fabs(std::exp(re[j]));   // |exp(L)| = exp(Re L)
-            if (phi <= o.phi_tol && pick < 0) pick = j;
-            if (phi < best) { best = phi; amin = j; }
-        }
-        const int i = pick >= 0 ? pick : amin;
-        reach[ax] = ks[i];
-        phic[ax] = std::exp(re[i]);
-    }
-    k_k_max = reach[0]; k_g_max = reach[1];
-    const long long nk_k = (long long)std::ceil(k_k_max / dk_k) + 1;
-    const long long nk_g = (long long)std::ceil(k_g_max / dk_g) + 1;
-    if (ctx->vp_on) {
-        // the positive closure's coarse grid follows ln R as the box grows, per axis
-        // (sgl_full.py:226-238); persistent, like the reference's Lam attributes
-        const double kks = k_k_max * sigma, kgs = k_g_max * sigma;
-        ctx->vp_xi_coarse = (int)std::min(401.0, std::max((double)ctx->vp_xi_coarse, 1.0 + std::ceil(12.65 * std::sqrt(kgs))));
-        ctx->vp_xi_coarse_k = (int)std::min(4001.0, std::max({(double)ctx->vp_xi_coarse_k, (double)ctx->vp_xi_coarse,
-                                                              1.0 + std::ceil(66.7 * std::sqrt(kks))}));
-    }
-    if ((double)n_kap * (double)n_gam > kOutGridMax)
-        return fail(ctx, SGL_ERR_UNSUPPORTED, "geometric output grid (n_kap * n_gam > OUT_GRID_MAX) not implemented");
-    // Above 2e7 k-points the reference accumulates Phi, the Hankel product and the kappa transform
-    // over k_kappa row blocks to bound host memory (_invert_blocked, sgl_full.py:97-157; "same sums,
-    // partial-sum order -> roundoff").  The whole grid fits in HBM here, so the same sums run
-    // unblocked; allocation failure is reported as such.  The Phi rows are one grid dimension of
-    // the composition kernel, hence the axis limit.
-    if (nk_k > 65535) return fail(ctx, SGL_ERR_UNSUPPORTED, "k_kappa axis longer than 65535 points");
-    if (nk_k < 2 || nk_g < 2) return fail(ctx, SGL_ERR_VALUE, "degenerate k grid");
-    const std::vector<double> kk = linspace(0.0, k_k_max, nk_k);
-    const std::vector<double> kg = linspace(0.0, k_g_max, nk_g);
-    const std::vector<double> kap = linspace(kap_min, kap_max, n_kap);
-    const std::vector<double> gam = linspace(0.0, gam_max, n_gam);
-    const int nk = (int)nk_k, nkg = (int)nk_g, nkap = (int)n_kap, ngam = (int)n_gam;
-    const int P = o.precision;
-    const size_t es = elem_size(P);
-
-    cudaEventRecord(ctx->ev[0], st);
-    // ---- Phi = exp(ln Phi) on the full grid
-    void* Phi = ctx->arena.get("phi", 2ULL * nk * nkg * es);
-    if (!Phi) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (phi)");
-    CKS(lambda_eval(ctx, P, kk.data(), nk, kg.data(), nkg, 1, Phi, (char*)Phi + (size_t)nk * nkg * es));
-    // window (sgl_full.py:254-258): 1 always, 2 ("auto") only when the reach did not converge
-    const bool use_win = o.window == 1 || (o.window == 2 && std::max(phic[0], phic[1]) > o.phi_tol);
-    if (use_win) {
-        std::vector<double> wk(nk), wg(nkg);
-        for (int i = 0; i < nk; ++i) {
-            const double x = std::fabs(kk[i]) * 2.0 / k_k_max;
-            const double v = x < 1 ? 2.0 / 3.0 - x * x + x * x * x / 2 : (x < 2 ? (2 - x) * (2 - x) * (2 - x) / 6 : 0.0);
-            wk[i] = v / (2.0 / 3.0);
-        }
-        for (int j = 0; j < nkg; ++j) {
-            const double r = std::min(1.0, std::max(0.0, std::fabs(kg[j]) / k_g_max));
-            wg[j] = std::pow(1 - r, 4) * (4 * r + 1);
-        }
-        DBUF(d_wk, double, "win_k", nk);
-        DBUF(d_wg, double, "win_g", nkg);
-        CKS(upload(ctx, d_wk, wk.data(), nk));
-        CKS(upload(ctx, d_wg, wg.data(), nkg));
-        launch_window(P, Phi, nk, nkg, d_wk, d_wg, st); CKLAUNCH();
-    }
-    cudaEventRecord(ctx->ev[1], st);
-    // ---- transforms: F = Phi @ M (Hankel), P3ext = c CS @ [F | va | vb]
-    DBUF(d_kk, double, "inv_kk", nk);
-    DBUF(d_kg, double, "inv_kg", nkg);
-    DBUF(d_kap, double, "inv_kap", nkap);
-    DBUF(d_gam, double, "inv_gam", ngam);
-    CKS(upload(ctx, d_kk, kk.data(), nk));
-    CKS(upload(ctx, d_kg, kg.data(), nkg));
-    CKS(upload(ctx, d_kap, kap.data(), nkap));
-    CKS(upload(ctx, d_gam, gam.data(), ngam));
-    const int ldF = ngam + 2;
-    void* M = ctx->arena.get("inv_M", (size_t)nkg * ldF * es * (P == SGL_FP64 ? 1 : 2));
-    void* F = ctx->arena.get("inv_F", 2ULL * nk * ldF * es);
-    void* CS = ctx->arena.get("inv_CS", (size_t)nkap * 2 * nk * es);
-    void* P3e = ctx->arena.get("inv_P3e", (size_t)nkap * ldF * es);
-    DBUF(d_P3, double, "inv_P3", (long long)nkap * ngam);
-    if (!M || !F || !CS || !P3e) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (transforms)");
-    const double dkg = kg[1] - kg[0], dkk = kk[1] - kk[0];
-    launch_hankel_matrix(P, d_kg, nkg, dkg, d_gam, ngam, ldF, M, st); CKLAUNCH();
-    launch_kappa_matrix(P, d_kk, nk, dkk, d_kap, nkap, CS, st); CKLAUNCH();
-    // mixed path: the transform sums run in >= 4 K-slices combined in float-float; within a slice
-    // the FP32 kernel's compensated blocked accumulation bounds the chain's rounding
-    constexpr int kTransformSplit = 4;
-    const double c = 1.0 / (2.0 * M_PI * M_PI);
-    if (P == SGL_FP64) {
-        CKS(gemm_splitk<double>(ctx, gd<double>(2 * nk, ngam, nkg, Phi, nkg, 1, M, ldF, 1, F, ldF), "hankel"));
-    } else {
-        // F = Phi M_hi + Phi M_lo (split Hankel matrix)
-        CKS(gemm_splitk<float>(ctx, gd<float>(2 * nk, ngam, nkg, Phi, nkg, 1, M, ldF, 1, F, ldF), "hankel", kTransformSplit));
-        // the M_lo term is a correction of relative size 2^-24: BF16 operands on the tensor cores
-        // carry it to ~0.4%, i.e. ~2e-10 of F
-        CKS(gemm_splitk_tc(ctx, gd<float>(2 * nk, ngam, nkg, Phi, nkg, 1, (const float*)M + (size_t)nkg * ldF, ldF,
-                                          1, F, ldF, 1.0, 1.0), "hankel_lo", 1, 1));
-    }
-    launch_em_columns(P, Phi, nk, nkg, dkg, F, ldF, ngam, st); CKLAUNCH();
-    if (P == SGL_FP64) {
-        CKS(gemm_splitk<double>(ctx, gd<double>(nkap, ldF, 2 * nk, CS, 2 * nk, 1, F, ldF, 1, P3e, ldF, c), "kappa"));
-    } else {
-        CKS(gemm_splitk<float>(ctx, gd<float>(nkap, ldF, 2 * nk, CS, 2 * nk, 1, F, ldF, 1, P3e, ldF, c), "kappa", kTransformSplit));
-    }
-    float* d_P3f = nullptr;
-    if (P == SGL_MIXED) {
-        d_P3f = dbuf<float>(ctx, "inv_P3f", (size_t)nkap * ngam);
-        if (!d_P3f) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (P3f)");
-    }
-    launch_p3_finish(P, P3e, nkap, ngam, ldF, d_gam, d_P3, d_P3f, st); CKLAUNCH();
-    cudaEventRecord(ctx->ev[2], st);
-    // ---- path integral on the wide grid and the output grid in one launch
-    const int nw = o.n_xi_wide;
-    const std::vector<double> xw = linspace(xi_min, xi_max, nw);
-    std::vector<double> xall(xw);
-    xall.insert(xall.end(), xi_out, xi_out + n_xi);
-    DBUF(d_x, double, "path_x", xall.size());
-    DBUF(d_pi, double, "path_out", xall.size());
-    CKS(upload(ctx, d_x, xall.data(), xall.size()));
-    const double g_def = std::min(g0, gam_max);
-    {
-        Timed t(ctx, "path_integral", 0.0, (double)xall.size() * o.n_k_int * 2 * 4 * 8);
-        launch_path_integral(d_P3, d_P3f, nkap, ngam, kap.front(), kap.back(), gam.back(), d_x, (int)xall.size(),
-                             gam_max, g_def, o.n_k_int, d_pi, st);
-    }
-    CKLAUNCH();
-    cudaEventRecord(ctx->ev[3], st);
-    std::vector<double> pall(xall.size());
-    CK(cudaMemcpyAsync(pall.data(), d_pi, pall.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CKS(sync_stream(ctx));
-    CKS(check_dev_err(ctx));
-    // ---- normalisation and moments (sgl_full.py:362-372)
-    const double* pw = pall.data();
-    const double norm = trapz(pw, xw.data(), nw);
-    std::vector<double> ps(nw), tmp(nw);
-    for (int i = 0; i < nw; ++i) ps[i] = pw[i] / norm;
-    for (int i = 0; i < nw; ++i) tmp[i] = xw[i] * ps[i];
-    const double mean = trapz(tmp.data(), xw.data(), nw);
-    for (int i = 0; i < nw; ++i) { const double d = xw[i] - mean; tmp[i] = d * d * ps[i]; }
-    const double var = trapz(tmp.data(), xw.data(), nw);
-    for (int i = 0; i < nw; ++i) { const double d = xw[i] - mean; tmp[i] = d * d * d * ps[i]; }
-    const double skew = trapz(tmp.data(), xw.data(), nw) / std::pow(var, 1.5);
-    std::vector<double> xe(nw);
-    for (int i = 0; i < nw; ++i) xe[i] = std::exp(-0.5 * xw[i]);
-    for (int i = 0; i < nw; ++i) tmp[i] = xe[i] * ps[i];
-    const double md = trapz(tmp.data(), xw.data(), nw);
-    for (int i = 0; i < nw; ++i) { const double d = xe[i] - md; tmp[i] = d * d * ps[i]; }
-    const double sDL = std::sqrt(trapz(tmp.data(), xw.data(), nw)) / md;
-    bool finite = std::isfinite(norm) && norm != 0.0;
-    for (int i = 0; i < n_xi; ++i) {
-        P_out[i] = pall[(size_t)nw + i] / norm;
-        finite = finite && std::isfinite(P_out[i]);
-    }
-    if (meta) {
-        meta->nk_k = nk_k; meta->nk_g = nk_g; meta->n_kap = n_kap; meta->n_gam = n_gam;
-        meta->k_k_max = k_k_max; meta->k_g_max = k_g_max; meta->kap_min = kap_min; meta->kap_max = kap_max;
-        meta->gam_max = gam_max; meta->xi_min = xi_min; meta->xi_max = xi_max; meta->sigma = sigma;
-        meta->phi_at_k_cut = phic[0]; meta->phi_at_g_cut = phic[1];
-        meta->mean = mean; meta->var = var; meta->skew = skew; meta->sigmaDL = sDL; meta->norm = norm;
-        float a = 0, b = 0, cc = 0;
-        cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
-        cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]);
-        cudaEventElapsedTime(&cc, ctx->ev[2], ctx->ev[3]);
-        meta->ms_lambda = a; meta->ms_transform = b; meta->ms_path = cc;
-        meta->window = use_win ? 1.0 : 0.0;
-        meta->xi_coarse = ctx->vp_on ? ctx->vp_xi_coarse : 0.0;
-        meta->xi_coarse_k = ctx->vp_on ? ctx->vp_xi_coarse_k : 0.0;
-    }
-    if (!finite) return fail(ctx, SGL_ERR_NONFINITE, "PDF inversion returned non-finite values");
     return SGL_OK;
 }
 

@@ -109,6 +109,18 @@ __global__ void k_window(TT* __restrict__ Phi, int nk, int nkg, const double* __
     Phi[npt + e] = (TT)((double)Phi[npt + e] * w);
 }
 
+// out[e] = (float)in[e]: a caller's FP64 Phi planes taken into the mixed path's FP32 layout
+__global__ void k_phi_to_f32(const double* __restrict__ in, long long n, float* __restrict__ out) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n) out[e] = (float)in[e];
+}
+
+void launch_phi_to_f32(const double* in, long long n, float* out, cudaStream_t st) {
+    if (n <= 0) return;
+    k_phi_to_f32<<<ceil_div(n, 256), 256, 0, st>>>(in, n, out);
+    SGL_COUNT(1);
+}
+
 void launch_window(int precision, void* Phi, int nk, int nkg, const double* wk, const double* wg, cudaStream_t st) {
     const long long tot = (long long)nk * nkg;
     if (precision == SGL_FP64) { k_window<double><<<ceil_div(tot, 256), 256, 0, st>>>((double*)Phi, nk, nkg, wk, wg); SGL_COUNT(1); }

@@ -133,6 +133,7 @@ void launch_kappa_matrix(int precision, const double* kk, int nk, double dkk, co
 void launch_em_columns(int precision, const void* Phi, int nk, int nkg, double dkg, void* F, int ldF, int col,
                        cudaStream_t st);
 void launch_window(int precision, void* Phi, int nk, int nkg, const double* wk, const double* wg, cudaStream_t st);
+void launch_phi_to_f32(const double* in, long long n, float* out, cudaStream_t st);
 void launch_p3_finish(int precision, const void* P3ext, int nkap, int ngam, int ld, const double* gam, double* P3,
                       float* P3f, cudaStream_t st);
 void launch_path_integral(const double* P3, const float* P3f, int nkap, int ngam, double kap0, double kap1,

@@ -9,8 +9,10 @@ pipeline.py:36-164; the cosmology domain of sgl.py:111-151), then
   2. ``Lam`` + ``invert`` on the GPU (this package);
   3. the reference's output dict (pipeline.py:243-271) for the keys the hot path determines.
 
-Only the default chain is on the GPU path: clustering "xilin", the gauss closure, edge "r200" or
-"rvir".  Everything else raises ``NotImplementedError`` (there is no CPU fallback).
+Only the default chain is on the GPU path: clustering "xilin" with the gauss or the vp closure, edge
+"r200" or "rvir".  Everything else raises ``NotImplementedError`` (there is no CPU fallback).  The vp
+closure's set-up (shells, chain, rates) comes with the population: a pre-built population carries it
+(``Population.vp``), a population built here gets it from the reference package.
 """
 from __future__ import annotations
 
@@ -24,6 +26,8 @@ P = dict(h=0.674, Om=0.315, s8=0.811, Ob=0.0493, ns=0.965, zeq=3402.0)
 EXTENSIONS = dict(Ok=0.0, w0=-1.0, wa=0.0, growth_mode="ode", radiation="engine")
 INGREDIENTS = ("ell", "fil", "sub", "bias")
 DE_REC_CAP = 1e-2
+# the fine (kappa, gamma) lattice of the population build (sgl_full.py:456): (lo, hi, bins per sign)
+FINE = dict(k=(1e-7, 30.0, 480), g=(1e-9, 30.0, 300))
 
 
 def on(cfg):
@@ -139,8 +143,6 @@ def run(zs, cfg="full", nord=4, grid_scale=1.0, xi_out=None, split=10.0, exact_s
     if xi_closure != "gauss" and not use_xi:
         raise ValueError(f"xi_closure={xi_closure!r} needs xilin clustering and the bias ingredient")
     cp = cosmology_params(cosmo)
-    if xi_closure != "gauss":
-        raise NotImplementedError("xi_closure='vp' is not on the GPU path")
     if clustering != "xilin" or edge == "kthr" or grid_scale != 1.0 or lam_coarse:
         raise NotImplementedError("only the default chain (clustering='xilin', edge r200/rvir) is on the GPU path")
     if {**EXTENSIONS, **(cosmo or {})}["growth_mode"] == "auto" and not (cp["w0"] == -1.0 and cp["wa"] == 0.0):
@@ -152,12 +154,23 @@ def run(zs, cfg="full", nord=4, grid_scale=1.0, xi_out=None, split=10.0, exact_s
     info = {}
     if population is not None:
         pop = _load_population(population)
+        if xi_closure != "gauss" and pop.vp is None:
+            raise ValueError(f"xi_closure={xi_closure!r} needs a population that carries its closure (Population.vp)")
     else:
         pop, info = _build_population_with_reference(zs, cfg, s, cp, sub_kw, split, edge, kap_floor, zint, zint_n,
-                                                     xi_kw, use_xi, nproc, nord)
+                                                     xi_kw, use_xi, nproc, nord, xi_closure)
     t_build = time.time()
     lam = Lam(pop, C=None, nord=nord, exactS=False, k3=False, s_taper=s_taper, q_coarse=q_coarse, xi=use_xi,
               precision=precision, device=device)
+    pos_info = None
+    if xi_closure != "gauss":
+        # the positive closure replaces the gauss term (pos_closure.install, pipeline.py:206-209)
+        t_pos = time.time()
+        lam.install_vp(pop.vp)
+        pos_info = dict(kind=xi_closure, eta=(float(pop.vp["eta"]) if "eta" in pop.vp else None),
+                        nstate=int(np.asarray(pop.vp["u"]).size), shells=int(np.asarray(pop.vp["sh_g"]).size - 1),
+                        eval_kernel="gpu", setup_seconds=info.get("pos_setup_seconds", 0.0) + time.time() - t_pos,
+                        lnR_seconds=None)
     sig = lam.sigma()
     t_lam = time.time()
     if xi_out is None:
@@ -177,18 +190,25 @@ def run(zs, cfg="full", nord=4, grid_scale=1.0, xi_out=None, split=10.0, exact_s
     xa, Pa, meta = invert(lam, sig, xi_out=xall, tail_box=tail_box, phi_tol=phi_tol, nproc=1, window=window,
                           n_xi_wide=n_xi_wide)
     t_inv = time.time()
+    # every key of the reference's output dict (pipeline.py:243-271); the ones the population build
+    # determines come from it when it ran here, None when the population was given
+    Or = cp["Om"] / (1.0 + cp["zeq"]) if cp["radiation"] == "engine" else 0.0
     out = dict(t_stages=dict(build=t_build - t0, lam=t_lam - t_build, invert=t_inv - t_lam), zs=zs,
                cfg=cfg_name(cfg), zint=zint, zint_n=(zint_n if zint == "gauss" else None), clustering=clustering,
-               edge=edge, lss_var=0.0, kap_floor=(kap_floor if edge != "kthr" else None),
-               h=cp["h"], Om=cp["Om"], s8=cp["s8"], Ob=cp["Ob"], ns=cp["ns"], zeq=cp["zeq"], sigma8=cp["s8"],
-               Ok=cp["Ok"], w0=cp["w0"], wa=cp["wa"], growth_mode=cp["growth_mode"], radiation=cp["radiation"],
-               nord=nord, grid_scale=grid_scale, split=split, nproc=nproc, k3=False, exactS=False,
-               s_taper=s_taper, sigma_kappa=sig, kbar=info.get("kbar"), N_expl=info.get("N_expl"),
+               xi_kperp=info.get("xi_kperp"), edge=edge, lss_var=0.0, kap_floor=(kap_floor if edge != "kthr" else None),
+               kbar=info.get("kbar"), h=cp["h"], Om=cp["Om"], s8=cp["s8"], Ob=cp["Ob"], ns=cp["ns"], zeq=cp["zeq"],
+               sigma8=cp["s8"], Ok=cp["Ok"], w0=cp["w0"], wa=cp["wa"], growth_mode=cp["growth_mode"],
+               radiation=cp["radiation"], Omega_r=Or, nord=nord, grid_scale=grid_scale, split=split, nproc=nproc,
+               sub_kw=info.get("sub_kw"), pair_angle=info.get("pair_angle"), k3=False, exactS=False,
+               s_taper=s_taper, sigma_kappa=sig, kthr=None, N_expl=info.get("N_expl"),
                N_fil=info.get("N_fil"), V_weak=info.get("V_weak"), mean=meta["mean"], var=meta["var"],
                skew=meta["skew"], sigmaDL=meta["sigmaDL"],
                grid={k: v for k, v in meta["grid"].items() if isinstance(v, (int, float))},
-               tail_box=bool(tail_box), xi_closure=xi_closure, window=window, n_xi_wide=n_xi_wide,
-               pos_closure=None, engine=dict(precision=precision, device_ms=meta["device_ms"]),
+               tail_box=bool(tail_box), fine=dict(FINE), s_is=bool(s_is), xi_closure=xi_closure, window=window,
+               n_xi_wide=n_xi_wide, pos_closure=pos_info, direct_product_backend="unused",
+               s_seed=(int(s_seed) if s_seed is not None else None), s_seed_effective=(int(s_seed) if s_seed is not None
+                                                                                       else 0),
+               s_ess=None, is_design=None, engine=dict(precision=precision, device_ms=meta["device_ms"]),
                seconds=time.time() - t0, xi=np.asarray(xa[:nx]).tolist(), P_s=np.asarray(Pa[:nx]).tolist())
     if xi_tail is not None:
         out.update(xi_tail=np.asarray(xa[nx:]).tolist(), P_s_tail=np.asarray(Pa[nx:]).tolist())
@@ -199,8 +219,10 @@ def run(zs, cfg="full", nord=4, grid_scale=1.0, xi_out=None, split=10.0, exact_s
 
 
 def _build_population_with_reference(zs, cfg, s, cp, sub_kw, split, edge, kap_floor, zint, zint_n, xi_kw, use_xi,
-                                     nproc, nord):
-    """The population build (upstream of the hot path) through the reference package."""
+                                     nproc, nord, xi_closure="gauss"):
+    """The population build (upstream of the hot path) through the reference package; for a
+    positive closure also the closure's set-up (pos_closure.install on the reference's own Lam,
+    pos_closure.py:708-733), whose arrays the GPU Lam then takes."""
     try:
         from sgl_analytic import sgl_full as F
         from sgl_analytic import subhalos
@@ -214,11 +236,35 @@ def _build_population_with_reference(zs, cfg, s, cp, sub_kw, split, edge, kap_fl
     skw.update(sub_kw or {})
     sub = subhalos.SubhaloModel(cos, zs, None, split=split, **skw) if "sub" in s else None
     xi = F.xi_kperp_grid(cos, **(xi_kw or {})) if use_xi else None
+    if xi is not None and xi_closure != "gauss":
+        xi["pos"] = True
     cells, info = F.build_population(cos, zs, ell="ell" in s, fils="fil" in s, nord=nord, kthr=None, subhalo=sub,
                                      nproc=nproc, zint=zint, zint_n=zint_n, xi=xi, kap_floor=kap_floor, trunc=trunc)
     pop = Population.from_cells(cells)
     pop.zs = float(zs)
+    info = dict(info)
+    info["xi_kperp"] = {k: xi[k] for k in ("kmin", "kmax", "per_decade", "mmax")} if xi else None
+    info["sub_kw"] = sub._init_kw if sub is not None else None
+    info["pair_angle"] = sub.pair_angle if sub is not None else None
+    if xi_closure != "gauss":
+        import time as _time
+        from sgl_analytic import pos_closure
+        t = _time.time()
+        ref_lam = F.Lam(cells, C=None, nord=1, exactS=False, k3=False, xi=True)
+        pos = pos_closure.install(ref_lam, cos, kind=xi_closure)
+        pop.vp = closure_arrays(pos)
+        info["pos_setup_seconds"] = _time.time() - t
     return pop, info
+
+
+def closure_arrays(pos):
+    """The arrays of a reference closure object (pos_closure.install's return; its FusedVP rate
+    intervals, pos_closure_fused.py:18-48) in the form Lam.install_vp takes."""
+    fused = pos.lnR_blocked.__self__
+    B = pos._B
+    return dict(u=pos.u, w=pos.w, K=pos._Karr, shear_var=float(pos.shear_var), eta=float(pos.eta), ku=pos.ku,
+                gu=pos.gu, cu=B["cu"].astype(np.int32), cw=B["cw"], gstart=B["gstart"], sh_g=B["sh_g"], ga=fused.a,
+                gb=fused.b, gc=fused.c, glo=fused.lo.astype(np.int32), ghi=fused.hi.astype(np.int32))
 
 
 def clipped_moments(xi, P, clip=1.0):

@@ -31,6 +31,12 @@ class Population:
     ce_g: np.ndarray | None = None
     xg_s0: float = 0.0          # > 0: largest row norm of the full set (for subsets of groups)
     zs: float | None = None
+    # positive (vp) closure built for this population (pos_closure.install): the arrays of
+    # Lam.install_vp (u, w, K, ku, gu, cu, cw, gstart, sh_g, ga, gb, gc, glo, ghi, shear_var, eta)
+    vp: dict | None = None
+
+    VP_FILE_KEYS = ("u", "w", "K", "ku", "gu", "cu", "cw", "gstart", "sh_g", "ga", "gb", "gc", "glo", "ghi",
+                    "shear_var", "eta")
 
     @property
     def n_cells(self):
@@ -83,6 +89,8 @@ class Population:
             kw.update(xg_m=np.asarray(m, np.int32), xg_nrow=np.asarray(nr, np.int32),
                       xg_nidx=np.asarray(ni, np.int32), xg_idx=np.asarray(idx, np.int32),
                       xg_rows=np.asarray(rows, float), ce_k=d["ce_k"], ce_g=d["ce_g"], xg_s0=s0)
+        if "vp_u" in d.files:
+            kw["vp"] = {k: d["vp_" + k] for k in cls.VP_FILE_KEYS if "vp_" + k in d.files}
         return cls(**kw)
 
     def save(self, path):
@@ -93,6 +101,8 @@ class Population:
             out.update(ce_k=self.ce_k, ce_g=self.ce_g)
         if self.zs is not None:
             out["zs"] = np.float64(self.zs)
+        if self.vp is not None:
+            out.update({"vp_" + k: np.asarray(v) for k, v in self.vp.items() if k in self.VP_FILE_KEYS})
         np.savez_compressed(path, **out)
 
     def groups(self):

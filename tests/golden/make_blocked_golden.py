@@ -10,7 +10,7 @@ Writes (committed, small):
   tests/golden/pop_blocked.npz  -- the population (cells only, no xi groups)
   tests/golden/ref_blocked.npz  -- invert(...) on the CLI xi grids: P, the grid, the moments
 
-Usage:  python tests/golden/make_blocked_golden.py   (needs the reference source and the z_s=1
+Usage:  python tests/golden/make_blocked_golden.py --reference PATH   (or SGL_REFERENCE=PATH; needs the reference source and the z_s=1
 cells pickle made by make_fixtures.py build)
 """
 from __future__ import annotations
@@ -22,8 +22,10 @@ from pathlib import Path
 
 import numpy as np
 
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+from _reference import reference_root  # noqa: E402
+
 REPO = Path(__file__).resolve().parents[2]
-REF = Path("/root/reference")
 GOLDEN = REPO / "tests" / "golden"
 FULL = GOLDEN / "full"
 N_CELLS, SEED, W_SCALE = 300, 7, 56.0
@@ -36,6 +38,7 @@ def subset(pop):
 
 
 def main():
+    REF = reference_root()
     sys.path.insert(0, str(REF / "src"))
     sys.path.insert(0, str(REPO))
     from sgl_analytic import sgl_full as F          # noqa: E402

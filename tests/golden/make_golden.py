@@ -16,7 +16,7 @@ Writes (committed, a few MB):
        pdfx_*   invert(Lam(xi=True))  on the same grids
 Also copies the reference's stored golden PDFs (tests/reference/pdf_zs*.json) next to them.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  python tests/golden/make_golden.py --reference PATH   (or SGL_REFERENCE=PATH)
 """
 from __future__ import annotations
 
@@ -28,8 +28,10 @@ from pathlib import Path
 
 import numpy as np
 
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+from _reference import reference_root  # noqa: E402
+
 REPO = Path(__file__).resolve().parents[2]
-REF = Path("/root/reference")
 GOLDEN = REPO / "tests" / "golden"
 FULL = REPO / "tests" / "golden" / "full"          # large, git-ignored
 WORK = FULL
@@ -37,6 +39,7 @@ SHELL = 30
 
 
 def main():
+    REF = reference_root()
     sys.path.insert(0, str(REF / "src"))
     sys.path.insert(0, str(REPO))
     from sgl_analytic import sgl_full as F          # noqa: E402  (no numba: NumPy paths)

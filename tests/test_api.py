@@ -2,6 +2,7 @@
 tests/test_api.py contracts: validation before any solve, forwarding, the mu Jacobian, the
 negative-residual warning) plus the GPU-path limits, the plugin and the CLI."""
 import json
+from pathlib import Path
 import types
 import warnings
 from unittest.mock import patch
@@ -69,10 +70,10 @@ def test_invalid_redshift_and_workers_fail_before_solve():
         lam.assert_not_called()
 
 
-def test_configurations_outside_the_gpu_path_raise():
+def test_configurations_outside_the_gpu_path_raise(pop_sub):
     with patch("sgl_analytic_gb300.lam.Lam") as lam:
-        with pytest.raises(NotImplementedError):
-            run(1, "full", xi_closure="vp")
+        with pytest.raises(ValueError):             # the vp closure needs a population that carries it
+            run(1, "full", xi_closure="vp", population=pop_sub)
         with pytest.raises(NotImplementedError):
             run(1, "full", clustering="limber")
         lam.assert_not_called()
@@ -160,3 +161,18 @@ def test_population_roundtrip(tmp_path, pop_sub):
     assert len(g) == 3 and g[0]["rows"].shape == (int(back.xg_nrow[0]), int(back.xg_nidx[0]) + 1)
     sub = Population.load(p, groups=[1])
     assert sub.xg_m.tolist() == [1] and sub.xg_s0 > 0
+
+
+def test_population_carries_the_vp_closure(tmp_path, pop_sub):
+    """A population saved with its vp closure loads it back (Lam.install_vp's arrays)."""
+    from dataclasses import replace
+    vp = dict(np.load(Path(__file__).resolve().parent / "golden" / "vp_zs1_sub.npz"))
+    vp = {k: vp[k] for k in Population.VP_FILE_KEYS if k in vp}
+    pop = replace(pop_sub, vp=vp)
+    p = tmp_path / "pop_vp.npz"
+    pop.save(p)
+    back = Population.load(p)
+    assert set(back.vp) == set(vp)
+    for k in vp:
+        np.testing.assert_array_equal(back.vp[k], vp[k])
+    assert Population.load(tmp_path / "pop_vp.npz").vp is not None

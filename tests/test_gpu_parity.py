@@ -264,6 +264,21 @@ def test_cli_end_to_end(tmp_path, ref_sub):
     P = np.array(d["P_s"] + d["P_s_tail"])
     dpeak, _, _ = _pdf_errors(P, ref_sub["pdfx_P"], ref_sub["xi_out"])
     assert dpeak <= TOL_PEAK
+    # the reference's output keys: pipeline.run's dict (pipeline.py:243-271) and the CLI's additions
+    # (cli.py:65-70)
+    run_keys = {"t_stages", "zs", "cfg", "zint", "zint_n", "clustering", "xi_kperp", "edge", "lss_var", "kap_floor",
+                "kbar", "h", "Om", "s8", "Ob", "ns", "zeq", "sigma8", "Ok", "w0", "wa", "growth_mode", "radiation",
+                "Omega_r", "nord", "grid_scale", "split", "nproc", "sub_kw", "pair_angle", "k3", "exactS", "s_taper",
+                "sigma_kappa", "kthr", "N_expl", "N_fil", "V_weak", "mean", "var", "skew", "sigmaDL", "grid",
+                "tail_box", "fine", "s_is", "xi_closure", "window", "n_xi_wide", "pos_closure",
+                "direct_product_backend", "s_seed", "s_seed_effective", "s_ess", "is_design", "seconds", "xi", "P_s",
+                "xi_tail", "P_s_tail"}
+    cli_keys = {"moment_interval", "diagnostics", "clipped"}
+    assert run_keys | cli_keys <= set(d), sorted(run_keys | cli_keys - set(d))
+    assert d["window"] is False and d["n_xi_wide"] == 500 and d["xi_closure"] == "gauss"
+    assert {"nk_k", "nk_g", "n_kap", "n_gam", "xi_min", "xi_max"} <= set(d["grid"])
+    assert {"grid_mass", "negative_mass", "minimum_density"} == set(d["diagnostics"])
+    assert {"mean", "var", "skew"} == set(d["clipped"])
 
 
 def test_xi_preparation_paths_agree(pop_sub, monkeypatch):
@@ -334,3 +349,70 @@ def test_other_redshifts_match_stored_golden(zs, precision):
         assert dpeak <= TOL_PEAK, dpeak
     else:
         assert l1 <= 1e-4 and rel_tail <= 1e-3, (dpeak, l1, rel_tail)
+
+
+def test_invert_caller_phi_matches_pdf_and_reference(lamx, ref_sub):
+    """sgl_plan_grid + sgl_invert on Phi = exp(ln Phi) evaluated by the caller (here through sgl_lnphi)
+    reproduce sgl_pdf and the reference's invert on the same population (FP64 bar)."""
+    eng = lamx.engine
+    x = ref_sub["xi_out"]
+    g = eng.plan_grid(phi_tol=1e-8)
+    assert [g["nk_k"], g["nk_g"], g["n_kap"], g["n_gam"]] == [int(v) for v in ref_sub["pdfx_grid"][[0, 1, 4, 5]]]
+    kk = np.linspace(0.0, g["k_k_max"], g["nk_k"])
+    kg = np.linspace(0.0, g["k_g_max"], g["nk_g"])
+    phi = np.exp(lamx(kk, kg))
+    P, meta = eng.invert_phi(phi, g, x, phi_tol=1e-8)
+    P_pdf, _ = eng.pdf(x, phi_tol=1e-8)
+    peak = np.max(P_pdf)
+    assert np.max(np.abs(P - P_pdf)) <= 1e-12 * peak
+    dpeak, l1, _ = _pdf_errors(P, ref_sub["pdfx_P"], x)
+    assert dpeak <= TOL_PEAK
+    assert meta["nk_k"] == g["nk_k"] and meta["window"] == 0.0
+    # the same Phi from device memory, and the mixed path on it
+    torch = pytest.importorskip("torch")
+    re = torch.tensor(phi.real, dtype=torch.float64, device="cuda:0")
+    im = torch.tensor(phi.imag, dtype=torch.float64, device="cuda:0")
+    torch.cuda.synchronize()
+    Pd, _ = eng.invert_phi((re.data_ptr(), im.data_ptr()), g, x, phi_tol=1e-8)
+    assert np.max(np.abs(Pd - P)) <= 1e-14 * peak
+    from sgl_analytic_gb300._lib import SGL_MIXED
+    Pm, _ = eng.invert_phi(phi, g, x, precision=SGL_MIXED, phi_tol=1e-8)
+    _, l1m, tailm = _pdf_errors(Pm, ref_sub["pdfx_P"], x)
+    assert l1m <= 1e-4 and tailm <= 1e-3, (l1m, tailm)
+
+
+def test_invert_rejects_bad_grids(lamx):
+    eng = lamx.engine
+    g = eng.plan_grid(phi_tol=1e-8)
+    phi = np.ones((g["nk_k"], g["nk_g"]), complex)
+    with pytest.raises(ValueError):
+        eng.invert_phi(phi[:, :-1], g, np.zeros(3))
+    bad = dict(g, sigma=-1.0)
+    with pytest.raises(ValueError):
+        eng.invert_phi(phi, bad, np.zeros(3))
+    bad = dict(g, nk_k=1, nk_g=g["nk_g"])
+    with pytest.raises(ValueError):
+        eng.invert_phi(np.ones((1, g["nk_g"]), complex), bad, np.zeros(3))
+
+
+def test_native_batch_matches_single_context(pop_sub, ref_sub):
+    """sgl_batch_*: PDFs on 3 slots from the batch's own host threads, jobs interleaved over the slots,
+    equal the single-context sgl_pdf result (FP64: the same sums in the same order)."""
+    from sgl_analytic_gb300 import Lam
+    from sgl_analytic_gb300._lib import Batch
+    x = ref_sub["xi_out"]
+    b = Batch(3)
+    try:
+        for i in range(3):
+            Lam(pop_sub, xi=True, engine=b.slot(i))
+        P, metas = b.pdf([0, 1, 2, 0, 2], x, phi_tol=1e-8)
+        assert P.shape == (5, x.size) and len(metas) == 5
+        single, _ = Lam(pop_sub, xi=True).engine.pdf(x, phi_tol=1e-8)
+        for row in P:
+            np.testing.assert_array_equal(row, single)
+        dpeak, _, _ = _pdf_errors(P[0], ref_sub["pdfx_P"], x)
+        assert dpeak <= TOL_PEAK
+        with pytest.raises(ValueError):
+            b.pdf([0, 3], x)                       # no slot 3
+    finally:
+        b.close()
