@@ -160,6 +160,21 @@ sgl_status sgl_vp_set(sgl_ctx* ctx, int nstate, const double* u, const double* w
                       const double* cw, int n_groups, const int64_t* gstart, const int32_t* sh_g, const double* ga,
                       const double* gb, const double* gc, const int32_t* glo, const int32_t* ghi, double shear_var);
 
+/* The same closure built by the engine from its per-shell population (the output of
+ * pos_closure.population, pos_closure.py:388-450): cells of shell s at [shell_start[s],
+ * shell_start[s+1]) with weight W, centroid (kap, gam) and loading phi; rho[s] the line-of-sight
+ * correlation of shells s and s + 1 (n_shells - 1 values); fvar[s]; the kappa and gamma clustering
+ * variance targets.  Builds nstate Gauss-Hermite latent states with stationary transitions, groups
+ * each shell's cells by loading, calibrates eta (the model's kappa variance = target_kappa; eta_in
+ * > 0 skips the calibration and uses it), forms the variance-preserving rates and their state
+ * intervals and the unique cells, then installs the closure as sgl_vp_set does.  Replaces
+ * Closure.__init__ / calibrate (pos_closure.py:453-591) and FusedVP's rate intervals
+ * (pos_closure_fused.py:18-67).  *eta_out (may be NULL) receives eta. */
+sgl_status sgl_vp_build(sgl_ctx* ctx, int nstate, int n_shells, const int64_t* shell_start, const double* W,
+                        const double* kap, const double* gam, const double* phi, const double* rho,
+                        const double* fvar, double target_kappa, double target_gamma, double eta_in,
+                        double* eta_out);
+
 /* ln R on the tensor grid kv x qv (nk x nq, row-major), principal branch, no shear term:
  * FusedVP.lnR_blocked (pos_closure_fused.py:119-140). */
 sgl_status sgl_vp_lnR(sgl_ctx* ctx, const double* kv, int nk, const double* qv, int nq, int precision,
@@ -248,6 +263,30 @@ int sgl_batch_slots(const sgl_batch* batch);
 sgl_ctx* sgl_batch_slot(sgl_batch* batch, int slot);
 sgl_status sgl_batch_pdf(sgl_batch* batch, int n_jobs, const int32_t* job_slot, const double* xi_out, int n_xi,
                          const sgl_invert_opts* opts, double* P_out, sgl_invert_meta* meta, int32_t* job_status);
+
+/* Batched CF solver over uneven instances ------------------------------------------------------
+ * No counterpart in the reference (one pipeline.run per instance, pipeline.py:114-274).  Instance i
+ * has planes inst_plane0[i] .. inst_plane0[i+1]-1; plane p has cells plane_cells[p] ..
+ * plane_cells[p+1]-1 (kap, w); its k grid is k_n = n dk[i], n < nk[i].  Its log-CF:
+ *   closure[i] = 0 (gauss): sum_c w (e^{i k kap} - 1 - i k kap) - V[i] k^2 / 2
+ *   closure[i] = 1 (vp):    sum_p Lambda_p(k) + ln E exp(sum_p (lam_p(U_p) - 1) Lambda_p(k)), U a stationary
+ *                           chain on nstate (<= 8) states: vp_D[p][s] = lam_p(u_s) - 1 per plane, and per vp
+ *                           instance (in order) vp_K[s][t] (transition) and vp_w[s] (stationary weights) --
+ *                           the positive Cox closure's chain (pos_closure.py:184-240) with one group per plane.
+ * sgl_cfb_set uploads the batch (host arrays).  sgl_cfb_tune times every (k points per work item, CTAs per
+ * SM) shape on a sample of the batch and keeps the fastest for that precision (run on first use otherwise).
+ * sgl_cfb_lnphi runs the persistent solve (one launch; CTAs take (instance, k tile) items from a device
+ * counter, longest instances first) and copies ln Phi out as (re, im) pairs per k, instances in order
+ * (out may be NULL).  sgl_cfb_pdf adds Phi = exp(ln Phi) and the inversion to dP/dln mu at the n_lnmu
+ * points (mu = (1 - kappa)^-2): P_out is n_inst x n_lnmu; use_graph = 1 captures the whole step in a CUDA
+ * graph on first use and replays it; *ms_out (may be NULL) receives the device time of the step. */
+sgl_status sgl_cfb_set(sgl_ctx* ctx, int n_inst, const int32_t* inst_plane0, const int64_t* plane_cells,
+                       const double* kap, const double* w, const int32_t* nk, const double* dk, const int32_t* closure,
+                       const double* V, int nstate, const double* vp_D, const double* vp_K, const double* vp_w);
+sgl_status sgl_cfb_tune(sgl_ctx* ctx, int precision, int* kt, int* ctas_per_sm);
+sgl_status sgl_cfb_lnphi(sgl_ctx* ctx, int precision, double* out);
+sgl_status sgl_cfb_pdf(sgl_ctx* ctx, int precision, const double* lnmu, int n_lnmu, double* P_out, int use_graph,
+                       double* ms_out);
 
 /* Allocation-free entry point ------------------------------------------------------------
  * No counterpart in the reference.  For callers that may not allocate device memory (a host that

@@ -21,10 +21,11 @@ PRECISIONS = {"fp64": SGL_FP64, "mixed": SGL_MIXED}
 EXPORTS = ("sgl_abi_version", "sgl_ctx_create", "sgl_ctx_destroy", "sgl_last_error", "sgl_ctx_stream",
            "sgl_ctx_profile", "sgl_stats_json", "sgl_lam_set_cells",
            "sgl_lam_set_xi", "sgl_lam_sigma", "sgl_lnphi", "sgl_xi_term", "sgl_sweep_set_cells", "sgl_sweep_eval", "sgl_measure_peak",
-           "sgl_vp_set", "sgl_vp_lnR", "sgl_invert_opts_default", "sgl_pdf",
+           "sgl_vp_set", "sgl_vp_build", "sgl_vp_lnR", "sgl_invert_opts_default", "sgl_pdf",
            "sgl_gemm_bf16", "sgl_mlp_bias_act", "sgl_mlp_act_grad", "sgl_mlp_col_sum", "sgl_mlp_mse", "sgl_mlp_adamw",
            "sgl_plan_grid", "sgl_invert", "sgl_batch_create", "sgl_batch_destroy", "sgl_batch_slots",
-           "sgl_batch_slot", "sgl_batch_pdf", "sgl_cf_kappa_noalloc")
+           "sgl_batch_slot", "sgl_batch_pdf", "sgl_cfb_set", "sgl_cfb_tune", "sgl_cfb_lnphi", "sgl_cfb_pdf",
+           "sgl_cf_kappa_noalloc")
 
 
 class InvertOpts(C.Structure):
@@ -95,6 +96,15 @@ def lib():
         L.sgl_vp_set.argtypes = [vp, C.c_int, dp, dp, C.c_int, dp, C.c_int, dp, dp, C.c_int64, ip, dp, C.c_int, lp,
                                  ip, dp, dp, dp, ip, ip, C.c_double]
         L.sgl_vp_lnR.argtypes = [vp, dp, C.c_int, dp, C.c_int, C.c_int, dp, dp]
+        L.sgl_vp_build.argtypes = [vp, C.c_int, C.c_int, lp, dp, dp, dp, dp, dp, dp, C.c_double, C.c_double,
+                                   C.c_double, dp]
+        L.sgl_vp_build.restype = C.c_int
+        L.sgl_cfb_set.argtypes = [vp, C.c_int, ip, lp, dp, dp, ip, dp, ip, dp, C.c_int, dp, dp, dp]
+        L.sgl_cfb_tune.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.sgl_cfb_lnphi.argtypes = [vp, C.c_int, dp]
+        L.sgl_cfb_pdf.argtypes = [vp, C.c_int, dp, C.c_int, dp, C.c_int, dp]
+        for name in ("sgl_cfb_set", "sgl_cfb_tune", "sgl_cfb_lnphi", "sgl_cfb_pdf"):
+            getattr(L, name).restype = C.c_int
         for name in ("sgl_sweep_set_cells", "sgl_sweep_eval", "sgl_measure_peak"):
             getattr(L, name).restype = C.c_int
         i64, f32 = C.c_int64, C.c_float
@@ -243,6 +253,59 @@ class Engine:
         self._check(self._L.sgl_xi_term(self._h, _ptr(kk), kk.size, _ptr(kg), kg.size, int(precision), _ptr(re),
                                         _ptr(im)), "sgl_xi_term")
         return re + 1j * im
+
+    # ---------------------------------------------------------------- batched CF solver
+    def cfb_set(self, b):
+        """Uploads a batch (a mapping as sgl_analytic_gb300.cfbatch.Batch.arrays() gives)."""
+        i32 = lambda a: np.ascontiguousarray(a, np.int32)
+        f64 = lambda a: np.ascontiguousarray(a, np.float64)
+        self._cfb = dict(inst_plane0=i32(b["inst_plane0"]), plane_cells=np.ascontiguousarray(b["plane_cells"], np.int64),
+                         kap=f64(b["kap"]), w=f64(b["w"]), nk=i32(b["nk"]), dk=f64(b["dk"]), closure=i32(b["closure"]),
+                         V=f64(b["V"]), vp_D=f64(b["vp_D"]), vp_K=f64(b["vp_K"]), vp_w=f64(b["vp_w"]))
+        a = self._cfb
+        self._check(self._L.sgl_cfb_set(self._h, a["nk"].size, _ptr(a["inst_plane0"], C.c_int32),
+                                        _ptr(a["plane_cells"], C.c_int64), _ptr(a["kap"]), _ptr(a["w"]),
+                                        _ptr(a["nk"], C.c_int32), _ptr(a["dk"]), _ptr(a["closure"], C.c_int32),
+                                        _ptr(a["V"]), int(b["nstate"]), _ptr(a["vp_D"]), _ptr(a["vp_K"]), _ptr(a["vp_w"])),
+                    "sgl_cfb_set")
+
+    def cfb_tune(self, precision=SGL_MIXED):
+        kt, cps = C.c_int(), C.c_int()
+        self._check(self._L.sgl_cfb_tune(self._h, int(precision), C.byref(kt), C.byref(cps)), "sgl_cfb_tune")
+        return kt.value, cps.value
+
+    def cfb_lnphi(self, precision=SGL_MIXED):
+        """ln Phi of every instance, concatenated (complex)."""
+        n = int(np.sum(self._cfb["nk"].astype(np.int64)))
+        out = np.empty(2 * n)
+        self._check(self._L.sgl_cfb_lnphi(self._h, int(precision), _ptr(out)), "sgl_cfb_lnphi")
+        return out[0::2] + 1j * out[1::2]
+
+    def cfb_pdf(self, lnmu, precision=SGL_MIXED, use_graph=True):
+        """(dP/dln mu [n_inst, n_lnmu], device ms of the step)."""
+        x = np.ascontiguousarray(lnmu, np.float64)
+        out = np.empty((self._cfb["nk"].size, x.size))
+        ms = C.c_double()
+        self._check(self._L.sgl_cfb_pdf(self._h, int(precision), _ptr(x), x.size, _ptr(out), int(bool(use_graph)),
+                                        C.byref(ms)), "sgl_cfb_pdf")
+        return out, ms.value
+
+    def vp_build(self, pop, nstate=48, eta=None):
+        """Builds and installs the vp closure from its per-shell population (sgl_vp_build): a mapping
+        with shell_start, W, kap, gam, phi, rho, fvar, target_kappa, target_gamma.  eta: None to
+        calibrate, else the value to use.  Returns eta."""
+        ss = np.ascontiguousarray(pop["shell_start"], np.int64)
+        W, kap, gam, phi = (np.ascontiguousarray(pop[k], np.float64) for k in ("W", "kap", "gam", "phi"))
+        rho, fvar = np.ascontiguousarray(pop["rho"], np.float64), np.ascontiguousarray(pop["fvar"], np.float64)
+        ns = ss.size - 1
+        if not (W.size == kap.size == gam.size == phi.size == ss[-1]) or rho.size != max(ns - 1, 0) or fvar.size != ns:
+            raise ValueError("vp population arrays do not match shell_start")
+        out = C.c_double()
+        self._check(self._L.sgl_vp_build(self._h, int(nstate), ns, _ptr(ss, C.c_int64), _ptr(W), _ptr(kap), _ptr(gam),
+                                         _ptr(phi), _ptr(rho), _ptr(fvar), float(pop["target_kappa"]),
+                                         float(pop["target_gamma"]), -1.0 if eta is None else float(eta),
+                                         C.byref(out)), "sgl_vp_build")
+        return out.value
 
     def set_vp(self, d):
         """Installs the positive (vp) closure from a mapping with the arrays of sgl_vp_set (u, w, K, ku,

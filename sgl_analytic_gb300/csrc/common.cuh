@@ -11,6 +11,22 @@
 
 namespace sgl {
 
+// two FP32 lanes in one 64-bit register for the packed FMA (fma.rn.f32x2 rounds each lane like fmaf)
+__device__ __forceinline__ unsigned long long f32x2_pack(float a, float b) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float2 f32x2_unpack(unsigned long long v) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+__device__ __forceinline__ void f32x2_fma(unsigned long long& acc, unsigned long long a, unsigned long long b) {
+    asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(acc) : "l"(a), "l"(b));
+}
+
+
 // ------------------------------------------------------------------ launch geometry
 constexpr int kNumSMs = 152;          // GB300: 2 dies x 76 SMs
 

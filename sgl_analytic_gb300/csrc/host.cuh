@@ -98,10 +98,14 @@ struct SepScratch {
     std::vector<int> grp;
 };
 
+struct CfbState;                         // batched CF solver state (host_cfbatch.cu)
+void cfb_state_free(CfbState* s);
+
 struct sgl_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     std::string err;
+    CfbState* cfb = nullptr;
     Arena arena;
     // population (host copies)
     std::vector<double> w0, k0, g0, fe_g;
@@ -429,12 +433,16 @@ inline sgl_status check_dev_err(sgl_ctx* ctx) {
 }
 
 // parts = 2: operands to ~22 bits (3 MMAs per K-step); parts = 3: FP32 operands exactly (6 MMAs)
-inline sgl_status run_tc_gemms(sgl_ctx* ctx, std::vector<TcGemmDesc>& d, const std::string& tag, int parts) {
+// drain = true: the drained-accumulation kernel (TMEM sums folded into TwoSum running sums every
+// 64 products), tiles of at most tc_drain_bn() columns
+inline sgl_status run_tc_gemms(sgl_ctx* ctx, std::vector<TcGemmDesc>& d, const std::string& tag, int parts,
+                               bool drain = false) {
     if (d.empty()) return SGL_OK;
     std::vector<TcPackDesc> pk(2 * d.size());
     int tiles = 0;
     long long quads = 0;
-    const long long pfl = tc_gemm_plan(d.data(), (int)d.size(), parts, pk.data(), &tiles, &quads);
+    const long long pfl = tc_gemm_plan(d.data(), (int)d.size(), parts, pk.data(), &tiles, &quads, true,
+                                       drain ? tc_drain_bn() : 256);     // 256: the TMEM columns of one tile
     DBUF(dd, TcGemmDesc, "tc_desc_" + tag, d.size());
     DBUF(dp, TcPackDesc, "tc_pack_" + tag, pk.size());
     DBUF(packed, float, "tc_packed", std::max<long long>(pfl, 1));
@@ -446,7 +454,8 @@ inline sgl_status run_tc_gemms(sgl_ctx* ctx, std::vector<TcGemmDesc>& d, const s
     for (auto& g : d) fl += 2.0 * g.M * (double)g.N * g.K;
     {
         Timed t(ctx, "gemm_tc_" + tag, fl, (double)pfl * 4.0);
-        launch_tc_gemm(parts, dd, (int)d.size(), tiles, dp, quads, packed, err, ctx->stream);
+        if (drain) launch_tc_gemm_drain(parts, dd, (int)d.size(), tiles, dp, quads, packed, err, ctx->stream);
+        else launch_tc_gemm(parts, dd, (int)d.size(), tiles, dp, quads, packed, err, ctx->stream);
     }
     CKLAUNCH();
     return SGL_OK;
@@ -500,7 +509,8 @@ inline sgl_status gemm_splitk_simt(sgl_ctx* ctx, GemmDesc<T> g, const std::strin
 
 // FP32 on the tensor cores.  K split into >= min_split slices (FP32 accumulation in TMEM within a
 // slice), slices combined in FP64 by the fixed-order sum.
-inline sgl_status gemm_splitk_tc(sgl_ctx* ctx, GemmDesc<float> g, const std::string& tag, int min_split, int parts = 3) {
+inline sgl_status gemm_splitk_tc(sgl_ctx* ctx, GemmDesc<float> g, const std::string& tag, int min_split, int parts = 3,
+                                 bool drain = false) {
     int split = std::max(1, std::min(min_split, std::max(1, g.K / 32)));
     const long long slice = (long long)g.M * g.N;
     const bool direct = split == 1 && g.beta == 0.f;
@@ -523,7 +533,7 @@ inline sgl_status gemm_splitk_tc(sgl_ctx* ctx, GemmDesc<float> g, const std::str
         t.alpha = g.alpha;
         v.push_back(t);
     }
-    CKS(run_tc_gemms(ctx, v, tag, parts));
+    CKS(run_tc_gemms(ctx, v, tag, parts, drain));
     if (!direct) {
         launch_sum_slices<float>(ws, (int)v.size(), g.M, g.N, g.C, g.ldc, g.beta, ctx->stream);
         CKLAUNCH();
@@ -539,14 +549,24 @@ inline sgl_status gemm_splitk_tc(sgl_ctx* ctx, GemmDesc<float> g, const std::str
 // sep2 + sep3 on tcgen05 1.30e-3, on SIMT 8.5e-4.  The tensor core's FP32 accumulation has a
 // per-instruction bias that the Fourier sums do not cancel, where SIMT FMAs round to nearest.
 // (The Hankel correction term, of relative size 2^-24, does run on BF16 tensor cores.)
-inline bool tc_for(const std::string& /*tag*/) {
+// Mixed-path GEMMs on the drained tcgen05 kernel (TF32 parts of FP32 operands, TMEM sums drained into
+// TwoSum running sums every 64 products).  Measured against the reference's PDFs (tail relative error,
+// bar 1e-3; all-SIMT: 2.1e-4 on its z_s = 1 cells with 3 groups, 6.5e-4 on the full z_s = 1
+// population, 1.7e-3 on the 300-cell blocked case): sep1 on tcgen05 gives 3.7e-4 / 5.3e-4 / 1.2e-3
+// and is 8% faster than on SIMT; the Hankel and kappa transforms on tcgen05 give 1.9e-3 on the z_s = 1
+// cells whether the sums are drained every 64 or every 16 products, and sep2 / sep3 are slower there.
+constexpr const char* kTcDrainTags[] = {"sep1"};
+constexpr int kTcDrainParts = 3;                // TF32 parts of its operands (3: FP32 operands exactly)
+inline bool tc_for(const std::string& tag) {
+    for (const char* t : kTcDrainTags)
+        if (tag == t) return true;
     return false;
 }
 
 template <typename T>
 inline sgl_status gemm_splitk(sgl_ctx* ctx, GemmDesc<T> g, const std::string& tag, int min_split = 1) {
     if constexpr (sizeof(T) == 4) {
-        if (tc_for(tag)) return gemm_splitk_tc(ctx, g, tag, min_split);
+        if (tc_for(tag)) return gemm_splitk_tc(ctx, g, tag, min_split, kTcDrainParts, true);
     }
     return gemm_splitk_simt<T>(ctx, g, tag, min_split);
 }

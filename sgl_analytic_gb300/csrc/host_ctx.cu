@@ -62,6 +62,7 @@ void sgl_ctx_destroy(sgl_ctx* ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     if (ctx->side) cudaStreamSynchronize(ctx->side);
+    if (ctx->cfb) cfb_state_free(ctx->cfb);
     ctx->arena.release();
     for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
     resolve_stats(ctx);

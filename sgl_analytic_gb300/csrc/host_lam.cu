@@ -5,6 +5,29 @@
 
 namespace sglh {
 
+// numpy's summation of a contiguous float64 array (np.sum): runs of at most 128 values summed with
+// 8 interleaved partial sums combined pairwise, longer runs split in two at a multiple of 8
+double pairwise_sum(const double* a, long long n) {
+    if (n < 8) {
+        double r = 0.0;
+        for (long long i = 0; i < n; ++i) r += a[i];
+        return r;
+    }
+    if (n <= 128) {
+        double r[8];
+        for (int j = 0; j < 8; ++j) r[j] = a[j];
+        long long i = 8;
+        for (; i < n - (n % 8); i += 8)
+            for (int j = 0; j < 8; ++j) r[j] += a[i + j];
+        double res = ((r[0] + r[1]) + (r[2] + r[3])) + ((r[4] + r[5]) + (r[6] + r[7]));
+        for (; i < n; ++i) res += a[i];
+        return res;
+    }
+    long long n2 = n / 2;
+    n2 -= n2 % 8;
+    return pairwise_sum(a, n2) + pairwise_sum(a + n2, n - n2);
+}
+
 // ------------------------------------------------------------------ separable plan
 // Restates _sep_gamma_nodes (sgl_full.py:2631-2661) for kg_max = key.
 sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
@@ -1226,8 +1249,11 @@ sgl_status sgl_lam_set_xi(sgl_ctx* ctx, int n_groups, const int32_t* m, const in
 sgl_status sgl_lam_sigma(sgl_ctx* ctx, double* sigma) {
     if (!ctx || !sigma) return SGL_ERR_VALUE;
     if (!ctx->has_cells) return fail(ctx, SGL_ERR_STATE, "cells not set");
-    double v = 0.0;
-    for (size_t c = 0; c < ctx->w0.size(); ++c) v += ctx->w0[c] * ctx->k0[c] * ctx->k0[c];
+    // sum w0 k0^2 in the reference's rounding (np.sum(w0 * k0**2)): the grid sizes are ceilings of
+    // ratios of sigma that can sit within an ulp of an integer, so the same sigma bits matter
+    std::vector<double> t(ctx->w0.size());
+    for (size_t c = 0; c < t.size(); ++c) t[c] = ctx->w0[c] * (ctx->k0[c] * ctx->k0[c]);
+    double v = pairwise_sum(t.data(), (long long)t.size());
     v += ctx->V;
     if (ctx->xi.on) v += ctx->xi.sigma_var;
     *sigma = std::sqrt(v);

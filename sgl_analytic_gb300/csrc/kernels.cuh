@@ -134,6 +134,24 @@ void launch_em_columns(int precision, const void* Phi, int nk, int nkg, double d
                        cudaStream_t st);
 void launch_window(int precision, void* Phi, int nk, int nkg, const double* wk, const double* wg, cudaStream_t st);
 void launch_phi_to_f32(const double* in, long long n, float* out, cudaStream_t st);
+
+// ---- batched CF solver (cfbatch.cu)
+struct CfbInst {                          // one instance of the batch
+    long long c0, c1;                     // its cells (all planes)
+    long long k_off;                      // first k-point in the per-instance output arrays
+    int p0, p1;                           // its planes
+    int nk, closure;                      // k points (k_n = n dk); closure 0 gauss, 1 vp
+    double dk, V;                         // k step; gauss: the clustering variance term V k^2 / 2
+    int vp_slot;                          // vp: index into the chain tables
+    int pad;
+};
+void launch_cfb_persistent(int precision, int kt, int ctas, const CfbInst* inst, const int2* items, int n_items,
+                           int* counter, const long long* plane_cells, const double* kap, const double* w,
+                           const float* kh, const float* kl, const float* wf, const double* vp_D, const double* vp_K,
+                           const double* vp_w, int nstate, double2* out, cudaStream_t st);
+void launch_cfb_pdf(int precision, const CfbInst* inst, int n_inst, const double2* lnphi, long long total,
+                    const long long* k_offs, void* phi, const double* lnmu, int nm, double* P, cudaStream_t st);
+int cfb_resident_ctas(int precision, int kt);
 void launch_p3_finish(int precision, const void* P3ext, int nkap, int ngam, int ld, const double* gam, double* P3,
                       float* P3f, cudaStream_t st);
 void launch_path_integral(const double* P3, const float* P3f, int nkap, int ngam, double kap0, double kap1,
@@ -159,7 +177,12 @@ struct TcPackDesc {                         // one operand to pack: X(r, k) = X[
 // fills tiles / packing descriptors (pk: 2 n entries) for operands split into `parts` (2 or 3)
 // TF32 parts; returns the packed buffer size in floats
 long long tc_gemm_plan(TcGemmDesc* d, int n, int parts, TcPackDesc* pk, int* tiles, long long* quads,
-                       bool pack_a = true);
+                       bool pack_a = true, int bn_max = 256);
+// FP32 GEMM with the TMEM accumulation drained every 64 products into TwoSum running sums (tiles of
+// at most tc_drain_bn() columns: plan with bn_max = tc_drain_bn())
+void launch_tc_gemm_drain(int parts, const TcGemmDesc* d_descs, int nprob, int tiles, const TcPackDesc* d_pack,
+                          long long quads, float* packed, int* err, cudaStream_t st);
+int tc_drain_bn();
 void launch_tc_gemm(int parts, const TcGemmDesc* d_descs, int nprob, int tiles, const TcPackDesc* d_pack,
                     long long quads, float* packed, int* err, cudaStream_t st);
 

@@ -333,23 +333,31 @@ k_sep_sweep_mixed(const double* __restrict__ kk, int nk, SepDevice sd, float* __
     const int c_begin = sd.chunk_begin[blockIdx.y], c_end = sd.chunk_begin[blockIdx.y + 1];
     const long long ld = 2LL * nk;
     float far = 0.f, fai = 0.f, car = 0.f, cai = 0.f;  // Kahan-compensated FP32
-    float tr[8], ti[8];
+    // the 8 node sums of the current group in weight pairs: tr2[q] = (tr[2q], tr[2q + 1]) for the
+    // packed FMA (each lane rounds like fmaf)
+    unsigned long long tr2[4], ti2[4];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) { tr[j] = 0.f; ti[j] = 0.f; }
+    for (int q = 0; q < 4; ++q) { tr2[q] = 0ull; ti2[q] = 0ull; }
     int cur = -1;
     auto flush = [&](int g) {
         if (g >= 0 && live) {
             const int col0 = sd.gcol0[g], nc = sd.gncol[g];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                if (j < nc) {
-                    Tt[(long long)(col0 + j) * ld + n] = tr[j];
-                    Tt[(long long)(col0 + j) * ld + nk + n] = ti[j];
+            for (int q = 0; q < 4; ++q) {
+                const float2 r2 = f32x2_unpack(tr2[q]), i2 = f32x2_unpack(ti2[q]);
+                const float rv[2] = {r2.x, r2.y}, iv[2] = {i2.x, i2.y};
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int j = 2 * q + h;
+                    if (j < nc) {
+                        Tt[(long long)(col0 + j) * ld + n] = rv[h];
+                        Tt[(long long)(col0 + j) * ld + nk + n] = iv[h];
+                    }
                 }
             }
         }
 #pragma unroll
-        for (int j = 0; j < 8; ++j) { tr[j] = 0.f; ti[j] = 0.f; }
+        for (int q = 0; q < 4; ++q) { tr2[q] = 0ull; ti2[q] = 0ull; }
     };
     for (int base = c_begin; base < c_end; base += kSweepStage) {
         const int cnt = min(kSweepStage, c_end - base);
@@ -390,11 +398,13 @@ k_sep_sweep_mixed(const double* __restrict__ kk, int nk, SepDevice sd, float* __
             y = fmaf(wf, smp, -cai); t = fai + y; cai = (t - fai) - y; fai = t;
             const float crr = cm1 + 1.f;
             const float4 w0 = s_c[e][1], w1 = s_c[e][2];
-            const float wv[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+            const unsigned long long wp[4] = {f32x2_pack(w0.x, w0.y), f32x2_pack(w0.z, w0.w), f32x2_pack(w1.x, w1.y),
+                                              f32x2_pack(w1.z, w1.w)};
+            const unsigned long long cp = f32x2_pack(crr, crr), sp = f32x2_pack(sn, sn);
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                tr[j] = fmaf(wv[j], crr, tr[j]);
-                ti[j] = fmaf(wv[j], sn, ti[j]);
+            for (int q = 0; q < 4; ++q) {
+                f32x2_fma(tr2[q], wp[q], cp);
+                f32x2_fma(ti2[q], wp[q], sp);
             }
         }
     }

@@ -231,14 +231,203 @@ k_tc_gemm(const TcGemmDesc* __restrict__ descs, int nprob, const float* __restri
     }
 }
 
+// ------------------------------------------------------------------ drained accumulation
+// The same packed operands and ring, N tiles of at most kTcDrainBN columns, and the accumulation
+// drained out of TMEM every kTcDrainKB K blocks: the MMAs of drain block b accumulate into one of
+// two TMEM accumulators (b & 1), the first MMA of the block starting it from zero, while the four
+// epilogue warps read the other accumulator (the previous block) with tcgen05.ld and add it to
+// FP32 running sums in registers by Knuth's TwoSum (hi + lo per output).  The tensor core's FP32
+// accumulation then runs over kTcDrainKB x 16 products only, from zero each time; its rounding
+// (which, unlike an FMA chain's, is not round-to-nearest) does not build up over the whole K, and
+// the running sums carry the block totals with their exact rounding errors.
+// Warps 0-3: epilogue (TMEM lanes 32w .. 32w + 31 = tile rows); warp 4 lane 0: bulk copies;
+// warp 5 lane 0: MMAs.  Every wait is bounded; a wait that runs out raises *err and the CTA frees
+// its TMEM and returns.
+constexpr int kTcDrainBN = 64;
+constexpr int kTcDrainKB = 4;                  // K blocks of 16 per drain
+constexpr int kTcDrainThreads = 192;
+
+template <int NP> struct TcDrainCfg {
+    static constexpr int kStages = NP == 3 ? 4 : 6;
+    static constexpr int kABytes = kTcAbytes;                          // 128 x 16 TF32 per part
+    static constexpr int kBBytes = kTcDrainBN * kTcBK * 4;              // 64 x 16 TF32 per part
+    static constexpr int kStageBytes = NP * (kABytes + kBBytes);       // 36 / 24 KB
+    static constexpr int kBarOff = kStages * kStageBytes;
+    static constexpr int kNBar = 2 * kStages + 5;                      // full, empty, acc full[2], acc empty[2], done
+    static constexpr int kSmem = kBarOff + 8 * kNBar + 32;
+};
+
+template <int NP>
+__global__ void __launch_bounds__(kTcDrainThreads, 1)
+k_tc_gemm_drain(const TcGemmDesc* __restrict__ descs, int nprob, const float* __restrict__ packed, int* __restrict__ err) {
+    using Cfg = TcDrainCfg<NP>;
+    constexpr int S = Cfg::kStages;
+    extern __shared__ __align__(1024) unsigned char tsm[];
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(tsm);
+    const uint32_t bar = sbase + Cfg::kBarOff;
+    auto full = [&](int s) { return bar + 8 * s; };
+    auto empty = [&](int s) { return bar + 8 * (S + s); };
+    auto accf = [&](int a) { return bar + 8 * (2 * S + a); };
+    auto acce = [&](int a) { return bar + 8 * (2 * S + 2 + a); };
+    const uint32_t done = bar + 8 * (2 * S + 4);
+    const uint32_t tslot = bar + 8 * Cfg::kNBar;
+    volatile int* s_fail = (volatile int*)(tsm + Cfg::kBarOff + 8 * Cfg::kNBar + 8);
+    volatile int* s_used = (volatile int*)(tsm + Cfg::kBarOff + 8 * Cfg::kNBar + 12);   // K blocks the MMAs took
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    const int tile = blockIdx.x;
+    int lo = 0, hi = nprob - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (descs[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+    }
+    const TcGemmDesc d = descs[lo];
+    const int local = tile - d.tile_begin;
+    const int i0 = (local / d.tiles_n) * kTcBM, bn = d.bn, j0 = (local % d.tiles_n) * bn;
+    const int nkb = (d.K + kTcBK - 1) / kTcBK;
+    const int nblk = (nkb + kTcDrainKB - 1) / kTcDrainKB;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(tslot), "r"(2 * kTcDrainBN) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < S; ++s) { mbar_init(full(s), 1); mbar_init(empty(s), 1); }
+        for (int a = 0; a < 2; ++a) { mbar_init(accf(a), 1); mbar_init(acce(a), 4); }
+        mbar_init(done, 1);
+        *s_fail = 0;
+        *s_used = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *(volatile uint32_t*)(tsm + Cfg::kBarOff + 8 * Cfg::kNBar);
+
+    const float* Ap = packed + d.a_off;       // [nkb][NP][Mpad][16]
+    const float* Bp = packed + d.b_off;       // [nkb][NP][Npad][16]
+    const long long a_part = (long long)d.Mpad * kTcBK, b_part = (long long)d.Npad * kTcBK;
+    const uint32_t a_bytes = Cfg::kABytes, b_bytes = (uint32_t)bn * kTcBK * 4;
+
+    int issued = 0;                            // K blocks whose copies the producer issued
+    if (warp == 4) {
+        if (lane == 0) {
+            for (int kb = 0; kb < nkb; ++kb) {
+                const int s = kb % S;
+                if (*s_fail || (kb >= S && !mbar_wait_bounded(empty(s), (uint32_t)(((kb / S) - 1) & 1)))) {
+                    *s_fail = 1;
+                    break;
+                }
+                issued = kb + 1;
+                const uint32_t st = sbase + s * Cfg::kStageBytes;
+                mbar_expect_tx(full(s), NP * (a_bytes + b_bytes));
+                const float* a = Ap + ((long long)NP * kb) * a_part + (long long)(i0 >> 3) * 128;
+                const float* b = Bp + ((long long)NP * kb) * b_part + (long long)(j0 >> 3) * 128;
+#pragma unroll
+                for (int pp = 0; pp < NP; ++pp) {
+                    bulk_g2s(st + pp * Cfg::kABytes, a + pp * a_part, a_bytes, full(s));
+                    bulk_g2s(st + NP * Cfg::kABytes + pp * Cfg::kBBytes, b + pp * b_part, b_bytes, full(s));
+                }
+            }
+        }
+    } else if (warp == 5) {
+        if (lane == 0) {
+            constexpr int NPROD = NP == 2 ? 3 : 6;
+            constexpr int PA[6] = {0, 0, 1, 0, 2, 1};
+            constexpr int PB[6] = {0, 1, 0, 2, 0, 1};
+            const uint32_t idesc = tc_idesc_tf32(kTcBM, bn);
+            for (int kb = 0; kb < nkb; ++kb) {
+                const int blk = kb / kTcDrainKB, a = blk & 1;
+                const bool first = kb % kTcDrainKB == 0;
+                // the accumulator of block blk was drained (block blk - 2) before its first MMA
+                if (first && blk >= 2 && (*s_fail || !mbar_wait_bounded(acce(a), (uint32_t)(((blk >> 1) - 1) & 1)))) {
+                    *s_fail = 1;
+                    break;
+                }
+                const int s = kb % S;
+                if (*s_fail || !mbar_wait_bounded(full(s), (uint32_t)((kb / S) & 1))) { *s_fail = 1; break; }
+                *s_used = kb + 1;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t a0 = sbase + s * Cfg::kStageBytes, b0 = a0 + NP * Cfg::kABytes;
+                const uint32_t acc = tmem + (uint32_t)(a * kTcDrainBN);
+#pragma unroll
+                for (int ks = 0; ks < kTcBK / 8; ++ks) {
+                    const uint32_t o = ks * 2 * kTcLBO;
+#pragma unroll
+                    for (int t = 0; t < NPROD; ++t)
+                        tc_mma(acc, tc_desc(a0 + PA[t] * Cfg::kABytes + o), tc_desc(b0 + PB[t] * Cfg::kBBytes + o), idesc,
+                               (first && ks == 0 && t == 0) ? 0u : 1u);
+                }
+                tc_commit(empty(s));
+                if (kb % kTcDrainKB == kTcDrainKB - 1 || kb == nkb - 1) tc_commit(accf(a));
+            }
+            // every MMA issued above has completed before TMEM can be freed
+            tc_commit(done);
+            if (!mbar_wait_bounded(done, 0u)) *s_fail = 1;
+        }
+    } else {
+        // epilogue warps: drain each block's accumulator into the running sums (row = TMEM lane)
+        float sh[kTcDrainBN], sl[kTcDrainBN];
+#pragma unroll
+        for (int c = 0; c < kTcDrainBN; ++c) { sh[c] = 0.f; sl[c] = 0.f; }
+        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+        bool ok = true;
+        for (int blk = 0; blk < nblk && ok; ++blk) {
+            const int a = blk & 1;
+            if (*s_fail || !mbar_wait_bounded(accf(a), (uint32_t)((blk >> 1) & 1))) { ok = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (int c0 = 0; c0 < kTcDrainBN; c0 += 16) {
+                float v[16];
+                if (c0 < bn) tmem_ld16(lane_base + (uint32_t)(a * kTcDrainBN + c0), v);
+                else {
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) v[q] = 0.f;
+                }
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const float h = sh[c0 + q], x = v[q];
+                    const float sum = h + x, bb = sum - h;
+                    sl[c0 + q] += (h - (sum - bb)) + (x - bb);
+                    sh[c0 + q] = sum;
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acce(a));
+        }
+        if (!ok) *s_fail = 1;
+        const int row = warp * 32 + lane, gi = i0 + row;
+        if (ok && gi < d.M) {
+#pragma unroll
+            for (int c = 0; c < kTcDrainBN; ++c) {
+                const int gj = j0 + c;
+                if (c < bn && gj < d.N) d.C[(long long)gi * d.c_rs + (long long)gj * d.c_cs] = d.alpha * (sh[c] + sl[c]);
+            }
+        }
+    }
+    // the MMAs have completed (the issuer waited on its final commit); after a failure no bulk copy
+    // may outlive the CTA: the producer waits (bounded) for the copies the MMAs never took
+    __syncthreads();
+    if (*s_fail && warp == 4 && lane == 0)
+        for (int kb = *s_used; kb < issued; ++kb) mbar_wait_bounded(full(kb % S), (uint32_t)((kb / S) & 1));
+    if (*s_fail && tid == 0) atomicExch(err, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(2 * kTcDrainBN) : "memory");
+    }
+}
+
 // ------------------------------------------------------------------ host planning / launch
 long long tc_gemm_plan(TcGemmDesc* d, int n, int parts, TcPackDesc* pk, int* tiles_out, long long* quads_out,
-                       bool pack_a) {
+                       bool pack_a, int bn_max) {
     long long off = 0, quads = 0;
     int tiles = 0;
     for (int i = 0; i < n; ++i) {
         TcGemmDesc& g = d[i];
-        const int bn = g.N <= kTcBNmax ? ((g.N + 15) / 16) * 16 : kTcBNmax;
+        const int bn = g.N <= bn_max ? ((g.N + 15) / 16) * 16 : bn_max;
         g.bn = bn < 16 ? 16 : bn;
         g.tiles_n = (g.N + g.bn - 1) / g.bn;
         g.tile_begin = tiles;
@@ -287,5 +476,21 @@ void launch_tc_gemm(int parts, const TcGemmDesc* d_descs, int nprob, int tiles, 
         SGL_COUNT(1);
     }
 }
+
+void launch_tc_gemm_drain(int parts, const TcGemmDesc* d_descs, int nprob, int tiles, const TcPackDesc* d_pack,
+                          long long quads, float* packed, int* err, cudaStream_t st) {
+    if (parts == 3) {
+        if (quads > 0) { k_tc_pack<3><<<ceil_div(quads, 256), 256, 0, st>>>(d_pack, 2 * nprob, packed); SGL_COUNT(1); }
+        cudaFuncSetAttribute(k_tc_gemm_drain<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcDrainCfg<3>::kSmem);
+        k_tc_gemm_drain<3><<<tiles, kTcDrainThreads, TcDrainCfg<3>::kSmem, st>>>(d_descs, nprob, packed, err);
+    } else {
+        if (quads > 0) { k_tc_pack<2><<<ceil_div(quads, 256), 256, 0, st>>>(d_pack, 2 * nprob, packed); SGL_COUNT(1); }
+        cudaFuncSetAttribute(k_tc_gemm_drain<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcDrainCfg<2>::kSmem);
+        k_tc_gemm_drain<2><<<tiles, kTcDrainThreads, TcDrainCfg<2>::kSmem, st>>>(d_descs, nprob, packed, err);
+    }
+    SGL_COUNT(1);
+}
+
+int tc_drain_bn() { return kTcDrainBN; }
 
 }  // namespace sgl

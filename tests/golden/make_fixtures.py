@@ -14,10 +14,10 @@ bin), the weak-arm variance, the xi_lin groups and the coarse lattice centres --
 the reference's sigma.  Output: ``tests/golden/full/cells_zs<z>_<closure>_full.npz`` (all xi groups;
 ~290 MB at z_s=1, not committed; the committed subset is made by ``make_golden.py``).
 
-Usage (from the repository root)::
+Usage (from the repository root; the reference checkout by --reference PATH or SGL_REFERENCE)::
 
-    python tests/golden/make_fixtures.py build   --zs 1 --closure gauss --nproc 8
-    python tests/golden/make_fixtures.py extract --zs 1 --closure gauss
+    python tests/golden/make_fixtures.py build   --zs 1 --closure gauss --nproc 8 --reference PATH
+    python tests/golden/make_fixtures.py extract --zs 1 --closure gauss --reference PATH
 """
 from __future__ import annotations
 
@@ -30,8 +30,10 @@ from pathlib import Path
 
 import numpy as np
 
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+from _reference import reference_root, strip_reference_args  # noqa: E402
+
 REPO = Path(__file__).resolve().parents[2]
-REF_SRC = Path("/root/reference/src")
 STANDIN = REPO / "oracle" / "numba_standin"
 FULL = REPO / "tests" / "golden" / "full"          # large, git-ignored
 WORK = FULL
@@ -39,6 +41,7 @@ GOLDEN = REPO / "tests" / "golden"
 
 
 def _setup_path():
+    REF_SRC = reference_root() / "src"
     for p in (str(REF_SRC), str(STANDIN)):
         if p not in sys.path:
             sys.path.insert(0, p)
@@ -104,7 +107,7 @@ def main():
     ap.add_argument("--zs", type=float, default=1.0)
     ap.add_argument("--closure", default="gauss", choices=("gauss", "vp"))
     ap.add_argument("--nproc", type=int, default=os.cpu_count())
-    a = ap.parse_args()
+    a = ap.parse_args(strip_reference_args(sys.argv[1:]))
     if a.stage == "build":
         build(a.zs, a.closure, a.nproc)
     else:

@@ -1,4 +1,5 @@
-"""vp (positive Cox) closure fixtures from the reference package (run in the development container).
+"""vp (positive Cox) closure fixtures from the reference package (run in the development container;
+the reference checkout by --reference PATH or SGL_REFERENCE).
 
 Needs the z_s=1 vp cells pickle (built by ``make_fixtures.py build --closure vp`` into tests/golden/full/).
 The reference's closure set-up runs UNMODIFIED (under ``oracle/numba_standin``, since
@@ -8,7 +9,10 @@ line-of-sight correlations), the rates calibrated to the xi_lin kappa variance (
 rate-interval parameters of FusedVP (pos_closure_fused.py:18-48).
 
 Writes
+  tests/golden/full/vp_zs1_pop.npz   the closure's per-shell population (cells W, kap, gam, phi per
+                                      shell; rho, fvar, the kappa / gamma targets; not committed)
   tests/golden/full/vp_zs1_full.npz  the whole closure (67 shells, ~2.45M cells; not committed)
+  tests/golden/vp_zs1_sub_pop.npz     shells 0-5 of the per-shell population (committed)
   tests/golden/vp_zs1_sub.npz         shells 0-5 of it (committed) and, computed by the reference's
                                       own _fused_groups + _chain_recursion on that sub-closure,
                                       lnR on a 5 x 4 (k_kappa, k_gamma) grid
@@ -25,13 +29,16 @@ from pathlib import Path
 
 import numpy as np
 
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+from _reference import reference_root  # noqa: E402
+
 REPO = Path(__file__).resolve().parents[2]
-REF_SRC = Path("/root/reference/src")
 STANDIN = REPO / "oracle" / "numba_standin"
 NSUB = 6
 
 
 def main():
+    REF_SRC = reference_root() / "src"
     for p in (str(REF_SRC), str(STANDIN)):
         sys.path.insert(0, p)
     from scipy.special import j0
@@ -43,6 +50,28 @@ def main():
     lam = F.Lam(cells, C=None, nord=1, exactS=False, k3=False, xi=True)
     pos = PC.install(lam, cos, kind="vp")
     print("install", time.time() - t, pos.eval_kernel, "eta", pos.eta, flush=True)
+    # the closure's per-shell population (pos_closure.population, pos_closure.py:388-450): the input
+    # of the closure set-up (Closure.__init__, calibrate, the rate intervals), which the engine
+    # restates; its output is the closure saved below
+    pp = pos.pop
+    cl = pp["cells"]
+    np.savez_compressed(REPO / "tests" / "golden" / "full" / "vp_zs1_pop.npz",
+                        shell_start=np.concatenate([[0], np.cumsum([c["W"].size for c in cl])]).astype(np.int64),
+                        W=np.concatenate([c["W"] for c in cl]), kap=np.concatenate([c["kap"] for c in cl]),
+                        gam=np.concatenate([c["gam"] for c in cl]), phi=np.concatenate([c["phi"] for c in cl]),
+                        rho=np.asarray(pp["rho"], float), fvar=np.asarray(pp["fvar"], float),
+                        target_kappa=np.float64(pp["target_kappa"]), target_gamma=np.float64(pp["target_gamma"]),
+                        eta=np.float64(pos.eta))
+    # shells 0 .. NSUB-1 of that population (committed): the input of the set-up for the sub-closure
+    # below, which uses the whole closure's eta
+    c1p = int(np.sum([c["W"].size for c in cl[:NSUB]]))
+    np.savez_compressed(REPO / "tests" / "golden" / "vp_zs1_sub_pop.npz",
+                        shell_start=np.concatenate([[0], np.cumsum([c["W"].size for c in cl[:NSUB]])]).astype(np.int64),
+                        W=np.concatenate([c["W"] for c in cl[:NSUB]]), kap=np.concatenate([c["kap"] for c in cl[:NSUB]]),
+                        gam=np.concatenate([c["gam"] for c in cl[:NSUB]]), phi=np.concatenate([c["phi"] for c in cl[:NSUB]]),
+                        rho=np.asarray(pp["rho"][:NSUB - 1], float), fvar=np.asarray(pp["fvar"][:NSUB], float),
+                        target_kappa=np.float64(pp["target_kappa"]), target_gamma=np.float64(pp["target_gamma"]),
+                        eta=np.float64(pos.eta), n_cells=np.int64(c1p))
     fused = pos.lnR_blocked.__self__               # the FusedVP instance
     B = pos._B
     full = dict(u=pos.u, w=pos.w, K=pos._Karr, shear_var=np.float64(pos.shear_var), eta=np.float64(pos.eta),

@@ -416,3 +416,27 @@ def test_native_batch_matches_single_context(pop_sub, ref_sub):
             b.pdf([0, 3], x)                       # no slot 3
     finally:
         b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_window_matches_reference(precision):
+    """The positive-definite box window (_window_pd, sgl_full.py:83-94, 254-258) against the reference's
+    invert(window=True) on a 1000-cell population (tests/golden/make_window_golden.py); the same
+    population without the window as well, so the window's effect is what is checked."""
+    from sgl_analytic_gb300 import Lam, Population, invert
+    ref = dict(np.load(GOLDEN / "ref_window.npz"))
+    lam = Lam(Population.load(GOLDEN / "pop_window.npz"), xi=False)
+    assert lam.sigma() == pytest.approx(float(ref["sigma"]), rel=1e-12)
+    x = ref["xi_out"]
+    effect = np.max(np.abs(ref["win_P"] - ref["raw_P"])) / np.max(ref["raw_P"])
+    assert effect > 1e-3                                  # the window changes this PDF
+    for tag, win in (("win", True), ("raw", False)):
+        _, P, meta = invert(lam, lam.sigma(), xi_out=x, phi_tol=1e-8, window=win, precision=precision)
+        g = meta["grid"]
+        assert [g["nk_k"], g["nk_g"], g["n_kap"], g["n_gam"]] == [int(v) for v in ref[tag + "_grid"][[0, 1, 4, 5]]]
+        assert g["window"] == float(ref[tag + "_grid"][11])
+        dpeak, l1, rel_tail = _pdf_errors(P, ref[tag + "_P"], x)
+        if precision == "fp64":
+            assert dpeak <= TOL_PEAK, (tag, dpeak)
+        else:
+            assert l1 <= 1e-4 and dpeak <= 1e-5, (tag, dpeak, l1)

@@ -198,3 +198,40 @@ def test_generate_pdf_lnmu_with_the_vp_closure(tmp_path):
     for k in ("nk_k", "nk_g", "n_kap", "n_gam", "xi_coarse", "xi_coarse_k", "window"):
         assert info["grid"][k] == ref["grid"][k], k
     assert np.abs(P - P0).max() / P0.max() <= VP_PEAK_BAR
+
+
+SUB_POP = GOLDEN / "vp_zs1_sub_pop.npz"
+
+
+@pytest.mark.skipif(not SUB_POP.exists(), reason="sub-population fixture not present")
+def test_closure_setup_on_the_engine_matches_the_reference(vp_sub):
+    """sgl_vp_build from the reference's per-shell population of shells 0-5 (with the whole closure's
+    eta): its ln R equals the reference's own _fused_groups + _chain_recursion on the sub-closure, and
+    ln R of the closure installed from the reference's arrays on a ragged grid."""
+    from sgl_analytic_gb300._lib import Engine
+    pop = dict(np.load(SUB_POP))
+    e = Engine(0)
+    eta = e.vp_build(pop, eta=float(pop["eta"]))
+    assert eta == float(pop["eta"])
+    L = e.vp_lnR(vp_sub["kv"], vp_sub["qv"])
+    assert _close(L, vp_sub["lnR"], 1e-14, 1e-10).all(), np.abs(L - vp_sub["lnR"]).max()
+    ref = Engine(0)
+    ref.set_vp(vp_sub)
+    kv, qv = KV[::2], QV[::3]
+    assert _close(e.vp_lnR(kv, qv), ref.vp_lnR(kv, qv), 1e-14, 1e-10).all()
+
+
+@pytest.mark.skipif(not (VP_FULL.exists() and (VP_FULL.parent / "vp_zs1_pop.npz").exists()),
+                    reason="full z_s=1 vp population not present")
+def test_closure_setup_calibrates_eta_like_the_reference():
+    """The whole z_s=1 closure built on the engine, eta calibrated by its Brent root on the chain
+    variance (Closure.calibrate): eta and ln R match the reference's closure."""
+    from sgl_analytic_gb300._lib import Engine
+    pop = dict(np.load(VP_FULL.parent / "vp_zs1_pop.npz"))
+    full = dict(np.load(VP_FULL))
+    e = Engine(0)
+    eta = e.vp_build(pop)
+    assert eta == pytest.approx(float(full["eta"]), rel=1e-9)
+    probe = np.load(GOLDEN / "vp_zs1_full_lnR_probe.npz")
+    L = e.vp_lnR(probe["kv"], probe["qv"])
+    assert _close(L, probe["fused"], 1e-13, 1e-10).all(), np.abs(L - probe["fused"]).max()
