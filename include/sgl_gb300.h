@@ -283,10 +283,41 @@ sgl_status sgl_batch_pdf(sgl_batch* batch, int n_jobs, const int32_t* job_slot, 
 sgl_status sgl_cfb_set(sgl_ctx* ctx, int n_inst, const int32_t* inst_plane0, const int64_t* plane_cells,
                        const double* kap, const double* w, const int32_t* nk, const double* dk, const int32_t* closure,
                        const double* V, int nstate, const double* vp_D, const double* vp_K, const double* vp_w);
+/* sgl_cfb_set_separable: a gauss-closure batch whose planes share one nm x nb cell template, built on the
+ * device: cell (m, b) of plane p (planes in order, nm * nb cells each) has kap = u[p][m] F[m][b] and
+ * w = v[p][m] g[b] (F nm x nb row-major, g nb, u and v n_planes x nm; host arrays).  A new batch keeps
+ * the launch shapes tuned for the previous one. */
+sgl_status sgl_cfb_set_separable(sgl_ctx* ctx, int nm, int nb, const double* F, const double* g, int n_inst,
+                                 const int32_t* inst_plane0, const int32_t* nk, const double* dk, const double* V,
+                                 const double* u, const double* v);
 sgl_status sgl_cfb_tune(sgl_ctx* ctx, int precision, int* kt, int* ctas_per_sm);
 sgl_status sgl_cfb_lnphi(sgl_ctx* ctx, int precision, double* out);
 sgl_status sgl_cfb_pdf(sgl_ctx* ctx, int precision, const double* lnmu, int n_lnmu, double* P_out, int use_graph,
                        double* ms_out);
+
+/* Surrogate + judge production sweep ------------------------------------------------------------
+ * No counterpart in the reference.  Instances i < n_inst with planes inst_plane0[i] .. inst_plane0[i+1]-1
+ * and uniform k grids k_n = n dk[i], n < nk[i]; plane p adds dz[p] H_p(s[p] k) to its instance's log-CF.
+ * H_p comes from a surrogate ensemble at nq >= 4 nodes ln q_j = lnq0[p] + j hq[p] as the residual over the
+ * plane's two-moment form H0(q) = -(mu2 / 2) q^2 / (1 - i q Sbar), Sbar = mu2 / (2 mu1) (mu1, mu2 > 0: the
+ * plane's sum w S and sum w S^2):  ln |H| = r0 + ln |H0|,  arg(-H) = r1 + arg(-H0)  (host arrays, sgl_sur_set).
+ * Y (device, float32) holds the members' normalised outputs [member][plane][node] = (y0, y1), r0 = y0 scale
+ * + shift, r1 = y1 scale; between nodes 4-point Lagrange interpolation, below the first node r q / q0.
+ * sgl_sur_judge sums the ensemble mean into ln Phi per instance and returns per plane dis_out (2 floats:
+ * the largest dz |spread| over the k grid, as is and weighted by |Phi| of the surrogate sum; spread =
+ * 2 max_m |H_m - mean|) and prefix_out (1 + the largest k index whose weighted spread exceeds tau, 0 if
+ * none).  sgl_sur_finish recomputes ln Phi with plane p taken from instance exact_inst[p] of the batched
+ * solver's last sgl_cfb_lnphi on that instance's k points (its nk <= the plane's; same dk; -1 = surrogate
+ * only).  sgl_sur_pdf inverts the current ln Phi to dP/dln mu at n_lnmu points (as sgl_cfb_pdf; P_out
+ * n_inst x n_lnmu) and copies ln Phi out as (re, im) pairs when lnphi_out is not NULL. */
+sgl_status sgl_sur_set(sgl_ctx* ctx, int n_inst, const int32_t* inst_plane0, const int32_t* nk, const double* dk,
+                       const double* s, const double* dz, const double* mu1, const double* mu2, const double* lnq0,
+                       const double* hq, int nq);
+sgl_status sgl_sur_judge(sgl_ctx* ctx, const float* Y, int members, double shift, double scale, double tau,
+                         float* dis_out, int32_t* prefix_out);
+sgl_status sgl_sur_finish(sgl_ctx* ctx, const float* Y, int members, double shift, double scale,
+                          const int32_t* exact_inst);
+sgl_status sgl_sur_pdf(sgl_ctx* ctx, int precision, const double* lnmu, int n_lnmu, double* P_out, double* lnphi_out);
 
 /* Allocation-free entry point ------------------------------------------------------------
  * No counterpart in the reference.  For callers that may not allocate device memory (a host that

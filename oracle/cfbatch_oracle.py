@@ -50,7 +50,12 @@ def lnphi(batch, i):
 def pdf_lnmu(batch, i, lnmu, lnphi_i=None):
     p0, p1, k = batch.instance(i)
     L = lnphi(batch, i) if lnphi_i is None else lnphi_i
-    wk = np.full(k.size, batch.dk[i])
+    return pdf_from_lnphi(L, k, lnmu)
+
+
+def pdf_from_lnphi(L, k, lnmu):
+    """dP/dln mu of the log-CF L on the uniform grid k (k[0] = 0)."""
+    wk = np.full(k.size, k[1] - k[0])
     wk[0] *= 0.5
     wk[-1] *= 0.5
     cf = np.exp(L) * wk / np.pi

@@ -25,7 +25,7 @@ EXPORTS = ("sgl_abi_version", "sgl_ctx_create", "sgl_ctx_destroy", "sgl_last_err
            "sgl_gemm_bf16", "sgl_mlp_bias_act", "sgl_mlp_act_grad", "sgl_mlp_col_sum", "sgl_mlp_mse", "sgl_mlp_adamw",
            "sgl_plan_grid", "sgl_invert", "sgl_batch_create", "sgl_batch_destroy", "sgl_batch_slots",
            "sgl_batch_slot", "sgl_batch_pdf", "sgl_cfb_set", "sgl_cfb_tune", "sgl_cfb_lnphi", "sgl_cfb_pdf",
-           "sgl_cf_kappa_noalloc")
+           "sgl_cfb_set_separable", "sgl_sur_set", "sgl_sur_judge", "sgl_sur_finish", "sgl_sur_pdf", "sgl_cf_kappa_noalloc")
 
 
 class InvertOpts(C.Structure):
@@ -103,7 +103,14 @@ def lib():
         L.sgl_cfb_tune.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.sgl_cfb_lnphi.argtypes = [vp, C.c_int, dp]
         L.sgl_cfb_pdf.argtypes = [vp, C.c_int, dp, C.c_int, dp, C.c_int, dp]
-        for name in ("sgl_cfb_set", "sgl_cfb_tune", "sgl_cfb_lnphi", "sgl_cfb_pdf"):
+        L.sgl_cfb_set_separable.argtypes = [vp, C.c_int, C.c_int, dp, dp, C.c_int, ip, ip, dp, dp, dp, dp]
+        for name in ("sgl_cfb_set", "sgl_cfb_tune", "sgl_cfb_lnphi", "sgl_cfb_pdf", "sgl_cfb_set_separable"):
+            getattr(L, name).restype = C.c_int
+        L.sgl_sur_set.argtypes = [vp, C.c_int, ip, ip, dp, dp, dp, dp, dp, dp, dp, C.c_int]
+        L.sgl_sur_judge.argtypes = [vp, vp, C.c_int, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_float), ip]
+        L.sgl_sur_finish.argtypes = [vp, vp, C.c_int, C.c_double, C.c_double, ip]
+        L.sgl_sur_pdf.argtypes = [vp, C.c_int, dp, C.c_int, dp, dp]
+        for name in ("sgl_sur_set", "sgl_sur_judge", "sgl_sur_finish", "sgl_sur_pdf"):
             getattr(L, name).restype = C.c_int
         for name in ("sgl_sweep_set_cells", "sgl_sweep_eval", "sgl_measure_peak"):
             getattr(L, name).restype = C.c_int
@@ -269,13 +276,34 @@ class Engine:
                                         _ptr(a["V"]), int(b["nstate"]), _ptr(a["vp_D"]), _ptr(a["vp_K"]), _ptr(a["vp_w"])),
                     "sgl_cfb_set")
 
+    def cfb_set_separable(self, F, g, inst_plane0, nk, dk, V, u, v):
+        """Uploads a gauss-closure batch of template planes: plane p's cell (m, b) has kap = u[p, m] F[m, b]
+        and w = v[p, m] g[b]; the cells are built on the device."""
+        F = np.ascontiguousarray(F, np.float64)
+        nm, nb = F.shape
+        g = np.ascontiguousarray(g, np.float64)
+        i32 = lambda a: np.ascontiguousarray(a, np.int32)
+        f64 = lambda a: np.ascontiguousarray(a, np.float64)
+        p0, nk, dk, V, u, v = i32(inst_plane0), i32(nk), f64(dk), f64(V), f64(u), f64(v)
+        n_planes = int(p0[-1])
+        if g.size != nb or u.shape != (n_planes, nm) or v.shape != (n_planes, nm) or nk.size != p0.size - 1 or \
+                dk.size != nk.size or V.size != nk.size:
+            raise ValueError("separable batch arrays have inconsistent sizes")
+        self._cfb = dict(nk=nk)
+        self._check(self._L.sgl_cfb_set_separable(self._h, nm, nb, _ptr(F), _ptr(g), nk.size, _ptr(p0, C.c_int32),
+                                                  _ptr(nk, C.c_int32), _ptr(dk), _ptr(V), _ptr(u), _ptr(v)),
+                    "sgl_cfb_set_separable")
+
     def cfb_tune(self, precision=SGL_MIXED):
         kt, cps = C.c_int(), C.c_int()
         self._check(self._L.sgl_cfb_tune(self._h, int(precision), C.byref(kt), C.byref(cps)), "sgl_cfb_tune")
         return kt.value, cps.value
 
-    def cfb_lnphi(self, precision=SGL_MIXED):
-        """ln Phi of every instance, concatenated (complex)."""
+    def cfb_lnphi(self, precision=SGL_MIXED, host=True):
+        """ln Phi of every instance, concatenated (complex); host=False leaves it on the device only."""
+        if not host:
+            self._check(self._L.sgl_cfb_lnphi(self._h, int(precision), None), "sgl_cfb_lnphi")
+            return None
         n = int(np.sum(self._cfb["nk"].astype(np.int64)))
         out = np.empty(2 * n)
         self._check(self._L.sgl_cfb_lnphi(self._h, int(precision), _ptr(out)), "sgl_cfb_lnphi")
@@ -289,6 +317,47 @@ class Engine:
         self._check(self._L.sgl_cfb_pdf(self._h, int(precision), _ptr(x), x.size, _ptr(out), int(bool(use_graph)),
                                         C.byref(ms)), "sgl_cfb_pdf")
         return out, ms.value
+
+    # ---------------------------------------------------------------- surrogate + judge sweep
+    def sur_set(self, inst_plane0, nk, dk, s, dz, mu1, mu2, lnq0, hq, nq):
+        i32 = lambda a: np.ascontiguousarray(a, np.int32)
+        f64 = lambda a: np.ascontiguousarray(a, np.float64)
+        self._sur = dict(inst_plane0=i32(inst_plane0), nk=i32(nk), dk=f64(dk), s=f64(s), dz=f64(dz), mu1=f64(mu1),
+                         mu2=f64(mu2), lnq0=f64(lnq0), hq=f64(hq))
+        a = self._sur
+        n = int(a["inst_plane0"][-1])
+        if not all(a[k].size == n for k in ("s", "dz", "mu1", "mu2", "lnq0", "hq")) or \
+                a["nk"].size != a["inst_plane0"].size - 1 or a["dk"].size != a["nk"].size:
+            raise ValueError("surrogate sweep arrays have inconsistent sizes")
+        self._check(self._L.sgl_sur_set(self._h, a["nk"].size, _ptr(a["inst_plane0"], C.c_int32), _ptr(a["nk"], C.c_int32),
+                                        _ptr(a["dk"]), _ptr(a["s"]), _ptr(a["dz"]), _ptr(a["mu1"]), _ptr(a["mu2"]),
+                                        _ptr(a["lnq0"]), _ptr(a["hq"]), int(nq)), "sgl_sur_set")
+
+    def sur_judge(self, Y, members, shift, scale, tau):
+        """Y: device tensor [members, planes * nq, 2] (float32).  Returns ((n_planes, 2) largest dz |spread|
+        per plane, as is and |Phi|-weighted; (n_planes,) k prefix whose weighted spread exceeds tau)."""
+        n = self._sur["s"].size
+        out = np.empty(2 * n, np.float32)
+        pre = np.empty(n, np.int32)
+        self._check(self._L.sgl_sur_judge(self._h, C.c_void_p(Y.data_ptr()), int(members), float(shift), float(scale),
+                                          float(tau), out.ctypes.data_as(C.POINTER(C.c_float)), _ptr(pre, C.c_int32)),
+                    "sgl_sur_judge")
+        return out.reshape(-1, 2), pre
+
+    def sur_finish(self, Y, members, shift, scale, exact_inst):
+        e = np.ascontiguousarray(exact_inst, np.int32)
+        if e.size != self._sur["s"].size:
+            raise ValueError("exact_inst needs one entry per plane")
+        self._check(self._L.sgl_sur_finish(self._h, C.c_void_p(Y.data_ptr()), int(members), float(shift), float(scale),
+                                           _ptr(e, C.c_int32)), "sgl_sur_finish")
+
+    def sur_pdf(self, lnmu, precision=SGL_FP64, want_lnphi=False):
+        x = np.ascontiguousarray(lnmu, np.float64)
+        out = np.empty((self._sur["nk"].size, x.size))
+        lp = np.empty(2 * int(np.sum(self._sur["nk"].astype(np.int64)))) if want_lnphi else None
+        self._check(self._L.sgl_sur_pdf(self._h, int(precision), _ptr(x), x.size, _ptr(out),
+                                        _ptr(lp) if want_lnphi else None), "sgl_sur_pdf")
+        return (out, lp[0::2] + 1j * lp[1::2]) if want_lnphi else out
 
     def vp_build(self, pop, nstate=48, eta=None):
         """Builds and installs the vp closure from its per-shell population (sgl_vp_build): a mapping

@@ -17,8 +17,8 @@
 // Then per instance Phi = exp(ln Phi) times the trapezoid weights, and the inversion to
 //   dP/dln mu = (1 - kappa) / 2 * (1/pi) sum_n w_n Re[Phi(k_n) e^{-i k_n kappa}],  kappa = 1 - mu^-1/2
 // at the caller's ln mu points: one thread per (instance, ln mu point), the instance's Phi staged
-// in shared memory, the phase rotated step by step in FP32 and re-seeded exactly every 32 steps
-// (mixed), or FP64 sincos per term (FP64).
+// in shared memory, the phase rotated step by step and re-seeded exactly every 32 steps (FP32
+// rotation from a float-float phase in mixed precision, FP64 rotation from an FP64 phase in FP64).
 #include "kernels.cuh"
 
 namespace sgl {
@@ -246,10 +246,19 @@ k_cfb_pdf(const CfbInst* __restrict__ inst, const void* __restrict__ phi_v, cons
         }
         __syncthreads();
         if (MODE == SGL_FP64) {
-            for (int e = 0; e < cnt; ++e) {
+            // exact FP64 phase every kCfbReseed steps, FP64 rotation by the step in between
+            double sd, cd;
+            sincos(I.dk * kap, &sd, &cd);
+            for (int e0 = 0; e0 < cnt; e0 += kCfbReseed) {
                 double s, c;
-                sincos((double)(base + e) * I.dk * kap, &s, &c);
-                acc = fma(s_pd[e].x, c, fma(s_pd[e].y, s, acc));
+                sincos((double)(base + e0) * I.dk * kap, &s, &c);
+                const int e1 = min(cnt, e0 + kCfbReseed);
+                for (int e = e0; e < e1; ++e) {
+                    acc = fma(s_pd[e].x, c, fma(s_pd[e].y, s, acc));
+                    const double c2 = fma(c, cd, -s * sd), s2 = fma(s, cd, c * sd);
+                    c = c2;
+                    s = s2;
+                }
             }
         } else {
             // exact phase (float-float n dk kappa, reduced mod pi/2) every kCfbReseed steps, rotation
@@ -324,6 +333,35 @@ void launch_cfb_pdf(int precision, const CfbInst* inst, int n_inst, const double
         SGL_COUNT(1);
         k_cfb_pdf<SGL_MIXED><<<dim3(ceil_div(nm, kCfbPdfThreads), n_inst), kCfbPdfThreads, 0, st>>>(inst, phi, lnmu, nm, P);
     }
+    SGL_COUNT(1);
+}
+
+// Cells of planes with a separable template: cell (m, b) of plane p has kap = u[p][m] F[m][b] and
+// w = v[p][m] g[b] (nm x nb cells per plane, plane after plane), in the solver's FP64, float-float
+// and FP32 forms
+__global__ void k_cfb_fill_separable(long long n_cells, int nm, int nb, const double* __restrict__ F,
+                                     const double* __restrict__ g, const double* __restrict__ u,
+                                     const double* __restrict__ v, double* __restrict__ kap, double* __restrict__ w,
+                                     float* __restrict__ kh, float* __restrict__ kl, float* __restrict__ wf) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_cells) return;
+    const long long per = (long long)nm * nb;
+    const long long p = c / per;
+    const int r = (int)(c - p * per);
+    const int m = r / nb, b = r - m * nb;
+    const double k = u[p * nm + m] * F[r];
+    const double ww = v[p * nm + m] * g[b];
+    kap[c] = k;
+    w[c] = ww;
+    const ff f = ff_from_double(k);
+    kh[c] = f.hi;
+    kl[c] = f.lo;
+    wf[c] = (float)ww;
+}
+
+void launch_cfb_fill_separable(long long n_cells, int nm, int nb, const double* F, const double* g, const double* u,
+                               const double* v, double* kap, double* w, float* kh, float* kl, float* wf, cudaStream_t st) {
+    k_cfb_fill_separable<<<(unsigned)ceil_div(n_cells, 256), 256, 0, st>>>(n_cells, nm, nb, F, g, u, v, kap, w, kh, kl, wf);
     SGL_COUNT(1);
 }
 

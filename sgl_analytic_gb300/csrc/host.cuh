@@ -100,12 +100,17 @@ struct SepScratch {
 
 struct CfbState;                         // batched CF solver state (host_cfbatch.cu)
 void cfb_state_free(CfbState* s);
+int cfb_n_inst(const CfbState* s);
+void cfb_inst_grid(const CfbState* s, int i, long long* k_off, int* nk, double* dk);
+struct SurState;                         // surrogate + judge assembly state (host_sur.cu)
+void sur_state_free(SurState* s);
 
 struct sgl_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     std::string err;
     CfbState* cfb = nullptr;
+    SurState* sur = nullptr;
     Arena arena;
     // population (host copies)
     std::vector<double> w0, k0, g0, fe_g;

@@ -30,6 +30,15 @@ void cfb_state_free(CfbState* s) {
     delete s;
 }
 
+int cfb_n_inst(const CfbState* s) { return s ? s->n_inst : 0; }
+
+void cfb_inst_grid(const CfbState* s, int i, long long* k_off, int* nk, double* dk) {
+    const CfbInst& I = s->inst[(size_t)i];
+    *k_off = I.k_off;
+    *nk = I.nk;
+    *dk = I.dk;
+}
+
 namespace sglh {
 namespace {
 
@@ -97,14 +106,11 @@ sgl_status cfb_tune(sgl_ctx* ctx, int precision) {
     return sync_stream(ctx);
 }
 
-}  // namespace
-}  // namespace sglh
-
-extern "C" {
-
-sgl_status sgl_cfb_set(sgl_ctx* ctx, int n_inst, const int32_t* inst_plane0, const int64_t* plane_cells,
-                       const double* kap, const double* w, const int32_t* nk, const double* dk, const int32_t* closure,
-                       const double* V, int nstate, const double* vp_D, const double* vp_K, const double* vp_w) {
+// Validates a batch's instance table and uploads it (instances, k offsets, plane offsets, vp chain
+// tables); the cells follow from the caller
+sgl_status cfb_tables(sgl_ctx* ctx, int n_inst, const int32_t* inst_plane0, const int64_t* plane_cells,
+                      const int32_t* nk, const double* dk, const int32_t* closure, const double* V, int nstate,
+                      const double* vp_D, const double* vp_K, const double* vp_w) {
     if (!ctx) return SGL_ERR_VALUE;
     if (n_inst < 1 || !inst_plane0 || !plane_cells || !nk || !dk || !closure || !V)
         return fail(ctx, SGL_ERR_VALUE, "sgl_cfb_set: invalid sizes or NULL arrays");
@@ -119,16 +125,20 @@ sgl_status sgl_cfb_set(sgl_ctx* ctx, int n_inst, const int32_t* inst_plane0, con
     for (int p = 0; p < n_planes; ++p)
         if (plane_cells[p + 1] < plane_cells[p]) return fail(ctx, SGL_ERR_VALUE, "sgl_cfb_set: plane_cells not ascending");
     const long long nc = plane_cells[n_planes];
-    if (nc < 1 || !kap || !w) return fail(ctx, SGL_ERR_VALUE, "sgl_cfb_set: no cells");
+    if (nc < 1) return fail(ctx, SGL_ERR_VALUE, "sgl_cfb_set: no cells");
     int n_vp = 0;
     for (int i = 0; i < n_inst; ++i) n_vp += closure[i] == 1;
     if (n_vp > 0 && (nstate < 2 || nstate > 8 || !vp_D || !vp_K || !vp_w))
         return fail(ctx, SGL_ERR_VALUE, "sgl_cfb_set: vp instances need 2..8 chain states and their tables");
     CK(cudaSetDevice(ctx->device));
     CKS(sync_stream(ctx));
-    if (ctx->cfb) cfb_state_free(ctx->cfb);
+    CfbState* prev = ctx->cfb;
     ctx->cfb = new CfbState();
     CfbState& S = *ctx->cfb;
+    if (prev) {                       // a new batch keeps the launch shapes tuned so far
+        for (int q = 0; q < 2; ++q) { S.kt[q] = prev->kt[q]; S.cps[q] = prev->cps[q]; S.tuned[q] = prev->tuned[q]; }
+        cfb_state_free(prev);
+    }
     S.n_inst = n_inst; S.n_planes = n_planes; S.nstate = n_vp > 0 ? nstate : 0; S.n_cells = nc;
     S.inst.resize((size_t)n_inst);
     S.cost.resize((size_t)n_inst);
@@ -151,37 +161,88 @@ sgl_status sgl_cfb_set(sgl_ctx* ctx, int n_inst, const int32_t* inst_plane0, con
     S.order.resize((size_t)n_inst);
     std::iota(S.order.begin(), S.order.end(), 0);
     std::stable_sort(S.order.begin(), S.order.end(), [&](int x, int y) { return S.cost[(size_t)x] > S.cost[(size_t)y]; });
-    // device tables: instances, k offsets, cells (FP64 and the mixed path's float-float / FP32)
-    std::vector<float> kh((size_t)nc), kl((size_t)nc), wf((size_t)nc);
-    for (long long c = 0; c < nc; ++c) {
-        const ff f = ff_from_double(kap[c]);
-        kh[(size_t)c] = f.hi; kl[(size_t)c] = f.lo; wf[(size_t)c] = (float)w[c];
-    }
     DBUF(d_inst, CfbInst, "cfb_inst", n_inst);
     DBUF(d_koffs, long long, "cfb_koffs", n_inst + 1);
     DBUF(d_pc, long long, "cfb_pcells", n_planes + 1);
-    DBUF(d_kap, double, "cfb_kap", nc);
-    DBUF(d_w, double, "cfb_w", nc);
-    DBUF(d_kh, float, "cfb_kh", nc);
-    DBUF(d_kl, float, "cfb_kl", nc);
-    DBUF(d_wf, float, "cfb_wf", nc);
     DBUF(d_vpD, double, "cfb_vpD", std::max(1, n_planes * std::max(1, S.nstate)));
     DBUF(d_vpK, double, "cfb_vpK", std::max(1, n_vp * S.nstate * S.nstate));
     DBUF(d_vpw, double, "cfb_vpw", std::max(1, n_vp * S.nstate));
     CKS(upload(ctx, d_inst, S.inst.data(), S.inst.size()));
     CKS(upload(ctx, d_koffs, k_offs.data(), k_offs.size()));
     CKS(upload(ctx, d_pc, (const long long*)plane_cells, (size_t)n_planes + 1));
-    CKS(upload(ctx, d_kap, kap, (size_t)nc));
-    CKS(upload(ctx, d_w, w, (size_t)nc));
-    CKS(upload(ctx, d_kh, kh.data(), kh.size()));
-    CKS(upload(ctx, d_kl, kl.data(), kl.size()));
-    CKS(upload(ctx, d_wf, wf.data(), wf.size()));
     if (n_vp > 0) {
         CKS(upload(ctx, d_vpD, vp_D, (size_t)n_planes * S.nstate));
         CKS(upload(ctx, d_vpK, vp_K, (size_t)n_vp * S.nstate * S.nstate));
         CKS(upload(ctx, d_vpw, vp_w, (size_t)n_vp * S.nstate));
     }
+    return sync_stream(ctx);          // k_offs goes out of scope
+}
+
+}  // namespace
+}  // namespace sglh
+
+extern "C" {
+
+sgl_status sgl_cfb_set(sgl_ctx* ctx, int n_inst, const int32_t* inst_plane0, const int64_t* plane_cells,
+                       const double* kap, const double* w, const int32_t* nk, const double* dk, const int32_t* closure,
+                       const double* V, int nstate, const double* vp_D, const double* vp_K, const double* vp_w) {
+    if (!ctx) return SGL_ERR_VALUE;
+    CKS(cfb_tables(ctx, n_inst, inst_plane0, plane_cells, nk, dk, closure, V, nstate, vp_D, vp_K, vp_w));
+    CfbState& S = *ctx->cfb;
+    const long long nc = S.n_cells;
+    if (!kap || !w) return fail(ctx, SGL_ERR_VALUE, "sgl_cfb_set: no cells");
+    std::vector<float> kh((size_t)nc), kl((size_t)nc), wf((size_t)nc);
+    for (long long c = 0; c < nc; ++c) {
+        const ff f = ff_from_double(kap[c]);
+        kh[(size_t)c] = f.hi; kl[(size_t)c] = f.lo; wf[(size_t)c] = (float)w[c];
+    }
+    DBUF(d_kap, double, "cfb_kap", nc);
+    DBUF(d_w, double, "cfb_w", nc);
+    DBUF(d_kh, float, "cfb_kh", nc);
+    DBUF(d_kl, float, "cfb_kl", nc);
+    DBUF(d_wf, float, "cfb_wf", nc);
+    CKS(upload(ctx, d_kap, kap, (size_t)nc));
+    CKS(upload(ctx, d_w, w, (size_t)nc));
+    CKS(upload(ctx, d_kh, kh.data(), kh.size()));
+    CKS(upload(ctx, d_kl, kl.data(), kl.size()));
+    CKS(upload(ctx, d_wf, wf.data(), wf.size()));
     return sync_stream(ctx);          // the host staging vectors go out of scope
+}
+
+sgl_status sgl_cfb_set_separable(sgl_ctx* ctx, int nm, int nb, const double* F, const double* g, int n_inst,
+                                 const int32_t* inst_plane0, const int32_t* nk, const double* dk, const double* V,
+                                 const double* u, const double* v) {
+    if (!ctx) return SGL_ERR_VALUE;
+    if (nm < 1 || nb < 1 || !F || !g || !u || !v || n_inst < 1 || !inst_plane0)
+        return fail(ctx, SGL_ERR_VALUE, "sgl_cfb_set_separable: invalid template or NULL arrays");
+    if (inst_plane0[0] != 0 || inst_plane0[n_inst] < 1) return fail(ctx, SGL_ERR_VALUE, "sgl_cfb_set_separable: invalid plane offsets");
+    const int n_planes = inst_plane0[n_inst];
+    const long long per = (long long)nm * nb;
+    std::vector<int64_t> pc((size_t)n_planes + 1);
+    for (int p = 0; p <= n_planes; ++p) pc[(size_t)p] = per * p;
+    std::vector<int32_t> closure((size_t)n_inst, 0);
+    CKS(cfb_tables(ctx, n_inst, inst_plane0, pc.data(), nk, dk, closure.data(), V, 0, nullptr, nullptr, nullptr));
+    const long long nc = ctx->cfb->n_cells;
+    for (long long e = 0; e < per; ++e) if (!std::isfinite(F[e])) return fail(ctx, SGL_ERR_VALUE, "non-finite template F");
+    for (int b = 0; b < nb; ++b) if (!std::isfinite(g[b])) return fail(ctx, SGL_ERR_VALUE, "non-finite template g");
+    for (long long e = 0; e < (long long)n_planes * nm; ++e)
+        if (!std::isfinite(u[e]) || !std::isfinite(v[e])) return fail(ctx, SGL_ERR_VALUE, "non-finite plane factors");
+    DBUF(d_F, double, "cfb_tF", per);
+    DBUF(d_g, double, "cfb_tg", nb);
+    DBUF(d_u, double, "cfb_tu", (long long)n_planes * nm);
+    DBUF(d_v, double, "cfb_tv", (long long)n_planes * nm);
+    DBUF(d_kap, double, "cfb_kap", nc);
+    DBUF(d_w, double, "cfb_w", nc);
+    DBUF(d_kh, float, "cfb_kh", nc);
+    DBUF(d_kl, float, "cfb_kl", nc);
+    DBUF(d_wf, float, "cfb_wf", nc);
+    CKS(upload(ctx, d_F, F, (size_t)per));
+    CKS(upload(ctx, d_g, g, (size_t)nb));
+    CKS(upload(ctx, d_u, u, (size_t)n_planes * nm));
+    CKS(upload(ctx, d_v, v, (size_t)n_planes * nm));
+    launch_cfb_fill_separable(nc, nm, nb, d_F, d_g, d_u, d_v, d_kap, d_w, d_kh, d_kl, d_wf, ctx->stream);
+    CKLAUNCH();
+    return sync_stream(ctx);
 }
 
 sgl_status sgl_cfb_tune(sgl_ctx* ctx, int precision, int* kt, int* ctas_per_sm) {

@@ -63,6 +63,7 @@ void sgl_ctx_destroy(sgl_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     if (ctx->side) cudaStreamSynchronize(ctx->side);
     if (ctx->cfb) cfb_state_free(ctx->cfb);
+    if (ctx->sur) sur_state_free(ctx->sur);
     ctx->arena.release();
     for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
     resolve_stats(ctx);

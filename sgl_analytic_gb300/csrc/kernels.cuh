@@ -152,6 +152,18 @@ void launch_cfb_persistent(int precision, int kt, int ctas, const CfbInst* inst,
 void launch_cfb_pdf(int precision, const CfbInst* inst, int n_inst, const double2* lnphi, long long total,
                     const long long* k_offs, void* phi, const double* lnmu, int nm, double* P, cudaStream_t st);
 int cfb_resident_ctas(int precision, int kt);
+void launch_cfb_fill_separable(long long n_cells, int nm, int nb, const double* F, const double* g, const double* u,
+                               const double* v, double* kap, double* w, float* kh, float* kl, float* wf, cudaStream_t st);
+struct SurPlane {                         // one plane of the surrogate sweep
+    double s, dz;                         // lensing efficiency, thickness: the plane adds dz H(s k)
+    double lnq0, hq;                      // its surrogate nodes ln q_j = lnq0 + j hq
+    double lnmu2h, sbar;                  // two-moment form: ln(mu2 / 2), Sbar = mu2 / (2 mu1)
+    long long exact_off;                  // finishing pass: first k of its exact ln Phi, or -1
+    int exact_nk, pad;                    // exact for k_n, n < exact_nk
+};
+void launch_sur_sum(bool judge, const CfbInst* inst, int n_inst, int max_nk, const SurPlane* planes, const float* Y,
+                    long long y_member_stride, int members, int nq, float shift, float scale, float tau,
+                    const double2* exact, double2* lnphi, unsigned int* dis, int* prefix, cudaStream_t st);
 void launch_p3_finish(int precision, const void* P3ext, int nkap, int ngam, int ld, const double* gam, double* P3,
                       float* P3f, cudaStream_t st);
 void launch_path_integral(const double* P3, const float* P3f, int nkap, int ngam, double kap0, double kap1,

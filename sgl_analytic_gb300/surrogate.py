@@ -1,26 +1,20 @@
 """Learned per-plane log-CF surrogate (BF16 MLP on the tensor cores) and its judge.
 
-The per-plane log-CF of a lens plane at redshift z_l (source z_s = 1) is the compensated
-compound-Poisson sum over the plane's (halo mass x impact parameter) cells,
-    Lambda_p(k) = sum_c w_c (e^{i k kap_c} - 1 - i k kap_c)
-              = L_raw(k) - i k sum_c w_c kap_c,      L_raw(k) = sum_c w_c (e^{i k kap_c} - 1).
-The exact solver is the engine's 1-D CF sweep (sgl_sweep_eval, FP64).  The MLP learns the
-compensated Lambda_p as a function of (h, Om, sigma8, Ok, w0, wa, z_l, ln k) through the outputs
-    t0 = ln |Lambda_p|,   t1 = arg(-Lambda_p)
-(Re(-Lambda_p) = sum w (1 - cos k kap) >= 0, so t1 stays in [-pi/2, pi/2] without wrapping: ~0 at
-small k, -> pi/2 at large k), so that a fixed absolute error in t is a fixed RELATIVE error in the
-log-CF.  (Learning the uncompensated L_raw instead and subtracting the exact i k sum w kap loses
-the small-k value to cancellation: its leading term is of second order in k.)  Architecture: 8 -> 6 x 256 SiLU -> 2, BF16 weights and
-activations in the GEMMs (tcgen05.mma.kind::f16, FP32 accumulation in TMEM), FP32 master weights,
-AdamW, MSE on t.  The judge is a two-member ensemble: a plane is re-evaluated by the exact solver
-when the members disagree by more than the threshold in ln CF (1e-5 by default).
-
-Synthetic planes (stand-in for the reference's population build, with the synthetic CF-sweep
-microbenchmark's shapes): 256 log-spaced masses 1e8-1e16 Msun/h x 512 log-spaced impact parameters
-1e-3-1e2 r_s; kappa = A(z_l, cosmology) (M/1e12)^0.3 F(b; c(M)) with the truncated-NFW projection F
-and c = 5 (M/1e12)^-0.1; rates w = R(z_l, cosmology) M^-0.9 exp(-M/M*) dlnM 2 pi b^2 dlnb with
-M* = 1e15 (sigma8/0.811)^4.  A follows the lensing efficiency D_l D_ls / D_s and R the comoving
-volume per unit redshift of a CPL (w0, wa) cosmology with curvature Ok.
+The surrogate stands in for the source-independent per-plane log-CF H(q; theta, z_l) of the lens planes
+of sgl_analytic_gb300.planes (theta = (h, Om, sigma8, Ok, w0, wa)): a plane of thickness dz and lensing
+efficiency s adds dz H(s k) to a source's log-CF.  The exact solver is the engine's compensated CF sweep
+over the plane's NM x NB cells (sgl_sweep_eval; batched: sgl_cfb_*).  An 8 -> 6 x 256 SiLU -> 2 MLP maps
+(h, Om, sigma8, Ok, w0, wa, z_l, ln q), each scaled to [-1, 1] (z_l through ln(1 + z_l)), to the residual
+of (ln |H|, arg(-H)) over the plane's two-moment form
+    H0(q) = -(mu2 / 2) q^2 / (1 - i q Sbar),   Sbar = mu2 / (2 mu1),
+(mu1 = sum w S, mu2 = sum w S^2, in closed form for these planes), which already has the exact small-q
+(-mu2 q^2 / 2) and large-q (-i mu1 q) behaviour, so that the network learns an O(1) shape rather than
+the 45 units of ln |H| over the q range.  -H lies in the first quadrant, so arg(-H) never wraps.  One
+common shift and scale normalise both outputs: a fixed output error is a fixed RELATIVE error of H.
+Below q_min = e^LNQ[0] the residual goes to zero as q / q_min (H0 holds the small-q limit).
+BF16 weights and activations in the GEMMs (tcgen05.mma.kind::f16, FP32 accumulation in TMEM), FP32
+master weights, AdamW, MSE, all on the engine's own kernels.  The judge is a two-member ensemble: the
+members' disagreement estimates the error of the mean.
 """
 from __future__ import annotations
 
@@ -28,110 +22,71 @@ import math
 
 import numpy as np
 
-from .workloads import nfw_trunc_projected
+from . import planes as P
 
-NM, NB = 256, 512
-BOX = np.array([[0.6, 0.8], [0.2, 0.4], [0.7, 0.9], [-0.05, 0.05], [-1.3, -0.7], [-0.5, 0.5]])
-ZS = 1.0
-LNK = (math.log(1e-2), math.log(1e6))
+LNQ = (math.log(1e-4), math.log(4e3))
+LZMAX = math.log1p(P.ZMAX)
 
 
-# ------------------------------------------------------------------ synthetic planes
-class PlaneModel:
-    """Cells of one lens plane for a cosmology theta = (h, Om, sigma8, Ok, w0, wa)."""
-
-    def __init__(self):
-        self.M = np.geomspace(1e8, 1e16, NM)
-        self.b = np.geomspace(1e-3, 1e2, NB)
-        c = 5.0 * (self.M / 1e12) ** -0.1
-        F = nfw_trunc_projected(self.b[None, :], c[:, None])                  # (NM, NB)
-        self.kapF = ((self.M / 1e12) ** 0.3)[:, None] * F
-        dlnb = math.log(self.b[1] / self.b[0])
-        self.dlnM = math.log(self.M[1] / self.M[0])
-        self.area = 2 * math.pi * self.b ** 2 * dlnb
-        a0, r0 = self._amp(np.array([0.674, 0.315, 0.811, 0.0, -1.0, 0.0]), 0.5)
-        self.A0, self.R0 = 0.05 / a0, 3.7e6 / 128 / (r0 * self._rate_sum(0.811))
-
-    @staticmethod
-    def _distances(theta, z):
-        h, Om, s8, Ok, w0, wa = theta
-        zz = np.linspace(0.0, max(ZS, float(np.max(z))), 2001)
-        Ode = 1.0 - Om - Ok
-        fde = (1 + zz) ** (3 * (1 + w0 + wa)) * np.exp(-3 * wa * zz / (1 + zz))
-        E = np.sqrt(Om * (1 + zz) ** 3 + Ok * (1 + zz) ** 2 + Ode * fde)
-        chi = np.concatenate([[0.0], np.cumsum(0.5 * (1 / E[1:] + 1 / E[:-1]) * np.diff(zz))])
-
-        def dm(x):
-            if Ok > 0:
-                return np.sinh(math.sqrt(Ok) * x) / math.sqrt(Ok)
-            if Ok < 0:
-                return np.sin(math.sqrt(-Ok) * x) / math.sqrt(-Ok)
-            return x
-        chi_z = np.interp(z, zz, chi)
-        E_z = np.interp(z, zz, E)
-        return dm(chi_z), dm(np.interp(ZS, zz, chi)), chi_z, E_z
-
-    def _amp(self, theta, zl):
-        Dl, Ds, chi, E = self._distances(theta, np.atleast_1d(zl))
-        Ok = theta[3]
-        Dls = (Ds * np.sqrt(1 + Ok * Dl ** 2) - Dl * math.sqrt(1 + Ok * Ds ** 2)) / (1 + ZS)
-        eff = (Dl / (1 + np.atleast_1d(zl))) * Dls / (Ds / (1 + ZS))
-        A = eff * math.sqrt(theta[1] / 0.315)
-        R = chi ** 2 / E * (theta[1] / 0.315) / 128.0
-        return float(A[0]), float(R[0])
-
-    def _rate_sum(self, s8):
-        Ms = 1e15 * (s8 / 0.811) ** 4
-        return float(np.sum(self.M ** -0.9 * np.exp(-self.M / Ms) * self.dlnM) * np.sum(self.area))
-
-    def cells(self, theta, zl):
-        """(kappa, w) of the plane, flattened (NM * NB)."""
-        a, r = self._amp(np.asarray(theta, float), zl)
-        Ms = 1e15 * (theta[2] / 0.811) ** 4
-        nm = self.M ** -0.9 * np.exp(-self.M / Ms) * self.dlnM
-        kap = (self.A0 * a) * self.kapF
-        w = (self.R0 * r) * nm[:, None] * self.area[None, :]
-        return kap.ravel(), w.ravel()
+# ------------------------------------------------------------------ inputs and targets
+def features(theta, zl, lnq):
+    """(n_planes * nq, 8) float32 inputs scaled to [-1, 1]; theta (n, 6), zl (n,), lnq (n, nq)."""
+    theta = np.atleast_2d(theta)
+    n, nq = lnq.shape
+    X = np.empty((n, nq, 8), np.float32)
+    X[:, :, :6] = (2 * (theta - P.BOX[:, 0]) / (P.BOX[:, 1] - P.BOX[:, 0]) - 1)[:, None, :]
+    X[:, :, 6] = (2 * np.log1p(zl) / LZMAX - 1)[:, None]
+    X[:, :, 7] = 2 * (lnq - LNQ[0]) / (LNQ[1] - LNQ[0]) - 1
+    return X.reshape(n * nq, 8)
 
 
-def sample_inputs(n_planes, nk, seed):
-    """Latin-hypercube cosmologies and planes (z_l in (0.02, 0.98)) and per-plane ln k in the range."""
+def baseline(lnq, mu1, mu2):
+    """(ln |H0|, arg(-H0)) of the two-moment form at ln q (arrays broadcast)."""
+    x = np.exp(lnq) * (mu2 / (2 * mu1))
+    return np.log(0.5 * mu2) + 2 * lnq - 0.5 * np.log1p(x * x), np.arctan(x)
+
+
+def targets(H, lnq, mu1, mu2):
+    """Residual (ln |H| - ln |H0|, arg(-H) - arg(-H0)) of the per-plane log-CF, (n, 2) float64; H, lnq
+    (planes, nq), mu1 / mu2 per plane."""
+    b0, b1 = baseline(lnq, np.asarray(mu1)[:, None], np.asarray(mu2)[:, None])
+    return np.stack([(np.log(np.abs(H)) - b0).ravel(), (np.angle(-H) - b1).ravel()], -1)
+
+
+def untarget(R, lnq, mu1, mu2):
+    """H from residuals R (..., planes * nq, 2)."""
+    b0, b1 = baseline(lnq, np.asarray(mu1)[:, None], np.asarray(mu2)[:, None])
+    return -np.exp(R[..., 0] + b0.ravel() + 1j * (R[..., 1] + b1.ravel()))
+
+
+def plane_moments(model, theta, zl):
+    """(mu1, mu2) of planes (theta[p], zl[p])."""
+    bg = P.Background(theta)
+    m = np.array([[v[0] for v in model.moments(bg, p, np.array([zl[p]]))] for p in range(len(zl))])
+    return m[:, 0], m[:, 1]
+
+
+# ------------------------------------------------------------------ exact per-plane log-CF
+def sample_planes(n, nq, seed):
+    """n planes: Latin-hypercube cosmologies, z_l uniform in ln(1 + z_l) on [0, ZMAX], and nq sorted
+    ln q per plane, uniform on LNQ."""
     rng = np.random.default_rng(seed)
-    u = (rng.permuted(np.tile(np.arange(n_planes), (7, 1)), axis=1).T + rng.random((n_planes, 7))) / n_planes
-    theta = BOX[:, 0] + u[:, :6] * (BOX[:, 1] - BOX[:, 0])
-    zl = 0.02 + 0.96 * u[:, 6]
-    lnk = LNK[0] + (LNK[1] - LNK[0]) * np.sort(rng.random((n_planes, nk)), axis=1)
-    return theta, zl, lnk
+    u = (np.argsort(rng.random((7, n)), axis=1).T + rng.random((n, 7))) / n
+    theta = P.BOX[:, 0] + u[:, :6] * (P.BOX[:, 1] - P.BOX[:, 0])
+    zl = np.expm1(u[:, 6] * LZMAX)
+    lnq = LNQ[0] + (LNQ[1] - LNQ[0]) * np.sort(rng.random((n, nq)), axis=1)
+    return theta, zl, lnq
 
 
-def solve_planes(engine, model, theta, zl, lnk, precision=0):
-    """Exact compensated per-plane log-CF Lambda_p(k) from the engine's CF sweep (FP64 default)."""
-    out = np.empty(lnk.shape, complex)
+def solve_planes(engine, model, theta, zl, lnq, precision=0):
+    """Exact H(q) of each plane (the engine's CF sweep over its cells; FP64 by default)."""
+    bg = P.Background(theta)
+    out = np.empty(lnq.shape, complex)
     for p in range(len(zl)):
-        kap, w = model.cells(theta[p], zl[p])
-        engine.sweep_set_cells(kap, w)
-        out[p] = engine.sweep(np.exp(lnk[p]), precision)
+        S, w = model.cells(bg, p, zl[p])
+        engine.sweep_set_cells(S, w)
+        out[p] = engine.sweep(np.exp(lnq[p]), precision)
     return out
-
-
-def features(theta, zl, lnk):
-    """(n_planes * nk, 8) inputs scaled to [-1, 1]."""
-    n, nk = lnk.shape
-    X = np.empty((n, nk, 8), np.float32)
-    th = 2 * (theta - BOX[:, 0]) / (BOX[:, 1] - BOX[:, 0]) - 1
-    X[:, :, :6] = th[:, None, :]
-    X[:, :, 6] = (2 * (zl - 0.02) / 0.96 - 1)[:, None]
-    X[:, :, 7] = 2 * (lnk - LNK[0]) / (LNK[1] - LNK[0]) - 1
-    return X.reshape(n * nk, 8)
-
-
-def targets(lam):
-    """(ln |Lambda|, arg(-Lambda)) of the compensated per-plane log-CF."""
-    return np.stack([np.log(np.abs(lam)), np.angle(-lam)], -1).reshape(-1, 2).astype(np.float32)
-
-
-def untarget(T):
-    return -np.exp(T[..., 0] + 1j * T[..., 1])
 
 
 # ------------------------------------------------------------------ the MLP (tensor-core kernels)
@@ -227,32 +182,29 @@ class MLP:
                      "sgl_mlp_mse")
         return loss.value, dY
 
-    def train(self, X, Y, epochs=20, batch=16384, lr=2e-3, lr_final=1e-5, seed=0, log=None):
-        """X, Y: float32 device tensors.  Cosine learning-rate decay; returns the per-epoch mean loss."""
+    def train(self, X, Y, steps=2000, batch=16384, lr=2e-3, lr_final=1e-5, seed=0, log=None, log_every=500):
+        """X, Y: float32 device tensors.  `steps` AdamW steps on batches drawn uniformly (with
+        replacement) on the device, cosine learning-rate decay; returns the loss every log_every steps."""
         torch = self.torch
         n = X.shape[0]
-        steps = max(1, n // batch)
-        rng = np.random.default_rng(seed)
-        hist = []
-        total = epochs * steps
-        it = 0
-        for ep in range(epochs):
+        gen = torch.Generator(device=self.dev)
+        gen.manual_seed(int(seed))
+        hist, tot, cnt = [], 0.0, 0
+        for it in range(steps):
+            lr_t = lr_final + 0.5 * (lr - lr_final) * (1 + math.cos(math.pi * it / max(1, steps)))
             with torch.cuda.stream(self.stream):
-                perm = torch.tensor(rng.permutation(n), device=self.dev)
-            tot = 0.0
-            for s in range(steps):
-                lr_t = lr_final + 0.5 * (lr - lr_final) * (1 + math.cos(math.pi * it / total))
-                with torch.cuda.stream(self.stream):
-                    idx = perm[s * batch:(s + 1) * batch]
-                    xb, yb = X[idx].contiguous(), Y[idx].contiguous()
-                pred = self.forward(xb, keep=True)
-                loss, dY = self.loss_grad(pred, yb)
-                self.backward_step(dY, lr_t)
-                tot += loss
-                it += 1
-            hist.append(tot / steps)
-            if log:
-                log(f"epoch {ep}: loss {hist[-1]:.3e}")
+                idx = torch.randint(0, n, (batch,), device=self.dev, generator=gen)
+                xb, yb = X[idx], Y[idx]
+            pred = self.forward(xb, keep=True)
+            loss, dY = self.loss_grad(pred, yb)
+            self.backward_step(dY, lr_t)
+            tot += loss
+            cnt += 1
+            if cnt == log_every or it == steps - 1:
+                hist.append(tot / cnt)
+                if log:
+                    log(f"step {it + 1}: loss {hist[-1]:.3e}")
+                tot, cnt = 0.0, 0
         return hist
 
     def predict(self, X, batch=65536, host=False):
@@ -296,7 +248,7 @@ def reference_grads(W, b, X, Y):
     return loss, out[::-1]
 
 
-# ------------------------------------------------------------------ ensemble and judge
+
 def to_device(engine, *arrays):
     import torch
     dev = torch.device("cuda", engine.device)
@@ -304,86 +256,208 @@ def to_device(engine, *arrays):
         return [torch.tensor(np.ascontiguousarray(a), device=dev) for a in arrays]
 
 
+# ------------------------------------------------------------------ ensemble
 class Surrogate:
-    """Two-member ensemble of MLPs; log-CF prediction, disagreement and the judge."""
+    """Two-member ensemble of MLPs with the common target normalisation (shift of t0, one scale)."""
 
     def __init__(self, engine, members=2, width=256, depth=6, seed=0):
         self.eng = engine
         self.mlps = [MLP(engine, width, depth, seed=seed + 17 * i) for i in range(members)]
+        self.shift, self.scale = 0.0, 1.0
 
-    def train(self, X, Y, epochs=20, batch=16384, lr=2e-3, log=None):
-        Xd, Yd = to_device(self.eng, X, Y)
-        return [m.train(Xd, Yd, epochs=epochs, batch=batch, lr=lr, seed=i, log=log) for i, m in enumerate(self.mlps)]
+    def fit_normalisation(self, T):
+        self.shift = float(np.mean(T[:, 0]))
+        self.scale = float(np.std(T[:, 0]))
+
+    def normalise(self, T):
+        return np.stack([(T[:, 0] - self.shift) / self.scale, T[:, 1] / self.scale], -1).astype(np.float32)
+
+    def denormalise(self, Y):
+        return np.stack([Y[..., 0] * self.scale + self.shift, Y[..., 1] * self.scale], -1)
+
+    def train(self, X, T, steps=2000, batch=16384, lr=2e-3, log=None):
+        """X features, T targets (ln |H|, arg(-H)); the normalisation is fitted on T."""
+        self.fit_normalisation(T)
+        Xd, Yd = to_device(self.eng, X, self.normalise(T))
+        return [m.train(Xd, Yd, steps=steps, batch=batch, lr=lr, seed=i, log=log) for i, m in enumerate(self.mlps)]
 
     def predict(self, X):
-        """Per-member transformed outputs, (members, n, 2) host arrays."""
+        """Per-member (t0, t1), (members, n, 2) host arrays."""
         (Xd,) = to_device(self.eng, X)
-        return np.stack([m.predict(Xd, host=True) for m in self.mlps])
+        return np.stack([self.denormalise(m.predict(Xd, host=True).astype(np.float64)) for m in self.mlps])
 
-    def log_cf(self, X):
-        """Ensemble-mean per-plane log-CF and the members' disagreement |Lambda_1 - Lambda_2| (the
-        judge's error estimate).  X rows are planes x k, flattened."""
-        L = untarget(self.predict(X))                            # (members, n)
-        disagree = np.abs(L[0] - L[-1]) if len(L) > 1 else np.zeros(L.shape[1])
-        return L.mean(0), disagree
-
-
-def judge(engine, model, sur, theta, zl, lnk, threshold=1e-5):
-    """Surrogate log-CF for every plane; planes whose ensemble disagreement exceeds `threshold` in
-    ln CF at any k are re-evaluated by the exact FP64 solver.  Returns (Lambda, fallback mask)."""
-    n, nk = lnk.shape
-    lam, dis = sur.log_cf(features(theta, zl, lnk))
-    lam = lam.astype(complex).reshape(n, nk)
-    bad = dis.reshape(n, nk).max(1) > threshold
-    if bad.any():
-        idx = np.nonzero(bad)[0]
-        lam[idx] = solve_planes(engine, model, theta[idx], zl[idx], lnk[idx])
-    return lam, bad
+    def log_cf(self, X, lnq, mu1, mu2):
+        """Ensemble-mean H and the members' disagreement |H_1 - H_2| at the rows of X (planes x nq, with
+        their ln q and plane moments)."""
+        H = untarget(self.predict(X), lnq, mu1, mu2)
+        dis = np.abs(H[0] - H[-1]) if len(H) > 1 else np.zeros(H.shape[1])
+        return H.mean(0), dis
 
 
-# ------------------------------------------------------------------ surrogate + judge PDF sweep
-def instance_planes(theta, n_planes=64):
-    """Lens planes of one z_s = 1 instance: midpoints of n_planes equal slices of (0, 1)."""
-    zl = (np.arange(n_planes) + 0.5) / n_planes
-    return np.repeat(np.asarray(theta, float)[None, :], n_planes, 0), zl
+# ------------------------------------------------------------------ production sweep (surrogate + judge)
+SWEEP_NQ = 128
 
 
-def kappa_pdf_from_logcf(lam_tot, k, lnmu):
-    """FP64 inversion of a 1-D kappa CF exp(lam_tot(k)) on a uniform k grid (k[0] = 0, trapezoid) to
-    dP/dln mu at lnmu, with mu = (1 - kappa)^-2:  P(kappa) = (1/pi) int_0^K Re[e^{lam - i k kappa}] dk,
-    dP/dln mu = P(kappa) (1 - kappa) / 2."""
-    kap = 1.0 - np.exp(-0.5 * lnmu)
-    wk = np.full(k.size, k[1] - k[0])
-    wk[0] *= 0.5
-    wk[-1] *= 0.5
-    cf = np.exp(lam_tot) * wk
-    P = (np.cos(np.outer(kap, k)) @ cf.real + np.sin(np.outer(kap, k)) @ cf.imag) / np.pi
-    return P * (1.0 - kap) / 2.0
+def sample_instances(n, seed, zs=None):
+    """n Latin-hypercube cosmologies of the box; source redshifts uniform on ZS_RANGE, or all zs."""
+    rng = np.random.default_rng(seed)
+    u = (np.argsort(rng.random((7, n)), axis=1).T + rng.random((n, 7))) / n
+    theta = P.BOX[:, 0] + u[:, :6] * (P.BOX[:, 1] - P.BOX[:, 0])
+    z = np.full(n, float(zs)) if zs is not None else P.ZS_RANGE[0] + u[:, 6] * (P.ZS_RANGE[1] - P.ZS_RANGE[0])
+    return theta, z
 
 
-def pdf_sweep(engine, model, sur, thetas, n_planes=64, nk=2048, kmax=2000.0, lnmu=None, threshold=1e-5):
-    """Surrogate + judge PDFs for instances (cosmologies at z_s = 1) and the plain-solver PDFs.
-    Returns dict with both PDF sets, per-instance fallback fractions and the wall times."""
+class SweepTables:
+    """Planes, k grids and surrogate nodes of a set of instances (theta, z_s): plane p of instance i
+    adds dz_p H(s_p k) on k_n = n dk_i, n < nk; its nq nodes span ln q from max(ln(s_p dk_i), LNQ[0])
+    to ln(s_p k_max,i)."""
+
+    def __init__(self, model, theta, zs, nk=4096, nq=SWEEP_NQ):
+        self.model, self.theta, self.zs, self.nq = model, np.atleast_2d(theta), np.asarray(zs, float), nq
+        self.bg = P.Background(self.theta)
+        p0, zl, dz, s, inst, dk, sig, m1, m2 = [0], [], [], [], [], [], [], [], []
+        for i in range(self.zs.size):
+            a, b, c, sg = model.instance(self.bg, i, self.zs[i])
+            u, v = model.moments(self.bg, i, a)
+            zl.append(a); dz.append(b); s.append(c); m1.append(u); m2.append(v)
+            inst.append(np.full(a.size, i))
+            p0.append(p0[-1] + a.size)
+            sig.append(sg)
+            dk.append(P.k_grid(sg, nk)[0])
+        self.inst_plane0 = np.array(p0, np.int32)
+        self.zl, self.dz, self.s = np.concatenate(zl), np.concatenate(dz), np.concatenate(s)
+        self.mu1, self.mu2 = np.concatenate(m1), np.concatenate(m2)
+        self.plane_inst = np.concatenate(inst)
+        self.sigma, self.dk = np.array(sig), np.array(dk)
+        self.nk = np.full(self.zs.size, nk, np.int32)
+        kmax = self.dk[self.plane_inst] * (nk - 1)
+        with np.errstate(divide="ignore"):
+            lo = np.maximum(np.log(self.s * self.dk[self.plane_inst]), LNQ[0])
+            top = np.log(self.s * kmax)
+        self.lnq0 = lo
+        self.hq = np.where(top > lo + 1e-6, (top - lo) / (nq - 1), 1e-3)
+        self.q_above_range = int(np.sum(top > LNQ[1] + 1e-9))
+
+    @property
+    def n_planes(self):
+        return int(self.zl.size)
+
+    def features(self, engine):
+        """The ensemble's inputs at every plane's nodes, built on the device: (planes * nq, 8) float32."""
+        import torch
+        dev = torch.device("cuda", engine.device)
+        with torch.cuda.stream(torch.cuda.ExternalStream(engine.stream, device=dev)):
+            th = torch.tensor(2 * (self.theta - P.BOX[:, 0]) / (P.BOX[:, 1] - P.BOX[:, 0]) - 1, device=dev,
+                              dtype=torch.float32)
+            pi = torch.tensor(self.plane_inst, device=dev)
+            zf = torch.tensor(2 * np.log1p(self.zl) / LZMAX - 1, device=dev, dtype=torch.float32)
+            l0 = torch.tensor(self.lnq0, device=dev)
+            hq = torch.tensor(self.hq, device=dev)
+            j = torch.arange(self.nq, device=dev, dtype=torch.float64)
+            lnq = l0[:, None] + hq[:, None] * j[None, :]
+            qf = (2 * (lnq - LNQ[0]) / (LNQ[1] - LNQ[0]) - 1).to(torch.float32)
+            n, nq = self.n_planes, self.nq
+            X = torch.empty((n, nq, 8), device=dev, dtype=torch.float32)
+            X[:, :, :6] = th[pi][:, None, :]
+            X[:, :, 6] = zf[:, None]
+            X[:, :, 7] = qf
+            return X.reshape(n * nq, 8)
+
+    def plane_cells(self, p):
+        """(kappa, w) of plane p for its source: kappa = s S, w = dz w."""
+        i = int(self.plane_inst[p])
+        S, w = self.model.cells(self.bg, i, self.zl[p])
+        return self.s[p] * S, self.dz[p] * w
+
+    def separable(self, planes=None, nk=None):
+        """sgl_cfb_set_separable arguments for whole instances (planes None), or for single planes on the
+        first nk[j] points of their instance's k grid; V = 0 (the plain compound-Poisson log-CF).  Plane
+        p's cells: kappa = s_p a[m] F[m, b], w = dz_p c[m] area[b]."""
+        if planes is None:
+            planes = np.arange(self.n_planes)
+            p0 = self.inst_plane0
+            nk, dk = self.nk, self.dk
+        else:
+            planes = np.asarray(planes)
+            p0 = np.arange(planes.size + 1, dtype=np.int32)
+            nk = self.nk[self.plane_inst[planes]] if nk is None else nk
+            dk = self.dk[self.plane_inst[planes]]
+        u = np.empty((planes.size, P.NM))
+        v = np.empty((planes.size, P.NM))
+        inst = self.plane_inst[planes]
+        for i in np.unique(inst):
+            sel = np.nonzero(inst == i)[0]
+            a, c = self.model.factors(self.bg, int(i), self.zl[planes[sel]])
+            u[sel] = self.s[planes[sel], None] * a
+            v[sel] = self.dz[planes[sel], None] * c
+        return dict(F=self.model.F, g=self.model.area, inst_plane0=p0, nk=nk, dk=dk, V=np.zeros(len(nk)), u=u, v=v)
+
+
+def plain_pdfs(engine, tables, lnmu, precision=1):
+    """The plain batched solver over every cell of every plane (built on the device from the planes'
+    template), then the inversion: (P, device ms of the solve and the inversion)."""
+    engine.cfb_set_separable(**tables.separable())
+    return engine.cfb_pdf(lnmu, precision=precision, use_graph=False)
+
+
+def judge_sweep(engine, sur, tables, lnmu, threshold=1e-5, mode="prefix", fallback_precision=0, pdf_precision=0):
+    """Surrogate + judge PDFs of the instances of `tables`.  The ensemble runs at every plane's nodes; the
+    judge measures, per plane, the members' spread dz |H_1 - H_2| on the instance's k grid and sends work
+    back to the plain solver (FP64 by default):
+      mode "plane":    every plane whose largest spread exceeds `threshold` (in ln CF), whole;
+      mode "weighted": every plane whose largest |Phi|-weighted spread exceeds it, whole;
+      mode "prefix":   every plane on the k prefix up to its last point whose |Phi|-weighted spread
+                       exceeds it (beyond, |Phi| times the spread -- the error the plane can put into
+                       Phi -- stays below the threshold).
+    Then the inversion.  Returns (P, info): info["fallback_fraction"] is the fraction of (plane, k)
+    terms re-solved, info["planes_fraction"] that of planes touched."""
     import time
-    if lnmu is None:
-        lnmu = np.linspace(-0.5, 2.0, 4096)
-    k = np.linspace(0.0, kmax, nk)
-    lnk = np.log(np.maximum(k[1:], 1e-300))
-    out = {"P_sur": [], "P_plain": [], "fallback": [], "t_sur": 0.0, "t_plain": 0.0}
-    for th in thetas:
-        T, zl = instance_planes(th, n_planes)
-        L = np.tile(lnk, (n_planes, 1))
-        t0 = time.perf_counter()
-        lam, bad = judge(engine, model, sur, T, zl, L, threshold=threshold)
-        tot = np.concatenate([[0.0], lam.sum(0)])
-        out["P_sur"].append(kappa_pdf_from_logcf(tot, k, lnmu))
-        t1 = time.perf_counter()
-        exact = solve_planes(engine, model, T, zl, L)
-        tot_x = np.concatenate([[0.0], exact.sum(0)])
-        out["P_plain"].append(kappa_pdf_from_logcf(tot_x, k, lnmu))
-        t2 = time.perf_counter()
-        out["t_sur"] += t1 - t0
-        out["t_plain"] += t2 - t1
-        out["fallback"].append(float(bad.mean()))
-    out["lnmu"] = lnmu
-    return out
+    import torch
+    t = {}
+    t0 = time.perf_counter()
+    engine.sur_set(tables.inst_plane0, tables.nk, tables.dk, tables.s, tables.dz, tables.mu1, tables.mu2, tables.lnq0,
+                   tables.hq, tables.nq)
+    X = tables.features(engine)
+    with torch.cuda.stream(torch.cuda.ExternalStream(engine.stream, device=X.device)):
+        Y = torch.stack([m.forward(X) for m in sur.mlps]).contiguous()
+    dis, prefix = engine.sur_judge(Y, len(sur.mlps), sur.shift, sur.scale, threshold)
+    t["judge"] = time.perf_counter() - t0
+    nk_pl = tables.nk[tables.plane_inst]
+    if mode == "plane":
+        bad = np.nonzero(dis[:, 0] > threshold)[0]
+        nk_bad = nk_pl[bad]
+    elif mode == "weighted":
+        bad = np.nonzero(dis[:, 1] > threshold)[0]
+        nk_bad = nk_pl[bad]
+    elif mode == "prefix":
+        bad = np.nonzero(prefix > 0)[0]
+        nk_bad = np.maximum(prefix[bad], 2)
+    else:
+        raise ValueError(f"unknown judge mode {mode!r}")
+    exact = np.full(tables.n_planes, -1, np.int32)
+    t1 = time.perf_counter()
+    if bad.size:
+        engine.cfb_set_separable(**tables.separable(bad, nk_bad))
+        engine.cfb_lnphi(fallback_precision, host=False)
+        exact[bad] = np.arange(bad.size, dtype=np.int32)
+    t["fallback"] = time.perf_counter() - t1
+    t2 = time.perf_counter()
+    engine.sur_finish(Y, len(sur.mlps), sur.shift, sur.scale, exact)
+    Pm = engine.sur_pdf(lnmu, precision=pdf_precision)
+    t["finish"] = time.perf_counter() - t2
+    t["total"] = time.perf_counter() - t0
+    frac = float(np.sum(nk_bad)) / float(np.sum(nk_pl)) if bad.size else 0.0
+    return Pm, dict(fallback=bad, fallback_nk=nk_bad, fallback_fraction=frac, planes_fraction=bad.size / tables.n_planes,
+                    dis=dis, prefix=prefix, times=t)
+
+
+def pdf_errors(P, Pref, lnmu, tail_from=1.0, tail_floor=1e-9):
+    """Per-instance PDF L1 over ln mu and the tail relative error (ln mu > tail_from where the reference
+    exceeds tail_floor times its peak)."""
+    l1 = np.trapezoid(np.abs(P - Pref), lnmu, axis=-1)
+    tail = lnmu > tail_from
+    out = []
+    for a, b in zip(np.atleast_2d(P), np.atleast_2d(Pref)):
+        m = tail & (b > tail_floor * b.max())
+        out.append(float(np.max(np.abs(a[m] - b[m]) / b[m])) if m.any() else 0.0)
+    return l1, np.array(out)

@@ -56,15 +56,102 @@ def test_backprop_matches_fp64_oracle(eng):
         assert np.linalg.norm(db.cpu().numpy() - gref[l][1]) <= 2e-2 * np.linalg.norm(gref[l][1])
 
 
-def test_training_reduces_loss_and_judge_falls_back_exactly(eng):
-    from sgl_analytic_gb300 import surrogate as S
-    model = S.PlaneModel()
-    th, zl, lnk = S.sample_inputs(24, 256, seed=3)
-    L = S.solve_planes(eng, model, th, zl, lnk)
+@pytest.fixture(scope="module")
+def small(eng):
+    """A small surrogate (3 x 64) trained briefly on 48 planes x 128 q of the FP64 solver."""
+    from sgl_analytic_gb300 import planes as P, surrogate as S
+    pm = P.PlaneModel()
+    th, zl, lnq = S.sample_planes(48, 128, seed=3)
+    H = S.solve_planes(eng, pm, th, zl, lnq)
+    m1, m2 = S.plane_moments(pm, th, zl)
     sur = S.Surrogate(eng, width=64, depth=3, seed=2)
-    hist = sur.train(S.features(th, zl, lnk), S.targets(L), epochs=8, batch=1024, lr=3e-3)
+    hist = sur.train(S.features(th, zl, lnq), S.targets(H, lnq, m1, m2), steps=400, batch=1024, lr=3e-3,
+                     log=None)
+    return pm, sur, hist
+
+
+def _ensemble(eng, sur, tables):
+    import torch
+    X = tables.features(eng)
+    with torch.cuda.stream(torch.cuda.ExternalStream(eng.stream, device=X.device)):
+        Y = torch.stack([m.forward(X) for m in sur.mlps]).contiguous()
+    torch.cuda.ExternalStream(eng.stream, device=X.device).synchronize()
+    return Y
+
+
+def test_training_reduces_loss(small):
+    _, _, hist = small
     for h in hist:
-        assert h[-1] < 0.5 * h[0]
-    lam, bad = S.judge(eng, model, sur, th, zl, lnk, threshold=1e-5)
-    assert bad.any()
-    assert np.array_equal(lam[bad], L[bad])                  # fallback planes are the solver's values
+        assert h[-1] < 0.3 * h[0]
+
+
+def test_judge_assembly_matches_oracle(eng, small):
+    """Judge pass (interpolation, two-moment form, ensemble mean and spread, |Phi| weighting, k prefix)
+    and the FP64 inversion against the NumPy restatement, on uneven instances."""
+    from oracle import cfbatch_oracle as CO
+    from oracle import sur_oracle as SO
+    from sgl_analytic_gb300 import surrogate as S
+    from sgl_analytic_gb300._lib import SGL_FP64
+    pm, sur, _ = small
+    th, zs = S.sample_instances(3, 5)
+    tables = S.SweepTables(pm, th, zs, nk=512, nq=32)
+    eng.sur_set(tables.inst_plane0, tables.nk, tables.dk, tables.s, tables.dz, tables.mu1, tables.mu2, tables.lnq0,
+                tables.hq, tables.nq)
+    Y = _ensemble(eng, sur, tables)
+    tau = 1e-6
+    dis, prefix = eng.sur_judge(Y, 2, sur.shift, sur.scale, tau)
+    lnmu = np.linspace(-1.0, 9.0, 257)
+    Pg, L = eng.sur_pdf(lnmu, precision=SGL_FP64, want_lnphi=True)
+    Lo, dis_o, pre_o = SO.assemble(tables, Y.cpu().numpy(), sur.shift, sur.scale, tau)
+    off = 0
+    for i, lo in enumerate(Lo):
+        lg = L[off:off + lo.size]
+        off += lo.size
+        assert np.max(np.abs(lg - lo) / (1.0 + np.abs(lo))) < 2e-5
+        k = np.arange(lo.size) * tables.dk[i]
+        Pref = CO.pdf_from_lnphi(lg, k, lnmu)
+        assert np.max(np.abs(Pg[i] - Pref)) <= 1e-10 * np.max(np.abs(Pref))
+    assert np.allclose(dis, dis_o, rtol=2e-3, atol=1e-30)
+    clear = np.abs(dis_o[:, 1] - tau) > 1e-2 * tau                     # away from the threshold
+    assert np.array_equal((prefix > 0)[clear], (pre_o > 0)[clear])
+
+
+def test_judge_fallback_takes_exact_values(eng, small):
+    """Planes sent back take the plain FP64 solver's values: all planes (mode "plane", threshold 0)
+    reproduce the plain batched solver; "prefix" takes them on each plane's prefix only."""
+    from oracle import sur_oracle as SO
+    from sgl_analytic_gb300 import surrogate as S
+    from sgl_analytic_gb300._lib import SGL_FP64
+    pm, sur, _ = small
+    th, zs = S.sample_instances(2, 9, zs=0.5)
+    tables = S.SweepTables(pm, th, zs, nk=384, nq=32)
+    lnmu = np.linspace(-1.0, 9.0, 129)
+    Pall, info = S.judge_sweep(eng, sur, tables, lnmu, threshold=0.0, mode="plane", fallback_precision=SGL_FP64)
+    assert info["planes_fraction"] == 1.0 and info["fallback_fraction"] == 1.0
+    _, Lall = eng.sur_pdf(lnmu, precision=SGL_FP64, want_lnphi=True)
+    Pp, _ = S.plain_pdfs(eng, tables, lnmu, precision=SGL_FP64)
+    Lp = eng.cfb_lnphi(SGL_FP64)
+    assert np.max(np.abs(Lall - Lp) / (1.0 + np.abs(Lp))) < 1e-12
+    assert np.max(np.abs(Pall - Pp)) <= 1e-10 * np.max(np.abs(Pp))
+    # prefix: exact on n < prefix_p, the surrogate beyond
+    tau = 1e-7
+    Ppre, info = S.judge_sweep(eng, sur, tables, lnmu, threshold=tau, mode="prefix", fallback_precision=SGL_FP64)
+    _, Lpre = eng.sur_pdf(lnmu, precision=SGL_FP64, want_lnphi=True)
+    Y = _ensemble(eng, sur, tables)
+    off = 0
+    for i in range(tables.zs.size):
+        nk = int(tables.nk[i])
+        k = np.arange(nk) * tables.dk[i]
+        ref = np.zeros(nk, complex)
+        for p in range(int(tables.inst_plane0[i]), int(tables.inst_plane0[i + 1])):
+            sur_p = np.concatenate([[0], tables.dz[p] * SO.plane_H(tables, Y.cpu().numpy(), p, k[1:], sur.shift,
+                                                                     sur.scale).mean(0)])
+            npre = int(info["prefix"][p])
+            if npre > 0:
+                kap, w = tables.plane_cells(p)
+                eng.sweep_set_cells(kap, w)
+                ex = eng.sweep(k[:max(npre, 2)], SGL_FP64)
+                sur_p[:ex.size] = ex
+            ref += sur_p
+        assert np.max(np.abs(Lpre[off:off + nk] - ref) / (1.0 + np.abs(ref))) < 2e-5
+        off += nk

@@ -149,11 +149,18 @@ def test_mlp_gradient_oracle_matches_finite_differences():
 
 
 def test_surrogate_targets_round_trip():
-    from sgl_analytic_gb300 import surrogate as S
-    m = S.PlaneModel()
-    kap, w = m.cells(np.array([0.674, 0.315, 0.811, 0.0, -1.0, 0.0]), 0.5)
-    k = np.geomspace(1e-2, 1e6, 40)
-    L = np.array([np.sum(w * (np.expm1(1j * kk * kap) - 1j * kk * kap)) for kk in k])
-    T = S.targets(L)
-    assert np.all(np.abs(np.diff(T[:, 1])) < 1.0)             # no 2 pi wrap of the phase
-    assert np.max(np.abs(S.untarget(T) - L) / np.abs(L)) < 1e-6
+    """The surrogate's residual targets over the two-moment form invert exactly, the plane moments in
+    closed form equal the cells' sums, and arg(-H) never wraps."""
+    from sgl_analytic_gb300 import planes as P, surrogate as S
+    m = P.PlaneModel()
+    bg = P.Background(P.FIDUCIAL)
+    S_, w = m.cells(bg, 0, 0.5)
+    mu1, mu2 = m.moments(bg, 0, np.array([0.5]))
+    assert mu1[0] == pytest.approx(np.sum(w * S_), rel=1e-12)
+    assert mu2[0] == pytest.approx(np.sum(w * S_ * S_), rel=1e-12)
+    q = np.geomspace(1e-4, 4e3, 40)
+    H = np.array([np.sum(w * (np.expm1(1j * qq * S_) - 1j * qq * S_)) for qq in q])[None, :]
+    R = S.targets(H, np.log(q)[None, :], mu1, mu2)
+    assert np.all(np.abs(np.diff(np.angle(-H[0]))) < 1.0)              # no 2 pi wrap of the phase
+    assert np.max(np.abs(R)) < 10.0                                     # an O(1) residual
+    assert np.max(np.abs(S.untarget(R, np.log(q)[None, :], mu1, mu2) - H.ravel()) / np.abs(H.ravel())) < 1e-9
