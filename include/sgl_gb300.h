@@ -285,11 +285,13 @@ sgl_status sgl_cfb_set(sgl_ctx* ctx, int n_inst, const int32_t* inst_plane0, con
                        const double* V, int nstate, const double* vp_D, const double* vp_K, const double* vp_w);
 /* sgl_cfb_set_separable: a gauss-closure batch whose planes share one nm x nb cell template, built on the
  * device: cell (m, b) of plane p (planes in order, nm * nb cells each) has kap = u[p][m] F[m][b] and
- * w = v[p][m] g[b] (F nm x nb row-major, g nb, u and v n_planes x nm; host arrays).  A new batch keeps
- * the launch shapes tuned for the previous one. */
+ * w = v[p][m] g[b] (F nm x nb row-major, g nb, u and v n_planes x nm; host arrays).  k0 (may be NULL =
+ * zeros) offsets instance i's k points to k0[i] + n dk[i] for sgl_cfb_lnphi, or with geom = 1 makes them
+ * log-spaced, exp(k0[i] + n dk[i]) (sgl_cfb_pdf needs k0 = 0 and geom = 0).  A new batch keeps the launch
+ * shapes tuned for the previous one. */
 sgl_status sgl_cfb_set_separable(sgl_ctx* ctx, int nm, int nb, const double* F, const double* g, int n_inst,
-                                 const int32_t* inst_plane0, const int32_t* nk, const double* dk, const double* V,
-                                 const double* u, const double* v);
+                                 const int32_t* inst_plane0, const int32_t* nk, const double* dk, const double* k0,
+                                 int geom, const double* V, const double* u, const double* v);
 sgl_status sgl_cfb_tune(sgl_ctx* ctx, int precision, int* kt, int* ctas_per_sm);
 sgl_status sgl_cfb_lnphi(sgl_ctx* ctx, int precision, double* out);
 sgl_status sgl_cfb_pdf(sgl_ctx* ctx, int precision, const double* lnmu, int n_lnmu, double* P_out, int use_graph,
@@ -305,19 +307,27 @@ sgl_status sgl_cfb_pdf(sgl_ctx* ctx, int precision, const double* lnmu, int n_ln
  * + shift, r1 = y1 scale; between nodes 4-point Lagrange interpolation, below the first node r q / q0.
  * sgl_sur_judge sums the ensemble mean into ln Phi per instance and returns per plane dis_out (2 floats:
  * the largest dz |spread| over the k grid, as is and weighted by |Phi| of the surrogate sum; spread =
- * 2 max_m |H_m - mean|) and prefix_out (1 + the largest k index whose weighted spread exceeds tau, 0 if
- * none).  sgl_sur_finish recomputes ln Phi with plane p taken from instance exact_inst[p] of the batched
- * solver's last sgl_cfb_lnphi on that instance's k points (its nk <= the plane's; same dk; -1 = surrogate
- * only).  sgl_sur_pdf inverts the current ln Phi to dP/dln mu at n_lnmu points (as sgl_cfb_pdf; P_out
- * n_inst x n_lnmu) and copies ln Phi out as (re, im) pairs when lnphi_out is not NULL. */
+ * 2 max_m |H_m - mean|) and band_out (2 ints: the first k index whose weighted spread exceeds tau and 1 +
+ * the last; 0, 0 if none).  sgl_sur_finish recomputes ln Phi with plane p taken, on k_n for exact_lo[p] <= n
+ * < exact_lo[p] + nk', from instance exact_inst[p] of the batched solver's last sgl_cfb_lnphi (its nk', dk
+ * equal, k0 = exact_lo[p] dk; exact_inst -1 = surrogate only; exact_lo may be NULL = zeros).  sgl_sur_pdf
+ * inverts the current ln Phi to dP/dln mu at n_lnmu points (as sgl_cfb_pdf; P_out n_inst x n_lnmu) and
+ * copies ln Phi out as (re, im) pairs when lnphi_out is not NULL. */
 sgl_status sgl_sur_set(sgl_ctx* ctx, int n_inst, const int32_t* inst_plane0, const int32_t* nk, const double* dk,
                        const double* s, const double* dz, const double* mu1, const double* mu2, const double* lnq0,
                        const double* hq, int nq);
 sgl_status sgl_sur_judge(sgl_ctx* ctx, const float* Y, int members, double shift, double scale, double tau,
-                         float* dis_out, int32_t* prefix_out);
+                         float* dis_out, int32_t* band_out);
 sgl_status sgl_sur_finish(sgl_ctx* ctx, const float* Y, int members, double shift, double scale,
-                          const int32_t* exact_inst);
+                          const int32_t* exact_inst, const int32_t* exact_lo);
 sgl_status sgl_sur_pdf(sgl_ctx* ctx, int precision, const double* lnmu, int n_lnmu, double* P_out, double* lnphi_out);
+/* sgl_sur_nodes_exact: instance j of the batched solver's last sgl_cfb_lnphi holds plane planes[j]'s cells
+ * on the k points of its nodes node_lo[j] .. node_lo[j] + nk_j - 1 (log-spaced: sgl_cfb_set_separable with
+ * geom = 1, k0 = lnq0 - ln s + node_lo hq, dk = hq; node_lo may be NULL = zeros), so its ln Phi is
+ * dz H(q_node); writes those nodes' normalised residuals into every member's slots of Y (device), which the
+ * next sgl_sur_judge / sgl_sur_finish then interpolate. */
+sgl_status sgl_sur_nodes_exact(sgl_ctx* ctx, int n, const int32_t* planes, const int32_t* node_lo, float* Y,
+                               int members, double shift, double scale);
 
 /* Allocation-free entry point ------------------------------------------------------------
  * No counterpart in the reference.  For callers that may not allocate device memory (a host that

@@ -10,7 +10,7 @@ outputs Y[member][plane * nq + j] = (y0, y1):
     mu2 / (2 mu1), per member; the mean over members and the spread 2 max_m |H_m - mean|;
   * ln Phi(k_n) = sum_p dz_p mean_p(s_p k_n), n >= 1 (0 at k = 0), per instance;
   * the judge's per-plane maxima of dz spread (as is, and times |Phi| of the surrogate sum) and the k
-    prefix (1 + the last n whose weighted spread exceeds tau).
+    band [first n, 1 + last n] whose weighted spread exceeds tau ((0, 0) if none).
 """
 from __future__ import annotations
 
@@ -48,8 +48,8 @@ def plane_H(tables, Y, p, k, shift, scale):
 
 
 def assemble(tables, Y, shift, scale, tau=0.0):
-    """(ln Phi per instance (list of arrays), dis (planes, 2), prefix (planes,))."""
-    lnphi, dis, prefix = [], np.zeros((tables.n_planes, 2)), np.zeros(tables.n_planes, np.int64)
+    """(ln Phi per instance (list of arrays), dis (planes, 2), band (planes, 2))."""
+    lnphi, dis, band = [], np.zeros((tables.n_planes, 2)), np.zeros((tables.n_planes, 2), np.int64)
     for i in range(tables.zs.size):
         k = np.arange(int(tables.nk[i])) * tables.dk[i]
         p0, p1 = int(tables.inst_plane0[i]), int(tables.inst_plane0[i + 1])
@@ -65,5 +65,6 @@ def assemble(tables, Y, shift, scale, tau=0.0):
         for p, sp in zip(range(p0, p1), spreads):
             dis[p] = (sp.max(), (sp * phim).max())
             above = np.nonzero(sp * phim > tau)[0]
-            prefix[p] = above[-1] + 2 if above.size else 0
-    return lnphi, dis, prefix
+            if above.size:
+                band[p] = (above[0] + 1, above[-1] + 2)
+    return lnphi, dis, band

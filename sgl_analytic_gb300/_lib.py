@@ -25,7 +25,8 @@ EXPORTS = ("sgl_abi_version", "sgl_ctx_create", "sgl_ctx_destroy", "sgl_last_err
            "sgl_gemm_bf16", "sgl_mlp_bias_act", "sgl_mlp_act_grad", "sgl_mlp_col_sum", "sgl_mlp_mse", "sgl_mlp_adamw",
            "sgl_plan_grid", "sgl_invert", "sgl_batch_create", "sgl_batch_destroy", "sgl_batch_slots",
            "sgl_batch_slot", "sgl_batch_pdf", "sgl_cfb_set", "sgl_cfb_tune", "sgl_cfb_lnphi", "sgl_cfb_pdf",
-           "sgl_cfb_set_separable", "sgl_sur_set", "sgl_sur_judge", "sgl_sur_finish", "sgl_sur_pdf", "sgl_cf_kappa_noalloc")
+           "sgl_cfb_set_separable", "sgl_sur_set", "sgl_sur_judge", "sgl_sur_finish", "sgl_sur_pdf", "sgl_sur_nodes_exact",
+           "sgl_cf_kappa_noalloc")
 
 
 class InvertOpts(C.Structure):
@@ -103,14 +104,15 @@ def lib():
         L.sgl_cfb_tune.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.sgl_cfb_lnphi.argtypes = [vp, C.c_int, dp]
         L.sgl_cfb_pdf.argtypes = [vp, C.c_int, dp, C.c_int, dp, C.c_int, dp]
-        L.sgl_cfb_set_separable.argtypes = [vp, C.c_int, C.c_int, dp, dp, C.c_int, ip, ip, dp, dp, dp, dp]
+        L.sgl_cfb_set_separable.argtypes = [vp, C.c_int, C.c_int, dp, dp, C.c_int, ip, ip, dp, dp, C.c_int, dp, dp, dp]
         for name in ("sgl_cfb_set", "sgl_cfb_tune", "sgl_cfb_lnphi", "sgl_cfb_pdf", "sgl_cfb_set_separable"):
             getattr(L, name).restype = C.c_int
         L.sgl_sur_set.argtypes = [vp, C.c_int, ip, ip, dp, dp, dp, dp, dp, dp, dp, C.c_int]
         L.sgl_sur_judge.argtypes = [vp, vp, C.c_int, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_float), ip]
-        L.sgl_sur_finish.argtypes = [vp, vp, C.c_int, C.c_double, C.c_double, ip]
+        L.sgl_sur_finish.argtypes = [vp, vp, C.c_int, C.c_double, C.c_double, ip, ip]
         L.sgl_sur_pdf.argtypes = [vp, C.c_int, dp, C.c_int, dp, dp]
-        for name in ("sgl_sur_set", "sgl_sur_judge", "sgl_sur_finish", "sgl_sur_pdf"):
+        L.sgl_sur_nodes_exact.argtypes = [vp, C.c_int, ip, ip, vp, C.c_int, C.c_double, C.c_double]
+        for name in ("sgl_sur_set", "sgl_sur_judge", "sgl_sur_finish", "sgl_sur_pdf", "sgl_sur_nodes_exact"):
             getattr(L, name).restype = C.c_int
         for name in ("sgl_sweep_set_cells", "sgl_sweep_eval", "sgl_measure_peak"):
             getattr(L, name).restype = C.c_int
@@ -276,9 +278,10 @@ class Engine:
                                         _ptr(a["V"]), int(b["nstate"]), _ptr(a["vp_D"]), _ptr(a["vp_K"]), _ptr(a["vp_w"])),
                     "sgl_cfb_set")
 
-    def cfb_set_separable(self, F, g, inst_plane0, nk, dk, V, u, v):
+    def cfb_set_separable(self, F, g, inst_plane0, nk, dk, V, u, v, k0=None, geom=False):
         """Uploads a gauss-closure batch of template planes: plane p's cell (m, b) has kap = u[p, m] F[m, b]
-        and w = v[p, m] g[b]; the cells are built on the device."""
+        and w = v[p, m] g[b]; the cells are built on the device.  k0: per-instance offset of the solve's
+        k points (k0 + n dk), or with geom their log-spaced form exp(k0 + n dk)."""
         F = np.ascontiguousarray(F, np.float64)
         nm, nb = F.shape
         g = np.ascontiguousarray(g, np.float64)
@@ -289,10 +292,13 @@ class Engine:
         if g.size != nb or u.shape != (n_planes, nm) or v.shape != (n_planes, nm) or nk.size != p0.size - 1 or \
                 dk.size != nk.size or V.size != nk.size:
             raise ValueError("separable batch arrays have inconsistent sizes")
+        k0 = None if k0 is None else f64(k0)
+        if k0 is not None and k0.size != nk.size:
+            raise ValueError("k0 needs one entry per instance")
         self._cfb = dict(nk=nk)
         self._check(self._L.sgl_cfb_set_separable(self._h, nm, nb, _ptr(F), _ptr(g), nk.size, _ptr(p0, C.c_int32),
-                                                  _ptr(nk, C.c_int32), _ptr(dk), _ptr(V), _ptr(u), _ptr(v)),
-                    "sgl_cfb_set_separable")
+                                                  _ptr(nk, C.c_int32), _ptr(dk), None if k0 is None else _ptr(k0),
+                                                  int(bool(geom)), _ptr(V), _ptr(u), _ptr(v)), "sgl_cfb_set_separable")
 
     def cfb_tune(self, precision=SGL_MIXED):
         kt, cps = C.c_int(), C.c_int()
@@ -335,21 +341,35 @@ class Engine:
 
     def sur_judge(self, Y, members, shift, scale, tau):
         """Y: device tensor [members, planes * nq, 2] (float32).  Returns ((n_planes, 2) largest dz |spread|
-        per plane, as is and |Phi|-weighted; (n_planes,) k prefix whose weighted spread exceeds tau)."""
+        per plane, as is and |Phi|-weighted; (n_planes, 2) band [first, end) of k indices whose weighted
+        spread exceeds tau, (0, 0) if none)."""
         n = self._sur["s"].size
         out = np.empty(2 * n, np.float32)
-        pre = np.empty(n, np.int32)
+        band = np.empty(2 * n, np.int32)
         self._check(self._L.sgl_sur_judge(self._h, C.c_void_p(Y.data_ptr()), int(members), float(shift), float(scale),
-                                          float(tau), out.ctypes.data_as(C.POINTER(C.c_float)), _ptr(pre, C.c_int32)),
+                                          float(tau), out.ctypes.data_as(C.POINTER(C.c_float)), _ptr(band, C.c_int32)),
                     "sgl_sur_judge")
-        return out.reshape(-1, 2), pre
+        return out.reshape(-1, 2), band.reshape(-1, 2)
 
-    def sur_finish(self, Y, members, shift, scale, exact_inst):
+    def sur_finish(self, Y, members, shift, scale, exact_inst, exact_lo=None):
         e = np.ascontiguousarray(exact_inst, np.int32)
-        if e.size != self._sur["s"].size:
-            raise ValueError("exact_inst needs one entry per plane")
+        lo = None if exact_lo is None else np.ascontiguousarray(exact_lo, np.int32)
+        if e.size != self._sur["s"].size or (lo is not None and lo.size != e.size):
+            raise ValueError("exact_inst / exact_lo need one entry per plane")
         self._check(self._L.sgl_sur_finish(self._h, C.c_void_p(Y.data_ptr()), int(members), float(shift), float(scale),
-                                           _ptr(e, C.c_int32)), "sgl_sur_finish")
+                                           _ptr(e, C.c_int32), None if lo is None else _ptr(lo, C.c_int32)),
+                    "sgl_sur_finish")
+
+    def sur_nodes_exact(self, planes, Y, members, shift, scale, node_lo=None):
+        """Writes the batched solver's node values of `planes` (instance j = planes[j], from node node_lo[j])
+        into Y."""
+        pl = np.ascontiguousarray(planes, np.int32)
+        lo = None if node_lo is None else np.ascontiguousarray(node_lo, np.int32)
+        if lo is not None and lo.size != pl.size:
+            raise ValueError("node_lo needs one entry per plane")
+        self._check(self._L.sgl_sur_nodes_exact(self._h, pl.size, _ptr(pl, C.c_int32),
+                                                None if lo is None else _ptr(lo, C.c_int32), C.c_void_p(Y.data_ptr()),
+                                                int(members), float(shift), float(scale)), "sgl_sur_nodes_exact")
 
     def sur_pdf(self, lnmu, precision=SGL_FP64, want_lnphi=False):
         x = np.ascontiguousarray(lnmu, np.float64)

@@ -122,7 +122,7 @@ k_cfb_persistent(CfbArgs a) {
         const CfbInst I = a.inst[wi.x];
         const int n = wi.y * KT + threadIdx.x;
         const bool live = n < I.nk;
-        const double k = live ? (double)n * I.dk : 0.0;
+        const double k = live ? (I.geom ? exp(I.k0 + (double)n * I.dk) : I.k0 + (double)n * I.dk) : 0.0;
         const ff kf = ff_from_double(k);
         double2 lp;
         if (I.closure == 0) {

@@ -101,7 +101,7 @@ struct SepScratch {
 struct CfbState;                         // batched CF solver state (host_cfbatch.cu)
 void cfb_state_free(CfbState* s);
 int cfb_n_inst(const CfbState* s);
-void cfb_inst_grid(const CfbState* s, int i, long long* k_off, int* nk, double* dk);
+void cfb_inst_grid(const CfbState* s, int i, long long* k_off, int* nk, double* dk, double* k0);
 struct SurState;                         // surrogate + judge assembly state (host_sur.cu)
 void sur_state_free(SurState* s);
 

@@ -32,11 +32,12 @@ void cfb_state_free(CfbState* s) {
 
 int cfb_n_inst(const CfbState* s) { return s ? s->n_inst : 0; }
 
-void cfb_inst_grid(const CfbState* s, int i, long long* k_off, int* nk, double* dk) {
+void cfb_inst_grid(const CfbState* s, int i, long long* k_off, int* nk, double* dk, double* k0) {
     const CfbInst& I = s->inst[(size_t)i];
     *k_off = I.k_off;
     *nk = I.nk;
     *dk = I.dk;
+    *k0 = I.k0;
 }
 
 namespace sglh {
@@ -150,7 +151,7 @@ sgl_status cfb_tables(sgl_ctx* ctx, int n_inst, const int32_t* inst_plane0, cons
         I.p0 = inst_plane0[i]; I.p1 = inst_plane0[i + 1];
         I.c0 = plane_cells[I.p0]; I.c1 = plane_cells[I.p1];
         I.k_off = koff; I.nk = nk[i]; I.dk = dk[i]; I.V = V[i]; I.closure = closure[i];
-        I.vp_slot = closure[i] == 1 ? slot++ : -1; I.pad = 0;
+        I.vp_slot = closure[i] == 1 ? slot++ : -1; I.geom = 0; I.k0 = 0.0;
         k_offs[(size_t)i] = koff;
         koff += nk[i];
         // work: cells x k, the chain about 2 S^2 cell-terms per plane
@@ -210,8 +211,8 @@ sgl_status sgl_cfb_set(sgl_ctx* ctx, int n_inst, const int32_t* inst_plane0, con
 }
 
 sgl_status sgl_cfb_set_separable(sgl_ctx* ctx, int nm, int nb, const double* F, const double* g, int n_inst,
-                                 const int32_t* inst_plane0, const int32_t* nk, const double* dk, const double* V,
-                                 const double* u, const double* v) {
+                                 const int32_t* inst_plane0, const int32_t* nk, const double* dk, const double* k0,
+                                 int geom, const double* V, const double* u, const double* v) {
     if (!ctx) return SGL_ERR_VALUE;
     if (nm < 1 || nb < 1 || !F || !g || !u || !v || n_inst < 1 || !inst_plane0)
         return fail(ctx, SGL_ERR_VALUE, "sgl_cfb_set_separable: invalid template or NULL arrays");
@@ -221,8 +222,22 @@ sgl_status sgl_cfb_set_separable(sgl_ctx* ctx, int nm, int nb, const double* F, 
     std::vector<int64_t> pc((size_t)n_planes + 1);
     for (int p = 0; p <= n_planes; ++p) pc[(size_t)p] = per * p;
     std::vector<int32_t> closure((size_t)n_inst, 0);
+    if (geom && !k0) return fail(ctx, SGL_ERR_VALUE, "sgl_cfb_set_separable: log-spaced k points need k0");
+    if (k0)
+        for (int i = 0; i < n_inst; ++i)
+            if (!std::isfinite(k0[i]) || (!geom && !(k0[i] >= 0)) || (geom && k0[i] + (nk[i] - 1) * dk[i] > 700.0))
+                return fail(ctx, SGL_ERR_VALUE, "sgl_cfb_set_separable: invalid k0");
     CKS(cfb_tables(ctx, n_inst, inst_plane0, pc.data(), nk, dk, closure.data(), V, 0, nullptr, nullptr, nullptr));
     const long long nc = ctx->cfb->n_cells;
+    if (k0) {
+        CfbState& S = *ctx->cfb;
+        for (int i = 0; i < n_inst; ++i) {
+            S.inst[(size_t)i].k0 = k0[i];
+            S.inst[(size_t)i].geom = geom ? 1 : 0;
+        }
+        DBUF(d_inst, CfbInst, "cfb_inst", n_inst);
+        CKS(upload(ctx, d_inst, S.inst.data(), S.inst.size()));
+    }
     for (long long e = 0; e < per; ++e) if (!std::isfinite(F[e])) return fail(ctx, SGL_ERR_VALUE, "non-finite template F");
     for (int b = 0; b < nb; ++b) if (!std::isfinite(g[b])) return fail(ctx, SGL_ERR_VALUE, "non-finite template g");
     for (long long e = 0; e < (long long)n_planes * nm; ++e)
@@ -280,6 +295,8 @@ sgl_status sgl_cfb_pdf(sgl_ctx* ctx, int precision, const double* lnmu, int n_ln
     for (int m = 0; m < n_lnmu; ++m) if (!std::isfinite(lnmu[m])) return fail(ctx, SGL_ERR_VALUE, "non-finite ln mu");
     CK(cudaSetDevice(ctx->device));
     CfbState& S = *ctx->cfb;
+    for (const CfbInst& I : S.inst)
+        if (I.k0 != 0.0 || I.geom) return fail(ctx, SGL_ERR_VALUE, "sgl_cfb_pdf: the inversion needs k grids n dk");
     const int P = precision == SGL_FP64 ? 0 : 1;
     if (!S.tuned[P]) CKS(cfb_tune(ctx, precision));
     // every buffer of the step exists before a capture (no allocation inside it)

@@ -22,14 +22,15 @@ sgl_status sur_launch(sgl_ctx* ctx, bool judge, const float* Y, int members, dou
     SurState& S = *ctx->sur;
     DBUF(lnphi, double2, "sur_lnphi", std::max<long long>(1, S.total_k));
     DBUF(dis, unsigned int, "sur_dis", 2LL * S.n_planes);
-    DBUF(prefix, int, "sur_prefix", S.n_planes);
+    DBUF(range, int, "sur_range", 2LL * S.n_planes);          // first indices, then ends
     if (judge) {
         CK(cudaMemsetAsync(dis, 0, sizeof(unsigned int) * 2 * (size_t)S.n_planes, ctx->stream));
-        CK(cudaMemsetAsync(prefix, 0, sizeof(int) * (size_t)S.n_planes, ctx->stream));
+        CK(cudaMemsetAsync(range, 0x7f, sizeof(int) * (size_t)S.n_planes, ctx->stream));   // 0x7f7f7f7f: none
+        CK(cudaMemsetAsync(range + S.n_planes, 0, sizeof(int) * (size_t)S.n_planes, ctx->stream));
     }
     launch_sur_sum(judge, (const CfbInst*)ctx->arena.find("sur_inst"), S.n_inst, S.max_nk,
                    (const SurPlane*)ctx->arena.find("sur_planes"), Y, 2LL * S.nq * S.n_planes, members, S.nq, (float)shift,
-                   (float)scale, (float)tau, (const double2*)ctx->arena.find("cfb_lnphi"), lnphi, dis, prefix, ctx->stream);
+                   (float)scale, (float)tau, (const double2*)ctx->arena.find("cfb_lnphi"), lnphi, dis, range, range + S.n_planes, ctx->stream);
     CKLAUNCH();
     return SGL_OK;
 }
@@ -97,25 +98,31 @@ sgl_status sgl_sur_set(sgl_ctx* ctx, int n_inst, const int32_t* inst_plane0, con
 }
 
 sgl_status sgl_sur_judge(sgl_ctx* ctx, const float* Y, int members, double shift, double scale, double tau,
-                         float* dis_out, int32_t* prefix_out) {
+                         float* dis_out, int32_t* band_out) {
     if (!ctx) return SGL_ERR_VALUE;
     CKS(check_Y(ctx, Y, members, shift, scale));
-    if (!dis_out || !prefix_out || !(tau >= 0)) return fail(ctx, SGL_ERR_VALUE, "sgl_sur_judge: NULL output or invalid threshold");
+    if (!dis_out || !band_out || !(tau >= 0)) return fail(ctx, SGL_ERR_VALUE, "sgl_sur_judge: NULL output or invalid threshold");
     CK(cudaSetDevice(ctx->device));
     SurState& S = *ctx->sur;
-    for (auto& P : S.planes) { P.exact_off = -1; P.exact_nk = 0; }
+    for (auto& P : S.planes) { P.exact_off = -1; P.exact_lo = 0; P.exact_nk = 0; }
     DBUF(d_planes, SurPlane, "sur_planes", S.n_planes);
     CKS(upload(ctx, d_planes, S.planes.data(), S.planes.size()));
     CKS(sur_launch(ctx, true, Y, members, shift, scale, tau));
     CK(cudaMemcpyAsync(dis_out, ctx->arena.find("sur_dis"), sizeof(float) * 2 * (size_t)S.n_planes, cudaMemcpyDeviceToHost,
                        ctx->stream));
-    CK(cudaMemcpyAsync(prefix_out, ctx->arena.find("sur_prefix"), sizeof(int) * (size_t)S.n_planes, cudaMemcpyDeviceToHost,
-                       ctx->stream));
-    return sync_stream(ctx);
+    std::vector<int32_t> r(2 * (size_t)S.n_planes);
+    CK(cudaMemcpyAsync(r.data(), ctx->arena.find("sur_range"), sizeof(int) * r.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    CKS(sync_stream(ctx));
+    for (int p = 0; p < S.n_planes; ++p) {
+        const int e = r[(size_t)S.n_planes + p];
+        band_out[2 * (size_t)p] = e > 0 ? r[(size_t)p] : 0;
+        band_out[2 * (size_t)p + 1] = e;
+    }
+    return SGL_OK;
 }
 
 sgl_status sgl_sur_finish(sgl_ctx* ctx, const float* Y, int members, double shift, double scale,
-                          const int32_t* exact_inst) {
+                          const int32_t* exact_inst, const int32_t* exact_lo) {
     if (!ctx) return SGL_ERR_VALUE;
     CKS(check_Y(ctx, Y, members, shift, scale));
     if (!exact_inst) return fail(ctx, SGL_ERR_VALUE, "sgl_sur_finish: NULL exact_inst");
@@ -126,19 +133,23 @@ sgl_status sgl_sur_finish(sgl_ctx* ctx, const float* Y, int members, double shif
         const CfbInst& I = S.inst[(size_t)i];
         for (int p = I.p0; p < I.p1; ++p) {
             const int e = exact_inst[p];
-            S.planes[(size_t)p].exact_off = -1;
-            S.planes[(size_t)p].exact_nk = 0;
+            SurPlane& P = S.planes[(size_t)p];
+            P.exact_off = -1;
+            P.exact_lo = 0;
+            P.exact_nk = 0;
             if (e < 0) continue;
             if (!ctx->cfb || e >= cfb_n_inst(ctx->cfb))
                 return fail(ctx, SGL_ERR_VALUE, "sgl_sur_finish: plane " + std::to_string(p) + " names no solved instance");
             long long off;
             int enk;
-            double edk;
-            cfb_inst_grid(ctx->cfb, e, &off, &enk, &edk);
-            if (enk > I.nk || edk != I.dk)
-                return fail(ctx, SGL_ERR_VALUE, "sgl_sur_finish: plane " + std::to_string(p) + "'s exact k grid differs");
-            S.planes[(size_t)p].exact_off = off;
-            S.planes[(size_t)p].exact_nk = enk;
+            double edk, ek0;
+            cfb_inst_grid(ctx->cfb, e, &off, &enk, &edk, &ek0);
+            const int lo = exact_lo ? exact_lo[p] : 0;
+            if (lo < 0 || (long long)lo + enk > I.nk || edk != I.dk || ek0 != (double)lo * I.dk)
+                return fail(ctx, SGL_ERR_VALUE, "sgl_sur_finish: plane " + std::to_string(p) + "'s exact k points differ");
+            P.exact_off = off;
+            P.exact_lo = lo;
+            P.exact_nk = enk;
             any = true;
         }
     }
@@ -147,6 +158,41 @@ sgl_status sgl_sur_finish(sgl_ctx* ctx, const float* Y, int members, double shif
     CKS(upload(ctx, d_planes, S.planes.data(), S.planes.size()));
     CKS(sur_launch(ctx, false, Y, members, shift, scale, 0.0));
     return SGL_OK;
+}
+
+sgl_status sgl_sur_nodes_exact(sgl_ctx* ctx, int n, const int32_t* planes, const int32_t* node_lo, float* Y,
+                               int members, double shift, double scale) {
+    if (!ctx) return SGL_ERR_VALUE;
+    CKS(check_Y(ctx, Y, members, shift, scale));
+    if (n < 1 || !planes) return fail(ctx, SGL_ERR_VALUE, "sgl_sur_nodes_exact: no planes");
+    CK(cudaSetDevice(ctx->device));
+    SurState& S = *ctx->sur;
+    if (!ctx->cfb || cfb_n_inst(ctx->cfb) != n || !ctx->arena.find("cfb_lnphi"))
+        return fail(ctx, SGL_ERR_STATE, "sgl_sur_nodes_exact: the batched solver does not hold one solved instance per plane");
+    for (int j = 0; j < n; ++j) {
+        const int p = planes[j];
+        if (p < 0 || p >= S.n_planes) return fail(ctx, SGL_ERR_VALUE, "sgl_sur_nodes_exact: plane out of range");
+        long long off;
+        int enk;
+        double edk, ek0;
+        cfb_inst_grid(ctx->cfb, j, &off, &enk, &edk, &ek0);
+        const SurPlane& P = S.planes[(size_t)p];
+        const int lo = node_lo ? node_lo[j] : 0;
+        if (lo < 0 || lo + enk > S.nq || edk != P.hq || !(P.dz > 0))
+            return fail(ctx, SGL_ERR_VALUE, "sgl_sur_nodes_exact: instance " + std::to_string(j) + " is not on plane " +
+                                                std::to_string(p) + "'s node grid");
+    }
+    std::vector<int> lo_v((size_t)n, 0);
+    if (node_lo) for (int j = 0; j < n; ++j) lo_v[(size_t)j] = node_lo[j];
+    DBUF(d_pl, int, "sur_exact_planes", n);
+    DBUF(d_lo, int, "sur_exact_lo", n);
+    CKS(upload(ctx, d_pl, (const int*)planes, (size_t)n));
+    CKS(upload(ctx, d_lo, lo_v.data(), (size_t)n));
+    launch_sur_nodes_exact(n, d_pl, d_lo, (const CfbInst*)ctx->arena.find("cfb_inst"), (const double2*)ctx->arena.find("cfb_lnphi"),
+                           (const SurPlane*)ctx->arena.find("sur_planes"), S.nq, Y, 2LL * S.nq * S.n_planes, members,
+                           (float)shift, (float)scale, ctx->stream);
+    CKLAUNCH();
+    return sync_stream(ctx);
 }
 
 sgl_status sgl_sur_pdf(sgl_ctx* ctx, int precision, const double* lnmu, int n_lnmu, double* P_out, double* lnphi_out) {

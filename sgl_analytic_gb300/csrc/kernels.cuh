@@ -143,7 +143,8 @@ struct CfbInst {                          // one instance of the batch
     int nk, closure;                      // k points (k_n = n dk); closure 0 gauss, 1 vp
     double dk, V;                         // k step; gauss: the clustering variance term V k^2 / 2
     int vp_slot;                          // vp: index into the chain tables
-    int pad;
+    int geom;                             // 1: the solve's k points are exp(k0 + n dk) (log-spaced)
+    double k0;                            // else k0 + n dk (the inversion assumes k0 = 0)
 };
 void launch_cfb_persistent(int precision, int kt, int ctas, const CfbInst* inst, const int2* items, int n_items,
                            int* counter, const long long* plane_cells, const double* kap, const double* w,
@@ -159,11 +160,14 @@ struct SurPlane {                         // one plane of the surrogate sweep
     double lnq0, hq;                      // its surrogate nodes ln q_j = lnq0 + j hq
     double lnmu2h, sbar;                  // two-moment form: ln(mu2 / 2), Sbar = mu2 / (2 mu1)
     long long exact_off;                  // finishing pass: first k of its exact ln Phi, or -1
-    int exact_nk, pad;                    // exact for k_n, n < exact_nk
+    int exact_lo, exact_nk;               // exact for k_n, exact_lo <= n < exact_lo + exact_nk
 };
+void launch_sur_nodes_exact(int n, const int* planes, const int* node_lo, const CfbInst* cfb_inst,
+                            const double2* cfb_lnphi, const SurPlane* sp, int nq, float* Y, long long y_member_stride,
+                            int members, float shift, float scale, cudaStream_t st);
 void launch_sur_sum(bool judge, const CfbInst* inst, int n_inst, int max_nk, const SurPlane* planes, const float* Y,
                     long long y_member_stride, int members, int nq, float shift, float scale, float tau,
-                    const double2* exact, double2* lnphi, unsigned int* dis, int* prefix, cudaStream_t st);
+                    const double2* exact, double2* lnphi, unsigned int* dis, int* first, int* last, cudaStream_t st);
 void launch_p3_finish(int precision, const void* P3ext, int nkap, int ngam, int ld, const double* gam, double* P3,
                       float* P3f, cudaStream_t st);
 void launch_path_integral(const double* P3, const float* P3f, int nkap, int ngam, double kap0, double kap1,

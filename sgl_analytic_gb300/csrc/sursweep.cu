@@ -1,9 +1,10 @@
 // Surrogate + judge assembly of instance log-CFs (the production sweep of the learned per-plane
 // log-CF).  Per instance and k-point, the sum over the instance's planes of dz H(s k), H from the
 // ensemble members' outputs at the plane's ln q nodes.  The judge pass also reduces, per plane, the
-// members' largest disagreement (as is, and weighted by |Phi| of the surrogate sum) and the k prefix
-// on which the weighted disagreement exceeds the threshold; the finishing pass takes the exact
-// solver's values on that prefix.
+// members' largest disagreement (as is, and weighted by |Phi| of the surrogate sum) and the band of k
+// points from the first to the last whose weighted disagreement exceeds the threshold; the finishing
+// pass takes the exact solver's values on each plane's band.  Planes can also be sent back for exact
+// values at their nodes (k_sur_nodes_exact), which then replace the members' outputs there.
 //
 // The members learn the residual of ln H over the two-moment form
 //     H0(q) = -(mu2 / 2) q^2 / (1 - i q Sbar),   Sbar = mu2 / (2 mu1),
@@ -11,6 +12,8 @@
 //     ln |H| = r0 + ln(mu2 / 2) + 2 ln q - ln(1 + (q Sbar)^2) / 2,   arg(-H) = r1 + atan(q Sbar).
 //
 // No counterpart in the reference.
+#include <climits>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -30,7 +33,8 @@ struct SurArgs {
     const double2* exact;                // the exact solver's ln Phi per plane (finishing pass)
     double2* lnphi;                      // out: per instance and k
     unsigned int* dis;                   // judge: per plane (max dz spread, max |Phi| dz spread) as float bits
-    int* prefix;                         // judge: per plane, 1 + the last k index above tau (0: none)
+    int* first;                          // judge: per plane, the first k index above tau (stays large: none)
+    int* last;                           // judge: per plane, 1 + the last k index above tau (stays 0: none)
 };
 
 // (r0, r1) of one member at node coordinate x = (ln q - lnq0) / hq: 4-point Lagrange interpolation
@@ -97,8 +101,8 @@ __global__ void __launch_bounds__(kSurThreads) k_sur_sum(SurArgs a) {
     double sr = 0.0, si = 0.0;
     for (int p = I.p0; p < I.p1; ++p) {
         const SurPlane P = a.planes[p];
-        if (!JUDGE && P.exact_off >= 0 && n < P.exact_nk) {
-            const double2 e = a.exact[P.exact_off + n];
+        if (!JUDGE && P.exact_off >= 0 && n >= P.exact_lo && n < P.exact_lo + P.exact_nk) {
+            const double2 e = a.exact[P.exact_off + (n - P.exact_lo)];
             sr += e.x;
             si += e.y;
             continue;
@@ -124,18 +128,52 @@ __global__ void __launch_bounds__(kSurThreads) k_sur_sum(SurArgs a) {
                 du *= (float)P.dz;
             }
             float dw = du * phim;
-            int last = dw > a.tau ? n + 1 : 0;
+            const bool above = dw > a.tau;
+            int first = above ? n : INT_MAX, last = above ? n + 1 : 0;
             for (int o = 16; o > 0; o >>= 1) {
                 du = fmaxf(du, __shfl_xor_sync(0xffffffffu, du, o));
                 dw = fmaxf(dw, __shfl_xor_sync(0xffffffffu, dw, o));
+                first = min(first, __shfl_xor_sync(0xffffffffu, first, o));
                 last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
             }
             if (lane == 0) {
                 atomicMax(a.dis + 2LL * p, __float_as_uint(du));            // non-negative: bits order as values
                 atomicMax(a.dis + 2LL * p + 1, __float_as_uint(dw));
-                if (last > 0) atomicMax(a.prefix + p, last);
+                if (last > 0) {
+                    atomicMin(a.first + p, first);
+                    atomicMax(a.last + p, last);
+                }
             }
         }
+    }
+}
+
+// Planes sent back for exact node values: instance j of the batched solver holds plane planes[j]'s
+// cells on the k points of its nodes node_lo[j] .. node_lo[j] + nk_j - 1 (q_node / s), so its ln Phi is
+// dz H(q_node); the node's residual over the two-moment form, normalised, replaces every member's output
+__global__ void k_sur_nodes_exact(long long total, const int* __restrict__ planes, const int* __restrict__ node_lo,
+                                  const CfbInst* __restrict__ ci, const double2* __restrict__ lnphi,
+                                  const SurPlane* __restrict__ sp, int nq, float* __restrict__ Y, long long stride,
+                                  int members, float shift, float scale) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= total) return;
+    const int j = (int)(e / nq), t = (int)(e - (long long)j * nq);
+    const CfbInst I = ci[j];
+    if (t >= I.nk) return;
+    const int p = planes[j];
+    const int node = node_lo[j] + t;
+    const SurPlane P = sp[p];
+    const double2 L = lnphi[I.k_off + t];
+    const double hr = L.x / P.dz, hi = L.y / P.dz;
+    const double lq = P.lnq0 + node * P.hq;
+    const double qs = exp(lq) * P.sbar;
+    const double r0 = 0.5 * log(hr * hr + hi * hi) - (P.lnmu2h + 2.0 * lq - 0.5 * log1p(qs * qs));
+    const double r1 = atan2(-hi, -hr) - atan(qs);
+    const float y0 = (float)((r0 - shift) / scale), y1 = (float)(r1 / scale);
+    for (int m = 0; m < members; ++m) {
+        float* o = Y + m * stride + ((long long)p * nq + node) * 2;
+        o[0] = y0;
+        o[1] = y1;
     }
 }
 
@@ -143,11 +181,20 @@ __global__ void __launch_bounds__(kSurThreads) k_sur_sum(SurArgs a) {
 
 void launch_sur_sum(bool judge, const CfbInst* inst, int n_inst, int max_nk, const SurPlane* planes, const float* Y,
                     long long y_member_stride, int members, int nq, float shift, float scale, float tau,
-                    const double2* exact, double2* lnphi, unsigned int* dis, int* prefix, cudaStream_t st) {
-    SurArgs a{inst, planes, Y, y_member_stride, members, nq, shift, scale, tau, exact, lnphi, dis, prefix};
+                    const double2* exact, double2* lnphi, unsigned int* dis, int* first, int* last, cudaStream_t st) {
+    SurArgs a{inst, planes, Y, y_member_stride, members, nq, shift, scale, tau, exact, lnphi, dis, first, last};
     const dim3 grid((unsigned)ceil_div(max_nk, kSurThreads), (unsigned)n_inst);
     if (judge) k_sur_sum<true><<<grid, kSurThreads, 0, st>>>(a);
     else k_sur_sum<false><<<grid, kSurThreads, 0, st>>>(a);
+    SGL_COUNT(1);
+}
+
+void launch_sur_nodes_exact(int n, const int* planes, const int* node_lo, const CfbInst* cfb_inst,
+                            const double2* cfb_lnphi, const SurPlane* sp, int nq, float* Y, long long y_member_stride,
+                            int members, float shift, float scale, cudaStream_t st) {
+    const long long total = (long long)n * nq;
+    k_sur_nodes_exact<<<(unsigned)ceil_div(total, 256), 256, 0, st>>>(total, planes, node_lo, cfb_inst, cfb_lnphi, sp,
+                                                                     nq, Y, y_member_stride, members, shift, scale);
     SGL_COUNT(1);
 }
 

@@ -91,11 +91,14 @@ def solve_planes(engine, model, theta, zl, lnq, precision=0):
 
 # ------------------------------------------------------------------ the MLP (tensor-core kernels)
 class MLP:
-    """8 -> width^depth SiLU -> 2 on the engine's stream; weights are torch tensors (device memory)."""
+    """8 -> width^depth SiLU -> 2 on the engine's stream; weights are torch tensors (device memory).
+    The GEMMs take BF16 weights; split=True feeds each layer's FP32 input as two BF16 parts (hi, lo) so
+    that only the weights are rounded to BF16 (twice the tensor-core work of plain BF16 inputs)."""
 
-    def __init__(self, engine, width=256, depth=6, seed=0, n_in=8, n_out=2):
+    def __init__(self, engine, width=256, depth=6, seed=0, n_in=8, n_out=2, split=True):
         import torch
         self.torch = torch
+        self.split = split
         self.eng = engine
         self.dev = torch.device("cuda", engine.device)
         self.stream = torch.cuda.ExternalStream(engine.stream, device=self.dev)
@@ -126,7 +129,15 @@ class MLP:
             for l, (W, b) in enumerate(zip(self.W, self.b)):
                 a, c = W.shape
                 Z = torch.empty((n, c), device=self.dev)
-                self._gemm(n, c, a, A, a, 1, W, c, 1, Z, c, 1)
+                if self.split:
+                    # the layer's input as two BF16 parts [A_hi | A_lo] against [W; W]: the product of the
+                    # FP32 input (to 2^-17) with the BF16 weights, FP32 accumulation
+                    Ah = A.to(torch.bfloat16).to(torch.float32)
+                    A2 = torch.cat([Ah, A - Ah], 1)
+                    W2 = torch.cat([W, W], 0)
+                    self._gemm(n, c, 2 * a, A2, 2 * a, 1, W2, c, 1, Z, c, 1)
+                else:
+                    self._gemm(n, c, a, A, a, 1, W, c, 1, Z, c, 1)
                 Zb = torch.empty_like(Z) if keep else Z
                 out = torch.empty_like(Z)
                 last = l == len(self.W) - 1
@@ -260,9 +271,9 @@ def to_device(engine, *arrays):
 class Surrogate:
     """Two-member ensemble of MLPs with the common target normalisation (shift of t0, one scale)."""
 
-    def __init__(self, engine, members=2, width=256, depth=6, seed=0):
+    def __init__(self, engine, members=2, width=256, depth=6, seed=0, split=True):
         self.eng = engine
-        self.mlps = [MLP(engine, width, depth, seed=seed + 17 * i) for i in range(members)]
+        self.mlps = [MLP(engine, width, depth, seed=seed + 17 * i, split=split) for i in range(members)]
         self.shift, self.scale = 0.0, 1.0
 
     def fit_normalisation(self, T):
@@ -275,11 +286,13 @@ class Surrogate:
     def denormalise(self, Y):
         return np.stack([Y[..., 0] * self.scale + self.shift, Y[..., 1] * self.scale], -1)
 
-    def train(self, X, T, steps=2000, batch=16384, lr=2e-3, log=None):
-        """X features, T targets (ln |H|, arg(-H)); the normalisation is fitted on T."""
+    def train(self, X, T, steps=2000, batch=16384, lr=2e-3, log=None, log_every=500):
+        """X features, T residual targets; the normalisation is fitted on T.  Returns each member's loss
+        history (every log_every steps)."""
         self.fit_normalisation(T)
         Xd, Yd = to_device(self.eng, X, self.normalise(T))
-        return [m.train(Xd, Yd, steps=steps, batch=batch, lr=lr, seed=i, log=log) for i, m in enumerate(self.mlps)]
+        return [m.train(Xd, Yd, steps=steps, batch=batch, lr=lr, seed=i, log=log, log_every=log_every)
+                for i, m in enumerate(self.mlps)]
 
     def predict(self, X):
         """Per-member (t0, t1), (members, n, 2) host arrays."""
@@ -369,10 +382,11 @@ class SweepTables:
         S, w = self.model.cells(self.bg, i, self.zl[p])
         return self.s[p] * S, self.dz[p] * w
 
-    def separable(self, planes=None, nk=None):
+    def separable(self, planes=None, nk=None, lo=None):
         """sgl_cfb_set_separable arguments for whole instances (planes None), or for single planes on the
-        first nk[j] points of their instance's k grid; V = 0 (the plain compound-Poisson log-CF).  Plane
-        p's cells: kappa = s_p a[m] F[m, b], w = dz_p c[m] area[b]."""
+        points lo[j] .. lo[j] + nk[j] - 1 of their instance's k grid; V = 0 (the plain compound-Poisson
+        log-CF).  Plane p's cells: kappa = s_p a[m] F[m, b], w = dz_p c[m] area[b]."""
+        k0 = None
         if planes is None:
             planes = np.arange(self.n_planes)
             p0 = self.inst_plane0
@@ -382,6 +396,7 @@ class SweepTables:
             p0 = np.arange(planes.size + 1, dtype=np.int32)
             nk = self.nk[self.plane_inst[planes]] if nk is None else nk
             dk = self.dk[self.plane_inst[planes]]
+            k0 = None if lo is None else np.asarray(lo) * dk
         u = np.empty((planes.size, P.NM))
         v = np.empty((planes.size, P.NM))
         inst = self.plane_inst[planes]
@@ -390,7 +405,56 @@ class SweepTables:
             a, c = self.model.factors(self.bg, int(i), self.zl[planes[sel]])
             u[sel] = self.s[planes[sel], None] * a
             v[sel] = self.dz[planes[sel], None] * c
-        return dict(F=self.model.F, g=self.model.area, inst_plane0=p0, nk=nk, dk=dk, V=np.zeros(len(nk)), u=u, v=v)
+        return dict(F=self.model.F, g=self.model.area, inst_plane0=p0, nk=nk, dk=dk, V=np.zeros(len(nk)), u=u, v=v,
+                    k0=k0)
+
+
+def node_separable(tables, planes, node_lo=None, n_nodes=None):
+    """sgl_cfb_set_separable arguments that put each of `planes` on its own nodes' k points, q_j / s_p =
+    exp(lnq0_p - ln s_p + j hq_p) (log-spaced: geom), j = node_lo .. node_lo + n_nodes - 1 (all nodes by
+    default)."""
+    planes = np.asarray(planes)
+    lo = np.zeros(planes.size, np.int64) if node_lo is None else np.asarray(node_lo)
+    nn = np.full(planes.size, tables.nq) if n_nodes is None else np.asarray(n_nodes)
+    d = tables.separable(planes)
+    d.update(nk=nn.astype(np.int32), dk=tables.hq[planes],
+             k0=tables.lnq0[planes] - np.log(tables.s[planes]) + lo * tables.hq[planes], geom=True)
+    return d
+
+
+def node_band(tables, planes, band, margin=2):
+    """Node range [lo, hi) of each plane that covers its k band [first, end) with the interpolation
+    stencil and `margin` more nodes on each side."""
+    planes = np.asarray(planes)
+    inst = tables.plane_inst[planes]
+    dk, s = tables.dk[inst], tables.s[planes]
+    x = lambda n: (np.log(s * np.maximum(n, 1) * dk) - tables.lnq0[planes]) / tables.hq[planes]
+    lo = np.floor(x(band[:, 0])).astype(np.int64) - 1 - margin
+    hi = np.ceil(x(band[:, 1] - 1)).astype(np.int64) + 3 + margin
+    lo = np.clip(lo, 0, tables.nq - 2)
+    hi = np.clip(hi, lo + 2, tables.nq)
+    return lo, hi
+
+
+def plain_node_pdfs(engine, tables, lnmu, precision=1, pdf_precision=0):
+    """The plain solver in node form: every plane exact at its nq log-spaced nodes (batched solver), the
+    4-point interpolation of the nodes onto the instance's k grid, then the inversion.  Returns (P, ms of
+    the node solve)."""
+    import time
+    import torch
+    engine.sur_set(tables.inst_plane0, tables.nk, tables.dk, tables.s, tables.dz, tables.mu1, tables.mu2, tables.lnq0,
+                   tables.hq, tables.nq)
+    dev = torch.device("cuda", engine.device)
+    with torch.cuda.stream(torch.cuda.ExternalStream(engine.stream, device=dev)):
+        Y = torch.zeros((1, tables.n_planes * tables.nq, 2), device=dev, dtype=torch.float32)
+    engine.cfb_set_separable(**node_separable(tables, np.arange(tables.n_planes)))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    engine.cfb_lnphi(precision, host=False)
+    ms = 1e3 * (time.perf_counter() - t0)
+    engine.sur_nodes_exact(np.arange(tables.n_planes), Y, 1, 0.0, 1.0)
+    engine.sur_finish(Y, 1, 0.0, 1.0, np.full(tables.n_planes, -1, np.int32))
+    return engine.sur_pdf(lnmu, precision=pdf_precision), ms
 
 
 def plain_pdfs(engine, tables, lnmu, precision=1):
@@ -400,17 +464,21 @@ def plain_pdfs(engine, tables, lnmu, precision=1):
     return engine.cfb_pdf(lnmu, precision=precision, use_graph=False)
 
 
-def judge_sweep(engine, sur, tables, lnmu, threshold=1e-5, mode="prefix", fallback_precision=0, pdf_precision=0):
+def judge_sweep(engine, sur, tables, lnmu, threshold=1e-5, mode="nodes", fallback_precision=1, pdf_precision=0):
     """Surrogate + judge PDFs of the instances of `tables`.  The ensemble runs at every plane's nodes; the
     judge measures, per plane, the members' spread dz |H_1 - H_2| on the instance's k grid and sends work
-    back to the plain solver (FP64 by default):
-      mode "plane":    every plane whose largest spread exceeds `threshold` (in ln CF), whole;
-      mode "weighted": every plane whose largest |Phi|-weighted spread exceeds it, whole;
-      mode "prefix":   every plane on the k prefix up to its last point whose |Phi|-weighted spread
-                       exceeds it (beyond, |Phi| times the spread -- the error the plane can put into
-                       Phi -- stays below the threshold).
-    Then the inversion.  Returns (P, info): info["fallback_fraction"] is the fraction of (plane, k)
-    terms re-solved, info["planes_fraction"] that of planes touched."""
+    back to the plain batched solver (fallback_precision: SGL_MIXED, within 1e-6 of FP64, by default):
+      mode "nodes":    every plane whose |Phi|-weighted spread -- the error it can put into Phi -- exceeds
+                       `threshold` somewhere, solved exactly at the nodes that cover that band of k (with
+                       the interpolation stencil and two more nodes each side), which replace the members'
+                       outputs there;
+      mode "plane":    every plane whose largest spread exceeds `threshold` (in ln CF), on the whole k grid;
+      mode "weighted": every plane whose largest |Phi|-weighted spread exceeds it, on the whole k grid;
+      mode "band":     every plane on the band of k from the first to the last point where its
+                       |Phi|-weighted spread exceeds it.
+    Then the inversion (pdf_precision, FP64 by default).  Returns (P, info): info["fallback_fraction"] is
+    the fallback's terms as a fraction of the plain solver's (plane, k) terms (a node counts as nk / nq
+    k points), info["planes_fraction"] the fraction of planes sent back."""
     import time
     import torch
     t = {}
@@ -420,35 +488,50 @@ def judge_sweep(engine, sur, tables, lnmu, threshold=1e-5, mode="prefix", fallba
     X = tables.features(engine)
     with torch.cuda.stream(torch.cuda.ExternalStream(engine.stream, device=X.device)):
         Y = torch.stack([m.forward(X) for m in sur.mlps]).contiguous()
-    dis, prefix = engine.sur_judge(Y, len(sur.mlps), sur.shift, sur.scale, threshold)
+    dis, band = engine.sur_judge(Y, len(sur.mlps), sur.shift, sur.scale, threshold)
     t["judge"] = time.perf_counter() - t0
     nk_pl = tables.nk[tables.plane_inst]
+    lo = None
     if mode == "plane":
         bad = np.nonzero(dis[:, 0] > threshold)[0]
         nk_bad = nk_pl[bad]
     elif mode == "weighted":
         bad = np.nonzero(dis[:, 1] > threshold)[0]
         nk_bad = nk_pl[bad]
-    elif mode == "prefix":
-        bad = np.nonzero(prefix > 0)[0]
-        nk_bad = np.maximum(prefix[bad], 2)
+    elif mode == "band":
+        bad = np.nonzero(band[:, 1] > 0)[0]
+        lo = band[bad, 0].astype(np.int64)
+        nk_bad = np.maximum(band[bad, 1] - lo, 2)
+        lo = np.minimum(lo, nk_pl[bad] - nk_bad)
+    elif mode == "nodes":
+        bad = np.nonzero(band[:, 1] > 0)[0]
+        node_lo, node_hi = node_band(tables, bad, band[bad])
+        nk_bad = node_hi - node_lo
     else:
         raise ValueError(f"unknown judge mode {mode!r}")
     exact = np.full(tables.n_planes, -1, np.int32)
+    exact_lo = np.zeros(tables.n_planes, np.int32)
     t1 = time.perf_counter()
-    if bad.size:
-        engine.cfb_set_separable(**tables.separable(bad, nk_bad))
+    if bad.size and mode == "nodes":
+        engine.cfb_set_separable(**node_separable(tables, bad, node_lo, nk_bad))
+        engine.cfb_lnphi(fallback_precision, host=False)
+        engine.sur_nodes_exact(bad, Y, len(sur.mlps), sur.shift, sur.scale, node_lo)
+        nk_bad = nk_bad * (nk_pl[bad] / tables.nq)          # in k-grid terms: a node costs nk / nq points
+    elif bad.size:
+        engine.cfb_set_separable(**tables.separable(bad, nk_bad, lo))
         engine.cfb_lnphi(fallback_precision, host=False)
         exact[bad] = np.arange(bad.size, dtype=np.int32)
+        if lo is not None:
+            exact_lo[bad] = lo
     t["fallback"] = time.perf_counter() - t1
     t2 = time.perf_counter()
-    engine.sur_finish(Y, len(sur.mlps), sur.shift, sur.scale, exact)
+    engine.sur_finish(Y, len(sur.mlps), sur.shift, sur.scale, exact, exact_lo)
     Pm = engine.sur_pdf(lnmu, precision=pdf_precision)
     t["finish"] = time.perf_counter() - t2
     t["total"] = time.perf_counter() - t0
     frac = float(np.sum(nk_bad)) / float(np.sum(nk_pl)) if bad.size else 0.0
-    return Pm, dict(fallback=bad, fallback_nk=nk_bad, fallback_fraction=frac, planes_fraction=bad.size / tables.n_planes,
-                    dis=dis, prefix=prefix, times=t)
+    return Pm, dict(fallback=bad, fallback_nk=nk_bad, fallback_lo=lo, fallback_fraction=frac,
+                    planes_fraction=bad.size / tables.n_planes, dis=dis, band=band, times=t)
 
 
 def pdf_errors(P, Pref, lnmu, tail_from=1.0, tail_floor=1e-9):

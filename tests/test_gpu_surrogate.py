@@ -66,7 +66,7 @@ def small(eng):
     m1, m2 = S.plane_moments(pm, th, zl)
     sur = S.Surrogate(eng, width=64, depth=3, seed=2)
     hist = sur.train(S.features(th, zl, lnq), S.targets(H, lnq, m1, m2), steps=400, batch=1024, lr=3e-3,
-                     log=None)
+                     log_every=100)
     return pm, sur, hist
 
 
@@ -86,7 +86,7 @@ def test_training_reduces_loss(small):
 
 
 def test_judge_assembly_matches_oracle(eng, small):
-    """Judge pass (interpolation, two-moment form, ensemble mean and spread, |Phi| weighting, k prefix)
+    """Judge pass (interpolation, two-moment form, ensemble mean and spread, |Phi| weighting, k band)
     and the FP64 inversion against the NumPy restatement, on uneven instances."""
     from oracle import cfbatch_oracle as CO
     from oracle import sur_oracle as SO
@@ -99,10 +99,10 @@ def test_judge_assembly_matches_oracle(eng, small):
                 tables.hq, tables.nq)
     Y = _ensemble(eng, sur, tables)
     tau = 1e-6
-    dis, prefix = eng.sur_judge(Y, 2, sur.shift, sur.scale, tau)
+    dis, band = eng.sur_judge(Y, 2, sur.shift, sur.scale, tau)
     lnmu = np.linspace(-1.0, 9.0, 257)
     Pg, L = eng.sur_pdf(lnmu, precision=SGL_FP64, want_lnphi=True)
-    Lo, dis_o, pre_o = SO.assemble(tables, Y.cpu().numpy(), sur.shift, sur.scale, tau)
+    Lo, dis_o, band_o = SO.assemble(tables, Y.cpu().numpy(), sur.shift, sur.scale, tau)
     off = 0
     for i, lo in enumerate(Lo):
         lg = L[off:off + lo.size]
@@ -113,12 +113,14 @@ def test_judge_assembly_matches_oracle(eng, small):
         assert np.max(np.abs(Pg[i] - Pref)) <= 1e-10 * np.max(np.abs(Pref))
     assert np.allclose(dis, dis_o, rtol=2e-3, atol=1e-30)
     clear = np.abs(dis_o[:, 1] - tau) > 1e-2 * tau                     # away from the threshold
-    assert np.array_equal((prefix > 0)[clear], (pre_o > 0)[clear])
+    assert np.array_equal((band[:, 1] > 0)[clear], (band_o[:, 1] > 0)[clear])
+    both = clear & (band[:, 1] > 0) & (band_o[:, 1] > 0)
+    assert np.max(np.abs(band[both] - band_o[both]), initial=0) <= 2        # edges may move by a point
 
 
 def test_judge_fallback_takes_exact_values(eng, small):
     """Planes sent back take the plain FP64 solver's values: all planes (mode "plane", threshold 0)
-    reproduce the plain batched solver; "prefix" takes them on each plane's prefix only."""
+    reproduce the plain batched solver; "band" takes them on each plane's band of k only."""
     from oracle import sur_oracle as SO
     from sgl_analytic_gb300 import surrogate as S
     from sgl_analytic_gb300._lib import SGL_FP64
@@ -133,9 +135,10 @@ def test_judge_fallback_takes_exact_values(eng, small):
     Lp = eng.cfb_lnphi(SGL_FP64)
     assert np.max(np.abs(Lall - Lp) / (1.0 + np.abs(Lp))) < 1e-12
     assert np.max(np.abs(Pall - Pp)) <= 1e-10 * np.max(np.abs(Pp))
-    # prefix: exact on n < prefix_p, the surrogate beyond
+    # band: exact on lo_p <= n < lo_p + nk_p, the surrogate elsewhere
     tau = 1e-7
-    Ppre, info = S.judge_sweep(eng, sur, tables, lnmu, threshold=tau, mode="prefix", fallback_precision=SGL_FP64)
+    Ppre, info = S.judge_sweep(eng, sur, tables, lnmu, threshold=tau, mode="band", fallback_precision=SGL_FP64)
+    assert 0 < info["planes_fraction"] and info["fallback_fraction"] < 1
     _, Lpre = eng.sur_pdf(lnmu, precision=SGL_FP64, want_lnphi=True)
     Y = _ensemble(eng, sur, tables)
     off = 0
@@ -143,15 +146,45 @@ def test_judge_fallback_takes_exact_values(eng, small):
         nk = int(tables.nk[i])
         k = np.arange(nk) * tables.dk[i]
         ref = np.zeros(nk, complex)
+        where = {int(p): j for j, p in enumerate(info["fallback"])}
         for p in range(int(tables.inst_plane0[i]), int(tables.inst_plane0[i + 1])):
             sur_p = np.concatenate([[0], tables.dz[p] * SO.plane_H(tables, Y.cpu().numpy(), p, k[1:], sur.shift,
                                                                      sur.scale).mean(0)])
-            npre = int(info["prefix"][p])
-            if npre > 0:
+            if p in where:
+                j = where[p]
+                lo, nb = int(info["fallback_lo"][j]), int(info["fallback_nk"][j])
                 kap, w = tables.plane_cells(p)
                 eng.sweep_set_cells(kap, w)
-                ex = eng.sweep(k[:max(npre, 2)], SGL_FP64)
-                sur_p[:ex.size] = ex
+                sur_p[lo:lo + nb] = eng.sweep(k[lo:lo + nb], SGL_FP64)
             ref += sur_p
         assert np.max(np.abs(Lpre[off:off + nk] - ref) / (1.0 + np.abs(ref))) < 2e-5
         off += nk
+
+
+def test_node_form_matches_plain_solver(eng, small):
+    """Planes solved exactly at their log-spaced nodes and interpolated (the judge's node fallback and the
+    plain solver's node form) reproduce the plain solver on the full k grid; with threshold 0 the judge
+    sends every plane back and equals the node-form plain solver."""
+    from sgl_analytic_gb300 import surrogate as S
+    from sgl_analytic_gb300._lib import SGL_FP64
+    pm, sur, _ = small
+    th, zs = S.sample_instances(2, 21, zs=1.0)
+    tables = S.SweepTables(pm, th, zs, nk=1024)
+    lnmu = np.linspace(-1.0, 9.0, 257)
+    Pn, _ = S.plain_node_pdfs(eng, tables, lnmu, precision=SGL_FP64)
+    _, Ln = eng.sur_pdf(lnmu, precision=SGL_FP64, want_lnphi=True)
+    Pj, info = S.judge_sweep(eng, sur, tables, lnmu, threshold=0.0, mode="nodes", fallback_precision=SGL_FP64)
+    _, Lj = eng.sur_pdf(lnmu, precision=SGL_FP64, want_lnphi=True)
+    assert info["planes_fraction"] == 1.0
+    # the same node values (held as normalised float32 residuals: one rounding of the scaling apart) where
+    # |Phi| does not underflow float32 (beyond, no weighted spread exceeds 0 and the band stops)
+    live = Ln.real > -80.0
+    assert np.max(np.abs(Lj - Ln)[live] / (1.0 + np.abs(Ln[live]))) < 1e-6
+    l1j, _ = S.pdf_errors(Pj, Pn, lnmu)
+    assert l1j.max() < 1e-9
+    Pp, _ = S.plain_pdfs(eng, tables, lnmu, precision=SGL_FP64)
+    Lp = eng.cfb_lnphi(SGL_FP64)
+    # node interpolation: float32 node residuals, 4-point Lagrange in ln q
+    assert np.max(np.abs(Ln - Lp) / (1.0 + np.abs(Lp))) < 1e-5
+    l1, _ = S.pdf_errors(Pn, Pp, lnmu)
+    assert l1.max() < 1e-5
