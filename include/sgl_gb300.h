@@ -329,6 +329,18 @@ sgl_status sgl_sur_pdf(sgl_ctx* ctx, int precision, const double* lnmu, int n_ln
 sgl_status sgl_sur_nodes_exact(sgl_ctx* ctx, int n, const int32_t* planes, const int32_t* node_lo, float* Y,
                                int members, double shift, double scale);
 
+/* Cosmology tables ------------------------------------------------------------------------------------
+ * Replaces the chain's Cosmology (sgl.py:65-640 as pipeline.make_cosmology builds it, pipeline.py:39-79:
+ * EH98 transfer, smooth-k sigma(M) window with the top-hat sigma_8 anchor, Ludlow+16 concentrations, the
+ * growth ODE, radiation Omega_r = Om / (1 + z_eq)) for n cosmologies at once, one CTA each.  params: n x 9
+ * (h, Om, Ob, s8, ns, zeq, Ok, w0, wa), checked against the reference's domain (SGL_ERR_VALUE).  At the nz
+ * ascending redshifts z: E, chi (radial comoving distance, Mpc), DM (transverse), D (growth, D(0) = 1), each
+ * n x nz; at the nm masses M (Msun): sigmaM (sigma(M) at z = 0) and dlnsig (d ln sigma / d ln M), n x nm; at
+ * the nzm redshifts zm: dndlnM (Sheth-Tormen, Mpc^-3) and conc (c_200c), n x nzm x nm.  All host arrays. */
+sgl_status sgl_cosmo_tables(sgl_ctx* ctx, int n, const double* params, int nz, const double* z, int nm, const double* M,
+                            int nzm, const double* zm, double* E, double* chi, double* DM, double* D, double* sigmaM,
+                            double* dlnsig, double* dndlnM, double* conc);
+
 /* Allocation-free entry point ------------------------------------------------------------
  * No counterpart in the reference.  For callers that may not allocate device memory (a host that
  * gives its whole device budget to its own pool or caching allocator, or that forbids third-party

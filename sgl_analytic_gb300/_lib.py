@@ -26,7 +26,7 @@ EXPORTS = ("sgl_abi_version", "sgl_ctx_create", "sgl_ctx_destroy", "sgl_last_err
            "sgl_plan_grid", "sgl_invert", "sgl_batch_create", "sgl_batch_destroy", "sgl_batch_slots",
            "sgl_batch_slot", "sgl_batch_pdf", "sgl_cfb_set", "sgl_cfb_tune", "sgl_cfb_lnphi", "sgl_cfb_pdf",
            "sgl_cfb_set_separable", "sgl_sur_set", "sgl_sur_judge", "sgl_sur_finish", "sgl_sur_pdf", "sgl_sur_nodes_exact",
-           "sgl_cf_kappa_noalloc")
+           "sgl_cosmo_tables", "sgl_cf_kappa_noalloc")
 
 
 class InvertOpts(C.Structure):
@@ -112,6 +112,8 @@ def lib():
         L.sgl_sur_finish.argtypes = [vp, vp, C.c_int, C.c_double, C.c_double, ip, ip]
         L.sgl_sur_pdf.argtypes = [vp, C.c_int, dp, C.c_int, dp, dp]
         L.sgl_sur_nodes_exact.argtypes = [vp, C.c_int, ip, ip, vp, C.c_int, C.c_double, C.c_double]
+        L.sgl_cosmo_tables.argtypes = [vp, C.c_int, dp, C.c_int, dp, C.c_int, dp, C.c_int, dp] + [dp] * 8
+        L.sgl_cosmo_tables.restype = C.c_int
         for name in ("sgl_sur_set", "sgl_sur_judge", "sgl_sur_finish", "sgl_sur_pdf", "sgl_sur_nodes_exact"):
             getattr(L, name).restype = C.c_int
         for name in ("sgl_sweep_set_cells", "sgl_sweep_eval", "sgl_measure_peak"):
@@ -441,6 +443,26 @@ class Engine:
         self._check(self._L.sgl_sweep_eval(self._h, _ptr(kk), kk.size, int(precision), _ptr(re), _ptr(im)),
                     "sgl_sweep_eval")
         return re + 1j * im
+
+    def cosmo_tables(self, params, z, M, zm=()):
+        """Tables of n cosmologies (rows of params: h, Om, Ob, s8, ns, zeq, Ok, w0, wa) -- the reference's
+        chain Cosmology: dict of E, chi, DM, D at z (n x nz), sigmaM, dlnsig at M (n x nm), dndlnM, conc at
+        zm x M (n x nzm x nm)."""
+        p = np.ascontiguousarray(np.atleast_2d(params), np.float64)
+        if p.shape[1] != 9:
+            raise ValueError("params rows are (h, Om, Ob, s8, ns, zeq, Ok, w0, wa)")
+        z, M, zm = (np.ascontiguousarray(np.atleast_1d(a), np.float64) for a in (z, M, zm))
+        n, nz, nm, nzm = p.shape[0], z.size, M.size, zm.size
+        out = {k: np.empty((n, nz)) for k in ("E", "chi", "DM", "D")}
+        out.update(sigmaM=np.empty((n, nm)), dlnsig=np.empty((n, nm)), dndlnM=np.empty((n, max(nzm, 1), nm)),
+                   conc=np.empty((n, max(nzm, 1), nm)))
+        self._check(self._L.sgl_cosmo_tables(self._h, n, _ptr(p), nz, _ptr(z), nm, _ptr(M), nzm,
+                                             _ptr(zm) if nzm else None, *[_ptr(out[k]) for k in
+                                             ("E", "chi", "DM", "D", "sigmaM", "dlnsig", "dndlnM", "conc")]),
+                    "sgl_cosmo_tables")
+        if nzm == 0:
+            del out["dndlnM"], out["conc"]
+        return out
 
     def measure_peak(self, fp64=True):
         t = C.c_double()

@@ -168,6 +168,11 @@ void launch_sur_nodes_exact(int n, const int* planes, const int* node_lo, const 
 void launch_sur_sum(bool judge, const CfbInst* inst, int n_inst, int max_nk, const SurPlane* planes, const float* Y,
                     long long y_member_stride, int members, int nq, float shift, float scale, float tau,
                     const double2* exact, double2* lnphi, unsigned int* dis, int* first, int* last, cudaStream_t st);
+long long cosmo_work_doubles(int nx);
+void launch_cosmo_tables(int n, const double* params, int nz, const double* z, const double* x_out, const int* x_slot,
+                         int nx, int nm, const double* M, int nzm, const double* zm, double A_st, double* E,
+                         double* chi, double* DM, double* D, double* Dm, double* sigM, double* dlnsig,
+                         double* dndlnM, double* conc, double* work, cudaStream_t st);
 void launch_p3_finish(int precision, const void* P3ext, int nkap, int ngam, int ld, const double* gam, double* P3,
                       float* P3f, cudaStream_t st);
 void launch_path_integral(const double* P3, const float* P3f, int nkap, int ngam, double kap0, double kap1,

@@ -356,7 +356,8 @@ class SweepTables:
         return int(self.zl.size)
 
     def features(self, engine):
-        """The ensemble's inputs at every plane's nodes, built on the device: (planes * nq, 8) float32."""
+        """The ensemble's inputs at every plane's nodes (as surrogate.features), built on the device:
+        (planes * nq, 8) float32."""
         import torch
         dev = torch.device("cuda", engine.device)
         with torch.cuda.stream(torch.cuda.ExternalStream(engine.stream, device=dev)):

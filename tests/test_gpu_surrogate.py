@@ -181,7 +181,7 @@ def test_node_form_matches_plain_solver(eng, small):
     live = Ln.real > -80.0
     assert np.max(np.abs(Lj - Ln)[live] / (1.0 + np.abs(Ln[live]))) < 1e-6
     l1j, _ = S.pdf_errors(Pj, Pn, lnmu)
-    assert l1j.max() < 1e-9
+    assert l1j.max() < 1e-7
     Pp, _ = S.plain_pdfs(eng, tables, lnmu, precision=SGL_FP64)
     Lp = eng.cfb_lnphi(SGL_FP64)
     # node interpolation: float32 node residuals, 4-point Lagrange in ln q
