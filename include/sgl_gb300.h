@@ -42,8 +42,9 @@ typedef enum {
     SGL_MIXED = 1   /* float-float phase with exact reduction, FP32 sin/cos/J0, SIMT GEMMs with
                        compensated blocked accumulation and float-float split-K combines, the gauss
                        xi term on tcgen05 (TF32 hi/lo); the k-reach probes sum FP32 terms in FP64.
-                       Bars: PDF L1 <= 1e-4, tail relative error <= 1e-3 (met on the reference's
-                       populations; few-cell, heavy-weight populations want FP64) */
+                       Bars: PDF L1 <= 1e-4, tail relative error <= 1e-3.  sgl_pdf evaluates ln Phi
+                       in FP64 for populations of at most 4096 cells (few heavy cells: FP32 rounding
+                       of single terms does not average out) */
 } sgl_precision;
 
 /* Options of the inversion; defaults = pipeline.run's gauss chain (pipeline.py:221-239). */

@@ -128,10 +128,11 @@ k_cfb_persistent(CfbArgs a) {
         if (I.closure == 0) {
             const double2 s = cfb_cells<MODE, KT>(a, I.c0, I.c1, k, kf, s_c, s_k, s_w);
             lp = make_double2(s.x - 0.5 * I.V * k * k, s.y);
-        } else {
+        } else if (MODE == SGL_FP64) {
             // Poisson sum plus the chain: alpha_t = (sum_s alpha_s K_st) e^{z_t}, z_t = D_pt Lambda_p,
             // rescaled by its largest modulus each plane (the scale kept as a logarithm)
             for (int e = threadIdx.x; e < S * S; e += KT) s_K[e] = a.vp_K[(long long)I.vp_slot * S * S + e];
+            __syncthreads();
             double ar[kCfbMaxStates], ai[kCfbMaxStates];
             double lnsc = 0.0, sr = 0.0, si = 0.0;
             for (int p = I.p0; p < I.p1; ++p) {
@@ -139,53 +140,118 @@ k_cfb_persistent(CfbArgs a) {
                 sr += L.x; si += L.y;
                 const double* D = a.vp_D + (long long)p * S;
                 double br[kCfbMaxStates], bi[kCfbMaxStates];
-                if (p == I.p0) {
-                    for (int t = 0; t < S; ++t) { br[t] = a.vp_w[(long long)I.vp_slot * S + t]; bi[t] = 0.0; }
-                } else {
-                    for (int t = 0; t < S; ++t) {
-                        double xr = 0.0, xi = 0.0;
-                        for (int s2 = 0; s2 < S; ++s2) {
-                            const double Kv = s_K[s2 * S + t];
-                            xr = fma(ar[s2], Kv, xr);
-                            xi = fma(ai[s2], Kv, xi);
+#pragma unroll
+                for (int t = 0; t < kCfbMaxStates; ++t) {
+                    double xr = 0.0, xi = 0.0;
+                    if (p == I.p0) {
+                        xr = t < S ? a.vp_w[(long long)I.vp_slot * S + t] : 0.0;
+                    } else {
+#pragma unroll
+                        for (int s2 = 0; s2 < kCfbMaxStates; ++s2) {
+                            if (s2 < S && t < S) {
+                                const double Kv = s_K[s2 * S + t];
+                                xr = fma(ar[s2], Kv, xr);
+                                xi = fma(ai[s2], Kv, xi);
+                            }
                         }
-                        br[t] = xr; bi[t] = xi;
                     }
+                    br[t] = xr; bi[t] = xi;
                 }
-                // e^{z_t} with the largest Re z taken out into the scale (no overflow); the mixed path
-                // reduces Im z mod 2 pi in FP64 and takes exp / sincos in FP32
+                // e^{z_t} with the largest Re z taken out into the scale (no overflow)
                 double zmax = -1e300;
-                for (int t = 0; t < S; ++t) zmax = fmax(zmax, D[t] * L.x);
+#pragma unroll
+                for (int t = 0; t < kCfbMaxStates; ++t) if (t < S) zmax = fmax(zmax, D[t] * L.x);
                 lnsc += zmax;
                 double mx = 0.0;
-                for (int t = 0; t < S; ++t) {
-                    const double zr = D[t] * L.x - zmax, zi = D[t] * L.y;
-                    double er, ei;
-                    if (MODE == SGL_FP64) {
-                        const double m = exp(zr);
+#pragma unroll
+                for (int t = 0; t < kCfbMaxStates; ++t) {
+                    ar[t] = 0.0; ai[t] = 0.0;
+                    if (t < S) {
+                        const double m = exp(D[t] * L.x - zmax);
                         double sn, cs;
-                        sincos(zi, &sn, &cs);
-                        er = m * cs; ei = m * sn;
-                    } else {
-                        const double red = zi - 6.283185307179586 * rint(zi * 0.15915494309189535);
-                        const float m = expf((float)zr);
-                        float sn, cs;
-                        sincosf((float)red, &sn, &cs);
-                        er = (double)(m * cs); ei = (double)(m * sn);
+                        sincos(D[t] * L.y, &sn, &cs);
+                        const double er = m * cs, ei = m * sn;
+                        ar[t] = br[t] * er - bi[t] * ei;
+                        ai[t] = br[t] * ei + bi[t] * er;
+                        mx = fmax(mx, fabs(ar[t]) + fabs(ai[t]));
                     }
-                    ar[t] = br[t] * er - bi[t] * ei;
-                    ai[t] = br[t] * ei + bi[t] * er;
-                    mx = fmax(mx, fabs(ar[t]) + fabs(ai[t]));
                 }
                 if (mx > 0.0) {
                     const double inv = 1.0 / mx;
-                    for (int t = 0; t < S; ++t) { ar[t] *= inv; ai[t] *= inv; }
+#pragma unroll
+                    for (int t = 0; t < kCfbMaxStates; ++t) { ar[t] *= inv; ai[t] *= inv; }
                     lnsc += log(mx);
                 }
             }
             double tr = 0.0, ti = 0.0;
-            for (int t = 0; t < S; ++t) { tr += ar[t]; ti += ai[t]; }
+#pragma unroll
+            for (int t = 0; t < kCfbMaxStates; ++t) { tr += ar[t]; ti += ai[t]; }
             lp = make_double2(sr + lnsc + 0.5 * log(tr * tr + ti * ti), si + atan2(ti, tr));
+        } else {
+            // the same chain in FP32 registers: z_t = D_pt Lambda_p and its largest real part in FP64, Im z
+            // reduced mod 2 pi in FP64, then exp / sincos, the transition and the products in FP32; the
+            // state is rescaled by a power of two each plane (exact), the exponents summed in FP64
+            float* s_Kf = reinterpret_cast<float*>(s_K);
+            for (int e = threadIdx.x; e < S * S; e += KT) s_Kf[e] = (float)a.vp_K[(long long)I.vp_slot * S * S + e];
+            __syncthreads();
+            float ar[kCfbMaxStates], ai[kCfbMaxStates];
+            double lnsc = 0.0, sr = 0.0, si = 0.0;
+            for (int p = I.p0; p < I.p1; ++p) {
+                const double2 L = cfb_cells<MODE, KT>(a, a.plane_cells[p], a.plane_cells[p + 1], k, kf, s_c, s_k, s_w);
+                sr += L.x; si += L.y;
+                const double* D = a.vp_D + (long long)p * S;
+                float br[kCfbMaxStates], bi[kCfbMaxStates];
+#pragma unroll
+                for (int t = 0; t < kCfbMaxStates; ++t) {
+                    float xr = 0.f, xi = 0.f;
+                    if (p == I.p0) {
+                        xr = t < S ? (float)a.vp_w[(long long)I.vp_slot * S + t] : 0.f;
+                    } else {
+#pragma unroll
+                        for (int s2 = 0; s2 < kCfbMaxStates; ++s2) {
+                            if (s2 < S && t < S) {
+                                const float Kv = s_Kf[s2 * S + t];
+                                xr = fmaf(ar[s2], Kv, xr);
+                                xi = fmaf(ai[s2], Kv, xi);
+                            }
+                        }
+                    }
+                    br[t] = xr; bi[t] = xi;
+                }
+                double zmax = -1e300;
+#pragma unroll
+                for (int t = 0; t < kCfbMaxStates; ++t) if (t < S) zmax = fmax(zmax, D[t] * L.x);
+                lnsc += zmax;
+                float mx = 0.f;
+#pragma unroll
+                for (int t = 0; t < kCfbMaxStates; ++t) {
+                    ar[t] = 0.f; ai[t] = 0.f;
+                    if (t < S) {
+                        const double zi = D[t] * L.y;
+                        const double red = zi - 6.283185307179586 * rint(zi * 0.15915494309189535);
+                        const float m = expf((float)(D[t] * L.x - zmax));
+                        float sn, cs;
+                        sincosf((float)red, &sn, &cs);
+                        const float er = m * cs, ei = m * sn;
+                        ar[t] = br[t] * er - bi[t] * ei;
+                        ai[t] = br[t] * ei + bi[t] * er;
+                        mx = fmaxf(mx, fabsf(ar[t]) + fabsf(ai[t]));
+                    }
+                }
+                if (mx > 0.f) {
+                    int ex;
+                    frexpf(mx, &ex);                        // mx = f 2^ex, f in [1/2, 1)
+                    const float sc = ldexpf(1.f, -ex);
+#pragma unroll
+                    for (int t = 0; t < kCfbMaxStates; ++t) { ar[t] *= sc; ai[t] *= sc; }
+                    lnsc += ex * 0.6931471805599453;
+                }
+            }
+            float tr = 0.f, ti = 0.f;
+#pragma unroll
+            for (int t = 0; t < kCfbMaxStates; ++t) { tr += ar[t]; ti += ai[t]; }
+            const double trd = tr, tid = ti;
+            lp = make_double2(sr + lnsc + 0.5 * log(trd * trd + tid * tid), si + atan2(tid, trd));
         }
         if (live) a.out[I.k_off + n] = lp;
     }

@@ -42,15 +42,22 @@ extern thread_local std::string g_create_error;   // message of the last failed 
 
 struct Arena {                         // grow-only named device buffers
     std::unordered_map<std::string, std::pair<void*, size_t>> bufs;
+    std::unordered_map<std::string, long long> gen;     // per name: which allocation it is
+    long long next_gen = 0;
     void* get(const std::string& name, size_t bytes) {
         auto it = bufs.find(name);
         if (bytes == 0) bytes = 16;
         if (it != bufs.end() && it->second.second >= bytes) return it->second.first;
         if (it != bufs.end()) { cudaFree(it->second.first); bufs.erase(it); }
         void* p = nullptr;
+        gen[name] = ++next_gen;
         if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
         bufs[name] = {p, bytes};
         return p;
+    }
+    long long generation(const std::string& name) const {
+        auto it = gen.find(name);
+        return it == gen.end() ? 0 : it->second;
     }
     void* find(const std::string& name) const {
         auto it = bufs.find(name);
@@ -61,6 +68,7 @@ struct Arena {                         // grow-only named device buffers
 
 struct SepHost {
     double key = -1.0;
+    long long version = 0;                // bumped by every new plan (nodes, columns)
     int n_cells = 0, n_groups = 0, n_cols = 0, n_cols_sep = 0, n_direct = 0;
     std::vector<int> chunk_begin;
     double max_sep_node = 0.0;
@@ -125,6 +133,9 @@ struct sgl_ctx {
     XiDevice xid;
     long long sweep_n = -1;          // cells of the 1-D sweep (sgl_sweep_set_cells)
     std::unordered_map<int, SplineHost> splines;   // not-a-knot collocation inverses by node count
+    // device tables that depend only on a grid or plan (Hankel / kappa matrices, the separable basis):
+    // the key they were built for, with the generation of the arena buffer that holds them
+    std::unordered_map<std::string, std::vector<double>> table_keys;
     // positive (vp) Cox closure replacing the gauss xi term (sgl_vp_set)
     bool vp_on = false;
     VpDevice vpd;
@@ -191,6 +202,18 @@ T* dbuf(sgl_ctx* ctx, const std::string& name, size_t count) {
 #define DBUF(var, T, name, count)                                                             \
     T* var = dbuf<T>(ctx, name, (size_t)(count));                                             \
     if (!var) return fail(ctx, SGL_ERR_CUDA, std::string("device allocation failed: ") + name)
+
+// A device table named `name` built for `key` is current when neither the key nor its buffer's
+// allocation changed since table_built(); the caller rebuilds it otherwise.
+inline bool table_current(sgl_ctx* ctx, const std::string& name, std::vector<double> key) {
+    key.push_back((double)ctx->arena.generation(name));
+    auto it = ctx->table_keys.find(name);
+    return it != ctx->table_keys.end() && it->second == key;
+}
+inline void table_built(sgl_ctx* ctx, const std::string& name, std::vector<double> key) {
+    key.push_back((double)ctx->arena.generation(name));
+    ctx->table_keys[name] = std::move(key);
+}
 
 inline sgl_status sync_stream(sgl_ctx* ctx) {
     CK(cudaStreamSynchronize(ctx->stream));

@@ -9,6 +9,9 @@
 //   sgl_invert     invert a caller-owned Phi given on such a grid.
 #include "host.cuh"
 
+// populations of at most this many cells evaluate ln Phi in FP64 on the mixed path as well
+constexpr long long kMixedFp64LambdaCells = 4096;
+
 namespace sglh {
 
 // the reference's invert grid (sgl_full.py:187-262) for one population: every quantity the
@@ -162,8 +165,17 @@ sgl_status invert_phi(sgl_ctx* ctx, const sgl_invert_opts& o, const GridPlan& G,
     DBUF(d_P3, double, "inv_P3", (long long)nkap * ngam);
     if (!M || !F || !CS || !P3e) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (transforms)");
     const double dkg = kg[1] - kg[0], dkk = kk[1] - kk[0];
-    launch_hankel_matrix(P, d_kg, nkg, dkg, d_gam, ngam, ldF, M, st); CKLAUNCH();
-    launch_kappa_matrix(P, d_kk, nk, dkk, d_kap, nkap, CS, st); CKLAUNCH();
+    // the transform matrices depend on the grid only: kept between PDFs on the same grid
+    const std::vector<double> kM{(double)P, (double)nkg, G.k_g_max, (double)ngam, G.gam_max};
+    if (!table_current(ctx, "inv_M", kM)) {
+        launch_hankel_matrix(P, d_kg, nkg, dkg, d_gam, ngam, ldF, M, st); CKLAUNCH();
+        table_built(ctx, "inv_M", kM);
+    }
+    const std::vector<double> kC{(double)P, (double)nk, G.k_k_max, (double)nkap, G.kap_min, G.kap_max};
+    if (!table_current(ctx, "inv_CS", kC)) {
+        launch_kappa_matrix(P, d_kk, nk, dkk, d_kap, nkap, CS, st); CKLAUNCH();
+        table_built(ctx, "inv_CS", kC);
+    }
     // mixed path: the transform sums run in >= 4 K-slices combined in float-float; within a slice
     // the FP32 kernel's compensated blocked accumulation bounds the chain's rounding
     constexpr int kTransformSplit = 4;
@@ -293,7 +305,18 @@ sgl_status sgl_pdf(sgl_ctx* ctx, const double* xi_out, int n_xi, const sgl_inver
     // ---- Phi = exp(ln Phi) on the full grid
     void* Phi = ctx->arena.get("phi", 2ULL * nk * nkg * es);
     if (!Phi) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (phi)");
-    CKS(lambda_eval(ctx, o.precision, kk.data(), nk, kg.data(), nkg, 1, Phi, (char*)Phi + (size_t)nk * nkg * es));
+    if (o.precision == SGL_MIXED && (long long)ctx->w0.size() <= kMixedFp64LambdaCells) {
+        // few cells: ln Phi is a sum of few large terms whose FP32 rounding does not average out (on a
+        // 300-cell population carrying the weight of 80k the mixed tail error was 1.2e-3 with FP32
+        // Lambda, 7.6e-4 with FP64 Lambda and FP32 transforms); for so few cells FP64 Lambda is cheap
+        const long long npt = (long long)nk * nkg;
+        DBUF(stage, double, "phi_in", 2 * npt);
+        CKS(lambda_eval(ctx, SGL_FP64, kk.data(), nk, kg.data(), nkg, 1, stage, stage + npt));
+        launch_phi_to_f32(stage, 2 * npt, (float*)Phi, ctx->stream);
+        CKLAUNCH();
+    } else {
+        CKS(lambda_eval(ctx, o.precision, kk.data(), nk, kg.data(), nkg, 1, Phi, (char*)Phi + (size_t)nk * nkg * es));
+    }
     return invert_phi(ctx, o, G, Phi, xi_out, n_xi, P_out, meta);
 }
 

@@ -191,7 +191,7 @@ sgl_status build_sep(sgl_ctx* ctx, double key, int nk) {
     cb.push_back((int)N);
 
     SepHost& S = ctx->sep;
-    S.key = key; S.n_cells = (int)N; S.n_groups = n_groups; S.n_cols_sep = n_cols_sep;
+    S.key = key; S.version++; S.n_cells = (int)N; S.n_groups = n_groups; S.n_cols_sep = n_cols_sep;
     S.n_cols = n_cols_sep + (int)n_dir; S.n_direct = (int)n_dir; S.chunk_begin = cb; S.max_sep_node = maxnode;
 
     ht.lap("sep_chunks");
@@ -497,19 +497,31 @@ sgl_status sep_gemms(sgl_ctx* ctx, int precision, const double* h_kg, const doub
     if (S.n_cols_sep > 0) {
         if (nkg > 1 && Nch > 0 && Nch < 0.6 * nkg && h_kg[0] >= 0.0) {
             DBUF(d_t, double, "cheb_t", Nch);
-            launch_cheb_points(Kg, Nch, d_t, st); CKLAUNCH();
             void* Bc = ctx->arena.get("cheb_B", (size_t)S.n_cols_sep * Nch * sizeof(TT));
             void* L = ctx->arena.get("cheb_L", (size_t)nkg * Nch * sizeof(TT));
             void* U = ctx->arena.get("cheb_U", (size_t)ld * Nch * sizeof(TT));
             if (!Bc || !L || !U) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (cheb)");
-            launch_j0m1_table(precision, d_nodes, S.n_cols_sep, d_t, Nch, Bc, st); CKLAUNCH();
-            launch_cheb_matrix(precision, Kg, Nch, d_t, d_kg, nkg, L, st); CKLAUNCH();
+            // the basis tables depend on the plan and the k_gamma grid only: kept between PDFs
+            std::vector<double> key{(double)precision, (double)S.version, Kg, (double)Nch,
+                                    (double)ctx->arena.generation("cheb_t"), (double)ctx->arena.generation("cheb_L")};
+            key.insert(key.end(), h_kg, h_kg + nkg);
+            if (!table_current(ctx, "cheb_B", key)) {
+                launch_cheb_points(Kg, Nch, d_t, st); CKLAUNCH();
+                launch_j0m1_table(precision, d_nodes, S.n_cols_sep, d_t, Nch, Bc, st); CKLAUNCH();
+                launch_cheb_matrix(precision, Kg, Nch, d_t, d_kg, nkg, L, st); CKLAUNCH();
+                table_built(ctx, "cheb_B", key);
+            }
             CKS(gemm_splitk<TT>(ctx, gd<TT>((int)ld, Nch, S.n_cols_sep, Tt, 1, ld, Bc, Nch, 1, U, Nch), "sep1", msplit));
             CKS(gemm_splitk<TT>(ctx, gd<TT>((int)ld, nkg, Nch, U, Nch, 1, L, 1, Nch, Gout, nkg), "sep2", msplit));
         } else {
             void* Bn = ctx->arena.get("sep_Bn", (size_t)S.n_cols_sep * nkg * sizeof(TT));
             if (!Bn) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (Bn)");
-            launch_j0m1_table(precision, d_nodes, S.n_cols_sep, d_kg, nkg, Bn, st); CKLAUNCH();
+            std::vector<double> key{(double)precision, (double)S.version};
+            key.insert(key.end(), h_kg, h_kg + nkg);
+            if (!table_current(ctx, "sep_Bn", key)) {
+                launch_j0m1_table(precision, d_nodes, S.n_cols_sep, d_kg, nkg, Bn, st); CKLAUNCH();
+                table_built(ctx, "sep_Bn", key);
+            }
             CKS(gemm_splitk<TT>(ctx, gd<TT>((int)ld, nkg, S.n_cols_sep, Tt, 1, ld, Bn, nkg, 1, Gout, nkg), "sep1", msplit));
         }
     } else {
@@ -518,7 +530,12 @@ sgl_status sep_gemms(sgl_ctx* ctx, int precision, const double* h_kg, const doub
     if (S.n_direct > 0) {
         void* Bd = ctx->arena.get("sep_Bd", (size_t)S.n_direct * nkg * sizeof(TT));
         if (!Bd) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (Bd)");
-        launch_j0m1_table(precision, d_nodes + S.n_cols_sep, S.n_direct, d_kg, nkg, Bd, st); CKLAUNCH();
+        std::vector<double> key{(double)precision, (double)S.version};
+        key.insert(key.end(), h_kg, h_kg + nkg);
+        if (!table_current(ctx, "sep_Bd", key)) {
+            launch_j0m1_table(precision, d_nodes + S.n_cols_sep, S.n_direct, d_kg, nkg, Bd, st); CKLAUNCH();
+            table_built(ctx, "sep_Bd", key);
+        }
         const TT* Td = (const TT*)Tt + (long long)S.n_cols_sep * ld;
         CKS(gemm_splitk<TT>(ctx, gd<TT>((int)ld, nkg, S.n_direct, Td, 1, ld, Bd, nkg, 1, Gout, nkg, 1.0, 1.0), "sep3", msplit));
     }
@@ -755,7 +772,9 @@ sgl_status sgl_lam_set_cells(sgl_ctx* ctx, int64_t n_cells, const double* w0, co
     CKS(upload(ctx, dg, g0, (size_t)n_cells));
     CKS(upload(ctx, dw, w0, (size_t)n_cells));
     CK(cudaStreamSynchronize(ctx->stream));
+    const long long sep_version = ctx->sep.version;
     ctx->sep = SepHost();
+    ctx->sep.version = sep_version + 1;            // tables built for the old plan are stale
     ctx->sep_precision_ready = -1;
     ctx->has_cells = true;
     return SGL_OK;

@@ -317,13 +317,11 @@ def test_grid_above_block_threshold_matches_reference(precision):
     if precision == "fp64":
         assert dpeak <= TOL_PEAK, dpeak
     else:
-        # 300 cells carrying the weight of 80k: ln Phi is a sum of few large terms.  The worst
-        # tail point sits at 1.0e-6 of the peak, where the mixed path's FP32 noise (about equal
-        # parts Lambda and inversion; no single stage dominates when run in FP64) leaves a
-        # relative error of 1.2e-3 to 1.7e-3.  The L1 bar holds; the tail bar is met on the
-        # reference's own populations (z_s = 0.5, 1, 3, 10), not on this one.
+        # 300 cells carrying the weight of 80k: ln Phi is a sum of few large terms, and the worst
+        # tail point sits at 1.0e-6 of the peak.  The mixed path evaluates ln Phi in FP64 for so
+        # few cells (FP32 transforms): tail 7.6e-4 (1.2e-3 with FP32 ln Phi).
         assert l1 <= 1e-4, (dpeak, l1, rel_tail)
-        assert rel_tail <= 3e-3, (dpeak, l1, rel_tail)
+        assert rel_tail <= 1e-3, (dpeak, l1, rel_tail)
 
 
 @pytest.mark.parametrize("zs", ["3", "10", "0.5"])
