@@ -651,10 +651,13 @@ def main():
                                  pop.xg_idx, pop.xg_rows, pop.ce_k, pop.ce_g))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    e2e_P = []
+    e2e_P, e2e_split = [], []
     for _ in range(args.e2e_steps):
+        ta = time.perf_counter()
         lam_e = Lam(pop, xi=True, engine=eng, precision=args.precision)
+        tb = time.perf_counter()
         _, Pe, _ = invert(lam_e, lam_e.sigma(), xi_out=XI_OUT, phi_tol=1e-8, precision=args.precision)
+        e2e_split.append((tb - ta, time.perf_counter() - tb))
         e2e_P.append(Pe)
     torch.cuda.synchronize()
     e2e = args.e2e_steps / (time.perf_counter() - t0)
@@ -722,6 +725,8 @@ def main():
                 "batched": batched,
                 "fp64_path": fp64_line,
                 "e2e": {"value": e2e, "unit": "PDF/s", "h2d_bytes_per_step": int(h2d),
+                        "ms_lam_median": 1e3 * float(np.median([a for a, _ in e2e_split])) if e2e_split else None,
+                        "ms_invert_median": 1e3 * float(np.median([b for _, b in e2e_split])) if e2e_split else None,
                         "d2h_bytes_per_step": int(XI_OUT.size * 8)},
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches * 1,
                 "stage_ms": meta.get("device_ms"), "kernels": tags}
