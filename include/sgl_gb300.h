@@ -209,6 +209,13 @@ sgl_status sgl_mlp_act_grad(sgl_ctx* ctx, int M, int N, const float* dA, const f
 sgl_status sgl_mlp_col_sum(sgl_ctx* ctx, int M, int N, const float* X, float* out);
 sgl_status sgl_mlp_mse(sgl_ctx* ctx, int64_t n, const float* pred, const float* target, float* dpred,
                        double* loss);
+/* sgl_mlp_infer: the trained 8 -> 6 x 256 SiLU -> 2 network's forward pass in one fused persistent kernel
+ * (activations kept on chip as BF16 hi / lo parts, weights streamed by bulk copies, accumulation in TMEM):
+ * X (n x 8) -> Y (n x 2), device float32; W, b: host arrays of the 7 layers' device pointers (W[l] in x out
+ * row-major FP32 masters, rounded to BF16 as the training forward's GEMMs use them; b[l] FP32).  The
+ * arithmetic is the training forward's (split BF16 inputs, BF16 weights, FP32 accumulation). */
+sgl_status sgl_mlp_infer(sgl_ctx* ctx, int n, const float* X, int n_layers, const float* const* W, const float* const* b,
+                         float* Y);
 sgl_status sgl_mlp_adamw(sgl_ctx* ctx, int64_t n, float* w, const float* g, float* m, float* v, float lr,
                          float b1, float b2, float eps, float wd, int step);
 

@@ -23,6 +23,7 @@ EXPORTS = ("sgl_abi_version", "sgl_ctx_create", "sgl_ctx_destroy", "sgl_last_err
            "sgl_lam_set_xi", "sgl_lam_sigma", "sgl_lnphi", "sgl_xi_term", "sgl_sweep_set_cells", "sgl_sweep_eval", "sgl_measure_peak",
            "sgl_vp_set", "sgl_vp_build", "sgl_vp_lnR", "sgl_invert_opts_default", "sgl_pdf",
            "sgl_gemm_bf16", "sgl_mlp_bias_act", "sgl_mlp_act_grad", "sgl_mlp_col_sum", "sgl_mlp_mse", "sgl_mlp_adamw",
+           "sgl_mlp_infer",
            "sgl_plan_grid", "sgl_invert", "sgl_batch_create", "sgl_batch_destroy", "sgl_batch_slots",
            "sgl_batch_slot", "sgl_batch_pdf", "sgl_cfb_set", "sgl_cfb_tune", "sgl_cfb_lnphi", "sgl_cfb_pdf",
            "sgl_cfb_set_separable", "sgl_sur_set", "sgl_sur_judge", "sgl_sur_finish", "sgl_sur_pdf", "sgl_sur_nodes_exact",
@@ -125,6 +126,8 @@ def lib():
         L.sgl_mlp_col_sum.argtypes = [vp, C.c_int, C.c_int, vp, vp]
         L.sgl_mlp_mse.argtypes = [vp, i64, vp, vp, vp, dp]
         L.sgl_mlp_adamw.argtypes = [vp, i64, vp, vp, vp, vp, f32, f32, f32, f32, f32, C.c_int]
+        L.sgl_mlp_infer.argtypes = [vp, C.c_int, vp, C.c_int, C.POINTER(vp), C.POINTER(vp), vp]
+        L.sgl_mlp_infer.restype = C.c_int
         for name in ("sgl_gemm_bf16", "sgl_mlp_bias_act", "sgl_mlp_act_grad", "sgl_mlp_col_sum", "sgl_mlp_mse",
                      "sgl_mlp_adamw"):
             getattr(L, name).restype = C.c_int

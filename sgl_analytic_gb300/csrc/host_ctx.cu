@@ -169,6 +169,32 @@ sgl_status sgl_mlp_col_sum(sgl_ctx* ctx, int M, int N, const float* X, float* ou
     return SGL_OK;
 }
 
+sgl_status sgl_mlp_infer(sgl_ctx* ctx, int n, const float* X, int n_layers, const float* const* W, const float* const* b,
+                         float* Y) {
+    if (!ctx) return SGL_ERR_VALUE;
+    if (n < 0 || !X || !W || !b || !Y) return fail(ctx, SGL_ERR_VALUE, "sgl_mlp_infer: invalid arguments");
+    if (n_layers != 7) return fail(ctx, SGL_ERR_UNSUPPORTED, "sgl_mlp_infer: the fused kernel is 8 -> 6 x 256 SiLU -> 2");
+    for (int l = 0; l < 7; ++l)
+        if (!W[l] || !b[l]) return fail(ctx, SGL_ERR_VALUE, "sgl_mlp_infer: NULL weight or bias");
+    if (n == 0) return SGL_OK;
+    CK(cudaSetDevice(ctx->device));
+    static thread_local int attr_device = -1;
+    if (attr_device != ctx->device) {
+        if (mlp_fused_attr() != SGL_OK) return fail(ctx, SGL_ERR_CUDA, "sgl_mlp_infer: shared-memory attribute");
+        attr_device = ctx->device;
+    }
+    DBUF(Wp, unsigned char, "mlp_Wp", mlp_fused_wp_bytes());
+    DBUF(small, float, "mlp_small", mlp_fused_small_floats());
+    DBUF(ptrs, const float*, "mlp_ptrs", 11);
+    const float* hp[11] = {W[1], W[2], W[3], W[4], W[5], b[0], b[1], b[2], b[3], b[4], b[5]};
+    CKS(upload(ctx, ptrs, hp, 11));
+    int* err = dev_err_flag(ctx);
+    if (!err) return fail(ctx, SGL_ERR_CUDA, "device allocation failed (error flag)");
+    launch_mlp_fused(n, X, W, b, Wp, small, ptrs, Y, err, kNumSMs, ctx->stream);
+    CKLAUNCH();
+    return check_dev_err(ctx);
+}
+
 sgl_status sgl_mlp_mse(sgl_ctx* ctx, int64_t n, const float* pred, const float* target, float* dpred, double* loss) {
     if (!ctx || n < 1 || !pred || !target || !dpred || !loss) return SGL_ERR_VALUE;
     const int nb = mse_blocks(n);

@@ -214,6 +214,12 @@ void launch_xi_stageA_pack(const XiDevice& x, const long long* d_p_prefix, const
                            float* packed, cudaStream_t st);
 
 // ---- surrogate MLP element-wise kernels
+int mlp_fused_smem();
+int mlp_fused_small_floats();
+long long mlp_fused_wp_bytes();
+sgl_status mlp_fused_attr();
+void launch_mlp_fused(int n, const float* X, const float* const* W_dev, const float* const* b_dev, unsigned char* Wp,
+                      float* small, const float** ptrs, float* Y, int* err, int ctas, cudaStream_t st);
 void launch_bias_act(int M, int N, const float* Z, const float* bias, float* Zb, float* A, int silu, cudaStream_t st);
 void launch_act_grad(int M, int N, const float* dA, const float* Zb, float* dZ, cudaStream_t st);
 void launch_col_sum(int M, int N, const float* X, float* out, cudaStream_t st);

@@ -218,6 +218,21 @@ class MLP:
                 tot, cnt = 0.0, 0
         return hist
 
+    def infer(self, X):
+        """Forward pass of the trained network in the engine's fused kernel (sgl_mlp_infer): the same
+        arithmetic as forward(), one launch.  X: (n, 8) float32 device tensor -> (n, 2)."""
+        import ctypes as C
+        torch, e = self.torch, self.eng
+        if self.sizes != [8] + [256] * 6 + [2]:
+            return self.forward(X)
+        with torch.cuda.stream(self.stream):
+            Xc = X.contiguous()
+            Y = torch.empty((X.shape[0], 2), device=self.dev)
+        Wp = (C.c_void_p * 7)(*[w.data_ptr() for w in self.W])
+        bp = (C.c_void_p * 7)(*[b.data_ptr() for b in self.b])
+        e._check(e._L.sgl_mlp_infer(e._h, int(X.shape[0]), Xc.data_ptr(), 7, Wp, bp, Y.data_ptr()), "sgl_mlp_infer")
+        return Y
+
     def predict(self, X, batch=65536, host=False):
         """Outputs for X (device tensor).  host=True returns a NumPy array after the engine's stream
         has finished (torch's own streams are not ordered after the engine's kernels)."""
@@ -488,7 +503,7 @@ def judge_sweep(engine, sur, tables, lnmu, threshold=1e-5, mode="nodes", fallbac
                    tables.hq, tables.nq)
     X = tables.features(engine)
     with torch.cuda.stream(torch.cuda.ExternalStream(engine.stream, device=X.device)):
-        Y = torch.stack([m.forward(X) for m in sur.mlps]).contiguous()
+        Y = torch.stack([m.infer(X) for m in sur.mlps]).contiguous()
     dis, band = engine.sur_judge(Y, len(sur.mlps), sur.shift, sur.scale, threshold)
     t["judge"] = time.perf_counter() - t0
     nk_pl = tables.nk[tables.plane_inst]

@@ -188,3 +188,20 @@ def test_node_form_matches_plain_solver(eng, small):
     assert np.max(np.abs(Ln - Lp) / (1.0 + np.abs(Lp))) < 1e-5
     l1, _ = S.pdf_errors(Pn, Pp, lnmu)
     assert l1.max() < 1e-5
+
+
+def test_fused_inference_matches_layerwise_forward(eng):
+    """sgl_mlp_infer (one fused kernel, activations on chip) against the layer-by-layer forward of the
+    same network (the training forward's arithmetic), on a ragged number of rows."""
+    import torch
+    from sgl_analytic_gb300 import surrogate as S
+    mlp = S.MLP(eng, width=256, depth=6, seed=5)
+    rng = np.random.default_rng(4)
+    for n in (1, 300, 4097):
+        (Xd,) = S.to_device(eng, rng.uniform(-1, 1, (n, 8)).astype(np.float32))
+        ref = mlp.forward(Xd)
+        got = mlp.infer(Xd)
+        mlp.stream.synchronize()
+        r, g = ref.cpu().numpy(), got.cpu().numpy()
+        assert g.shape == (n, 2)
+        assert np.max(np.abs(g - r)) <= 1e-4 * max(1.0, np.max(np.abs(r))), n
