@@ -172,8 +172,11 @@ k_mlp_fused(int n, const float* __restrict__ X, const unsigned char* __restrict_
             fence_proxy_async_smem();
             mbar_arrive(b_ready);
             float y0 = 0.f, y1 = 0.f;
+            bool bad = false;
             for (int l = 0; l < kMfHidden; ++l, ++use) {
-                if (*s_fail || !mbar_wait_bounded(b_done, (uint32_t)(use & 1))) { *s_fail = 1; break; }
+                // the decision to stop is the whole warp's: tcgen05.ld below is warp-collective
+                bad = *s_fail != 0 || !mbar_wait_bounded(b_done, (uint32_t)(use & 1));
+                if (__any_sync(0xffffffffu, bad)) { bad = true; *s_fail = 1; break; }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const float* bl = s_b + (l + 1) * kMfW;
                 for (int c0 = 0; c0 < kMfW; c0 += 16) {
@@ -198,7 +201,7 @@ k_mlp_fused(int n, const float* __restrict__ X, const unsigned char* __restrict_
                     mbar_arrive(b_ready);
                 }
             }
-            if (*s_fail) break;
+            if (bad) break;
             if (gr < n) {
                 Y[2 * gr] = y0 + s_b6[0];
                 Y[2 * gr + 1] = y1 + s_b6[1];
