@@ -119,6 +119,8 @@ struct sgl_ctx {
     std::string err;
     CfbState* cfb = nullptr;
     SurState* sur = nullptr;
+    // batched solver launch shapes found by the autotuner, per precision and batch shape class
+    std::unordered_map<long long, std::pair<int, int>> cfb_shapes;
     Arena arena;
     // population (host copies)
     std::vector<double> w0, k0, g0, fe_g;

@@ -6,12 +6,14 @@
 // No counterpart in the reference, which solves one pipeline.run per instance
 // (pipeline.py:114-274).
 #include <chrono>
+#include <cmath>
 #include <numeric>
 
 #include "host.cuh"
 
 struct CfbState {
     int n_inst = 0, n_planes = 0, nstate = 0;
+    int shape_class = 0;                       // log2 buckets of the largest k grid and the mean cells
     long long n_cells = 0, total_k = 0;
     std::vector<CfbInst> inst;
     std::vector<double> cost;                  // per instance: cells x k (+ chain) work
@@ -104,6 +106,7 @@ sgl_status cfb_tune(sgl_ctx* ctx, int precision) {
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     S.tuned[P] = true;
+    ctx->cfb_shapes[2LL * S.shape_class + P] = {S.kt[P], S.cps[P]};
     return sync_stream(ctx);
 }
 
@@ -133,13 +136,9 @@ sgl_status cfb_tables(sgl_ctx* ctx, int n_inst, const int32_t* inst_plane0, cons
         return fail(ctx, SGL_ERR_VALUE, "sgl_cfb_set: vp instances need 2..8 chain states and their tables");
     CK(cudaSetDevice(ctx->device));
     CKS(sync_stream(ctx));
-    CfbState* prev = ctx->cfb;
+    if (ctx->cfb) cfb_state_free(ctx->cfb);
     ctx->cfb = new CfbState();
     CfbState& S = *ctx->cfb;
-    if (prev) {                       // a new batch keeps the launch shapes tuned so far
-        for (int q = 0; q < 2; ++q) { S.kt[q] = prev->kt[q]; S.cps[q] = prev->cps[q]; S.tuned[q] = prev->tuned[q]; }
-        cfb_state_free(prev);
-    }
     S.n_inst = n_inst; S.n_planes = n_planes; S.nstate = n_vp > 0 ? nstate : 0; S.n_cells = nc;
     S.inst.resize((size_t)n_inst);
     S.cost.resize((size_t)n_inst);
@@ -159,6 +158,19 @@ sgl_status cfb_tables(sgl_ctx* ctx, int n_inst, const int32_t* inst_plane0, cons
     }
     k_offs[(size_t)n_inst] = koff;
     S.total_k = koff;
+    // batches of the same shape class (largest k grid, mean cells per instance, both in powers of
+    // two) reuse the launch shapes the autotuner found for the first of them
+    {
+        int max_nk = 0;
+        for (int i = 0; i < n_inst; ++i) max_nk = std::max(max_nk, nk[i]);
+        const int kb = (int)std::ceil(std::log2((double)max_nk));
+        const int cb = (int)std::ceil(std::log2(std::max(1.0, (double)nc / n_inst)));
+        S.shape_class = 100 * kb + cb;
+        for (int q = 0; q < 2; ++q) {
+            auto it = ctx->cfb_shapes.find(2LL * S.shape_class + q);
+            if (it != ctx->cfb_shapes.end()) { S.kt[q] = it->second.first; S.cps[q] = it->second.second; S.tuned[q] = true; }
+        }
+    }
     S.order.resize((size_t)n_inst);
     std::iota(S.order.begin(), S.order.end(), 0);
     std::stable_sort(S.order.begin(), S.order.end(), [&](int x, int y) { return S.cost[(size_t)x] > S.cost[(size_t)y]; });
