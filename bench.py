@@ -510,6 +510,89 @@ def run_surrogate(args, rank, world, local):
         print(json.dumps(line))
 
 
+def run_cells(args, rank, world, local):
+    """Population-build deposit: each step is one lens-redshift node of emitter-shaped objects (2048
+    pseudo-elliptical truncated NFW hosts of 12 x 260 cells and 512 filaments of 120 x 12, 7.1e6 points
+    with lens distances) binned into the fine and coarse lattices and the xi_lin node (42 k_perp nodes,
+    m <= 2), then the node's row compression.  value: points per second of device time (the deposit
+    kernels, inputs resident); e2e: the same through Cells.add_many from host arrays, per wall second."""
+    import torch
+    from sgl_analytic_gb300.cells import Cells
+    from sgl_analytic_gb300.workloads import deposit_node
+    torch.cuda.set_device(local)
+    objs, dchi = deposit_node(seed=rank)
+    g = np.load(ROOT / "tests" / "golden" / "cells_ref.npz")
+    xi = dict(kp=g["xi_kp"], c=g["xi_c"], mmax=2)
+    cells = Cells(1, 1, xi=xi, device=local)
+    eng = cells.engine
+    npts = int(sum(o["K"].size for o in objs))
+
+    def node():
+        cells.xi_groups = []
+        cells.xi_begin(dchi)
+        cells.add_many(objs)
+        cells.xi_end(0)
+
+    for _ in range(max(3, args.warmup)):
+        node()
+    clocks = Clocks(local)
+    torch.cuda.synchronize()
+    clocks.start()
+    eng.stats(reset=True)
+    eng.profile(True)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        node()
+    wall = time.perf_counter() - t0
+    eng.profile(False)
+    st = eng.stats(reset=True)
+    clk = clocks.stop()
+    ms_hist = st["cells_hist"]["ms"] / args.steps
+    ms_xi = st["cells_xi"]["ms"] / args.steps
+    ms_dev = ms_hist + ms_xi
+    launches = int(st.get("_launches", {}).get("launches", 0))
+    f64 = eng.measure_peak(True)
+    pk, pk_src = peaks()
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle.cells_oracle import CellsOracle
+        sample = objs[:48] + objs[-16:]
+        o = CellsOracle(1, 1, xi=xi)
+        o.xi_begin(dchi)
+        tc = time.perf_counter()
+        for ob in sample:
+            o.add(ob["K"], ob["G"], ob["W"], 0, ob["beta"], R=ob["R"], tang=ob["tang"])
+        o.xi_end(0)
+        dtc = time.perf_counter() - tc
+        ns = sum(ob["K"].size for ob in sample)
+        cpu = {"value": ns / dtc, "unit": "points/s", "cores": 1, "kind": "port",
+               "sample": f"{len(sample)} of the node's objects ({ns} points) through the NumPy oracle, one core"}
+    if rank == 0:
+        hist_gbs = 24.0 * npts / (ms_hist / 1e3) / 1e9
+        line = {"metric": "population-build deposit: points/sec binned into the lattices and the xi_lin node",
+                "value": world * npts / (ms_dev / 1e3), "unit": "points/s", "n_gpus": world, "steps": args.steps,
+                "warmup": max(3, args.warmup), "ms_per_step": ms_dev, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded emitter-shaped objects)",
+                "config": {"workload": "one lens-redshift node: 2048 elliptical truncated NFW hosts (12 x 260 cells) + "
+                                       "512 filaments (120 x 12), fine 961 x 300 and coarse 341 x 110 lattices, "
+                                       "xi_lin on 42 k_perp nodes, m <= 2",
+                           "points": npts, "objects": len(objs),
+                           "l2": "inputs 32 B per point (228 MB) larger than L2"},
+                "kernels_ms_per_step": {"k_cells_hist": ms_hist, "k_cells_xi": ms_xi},
+                "e2e": {"value": world * npts * args.steps / wall, "unit": "points/s",
+                        "h2d_bytes_per_step": 32 * npts, "d2h_bytes_per_step": int(sum(
+                            np.asarray(gr["rows"]).nbytes for gr in cells.xi_groups))},
+                "roofline": {"kernel": "k_cells_xi (FP64 Bessel J0/J2/J4 per point x 42 nodes, FP64 atomics)",
+                             "bound": "fp64-pipe", "achieved": None, "peak": f64, "unit": "TFLOP/s",
+                             "frac": None, "traffic": None,
+                             "hist": {"kernel": "k_cells_hist", "bound": "hbm", "achieved": hist_gbs,
+                                      "peak": float(pk["hbm_gbs"]), "unit": "GB/s",
+                                      "frac": hist_gbs / float(pk["hbm_gbs"]), "bytes_per_point": 24,
+                                      "peak_source": f"{pk_src} hbm_gbs"}},
+                "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk}
+        print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -522,7 +605,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=10)
-    ap.add_argument("--workload", default="zs1_pdf", choices=("zs1_pdf", "cf_sweep", "surrogate", "batched"))
+    ap.add_argument("--workload", default="zs1_pdf", choices=("zs1_pdf", "cf_sweep", "surrogate", "batched", "cells"))
     ap.add_argument("--batch-instances", type=int, default=4096)
     ap.add_argument("--sur-steps", type=int, default=12000)
     ap.add_argument("--sur-instances", type=int, default=512)
@@ -539,9 +622,9 @@ def main():
             dist.destroy_process_group()
         return
 
-    if args.workload in ("cf_sweep", "surrogate", "batched"):
-        {"cf_sweep": run_cf_sweep, "surrogate": run_surrogate, "batched": run_batched}[args.workload](args, rank, world,
-                                                                                                    local)
+    if args.workload in ("cf_sweep", "surrogate", "batched", "cells"):
+        {"cf_sweep": run_cf_sweep, "surrogate": run_surrogate, "batched": run_batched,
+         "cells": run_cells}[args.workload](args, rank, world, local)
         if world > 1:
             import torch.distributed as dist
             dist.destroy_process_group()

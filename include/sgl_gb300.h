@@ -349,6 +349,43 @@ sgl_status sgl_cosmo_tables(sgl_ctx* ctx, int n, const double* params, int nz, c
                             int nzm, const double* zm, double* E, double* chi, double* DM, double* D, double* sigmaM,
                             double* dlnsig, double* dndlnM, double* conc);
 
+/* Binned-cell deposit of the population build ------------------------------------------------------------
+ * Replaces the build's Cells accumulator (sgl_full.py:1282-1533): every emitter's points binned on the fine
+ * and coarse (kappa, gamma) lattices, which stay in device memory between calls.
+ * sgl_cells_init starts a build (the context holds one): nshell shells, moments n = 0..nord, the lattices'
+ * edges (ascending; kappa signed-log, gamma geometric, as Cells.fe / Cells.ce, sgl_full.py:1293-1294; at most
+ * 6144 edges in all), gamma clipped below at g_clip (sgl_full.py:1324: 1.0000001 x the fine grid's lowest
+ * gamma), and k_max_fine, the |kappa| bound of the linear sums (the fine grid's top kappa).
+ * sgl_cells_add deposits n_obj objects in order (Cells.add, sgl_full.py:1314-1385): object o is points
+ * off[o] .. off[o + 1] - 1 of K, G, W (and R), in shell[o] with bias weight beta[o] (finite) and tangential
+ * shear tang[o] (NULL = all tangential).  Bins are searchsorted(side='right') with the last edge in the last
+ * bin, exactly; a point adds w, w kappa, w gamma to its fine bin and w beta^n to its coarse bin of its shell.
+ * sums (n_obj x 3, host) receives each object's total w, w inside the fine lattice, and w kappa over
+ * |kappa| < k_max_fine, from which the caller keeps N, dropped and lin.  Bin sums are FP64 atomics: the
+ * reference's sums in another order.  All point arrays are host arrays.
+ * sgl_cells_xi_init turns on the xi_lin term (Cells(xi=...), sgl_full.py:2483-2512): nkp <= 64 k_perp nodes
+ * kp with weights c, mmax <= 2, pos = 1 for the positive closure's rate deposit; every deposit then needs R
+ * (the lens distance of each point, Mpc) inside a node opened by sgl_cells_xi_begin (dchi, Mpc) and closed by
+ * sgl_cells_xi_end (sgl_full.py:1478-1523), which compresses the node into *n_groups row groups fetched by
+ * sgl_cells_xi_group (m, nidx, nrow; then idx nidx ints, rows nrow x (nidx + 1), for m = 0 with pos also W
+ * nidx and v0 nkp; any output may be NULL).  Rows are fixed up to sign and rotation within the kept modes.
+ * sgl_cells_xi_shear_tail adds the analytic shear tail beyond radius Rm (sgl_full.py:1466-1476).
+ * sgl_cells_read copies the lattices out: H0, H0k, H0g (fine, nkf x ngf) and Hc (nshell x (nord+1) x nkc x
+ * ngc); any may be NULL. */
+sgl_status sgl_cells_init(sgl_ctx* ctx, int nshell, int nord, int nekf, const double* ekf, int negf,
+                          const double* egf, int nekc, const double* ekc, int negc, const double* egc,
+                          double g_clip, double k_max_fine);
+sgl_status sgl_cells_add(sgl_ctx* ctx, int n_obj, const int64_t* off, const double* K, const double* G,
+                         const double* W, const double* R, const int32_t* shell, const double* beta,
+                         const unsigned char* tang, double* sums);
+sgl_status sgl_cells_xi_init(sgl_ctx* ctx, int nkp, const double* kp, const double* c, int mmax, int pos);
+sgl_status sgl_cells_xi_begin(sgl_ctx* ctx, double dchi);
+sgl_status sgl_cells_xi_shear_tail(sgl_ctx* ctx, double beta, double Gam, double Rm, double n_area);
+sgl_status sgl_cells_xi_end(sgl_ctx* ctx, int* n_groups);
+sgl_status sgl_cells_xi_group(sgl_ctx* ctx, int g, int32_t* m, int32_t* nidx, int32_t* nrow, int32_t* idx,
+                              double* rows, double* W, double* v0);
+sgl_status sgl_cells_read(sgl_ctx* ctx, double* H0, double* H0k, double* H0g, double* Hc);
+
 /* Allocation-free entry point ------------------------------------------------------------
  * No counterpart in the reference.  For callers that may not allocate device memory (a host that
  * gives its whole device budget to its own pool or caching allocator, or that forbids third-party

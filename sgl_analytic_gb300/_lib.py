@@ -27,7 +27,9 @@ EXPORTS = ("sgl_abi_version", "sgl_ctx_create", "sgl_ctx_destroy", "sgl_last_err
            "sgl_plan_grid", "sgl_invert", "sgl_batch_create", "sgl_batch_destroy", "sgl_batch_slots",
            "sgl_batch_slot", "sgl_batch_pdf", "sgl_cfb_set", "sgl_cfb_tune", "sgl_cfb_lnphi", "sgl_cfb_pdf",
            "sgl_cfb_set_separable", "sgl_sur_set", "sgl_sur_judge", "sgl_sur_finish", "sgl_sur_pdf", "sgl_sur_nodes_exact",
-           "sgl_cosmo_tables", "sgl_cf_kappa_noalloc")
+           "sgl_cosmo_tables", "sgl_cells_init", "sgl_cells_add", "sgl_cells_xi_init", "sgl_cells_xi_begin",
+           "sgl_cells_xi_shear_tail", "sgl_cells_xi_end", "sgl_cells_xi_group", "sgl_cells_read",
+           "sgl_cf_kappa_noalloc")
 
 
 class InvertOpts(C.Structure):
@@ -115,6 +117,19 @@ def lib():
         L.sgl_sur_nodes_exact.argtypes = [vp, C.c_int, ip, ip, vp, C.c_int, C.c_double, C.c_double]
         L.sgl_cosmo_tables.argtypes = [vp, C.c_int, dp, C.c_int, dp, C.c_int, dp, C.c_int, dp] + [dp] * 8
         L.sgl_cosmo_tables.restype = C.c_int
+        ub = C.POINTER(C.c_ubyte)
+        L.sgl_cells_init.argtypes = [vp, C.c_int, C.c_int, C.c_int, dp, C.c_int, dp, C.c_int, dp, C.c_int, dp,
+                                     C.c_double, C.c_double]
+        L.sgl_cells_add.argtypes = [vp, C.c_int, lp, dp, dp, dp, dp, ip, dp, ub, dp]
+        L.sgl_cells_xi_init.argtypes = [vp, C.c_int, dp, dp, C.c_int, C.c_int]
+        L.sgl_cells_xi_begin.argtypes = [vp, C.c_double]
+        L.sgl_cells_xi_shear_tail.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double]
+        L.sgl_cells_xi_end.argtypes = [vp, C.POINTER(C.c_int)]
+        L.sgl_cells_xi_group.argtypes = [vp, C.c_int, ip, ip, ip, ip, dp, dp, dp]
+        L.sgl_cells_read.argtypes = [vp, dp, dp, dp, dp]
+        for name in ("sgl_cells_init", "sgl_cells_add", "sgl_cells_xi_init", "sgl_cells_xi_begin",
+                     "sgl_cells_xi_shear_tail", "sgl_cells_xi_end", "sgl_cells_xi_group", "sgl_cells_read"):
+            getattr(L, name).restype = C.c_int
         for name in ("sgl_sur_set", "sgl_sur_judge", "sgl_sur_finish", "sgl_sur_pdf", "sgl_sur_nodes_exact"):
             getattr(L, name).restype = C.c_int
         for name in ("sgl_sweep_set_cells", "sgl_sweep_eval", "sgl_measure_peak"):

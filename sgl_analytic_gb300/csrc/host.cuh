@@ -112,6 +112,8 @@ int cfb_n_inst(const CfbState* s);
 void cfb_inst_grid(const CfbState* s, int i, long long* k_off, int* nk, double* dk, double* k0);
 struct SurState;                         // surrogate + judge assembly state (host_sur.cu)
 void sur_state_free(SurState* s);
+struct CellsState;                       // binned-cell deposit state (host_cells.cu)
+void cells_state_free(CellsState* s);
 
 struct sgl_ctx {
     int device = 0;
@@ -119,6 +121,7 @@ struct sgl_ctx {
     std::string err;
     CfbState* cfb = nullptr;
     SurState* sur = nullptr;
+    CellsState* cells = nullptr;
     // batched solver launch shapes found by the autotuner, per precision and batch shape class
     std::unordered_map<long long, std::pair<int, int>> cfb_shapes;
     Arena arena;

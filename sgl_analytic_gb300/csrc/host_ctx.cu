@@ -64,6 +64,7 @@ void sgl_ctx_destroy(sgl_ctx* ctx) {
     if (ctx->side) cudaStreamSynchronize(ctx->side);
     if (ctx->cfb) cfb_state_free(ctx->cfb);
     if (ctx->sur) sur_state_free(ctx->sur);
+    if (ctx->cells) cells_state_free(ctx->cells);
     ctx->arena.release();
     for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
     resolve_stats(ctx);

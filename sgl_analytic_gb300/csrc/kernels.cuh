@@ -295,4 +295,31 @@ void launch_sweep1d(int precision, const double* kk, int nk, const double* kap, 
                     double* im, cudaStream_t st);
 void launch_fma_probe(int fp64, void* out, int blocks, int iters, cudaStream_t st);
 
+// ---- binned-cell deposit of the population build (cells.cu)
+struct CellsGeom {                        // the lattices: edge counts and the parameters of the log bin guess
+    int nekf, negf, nekc, negc;           // edges, stored [ekf | egf | ekc | egc]
+    double kf_lo, kf_dl, gf_lo, gf_dl, kc_lo, kc_dl, gc_lo, gc_dl;
+    double g_clip, k_max_fine;            // gamma clipped below at g_clip; |kappa| < k_max_fine enters lin
+    int nord;
+};
+int cells_edge_smem_bytes(const CellsGeom& g);
+void launch_cells_hist(const CellsGeom& g, const double* edges, long long n, const double* K, const double* Gm,
+                       const double* W, const long long* off, int n_obj, const int* shell, const double* betas,
+                       double* H0, double* H0k, double* H0g, double* Hc, double* sums, int n_sm, cudaStream_t st);
+constexpr int kXiChunk = 1024;            // points of one object per xi work item
+constexpr int kCellsXiMaxEdges = 1024;    // coarse kappa + gamma edges the xi kernel holds in shared memory
+struct CellsXiItem { long long first; int count, obj; };
+void launch_cells_xi(const CellsGeom& g, const double* edges, const CellsXiItem* items, int n_items,
+                     const double* K, const double* Gm, const double* W, const double* R, const double* beta,
+                     const unsigned char* tang, const double* kp, int nkp, int mm, double* Hx, double* lx, double* Wb,
+                     cudaStream_t st);
+void launch_cells_xi_tail(const double* kp, int nkp, double coef, double Rm, double* lx, cudaStream_t st);
+void launch_cells_xi_flags(const double* Hx, int nbins, int mm, int nkp, unsigned char* flags, cudaStream_t st);
+void launch_cells_xi_rows(const double* Hx, int mm, int nkp, int m, const int* idx, int nidx, const double* cen,
+                          int ngc, int cen_axis, const double* lxm, const double* sw, double* A, cudaStream_t st);
+int cells_gram_parts(long long nrows, int chunk);
+void launch_cells_gram(const double* A, long long nrows, int nkp, int chunk, double* part, double* Gram, cudaStream_t st);
+void launch_cells_project(const double* A, long long nrows, int nkp, const double* V, int nkeep, double* rows,
+                          cudaStream_t st);
+
 }  // namespace sgl

@@ -91,3 +91,41 @@ def cf_sweep_problem(seed=0, nz=128, nm=256, nb=512, nk=16384, total_rate=3.7e6)
     w *= total_rate / w.sum()
     kk = np.geomspace(1e-2, 1e6, nk)
     return kap.ravel(), w.ravel(), kk
+
+
+def deposit_node(seed=0, n_host=2048, n_fil=512, nphi=12, nx=260, nu=120):
+    """One lens-redshift node's deposits, shaped like the population build's emitters (sgl_full.py:1848-2011):
+    n_host pseudo-elliptical truncated NFW hosts, each nphi orientations x nx radial cells (kappa from the
+    truncated projected profile times 1 + eps cos 2 phi, gamma 0.8 kappa, weights N_bar d(x^2) / x_m^2 / nphi,
+    lens distance R = x r_s), and n_fil filaments of nu cells x nphi orientations (kappa of a cylinder core,
+    gamma kappa / 2, untangential).  Masses log-uniform, kappa_s over 1e-4..3, seeded.  Returns a list of
+    objects for Cells.add_many (with R and tang) and the node's dchi."""
+    rng = np.random.default_rng(seed)
+    phis = (np.arange(nphi) + 0.5) * (0.5 * np.pi / nphi)
+    objs = []
+    for h in range(n_host):
+        ks = float(np.exp(rng.uniform(np.log(1e-4), np.log(3.0))))
+        c = float(rng.uniform(3.0, 12.0))
+        rs = float(np.exp(rng.uniform(np.log(0.02), np.log(0.4))))
+        eps = float(rng.uniform(0.0, 0.3))
+        nbar = float(np.exp(rng.uniform(np.log(1e-3), np.log(1e3))))
+        xm = c * 1.5
+        xe = np.concatenate([[0.0], xm * np.geomspace(1e-6, 1.0, nx)])
+        xc = np.where(xe[:-1] > 0, np.sqrt(xe[:-1] * np.maximum(xe[1:], 1e-300)), 0.5 * xe[1])
+        base = ks * 4.0 * nfw_trunc_projected(xc, c)
+        K = (base[None, :] * (1.0 + eps * np.cos(2 * phis)[:, None])).ravel()
+        G = 0.8 * K
+        W = np.tile(nbar * (xe[1:] ** 2 - xe[:-1] ** 2) / xm ** 2 / nphi, nphi)
+        objs.append(dict(K=K, G=G, W=W, R=np.tile(xc * rs, nphi), shell=0, beta=float(rng.uniform(0.8, 3.0)),
+                         tang=True))
+    for f in range(n_fil):
+        k0 = float(np.exp(rng.uniform(np.log(1e-4), np.log(0.3))))
+        rsf = float(np.exp(rng.uniform(np.log(0.05), np.log(2.0))))
+        ue = np.concatenate([[0.0], np.geomspace(1e-5, 1.0, nu)])
+        uc = np.where(ue[:-1] > 0, np.sqrt(ue[:-1] * np.maximum(ue[1:], 1e-300)), 0.5 * ue[1])
+        kk = k0 * np.sqrt(np.maximum(1.0 - uc ** 2, 0.0))
+        K = np.repeat(kk[:, None], nphi, 1).ravel() * np.tile(1.0 / np.maximum(np.cos(phis), 0.1), nu) / 10.0
+        W = np.repeat(((ue[1:] ** 2 - ue[:-1] ** 2))[:, None], nphi, 1).ravel() * float(rng.uniform(0.1, 10.0)) / nphi
+        objs.append(dict(K=K, G=0.5 * K, W=W, R=np.repeat(uc * rsf, nphi), shell=0,
+                         beta=float(rng.uniform(0.5, 2.0)), tang=False))
+    return objs, 40.0
