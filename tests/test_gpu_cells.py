@@ -125,3 +125,17 @@ def test_real_shell_matches_reference():
         pytest.skip("recorded shell not present")
     c = Cells(1, int(d["nord"]), xi=dict(kp=d["xi_kp"], c=d["xi_c"], mmax=int(d["xi_mmax"])))
     CR.check_shell(CR.replay_shell(c, d), d, RTOL_BINS, TOL_ROWS)
+
+
+def test_lattice_attributes_are_stable_arrays():
+    """The reference's build merges per-shell pieces into a result Cells by editing H0 / Hc in place
+    (sgl_full.py:1790-1797) and reads them back later: the arrays returned stay the same objects until
+    the next deposit."""
+    from sgl_analytic_gb300.cells import Cells
+    c = Cells(2, 1)
+    h = c.H0
+    h.reshape(-1)[[3, 7]] += [1.5, 2.5]
+    c.Hc[1] += 1.0
+    assert c.H0 is h and c.H0.reshape(-1)[7] == 2.5 and np.all(c.Hc[1] == 1.0)
+    c.add(np.array([0.5]), np.array([0.5]), np.array([1.0]), 0, 1.0)
+    assert c.H0.reshape(-1)[7] == 0.0 and c.H0.sum() == 1.0     # a deposit reads the device lattices again
