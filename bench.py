@@ -14,7 +14,8 @@ Without that file a labelled stand-in (xi groups synthesised from one shell) is 
 * value    PDFs/s with the population resident in HBM, device-timed with CUDA events on the
            engine's streams (max over ranks; N ranks run N independent replicas: weak scaling).
 * e2e      the same metric through the drop-in call Lam(population) + invert(...) with HOST
-           buffers: population upload (H2D), every PDF stage, P_s read back (D2H) per step.
+           buffers: population upload (H2D), every PDF stage, P_s read back (D2H) per step; one
+           such loop per context on --slots host threads (value_one_context: a single loop).
 * roofline the kernel with the largest device time in the timed region: its algorithmic FLOPs
            (or bytes) per launch / its event-timed duration, against the measured peak.
 * accuracy every PDF of the timed regions and of the e2e loop, against the reference's stored
@@ -336,7 +337,8 @@ def run_batched(args, rank, world, local):
                            "l2": "cells (1.7 GB FP32 + float-float) and ln Phi (1.2 GB) larger than L2"},
                 "accuracy": {"instances_checked": len(sel), "pdf_l1_vs_fp64_max": max(l1), "max_dP_over_peak": max(dpk),
                              "bar_l1": 1e-4},
-                "e2e": {"value": e2e, "unit": "PDF/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(P.nbytes)},
+                "e2e": {"value": e2e, "unit": "PDF/s", "h2d_bytes_per_step": int(h2d), "contexts": e2e_slots,
+                        "value_one_context": e2e_one, "d2h_bytes_per_step": int(P.nbytes)},
                 "roofline": {"kernel": "k_cfb_persistent (+ inversion)", "bound": "fp32-pipe", "achieved": ach,
                              "peak": f32 / 2, "unit": "T inst/s", "frac": ach / (f32 / 2),
                              "ops_per_term": MIXED_OPS_PER_TERM, "terms_per_s": terms / (ms / args.steps / 1e3),
@@ -740,18 +742,44 @@ def main():
     # ---- e2e: drop-in call with host buffers (population upload + PDF + read-back)
     h2d = sum(a.nbytes for a in (pop.w0, pop.k0, pop.g0, pop.ig, pop.fe_g, pop.xg_m, pop.xg_nrow, pop.xg_nidx,
                                  pop.xg_idx, pop.xg_rows, pop.ce_k, pop.ce_g))
+
+    def e2e_loop(e, n):
+        outs, split = [], []
+        for _ in range(n):
+            ta = time.perf_counter()
+            lam_e = Lam(pop, xi=True, engine=e, precision=args.precision)
+            tb = time.perf_counter()
+            _, Pe, _ = invert(lam_e, lam_e.sigma(), xi_out=XI_OUT, phi_tol=1e-8, precision=args.precision)
+            split.append((tb - ta, time.perf_counter() - tb))
+            outs.append(Pe)
+        return outs, split
+
+    # one context, one PDF after another
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    e2e_P, e2e_split = [], []
-    for _ in range(args.e2e_steps):
-        ta = time.perf_counter()
-        lam_e = Lam(pop, xi=True, engine=eng, precision=args.precision)
-        tb = time.perf_counter()
-        _, Pe, _ = invert(lam_e, lam_e.sigma(), xi_out=XI_OUT, phi_tol=1e-8, precision=args.precision)
-        e2e_split.append((tb - ta, time.perf_counter() - tb))
-        e2e_P.append(Pe)
+    e2e_P, e2e_split = e2e_loop(eng, args.e2e_steps)
     torch.cuda.synchronize()
-    e2e = args.e2e_steps / (time.perf_counter() - t0)
+    e2e_one = args.e2e_steps / (time.perf_counter() - t0)
+    e2e = e2e_one
+    # `slots` contexts, each on its own host thread running the same drop-in loop (the engine's calls
+    # release the interpreter lock): uploads, kernels and read-backs of different PDFs overlap, as with
+    # the batched solver of the timed region
+    e2e_slots = 1
+    if args.slots > 1 and args.e2e_steps > 0:
+        from concurrent.futures import ThreadPoolExecutor
+        engs = [eng] + [Engine(local) for _ in range(args.slots - 1)]
+        with ThreadPoolExecutor(args.slots) as ex:
+            list(ex.map(lambda e: e2e_loop(e, 1), engs[1:]))          # untimed first use of the new contexts
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = list(ex.map(lambda e: e2e_loop(e, args.e2e_steps), engs))
+            torch.cuda.synchronize()
+            e2e = args.slots * args.e2e_steps / (time.perf_counter() - t0)
+        e2e_slots = args.slots
+        for outs, split in res:
+            e2e_P += outs
+        for e in engs[1:]:
+            e.close()
     accuracy = {"bar_l1": 1e-4, "bar_tail": 1e-3, "vs_fp64_path": worst(all_P + e2e_P, P64)}
     if Pref is not None:
         accuracy["vs_reference_pdf"] = worst(all_P + e2e_P, Pref)
@@ -815,7 +843,8 @@ def main():
                 "single_stream": {"value": single_value, "unit": "PDF/s", "ms_per_pdf": single_ms},
                 "batched": batched,
                 "fp64_path": fp64_line,
-                "e2e": {"value": e2e, "unit": "PDF/s", "h2d_bytes_per_step": int(h2d),
+                "e2e": {"value": e2e, "unit": "PDF/s", "h2d_bytes_per_step": int(h2d), "contexts": e2e_slots,
+                        "value_one_context": e2e_one,
                         "ms_lam_median": 1e3 * float(np.median([a for a, _ in e2e_split])) if e2e_split else None,
                         "ms_invert_median": 1e3 * float(np.median([b for _, b in e2e_split])) if e2e_split else None,
                         "d2h_bytes_per_step": int(XI_OUT.size * 8)},
