@@ -77,13 +77,20 @@ sgl_status cfb_launch(sgl_ctx* ctx, int precision, int kt, int cps, const std::v
 }
 
 // The launch shape: each (tile width, CTAs per SM) allowed by occupancy is timed on a sample of the
-// batch (every 16th instance in cost order, at most 256), the fastest kept for this precision.
+// batch, the fastest kept for this precision.  The sample takes instances evenly spread in cost
+// order, at most 256 of them and about kTuneTerms (cells x k) of work, so that a tune costs well
+// under a second whatever the batch.
 sgl_status cfb_tune(sgl_ctx* ctx, int precision) {
     CfbState& S = *ctx->cfb;
     const int P = precision == SGL_FP64 ? 0 : 1;
+    const double kTuneTerms = precision == SGL_FP64 ? 1e9 : 4e10;
+    double total = 0.0;
+    for (double c : S.cost) total += c;
     std::vector<int> sample;
-    const int stride = std::max(1, (int)S.order.size() / 256);
-    for (size_t i = 0; i < S.order.size(); i += (size_t)stride) sample.push_back(S.order[i]);
+    const size_t n = S.order.size();
+    size_t stride = std::max<size_t>(1, n / 256);
+    if (total > kTuneTerms) stride = std::max(stride, (size_t)std::ceil(total / kTuneTerms));
+    for (size_t i = 0; i < n; i += stride) sample.push_back(S.order[i]);
     cudaEvent_t a, b;
     CK(cudaEventCreate(&a));
     CK(cudaEventCreate(&b));
