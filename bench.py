@@ -337,8 +337,7 @@ def run_batched(args, rank, world, local):
                            "l2": "cells (1.7 GB FP32 + float-float) and ln Phi (1.2 GB) larger than L2"},
                 "accuracy": {"instances_checked": len(sel), "pdf_l1_vs_fp64_max": max(l1), "max_dP_over_peak": max(dpk),
                              "bar_l1": 1e-4},
-                "e2e": {"value": e2e, "unit": "PDF/s", "h2d_bytes_per_step": int(h2d), "contexts": e2e_slots,
-                        "value_one_context": e2e_one, "d2h_bytes_per_step": int(P.nbytes)},
+                "e2e": {"value": e2e, "unit": "PDF/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(P.nbytes)},
                 "roofline": {"kernel": "k_cfb_persistent (+ inversion)", "bound": "fp32-pipe", "achieved": ach,
                              "peak": f32 / 2, "unit": "T inst/s", "frac": ach / (f32 / 2),
                              "ops_per_term": MIXED_OPS_PER_TERM, "terms_per_s": terms / (ms / args.steps / 1e3),
