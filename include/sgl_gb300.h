@@ -282,7 +282,9 @@ sgl_status sgl_batch_pdf(sgl_batch* batch, int n_jobs, const int32_t* job_slot, 
  *                           instance (in order) vp_K[s][t] (transition) and vp_w[s] (stationary weights) --
  *                           the positive Cox closure's chain (pos_closure.py:184-240) with one group per plane.
  * sgl_cfb_set uploads the batch (host arrays).  sgl_cfb_tune times every (k points per work item, CTAs per
- * SM) shape on a sample of the batch and keeps the fastest for that precision (run on first use otherwise).
+ * SM) shape on a work-bounded sample of the batch and keeps the fastest (SGL_MIXED; SGL_FP64 takes 128
+ * k-points per item and every resident CTA); it runs on first use otherwise, once per batch shape class
+ * (largest k grid and mean cells per instance, in powers of two) and context.
  * sgl_cfb_lnphi runs the persistent solve (one launch; CTAs take (instance, k tile) items from a device
  * counter, longest instances first) and copies ln Phi out as (re, im) pairs per k, instances in order
  * (out may be NULL).  sgl_cfb_pdf adds Phi = exp(ln Phi) and the inversion to dP/dln mu at the n_lnmu

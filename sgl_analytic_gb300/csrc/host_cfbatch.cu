@@ -76,28 +76,42 @@ sgl_status cfb_launch(sgl_ctx* ctx, int precision, int kt, int cps, const std::v
     return SGL_OK;
 }
 
-// The launch shape: each (tile width, CTAs per SM) allowed by occupancy is timed on a sample of the
-// batch, the fastest kept for this precision.  The sample takes instances evenly spread in cost
-// order, at most 256 of them and about kTuneTerms (cells x k) of work, so that a tune costs well
-// under a second whatever the batch.
+// The launch shape.  FP64 (the parity path, whose FP64 pipe makes every term slow here) takes a fixed
+// shape: 128 k-points per item, as many CTAs per SM as fit.  The mixed path times each (tile width,
+// CTAs per SM) allowed by occupancy on a sample of the batch and keeps the fastest: instances evenly
+// spread in cost order (at most 256), then every s-th of their work items so that a timed launch holds
+// about kTuneTerms cell-k terms, the same fraction for every tile width; a tune costs about a second.
 sgl_status cfb_tune(sgl_ctx* ctx, int precision) {
     CfbState& S = *ctx->cfb;
     const int P = precision == SGL_FP64 ? 0 : 1;
-    const double kTuneTerms = precision == SGL_FP64 ? 1e9 : 4e10;
-    double total = 0.0;
-    for (double c : S.cost) total += c;
+    if (precision == SGL_FP64) {
+        S.kt[P] = 128;
+        S.cps[P] = std::max(1, cfb_resident_ctas(precision, 128));
+        S.tuned[P] = true;
+        ctx->cfb_shapes[2LL * S.shape_class + P] = {S.kt[P], S.cps[P]};
+        return SGL_OK;
+    }
+    constexpr double kTuneTerms = 2e10;
     std::vector<int> sample;
-    const size_t n = S.order.size();
-    size_t stride = std::max<size_t>(1, n / 256);
-    if (total > kTuneTerms) stride = std::max(stride, (size_t)std::ceil(total / kTuneTerms));
-    for (size_t i = 0; i < n; i += stride) sample.push_back(S.order[i]);
+    const size_t stride = std::max<size_t>(1, S.order.size() / 256);
+    double scost = 0.0;
+    for (size_t i = 0; i < S.order.size(); i += stride) {
+        sample.push_back(S.order[i]);
+        scost += S.cost[(size_t)S.order[i]];
+    }
+    const size_t istride = scost > kTuneTerms ? (size_t)std::ceil(scost / kTuneTerms) : 1;
     cudaEvent_t a, b;
     CK(cudaEventCreate(&a));
     CK(cudaEventCreate(&b));
     double best = 1e300;
     for (int kt : {64, 128, 256}) {
         const int res = cfb_resident_ctas(precision, kt);
-        const std::vector<int2> items = cfb_items(S, kt, sample);
+        std::vector<int2> items = cfb_items(S, kt, sample);
+        if (istride > 1) {
+            std::vector<int2> sub;
+            for (size_t q = 0; q < items.size(); q += istride) sub.push_back(items[q]);
+            items.swap(sub);
+        }
         for (int cps : {1, 2, 4, 8, 16}) {
             if (cps > res) continue;
             CKS(cfb_launch(ctx, precision, kt, cps, items, "tune"));       // warm
