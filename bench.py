@@ -91,6 +91,18 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(x, world):
+    """The largest x over the ranks (timed regions are reported as the slowest rank's); a device tensor
+    under NCCL, a host tensor under gloo."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 class Clocks:
     """nvidia-smi clock / throttle sampling during the timed region."""
 
@@ -222,11 +234,7 @@ def run_cf_sweep(args, rank, world, local):
     torch.cuda.synchronize()
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world)
     f32 = eng.measure_peak(False)
     f64 = eng.measure_peak(True)
     rate = world * args.steps * terms / (ms / 1e3)
@@ -285,11 +293,7 @@ def run_batched(args, rank, world, local):
     torch.cuda.nvtx.range_pop()
     clk = clocks.stop()
     ms = float(np.sum(ms_steps))
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world)
     terms = b.terms()
     rate = world * args.steps * n / (ms / 1e3)
     # accuracy: a sample of the instances (every 256th) solved again alone in FP64
@@ -550,7 +554,7 @@ def run_cells(args, rank, world, local):
     clk = clocks.stop()
     ms_hist = st["cells_hist"]["ms"] / args.steps
     ms_xi = st["cells_xi"]["ms"] / args.steps
-    ms_dev = ms_hist + ms_xi
+    ms_dev = max_over_ranks(ms_hist + ms_xi, world)
     launches = int(st.get("_launches", {}).get("launches", 0))
     f64 = eng.measure_peak(True)
     pk, pk_src = peaks()
@@ -678,11 +682,7 @@ def main():
     torch.cuda.synchronize()
     stats = eng.stats(reset=True)
     eng.profile(False)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world)
     single_value, single_ms = world * args.steps / (ms / 1e3), ms / args.steps
     value = single_value
     # ---- batched plain solver: `slots` resident copies of the workload, one context (stream) each,
@@ -712,11 +712,7 @@ def main():
         b1.record(master)
         torch.cuda.synchronize()
         bms = b0.elapsed_time(b1)
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([bms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            bms = float(t.item())
+        bms = max_over_ranks(bms, world)
         batched_P = [P_ for slot in outs for P_ in slot]
         batched = {"slots": args.slots, "pdfs": args.slots * args.steps * world,
                    "value": world * args.slots * args.steps / (bms / 1e3), "ms": bms}
