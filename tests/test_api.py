@@ -4,7 +4,6 @@ negative-residual warning) plus the GPU-path limits, the plugin and the CLI."""
 import json
 from pathlib import Path
 import types
-import warnings
 from unittest.mock import patch
 
 import numpy as np
