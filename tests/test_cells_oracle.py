@@ -42,3 +42,19 @@ def test_oracle_real_shell():
         pytest.skip("recorded shell not present")
     c = CellsOracle(1, int(d["nord"]), xi=dict(kp=d["xi_kp"], c=d["xi_c"], mmax=int(d["xi_mmax"])))
     CR.check_shell(CR.replay_shell(c, d), d, 0.0, 1e-10, exact=True)
+
+
+def test_deposit_bench_workload_shape():
+    """The bench's deposit node: 2048 hosts of 12 x 260 cells and 512 filaments of 120 x 12, each
+    object's arrays aligned, weights positive, lens distances positive, filaments untangential."""
+    from sgl_analytic_gb300.workloads import deposit_node
+    objs, dchi = deposit_node(seed=0, n_host=8, n_fil=4)
+    assert dchi > 0 and len(objs) == 12
+    for o in objs[:8]:
+        assert o["K"].size == o["G"].size == o["W"].size == o["R"].size == 12 * 260 and o["tang"]
+    for o in objs[8:]:
+        assert o["K"].size == 120 * 12 and not o["tang"]
+    for o in objs:
+        assert np.all(o["W"] >= 0) and np.all(o["R"] > 0) and np.all(np.isfinite(o["K"]))
+    full, _ = deposit_node(seed=0)
+    assert sum(o["K"].size for o in full) == 2048 * 3120 + 512 * 1440
